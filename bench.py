@@ -1,0 +1,396 @@
+"""Benchmark of the Krylov hot path on one GB300 (or N replicas).
+
+Workload (default): 3-D variable-coefficient diffusion on a 256^3 grid
+(16,777,216 rows, 117,047,296 nonzeros), log-normal cell coefficients
+(sigma = 1, seed 2) with harmonic face averaging, RHS U[-1, 1] (seed 3),
+Jacobi-preconditioned CG to rtol 1e-8, zero initial guess.  A "step" is one
+full solve.  The headline `value` is the time-to-rtol of the mixed-precision
+refined PCG (FP32 inner iterations, FP64 residual / update / stopping test);
+the plain FP64 GPU PCG is timed the same way and their ratio is reported.
+
+The matrix (1.7 GB FP64) is larger than L2 (129 MB), so no flush is needed
+between steps.  Timing: CUDA events on the library's stream around exactly
+K steps, after W warm-up steps, with nvidia-smi clock sampling during the
+timed region.  `e2e` times the same solve through the public C ABI with the
+right-hand side uploaded from pinned host memory and the solution downloaded
+every step.
+
+`--impl reference` times the reference's own CPU algorithm instead (the
+oracle restatement, pinned bit-exact to the reference's templates) on a
+bounded sample of PCG iterations of the same workload and projects the
+time-to-rtol with the reference's iteration count for this workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "PCG time-to-rtol1e-8 & SpMV HBM GB/s; mixed-prec vs FP64 speedup, 1 GB300"
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def spmv_bytes(nrows, nnz, val_bytes):
+    """Algorithmic bytes of one CSR SpMV: values + int32 columns, int32 row
+    offsets, x read once, y written once."""
+    return nnz * (val_bytes + 4) + 4 * (nrows + 1) + 2 * nrows * val_bytes
+
+
+def pcg_iter_bytes(nrows, nnz, val_bytes):
+    """Algorithmic bytes of one fused Jacobi-PCG iteration: SpMV + update
+    (read x, p, r, w, D^-1; write x, r) + direction (read p, r, D^-1; write p)."""
+    return spmv_bytes(nrows, nnz, val_bytes) + 11 * nrows * val_bytes
+
+
+def _traffic_from_profiles(kernel_key):
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get(kernel_key)
+        except Exception:
+            return None
+    return None
+
+
+def reference_iters(workload):
+    p = ROOT / "tests" / "golden" / "full_size.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        c = d.get(workload, {}).get("cg")
+        if c:
+            return int(c["iters"])
+    return None
+
+
+# ------------------------------------------------------------ CPU side --
+
+def cpu_sample(A, b, seconds_target=15.0, max_iters=60):
+    """Time the oracle (the reference's serial PCG restated in C) on a bounded
+    number of iterations of the workload; returns seconds per iteration."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle as O
+    # one short probe to size the sample
+    t0 = time.perf_counter()
+    O.solve("cg", A, b, maxiter=2, rtol=1e-30)
+    probe = (time.perf_counter() - t0) / 2
+    iters = int(max(3, min(max_iters, seconds_target / max(probe, 1e-6))))
+    t0 = time.perf_counter()
+    O.solve("cg", A, b, maxiter=iters, rtol=1e-30)
+    dt = time.perf_counter() - t0
+    return dt / iters, iters
+
+
+# ------------------------------------------------------------ GPU side --
+
+def run_ours(args, ws, rank, local):
+    import flecsolve_gb300 as fs
+    from flecsolve_gb300 import problems as P
+
+    wl = args.workload
+    t0 = time.perf_counter()
+    A, b = P.workload(wl)
+    gen_s = time.perf_counter() - t0
+    n, nnz = A.nrows, A.nnz
+    ctx = fs.Context(local)
+    dA = fs.CSR(ctx, A)
+    vb = fs.Vector(ctx, b)
+    vx = fs.Vector(ctx, n)
+    s64 = fs.cg.settings(maxiter=args.maxiter, rtol=1e-8, use_zero_guess=True)
+    smx = fs.mixed_cg.settings(maxiter=args.maxiter, rtol=1e-8, use_zero_guess=True,
+                               inner_rtol=args.inner_rtol, refine=args.refine)
+    cg64 = fs.cg.solver(s64, fs.cg.make_work(vb))(fs.op.ref(dA), fs.op.jacobi)
+    cgmx = fs.mixed_cg.solver(smx, fs.mixed_cg.make_work(vb))(fs.op.ref(dA), fs.op.jacobi)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed(slv, K, W, tag):
+        for _ in range(W):
+            info = slv(vb, vx)
+        barrier()
+        ctx.sync()
+        l0 = ctx.launches
+        ctx.record(0)
+        infos = []
+        for _ in range(K):
+            infos.append(slv(vb, vx))
+        ctx.record(1)
+        ms = ctx.elapsed_ms(0, 1)
+        ctx.sync()
+        barrier()
+        return ms / K, infos[-1], ctx.launches - l0
+
+    with ClockSampler(local) as clk:
+        ms_mx, info_mx, launches_mx = timed(cgmx, args.steps, args.warmup, "mixed")
+    clocks = clk.summary()
+    x_mx = vx.numpy()
+    ms_64, info_64, launches_64 = timed(cg64, args.steps, max(1, args.warmup // 3), "fp64")
+    x_64 = vx.numpy()
+
+    # max over ranks of the per-step time
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms_mx, ms_64], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_mx, ms_64 = float(t[0]), float(t[1])
+
+    # SpMV kernel alone (the dominant kernel), CUDA events on the same stream
+    def spmv_time(dtype, reps=20):
+        xv = fs.Vector(ctx, n, dtype)
+        yv = fs.Vector(ctx, n, dtype)
+        xv.set_random(5)
+        for _ in range(3):
+            dA.apply(xv, yv)
+        ctx.sync()
+        ctx.record(2)
+        for _ in range(reps):
+            dA.apply(xv, yv)
+        ctx.record(3)
+        return ctx.elapsed_ms(2, 3) / reps
+
+    spmv64_ms = spmv_time("f64")
+    spmv32_ms = spmv_time("f32")
+    peak, peak_kind = _peaks()
+    b64 = spmv_bytes(n, nnz, 8)
+    b32 = spmv_bytes(n, nnz, 4)
+    gbs64 = b64 / (spmv64_ms * 1e-3) / 1e9
+    gbs32 = b32 / (spmv32_ms * 1e-3) / 1e9
+
+    # e2e: through the public API with host buffers
+    import torch
+    hb = torch.from_numpy(b).pin_memory()
+    hx = torch.empty(n, dtype=torch.float64).pin_memory()
+    import ctypes as C
+    from flecsolve_gb300._lib import lib, check
+    L = lib()
+    for _ in range(max(1, args.warmup // 3)):
+        check(L.fs_vec_upload(vb.h, C.c_void_p(hb.data_ptr()), n), ctx.h)
+        cgmx(vb, vx)
+        check(L.fs_vec_download(vx.h, C.c_void_p(hx.data_ptr()), n), ctx.h)
+    barrier()
+    ctx.sync()
+    ctx.record(4)
+    for _ in range(args.steps):
+        check(L.fs_vec_upload(vb.h, C.c_void_p(hb.data_ptr()), n), ctx.h)
+        cgmx(vb, vx)
+        check(L.fs_vec_download(vx.h, C.c_void_p(hx.data_ptr()), n), ctx.h)
+    ctx.record(5)
+    e2e_ms = ctx.elapsed_ms(4, 5) / args.steps
+    barrier()
+
+    # accuracy of the headline result against the FP64 GPU solve, and the
+    # true FP64 relative residual of both
+    sys.path.insert(0, str(ROOT / "oracle"))
+    relres_mx = float(np.linalg.norm(b - A.to_scipy() @ x_mx) / np.linalg.norm(b))
+    relres_64 = float(np.linalg.norm(b - A.to_scipy() @ x_64) / np.linalg.norm(b))
+    err_vs_fp64 = float(np.linalg.norm(x_mx - x_64) / np.linalg.norm(x_64))
+
+    out = {
+        "metric": METRIC,
+        "value": ms_mx * 1e-3,
+        "unit": "s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_mx,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32-inner/f64-refine",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": f"{wl} variable-coefficient diffusion, log-normal sigma=1, "
+                               f"harmonic faces, Jacobi PCG rtol 1e-8",
+                   "rows": n, "nnz": nnz, "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "inputs larger than L2 (matrix 1.7 GB), no flush"},
+        "fp64_pcg": {"s": ms_64 * 1e-3, "iters": info_64.iters, "status": info_64.status,
+                     "true_relres": relres_64, "launches_per_step": launches_64 / args.steps},
+        "mixed_pcg": {"s": ms_mx * 1e-3, "iters": info_mx.iters, "outer": info_mx.restarts,
+                      "status": info_mx.status, "true_relres": relres_mx,
+                      "rel_err_vs_fp64_gpu": err_vs_fp64, "refine": args.refine,
+                      "inner_rtol": args.inner_rtol},
+        "speedup_mixed_vs_fp64": ms_64 / ms_mx,
+        "spmv_hbm_gbs": {"f64": gbs64, "f32": gbs32, "f64_ms": spmv64_ms, "f32_ms": spmv32_ms},
+        "roofline": {"bound": "hbm", "kernel": "spmv_rb_kernel<float> (FP32 CSR SpMV)",
+                     "achieved": gbs32, "peak": peak, "unit": "GB/s", "frac": gbs32 / peak,
+                     "peak_source": f"hbm_gbs of {peak_kind}",
+                     "algorithmic_bytes_per_launch": b32,
+                     "traffic": _traffic_from_profiles("spmv_f32")},
+        "roofline_fp64_spmv": {"achieved": gbs64, "peak": peak, "frac": gbs64 / peak,
+                               "algorithmic_bytes_per_launch": b64,
+                               "traffic": _traffic_from_profiles("spmv_f64")},
+        "e2e": {"value": e2e_ms * 1e-3, "unit": "s", "h2d_bytes_per_step": 8 * n,
+                "d2h_bytes_per_step": 8 * n},
+        "gpu_launches": launches_mx,
+        "clocks": clocks,
+        "setup": {"generate_s": gen_s},
+    }
+    if rank == 0 and not args.no_cpu:
+        per_it, its = cpu_sample(A, b, args.cpu_seconds)
+        ref_it = reference_iters(wl) or info_64.iters
+        out["cpu_baseline"] = {"value": per_it * ref_it, "unit": "s", "cores": 1, "kind": "port",
+                               "sample": f"{its} Jacobi-PCG iterations of {wl} timed with the "
+                                         f"oracle (reference serial PCG restated in C, pinned "
+                                         f"bit-exact to the reference), {per_it:.4f} s/iter x "
+                                         f"{ref_it} reference iterations"}
+    return out
+
+
+def run_reference(args, ws, rank, local):
+    from flecsolve_gb300 import problems as P
+    wl = args.workload
+    A, b = P.workload(wl)
+    ref_it = reference_iters(wl)
+    samples = []
+    for i in range(args.warmup + args.steps):
+        per_it, its = cpu_sample(A, b, args.cpu_seconds / 2, max_iters=40)
+        if i >= args.warmup:
+            samples.append(per_it)
+    per_it = statistics.median(samples)
+    iters = ref_it if ref_it else None
+    val = per_it * iters if iters else per_it
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": val,
+        "unit": "s" if iters else "s/iteration",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": val * 1e3,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": f"{wl} variable-coefficient diffusion, Jacobi PCG rtol 1e-8",
+                   "rows": A.nrows, "nnz": A.nnz},
+        "cpu_baseline": {"value": val, "unit": "s", "cores": 1, "kind": "port",
+                         "sample": f"median per-iteration time of bounded PCG samples "
+                                   f"(<= 40 iterations each) of the oracle, the reference's "
+                                   f"serial PCG restated in C (single-threaded as the "
+                                   f"reference's seq path), x {iters} reference iterations"},
+        "e2e": {"value": val, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="diffusion3d-256")
+    ap.add_argument("--maxiter", type=int, default=20000)
+    ap.add_argument("--inner-rtol", dest="inner_rtol", type=float, default=1e-4)
+    ap.add_argument("--refine", default="restart", choices=["restart", "reliable"])
+    ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        if args.impl == "reference":
+            if rank != 0:
+                return
+        else:
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if args.impl == "reference":
+        out = run_reference(args, ws, rank, local)
+    else:
+        out = run_ours(args, ws, rank, local)
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1 and args.impl != "reference":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,177 @@
+"""ctypes binding of ``libfsgpu.so`` (the C ABI of ``include/fsgpu.h``).
+
+The product path is the CUDA library: importing this module loads it and
+raises if it is missing or if no CUDA device is usable -- there is no CPU
+fallback anywhere in the package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from functools import lru_cache
+from pathlib import Path
+
+from . import build as _build
+
+LIB_PATH = _build.BUILD / "libfsgpu.so"
+
+# enum fs_status
+OK = 0
+STATUS_NAMES = {0: "ok", 1: "bad handle", 2: "size mismatch", 3: "out of memory",
+                4: "CUDA error", 5: "non-finite", 6: "breakdown", 7: "invalid argument",
+                8: "no device", 9: "unsupported"}
+ERR_BAD_HANDLE, ERR_SIZE_MISMATCH, ERR_OUT_OF_MEMORY, ERR_CUDA = 1, 2, 3, 4
+ERR_NON_FINITE, ERR_BREAKDOWN, ERR_INVALID_ARG, ERR_NO_DEVICE, ERR_UNSUPPORTED = 5, 6, 7, 8, 9
+
+F64, F32 = 0, 1
+CG, BICGSTAB, GMRES, CG_MIXED = 0, 1, 2, 3
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_DIAG, PRECOND_CSR = 0, 1, 2, 3
+LEFT, RIGHT = 0, 1
+ORTHO_CGS2, ORTHO_MGS = 0, 1
+REFINE_RESTART, REFINE_RELIABLE = 0, 1
+SPMV_FMA, SPMV_EXACT = 0, 1
+
+# solve_info::stop_reason, flecsolve/solvers/solver_settings.hh:64-72
+STOP_REASONS = {0: "converged_atol", 1: "converged_rtol", 2: "converged_user",
+                3: "diverged_dtol", 4: "diverged_iters", 5: "diverged_breakdown",
+                6: "unknown"}
+
+
+class SolverSettings(C.Structure):
+    _fields_ = [("maxiter", C.c_int), ("rtol", C.c_float), ("atol", C.c_float),
+                ("use_zero_guess", C.c_int)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("iters", C.c_int), ("restarts", C.c_int),
+                ("res_norm_initial", C.c_float), ("res_norm_final", C.c_float),
+                ("sol_norm_initial", C.c_float), ("sol_norm_final", C.c_float),
+                ("rhs_norm", C.c_float)]
+
+
+class KrylovSettings(C.Structure):
+    _fields_ = [("base", SolverSettings), ("max_krylov_dim", C.c_int),
+                ("pre_side", C.c_int), ("restart", C.c_int), ("ortho", C.c_int),
+                ("k_readback", C.c_int), ("refine", C.c_int),
+                ("inner_rtol", C.c_double), ("max_outer", C.c_int)]
+
+
+class Precond(C.Structure):
+    _fields_ = [("kind", C.c_int), ("diag", C.c_void_p), ("op", C.c_void_p)]
+
+
+DIAG_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_double)
+
+_vp = C.c_void_p
+_i64 = C.c_int64
+_dp = C.POINTER(C.c_double)
+
+
+# name -> (argtypes); every function returns int status
+_PROTOS = {
+    "fs_ctx_create": [C.c_int, C.POINTER(_vp)],
+    "fs_ctx_destroy": [_vp],
+    "fs_ctx_sync": [_vp],
+    "fs_ctx_stream": [_vp, C.POINTER(_vp)],
+    "fs_ctx_sm_count": [_vp, C.POINTER(C.c_int)],
+    "fs_ctx_launch_count": [_vp, C.POINTER(_i64)],
+    "fs_ctx_event_record": [_vp, C.c_int],
+    "fs_ctx_event_elapsed": [_vp, C.c_int, C.c_int, C.POINTER(C.c_float)],
+    "fs_vec_create": [_vp, _i64, C.c_int, C.POINTER(_vp)],
+    "fs_vec_wrap": [_vp, _i64, C.c_int, _vp, C.POINTER(_vp)],
+    "fs_vec_destroy": [_vp],
+    "fs_vec_size": [_vp, C.POINTER(_i64)],
+    "fs_vec_dtype": [_vp, C.POINTER(C.c_int)],
+    "fs_vec_device_ptr": [_vp, C.POINTER(_vp)],
+    "fs_vec_upload": [_vp, _vp, _i64],
+    "fs_vec_download": [_vp, _vp, _i64],
+    "fs_vec_copy": [_vp, _vp],
+    "fs_vec_zero": [_vp],
+    "fs_vec_set_scalar": [_vp, C.c_double],
+    "fs_vec_scale": [C.c_double, _vp, _vp],
+    "fs_vec_scale_self": [C.c_double, _vp],
+    "fs_vec_add": [_vp, _vp, _vp],
+    "fs_vec_subtract": [_vp, _vp, _vp],
+    "fs_vec_multiply": [_vp, _vp, _vp],
+    "fs_vec_divide": [_vp, _vp, _vp],
+    "fs_vec_reciprocal": [_vp, _vp],
+    "fs_vec_linear_sum": [C.c_double, _vp, C.c_double, _vp, _vp],
+    "fs_vec_axpy": [C.c_double, _vp, _vp, _vp],
+    "fs_vec_axpby": [C.c_double, C.c_double, _vp, _vp],
+    "fs_vec_abs": [_vp, _vp],
+    "fs_vec_add_scalar": [_vp, C.c_double, _vp],
+    "fs_vec_set_random": [_vp, C.c_uint64],
+    "fs_vec_dot": [_vp, _vp, _dp],
+    "fs_vec_l1norm": [_vp, _dp],
+    "fs_vec_l2norm": [_vp, _dp],
+    "fs_vec_inf_norm": [_vp, _dp],
+    "fs_vec_min": [_vp, _dp],
+    "fs_vec_max": [_vp, _dp],
+    "fs_csr_create": [_vp, _i64, _i64, _i64, _vp, _vp, C.c_int, _vp, C.POINTER(_vp)],
+    "fs_csr_destroy": [_vp],
+    "fs_csr_shape": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)],
+    "fs_csr_update_values": [_vp, _vp],
+    "fs_csr_update_values_device": [_vp, _vp],
+    "fs_csr_values_device_ptr": [_vp, C.POINTER(_vp)],
+    "fs_csr_spmv": [_vp, _vp, _vp, C.c_int],
+    "fs_csr_residual": [_vp, _vp, _vp, _vp],
+    "fs_csr_spmv_transpose": [_vp, _vp, _vp],
+    "fs_csr_diag_inv": [_vp, _vp],
+    "fs_parcsr_spmv": [_vp, C.c_int, _vp, _vp],
+    "fs_krylov_settings_default": [C.POINTER(KrylovSettings)],
+    "fs_krylov_create": [_vp, C.c_int, C.POINTER(KrylovSettings), _vp,
+                         C.POINTER(Precond), C.POINTER(_vp)],
+    "fs_krylov_destroy": [_vp],
+    "fs_krylov_set_diagnostic": [_vp, DIAG_FN, _vp],
+    "fs_krylov_settings_get": [_vp, C.POINTER(KrylovSettings)],
+    "fs_krylov_settings_set": [_vp, C.POINTER(KrylovSettings)],
+    "fs_krylov_apply": [_vp, _vp, _vp, C.POINTER(SolveInfo)],
+    "fs_krylov_history": [_vp, _dp, C.POINTER(_i64)],
+    "fs_krylov_mixed_stats": [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)],
+}
+
+# entry points that exist in the header but are optional for older builds
+OPTIONAL = set()
+
+
+def header_symbols() -> list[str]:
+    """Every FS_API function declared in include/*.h."""
+    import re
+    names = []
+    inc = _build.INCLUDE
+    for h in sorted(inc.glob("*.h")):
+        txt = h.read_text()
+        names += re.findall(r"FS_API\s+[^;{]*?\b(fs_\w+)\s*\(", txt)
+    return names
+
+
+@lru_cache(maxsize=1)
+def lib(build_if_missing: bool = True) -> C.CDLL:
+    if not LIB_PATH.exists():
+        if not build_if_missing:
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build()")
+        _build.build_gpu()
+    L = C.CDLL(str(LIB_PATH))
+    for name, args in _PROTOS.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.fs_last_error.argtypes = [_vp]
+    L.fs_last_error.restype = C.c_char_p
+    L.fs_status_string.argtypes = [C.c_int]
+    L.fs_status_string.restype = C.c_char_p
+    return L
+
+
+class FsError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def check(status: int, ctx=None, what: str = ""):
+    if status != OK:
+        msg = ""
+        if ctx is not None:
+            raw = lib().fs_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        raise FsError(status, f"{what} {msg}".strip())

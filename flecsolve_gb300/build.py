@@ -1,0 +1,110 @@
+"""In-tree build of the native parts.
+
+* ``_build/libfsproblems.so`` -- the seeded problem generators (plain C, host
+  only, compiled with ``-ffp-contract=off`` so they give the same bits on
+  every host).
+* ``_build/libfsgpu.so`` -- the CUDA kernels, the device solver loops and the
+  C ABI declared in ``include/fsgpu.h``, compiled for sm_103a only.
+* ``oracle/`` -- the CPU checker (``make -C oracle``), and the reference
+  driver when the reference headers are present.
+
+Everything is compiled directly with gcc / nvcc (no cmake), translation units
+in parallel, so a cold build takes about a minute.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+INCLUDE = ROOT / "include"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr",
+              "-I", str(INCLUDE), "-I", str(CSRC)]
+
+CU_SOURCES = ["context.cu", "vecops.cu", "spmv.cu", "krylov.cu", "gmres.cu",
+              "batched.cu", "adjoint.cu"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"),
+                 "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libfsgpu.so")
+
+
+def _run(cmd, cwd=None):
+    r = subprocess.run(cmd, cwd=cwd, stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"command failed ({r.returncode}): {' '.join(map(str, cmd))}\n{r.stdout}")
+    return r.stdout
+
+
+def _stale(out: Path, deps) -> bool:
+    if not out.exists():
+        return True
+    t = out.stat().st_mtime
+    return any(Path(d).stat().st_mtime > t for d in deps)
+
+
+def build_problems(force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    out = BUILD / "libfsproblems.so"
+    src = CSRC / "problems.c"
+    if force or _stale(out, [src]):
+        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off",
+              "-fno-fast-math", "-o", str(out), str(src), "-lm"])
+    return out
+
+
+def build_gpu(force: bool = False, verbose: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    out = BUILD / "libfsgpu.so"
+    headers = list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
+    srcs = [CSRC / s for s in CU_SOURCES if (CSRC / s).exists()]
+    nvcc = _nvcc()
+    objs = []
+
+    def compile_one(src: Path):
+        obj = BUILD / (src.stem + ".o")
+        if force or _stale(obj, [src] + headers):
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+            if verbose:
+                cmd.insert(1, "-Xptxas=-v")
+            log = _run(cmd)
+            if verbose and log:
+                sys.stdout.write(log)
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    if force or _stale(out, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", str(out), *map(str, objs),
+              "-lcudart", "-Xcompiler", "-fPIC"])
+    return out
+
+
+def build_oracle() -> None:
+    _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"])
+
+
+def build_all(force: bool = False, verbose: bool = False) -> None:
+    build_problems(force)
+    build_oracle()
+    build_gpu(force, verbose)
+
+
+if __name__ == "__main__":
+    build_all(force="--force" in sys.argv, verbose="-v" in sys.argv)
+    print("built", BUILD)

@@ -1,0 +1,255 @@
+// Internal declarations shared by the translation units of libfsgpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fsgpu.h"
+
+namespace fsg {
+
+constexpr int kMagicCtx = 0x46534358;  // 'FSCX'
+constexpr int kMagicVec = 0x46535658;  // 'FSVX'
+constexpr int kMagicCsr = 0x46534D58;  // 'FSMX'
+constexpr int kMagicSlv = 0x46535358;  // 'FSSX'
+
+// Reduction scratch: one slot of partials per concurrent reduction.
+constexpr int kRedThreads = 256;
+constexpr int kMaxRedBlocks = 4096;
+
+struct Ctx {
+	int magic = kMagicCtx;
+	int device = 0;
+	int sms = 0;
+	cudaStream_t stream = nullptr;
+	std::string err;
+	int64_t launches = 0;
+	// scratch for generic reductions: partials + result + counter
+	double *red_part = nullptr;     // kMaxRedBlocks * 4 doubles
+	double *red_out = nullptr;      // 8 doubles (device)
+	unsigned *red_count = nullptr;  // completion counters (device)
+	double *host_out = nullptr;     // pinned
+	cudaEvent_t ev[16] = {};        // timing events (fs_ctx_event_*)
+};
+
+struct Vec {
+	int magic = kMagicVec;
+	Ctx *ctx = nullptr;
+	int64_t n = 0;
+	int dtype = FS_F64;
+	void *d = nullptr;
+	bool owns = true;
+	size_t bytes() const { return (size_t)n * (dtype == FS_F64 ? 8 : 4); }
+};
+
+// Row blocks for the staged CSR SpMV: block b covers rows
+// [blk[b], blk[b+1]); a block holds at most kBlkRows rows and kBlkNnz
+// nonzeros unless it is a single row longer than kBlkNnz ("long row").
+constexpr int kBlkRows = 256;
+constexpr int kBlkNnz = 2048;
+
+struct Csr {
+	int magic = kMagicCsr;
+	Ctx *ctx = nullptr;
+	int64_t nrows = 0, ncols = 0, nnz = 0;
+	int *rowptr = nullptr;     // nrows + 1 (int32 offsets; nnz < 2^31)
+	int *col = nullptr;        // nnz (padded to a multiple of 16)
+	double *val = nullptr;     // nnz (padded)
+	float *val32 = nullptr;    // float copy, built on first use
+	bool val32_valid = false;
+	int *blk = nullptr;        // row blocks, nblk + 1
+	int nblk = 0;
+	double *dinv = nullptr;    // 1 / a_ii, built on first use
+	float *dinv32 = nullptr;
+	bool dinv_valid = false;
+	// CSC view (transpose) for A^T x
+	int *t_colptr = nullptr;   // ncols + 1
+	int *t_row = nullptr;      // nnz
+	int *t_perm = nullptr;     // nnz: CSC slot -> CSR slot
+	double *t_val = nullptr;   // nnz
+	int *t_blk = nullptr;
+	int t_nblk = 0;
+	bool t_valid = false;
+	bool t_vals_valid = false;
+	std::vector<int> h_rowptr; // host copy of offsets (parcsr splitting)
+};
+
+// ------------------------------------------------------------ errors --
+
+int set_err(Ctx *ctx, int status, const char *fmt, ...);
+
+#define FS_CUDA_TRY(ctx, call)                                                   \
+	do {                                                                         \
+		cudaError_t _e = (call);                                                 \
+		if (_e != cudaSuccess)                                                   \
+			return ::fsg::set_err((ctx), _e == cudaErrorMemoryAllocation         \
+			                                 ? FS_ERR_OUT_OF_MEMORY               \
+			                                 : FS_ERR_CUDA,                      \
+			                      "%s failed: %s (%s:%d)", #call,                \
+			                      cudaGetErrorString(_e), __FILE__, __LINE__);   \
+	} while (0)
+
+#define FS_TRY(...)                   \
+	do {                              \
+		int _s = (__VA_ARGS__);       \
+		if (_s != FS_OK)              \
+			return _s;                \
+	} while (0)
+
+int check_launch(Ctx *ctx, const char *what);
+
+inline bool ok_ctx(const Ctx *c) { return c && c->magic == kMagicCtx; }
+inline bool ok_vec(const Vec *v) { return v && v->magic == kMagicVec && ok_ctx(v->ctx); }
+inline bool ok_csr(const Csr *a) { return a && a->magic == kMagicCsr && ok_ctx(a->ctx); }
+
+int grid_for(Ctx *ctx, int64_t n, int threads, int per_thread);
+
+// --------------------------------------------- device helper routines --
+
+// Error-free transforms for compensated single-precision sums
+// (Ogita, Rump, Oishi, "Accurate sum and dot product", SISC 2005).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+	s = __fadd_rn(a, b);
+	float bb = __fsub_rn(s, a);
+	e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+	p = __fmul_rn(a, b);
+	e = __fmaf_rn(a, b, -p);
+}
+
+// compensated accumulator: value = hi + lo
+struct cf32 {
+	float hi, lo;
+	__device__ __forceinline__ void add(float v) {
+		float s, e;
+		two_sum(hi, v, s, e);
+		hi = s;
+		lo = __fadd_rn(lo, e);
+	}
+	__device__ __forceinline__ void add_prod(float a, float b) {
+		float p, pe, s, se;
+		two_prod(a, b, p, pe);
+		two_sum(hi, p, s, se);
+		hi = s;
+		lo = __fadd_rn(lo, __fadd_rn(pe, se));
+	}
+	__device__ __forceinline__ void merge(cf32 o) {
+		float s, e;
+		two_sum(hi, o.hi, s, e);
+		hi = s;
+		lo = __fadd_rn(__fadd_rn(lo, o.lo), e);
+	}
+};
+
+// Fixed-order block sum of NV doubles per thread (warp butterfly-free tree:
+// shuffle-down by 16, 8, 4, 2, 1 then warp 0 sums the warp results in warp
+// order).  Result valid in thread 0.  `sh` needs NV * 32 doubles.
+template<int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double *sh) {
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+	for (int k = 0; k < NV; ++k)
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1)
+			v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+	__syncthreads();
+	if (lane == 0)
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			sh[k * 32 + wid] = v[k];
+	__syncthreads();
+	if (wid == 0) {
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			double t = lane < nw ? sh[k * 32 + lane] : 0.0;
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1)
+				t += __shfl_down_sync(0xffffffffu, t, o);
+			v[k] = t;
+		}
+	}
+}
+
+template<int NV>
+__device__ __forceinline__ void block_sum_cf(cf32 (&v)[NV], float *sh) {
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+	for (int k = 0; k < NV; ++k)
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			cf32 t;
+			t.hi = __shfl_down_sync(0xffffffffu, v[k].hi, o);
+			t.lo = __shfl_down_sync(0xffffffffu, v[k].lo, o);
+			v[k].merge(t);
+		}
+	__syncthreads();
+	if (lane == 0)
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			sh[(2 * k) * 32 + wid] = v[k].hi;
+			sh[(2 * k + 1) * 32 + wid] = v[k].lo;
+		}
+	__syncthreads();
+	if (wid == 0) {
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			cf32 t{0.f, 0.f};
+			if (lane < nw) {
+				t.hi = sh[(2 * k) * 32 + lane];
+				t.lo = sh[(2 * k + 1) * 32 + lane];
+			}
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) {
+				cf32 u;
+				u.hi = __shfl_down_sync(0xffffffffu, t.hi, o);
+				u.lo = __shfl_down_sync(0xffffffffu, t.lo, o);
+				t.merge(u);
+			}
+			v[k] = t;
+		}
+	}
+}
+
+// Last-block completion: every block stores its partials, fences, and bumps
+// `counter`; the block that sees count == gridDim.x - 1 is the last one and
+// may read all partials (no block ever waits on another).  Returns true in
+// all threads of the last block; the caller resets the counter there.
+__device__ __forceinline__ bool last_block(unsigned *counter) {
+	__shared__ bool am_last;
+	__threadfence();
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		unsigned prev = atomicAdd(counter, 1u);
+		am_last = (prev == gridDim.x - 1);
+	}
+	__syncthreads();
+	if (am_last)
+		__threadfence();
+	return am_last;
+}
+
+// Fixed-order sum of `n` partials (stride `stride`, component k) by one block:
+// thread t sums t, t + bd, ... in order, then block_sum.  All threads call it.
+template<int NV>
+__device__ __forceinline__ void sum_partials(const double *part, int n,
+                                             double (&out)[NV], double *sh) {
+#pragma unroll
+	for (int k = 0; k < NV; ++k)
+		out[k] = 0.0;
+	for (int i = threadIdx.x; i < n; i += blockDim.x)
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			out[k] += __ldcg(part + (size_t)i * NV + k);
+	block_sum<NV>(out, sh);
+}
+
+}  // namespace fsg

@@ -1,0 +1,1287 @@
+// Device Krylov loops: CG, BiCGSTAB, mixed-precision refined CG, and the
+// solver object / C ABI shared with GMRES (gmres.cu).
+//
+// The loops follow the reference's control flow and scalar recurrences
+// (flecsolve/solvers/cg.hh:43-139, bicgstab.hh:39-187); what changes is where
+// the work runs.  Each reduction the reference performs with a host `.get()`
+// (a FleCSI fold + MPI allreduce, vectors/operations/topo_view.hh:212-274)
+// is fused into the kernel that produces its operands, and the kernel's last
+// block finishes the scalar recurrence (alpha, beta, omega, convergence test)
+// into a device-resident KState.  Nothing in an iteration needs the host, so
+// k iterations are captured into one CUDA graph and the host reads the state
+// back once per graph launch.  After convergence the remaining kernels of a
+// graph return at their first instruction.
+#include <cmath>
+#include <cstring>
+
+#include "solver.cuh"
+
+namespace fsg {
+
+#define FOR_EACH(i, n)                                                          \
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n);  \
+	     i += (int64_t)gridDim.x * blockDim.x)
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ bool stopped(const KState *st) {
+	return st->done || (st->flags & KF_RESTART);
+}
+
+// ------------------------------------------------------ setup kernels --
+
+// bnorm = ||b||, sol0 = ||x|| (when x is given); terminate_tol as cg.hh:55-62
+// (CG/BiCGSTAB: b_norm == 0 -> 1) or gmres.hh:98-106 (b_norm < eps -> 1).
+template<class V>
+__global__ void __launch_bounds__(kThreads)
+k_norms(int64_t n, const V *__restrict__ b, const V *__restrict__ x, KState *st,
+        double *part, unsigned *counter, int gmres_rule) {
+	__shared__ double sh[128];
+	Acc<V, 2> acc;
+	acc.init();
+	FOR_EACH(i, n) {
+		acc.add_prod(0, b[i], b[i]);
+		if (x)
+			acc.add_prod(1, x[i], x[i]);
+	}
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double s[2];
+		sum_partials<2>(part, gridDim.x, s, sh);
+		if (threadIdx.x == 0) {
+			double bn = sqrt(s[0]);
+			if (gmres_rule) {
+				st->rhs_norm = bn;
+				if (bn < 2.220446049250313e-16)
+					bn = 1.0;
+			}
+			else {
+				if (bn == 0.0)
+					bn = 1.0;
+				st->rhs_norm = bn;
+			}
+			st->bnorm = bn;
+			st->tol = st->rtol * bn;
+			st->sol0 = x ? sqrt(s[1]) : 0.0;
+			*counter = 0;
+		}
+	}
+}
+
+template<class V>
+__global__ void k_fill(int64_t n, V *__restrict__ x, V a) {
+	FOR_EACH(i, n) x[i] = a;
+}
+
+template<class V>
+__global__ void k_copy(int64_t n, const V *__restrict__ s, V *__restrict__ d) {
+	FOR_EACH(i, n) d[i] = s[i];
+}
+
+// ---------------------------------------------------------------- CG --
+
+// z = P r (PK 0: identity, 1: diagonal); p = z; rho = z'r; res0 = ||r||
+// (cg.hh:75-90).  Early exit when res0 < tol (cg.hh:77-82).
+template<class V, int PK>
+__global__ void __launch_bounds__(kThreads)
+k_cg_start(int64_t n, const V *__restrict__ r, const V *__restrict__ dinv,
+           V *__restrict__ p, KState *st, double *part, unsigned *counter) {
+	__shared__ double sh[128];
+	Acc<V, 2> acc;
+	acc.init();
+	FOR_EACH(i, n) {
+		V ri = r[i];
+		V zi = PK ? dinv[i] * ri : ri;
+		p[i] = zi;
+		acc.add_prod(0, ri, ri);
+		acc.add_prod(1, zi, ri);
+	}
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double s[2];
+		sum_partials<2>(part, gridDim.x, s, sh);
+		if (threadIdx.x == 0) {
+			double res = sqrt(s[0]);
+			st->res0 = res;
+			st->res = res;
+			st->rho = s[1];
+			st->rho_old = s[1];
+			st->iter = 0;
+			st->flags = 0;
+			if (res < st->tol) {
+				st->done = 1;
+				st->status = FS_CONVERGED_RTOL;
+				st->info_iters = 0;
+			}
+			else if (st->maxiter <= 0) {
+				st->done = 1;
+				st->status = FS_DIVERGED_ITERS;
+			}
+			*counter = 0;
+		}
+	}
+}
+
+// w = A p and p'Ap -> alpha = rho / p'Ap (cg.hh:94-106)
+template<class V>
+struct EpiCgAp {
+	static constexpr int NV = 1;
+	V *w;
+	const V *p;
+	KState *st;
+	double *part;
+	unsigned *counter;
+	__device__ bool skip() const { return stopped(st); }
+	template<class A>
+	__device__ void row(int r, V s, A &acc) const {
+		w[r] = s;
+		acc.add_prod(0, s, p[r]);
+	}
+	__device__ void finish(const double *s) const {
+		double pap = s[0];
+		st->pAp = pap;
+		if (!(pap > 0.0))
+			st->flags |= KF_NEG_CURVATURE;
+		st->alpha = st->rho / pap;
+	}
+};
+
+// x += alpha p; r -= alpha w; z = P r; ||r||, r'z; convergence test and
+// beta = rho_new / rho_old (cg.hh:108-129)
+template<class V, int PK>
+__global__ void __launch_bounds__(kThreads)
+k_cg_update(int64_t n, V *__restrict__ x, const V *__restrict__ p, V *__restrict__ r,
+            const V *__restrict__ w, const V *__restrict__ dinv, KState *st,
+            double *part, unsigned *counter, double *hist) {
+	__shared__ double sh[128];
+	if (stopped(st))
+		return;
+	const V alpha = (V)st->alpha;
+	Acc<V, 2> acc;
+	acc.init();
+	FOR_EACH(i, n) {
+		V xi = fma(alpha, p[i], x[i]);
+		V ri = fma(-alpha, w[i], r[i]);
+		x[i] = xi;
+		r[i] = ri;
+		V zi = PK ? dinv[i] * ri : ri;
+		acc.add_prod(0, ri, ri);
+		acc.add_prod(1, ri, zi);
+	}
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double s[2];
+		sum_partials<2>(part, gridDim.x, s, sh);
+		if (threadIdx.x == 0) {
+			double res = sqrt(s[0]);
+			int it = st->iter + 1;
+			st->iter = it;
+			st->res = res;
+			if (it <= st->hist_cap)
+				hist[it - 1] = res;
+			if (!isfinite(res))
+				st->flags |= KF_NONFINITE;
+			if (res < st->tol) {
+				st->done = 1;
+				st->status = FS_CONVERGED_RTOL;
+				st->info_iters = it;
+			}
+			else if (it >= st->maxiter || (st->flags & KF_NONFINITE)) {
+				st->done = 1;
+				st->status = FS_DIVERGED_ITERS;
+				st->info_iters = 0;
+			}
+			st->rho_old = st->rho;
+			st->rho = s[1];
+			st->beta = s[1] / st->rho_old;
+			*counter = 0;
+		}
+	}
+}
+
+// p = beta p + z, z = P r (cg.hh:124-130)
+template<class V, int PK>
+__global__ void __launch_bounds__(kThreads)
+k_cg_dir(int64_t n, V *__restrict__ p, const V *__restrict__ r,
+         const V *__restrict__ dinv, const KState *st) {
+	if (stopped(st))
+		return;
+	const V beta = (V)st->beta;
+	FOR_EACH(i, n) {
+		V zi = PK ? dinv[i] * r[i] : r[i];
+		p[i] = fma(beta, p[i], zi);
+	}
+}
+
+// -------------------------------------------------------- mixed (IR) --
+
+// x64 += (double) d32 (refinement update)
+__global__ void k_ir_update(int64_t n, double *__restrict__ x, const float *__restrict__ d) {
+	FOR_EACH(i, n) x[i] += (double)d[i];
+}
+
+// r64 = b - A x (FP64), r32 = (float) r64, res = ||r64|| -> outer state
+struct EpiIrResidual {
+	static constexpr int NV = 1;
+	const double *b;
+	double *r64;
+	float *r32;
+	KState *st;
+	double *part;
+	unsigned *counter;
+	__device__ bool skip() const { return false; }
+	template<class A>
+	__device__ void row(int r, double s, A &acc) const {
+		double v = b[r] - s;
+		r64[r] = v;
+		r32[r] = (float)v;
+		acc.add_prod(0, v, v);
+	}
+	__device__ void finish(const double *s) const {
+		st->res = sqrt(s[0]);
+		if (!isfinite(st->res))
+			st->flags |= KF_NONFINITE;
+	}
+};
+
+// inner solve set-up: tol_in = inner_rtol * ||r32||
+__global__ void k_inner_init(KState *in, const KState *out, double inner_rtol, int maxiter) {
+	in->tol = inner_rtol * out->res;
+	in->rtol = inner_rtol;
+	in->maxiter = maxiter;
+	in->done = 0;
+	in->status = FS_STATUS_UNKNOWN;
+	in->iter = 0;
+	in->flags = 0;
+	in->info_iters = 0;
+}
+
+// --------------------------------------------------------- BiCGSTAB --
+
+// res = b (zero guess) or b - A x done before; here: res_norm, r~ = res,
+// p = v = 0, rho = r~'res (bicgstab.hh:73-98)
+template<class V>
+__global__ void __launch_bounds__(kThreads)
+k_bi_start(int64_t n, const V *__restrict__ res, V *__restrict__ rt, V *__restrict__ p,
+           V *__restrict__ v, KState *st, double *part, unsigned *counter) {
+	__shared__ double sh[128];
+	Acc<V, 1> acc;
+	acc.init();
+	FOR_EACH(i, n) {
+		V ri = res[i];
+		rt[i] = ri;
+		p[i] = V(0);
+		v[i] = V(0);
+		acc.add_prod(0, ri, ri);
+	}
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double s[1];
+		sum_partials<1>(part, gridDim.x, s, sh);
+		if (threadIdx.x == 0) {
+			double rn = sqrt(s[0]);
+			st->res0 = rn;
+			st->res = rn;
+			st->r_tilde_norm = rn;
+			st->alpha = 1.0;
+			st->beta = 0.0;
+			st->omega = 1.0;
+			st->rho_old = 2.0;  // std::vector<real> rho{2, 1.0}
+			st->rho = s[0];     // r~'res with r~ = res
+			st->iter = 0;
+			st->flags = 0;
+			if (rn < st->tol) {
+				st->done = 1;
+				st->status = FS_CONVERGED_RTOL;
+			}
+			else if (st->maxiter <= 0) {
+				st->done = 1;
+				st->status = FS_DIVERGED_ITERS;
+			}
+			*counter = 0;
+		}
+	}
+}
+
+// p update (bicgstab.hh:115-122)
+template<class V>
+__global__ void k_bi_p(int64_t n, V *__restrict__ p, const V *__restrict__ v,
+                       const V *__restrict__ res, const KState *st) {
+	if (stopped(st))
+		return;
+	if (st->iter == 0) {
+		FOR_EACH(i, n) p[i] = res[i];
+	}
+	else {
+		const double bd = (st->rho / st->rho_old) * (st->alpha / st->omega);
+		const V beta = (V)bd, om = (V)st->omega;
+		FOR_EACH(i, n) {
+			V t = fma(-om, v[i], p[i]);
+			p[i] = fma(beta, t, res[i]);
+		}
+	}
+}
+
+// v = A P p, alpha = rho / r~'v (bicgstab.hh:124-130)
+template<class V>
+struct EpiBiV {
+	static constexpr int NV = 1;
+	V *v;
+	const V *rt;
+	KState *st;
+	double *part;
+	unsigned *counter;
+	__device__ bool skip() const { return stopped(st); }
+	template<class A>
+	__device__ void row(int r, V s, A &acc) const {
+		v[r] = s;
+		acc.add_prod(0, rt[r], s);
+	}
+	__device__ void finish(const double *s) const {
+		if (!(s[0] != 0.0)) {
+			st->flags |= KF_ALPHA_ZERO;
+			st->done = 1;
+			st->status = FS_DIVERGED_BREAKDOWN;
+			return;
+		}
+		st->alpha = st->rho / s[0];
+	}
+};
+
+// s = res - alpha v, s_norm; early exit when s_norm < rtol (bicgstab.hh:132-143)
+template<class V>
+__global__ void __launch_bounds__(kThreads)
+k_bi_s(int64_t n, V *__restrict__ s, const V *__restrict__ v, const V *__restrict__ res,
+       KState *st, double *part, unsigned *counter) {
+	__shared__ double sh[128];
+	if (stopped(st))
+		return;
+	const V a = (V)st->alpha;
+	Acc<V, 1> acc;
+	acc.init();
+	FOR_EACH(i, n) {
+		V si = fma(-a, v[i], res[i]);
+		s[i] = si;
+		acc.add_prod(0, si, si);
+	}
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double sum[1];
+		sum_partials<1>(part, gridDim.x, sum, sh);
+		if (threadIdx.x == 0) {
+			double sn = sqrt(sum[0]);
+			st->s_norm = sn;
+			if (sn < st->rtol)
+				st->flags |= KF_EARLY;
+			*counter = 0;
+		}
+	}
+}
+
+// t = A P s, t't, t's -> omega (bicgstab.hh:145-151)
+template<class V>
+struct EpiBiT {
+	static constexpr int NV = 2;
+	V *t;
+	const V *s;
+	KState *st;
+	double *part;
+	unsigned *counter;
+	__device__ bool skip() const { return stopped(st) || (st->flags & KF_EARLY); }
+	template<class A>
+	__device__ void row(int r, V val, A &acc) const {
+		t[r] = val;
+		acc.add_prod(0, val, val);
+		acc.add_prod(1, val, s[r]);
+	}
+	__device__ void finish(const double *q) const {
+		st->t_sq = q[0];
+		st->t_s = q[1];
+		st->omega = (q[0] == 0.0) ? 0.0 : q[1] / q[0];
+	}
+};
+
+// x += alpha P p (+ omega P s); res = s - omega t; ||res||, r~'res; tests
+// (bicgstab.hh:136-178, with the next iteration's rho = r~'res fused in)
+template<class V, int PK>
+__global__ void __launch_bounds__(kThreads)
+k_bi_x(int64_t n, V *__restrict__ x, const V *__restrict__ p, const V *__restrict__ s,
+       const V *__restrict__ t, V *__restrict__ res, const V *__restrict__ rt,
+       const V *__restrict__ dinv, KState *st, double *part, unsigned *counter,
+       double *hist) {
+	__shared__ double sh[128];
+	if (stopped(st))
+		return;
+	const V a = (V)st->alpha;
+	if (st->flags & KF_EARLY) {
+		FOR_EACH(i, n) {
+			V ph = PK ? dinv[i] * p[i] : p[i];
+			x[i] = fma(a, ph, x[i]);
+		}
+		// the state changes only once every block has passed its entry test
+		if (last_block(counter) && threadIdx.x == 0) {
+			st->info_iters = st->iter;
+			st->done = 1;
+			st->status = FS_CONVERGED_RTOL;
+			*counter = 0;
+		}
+		return;
+	}
+	const V om = (V)st->omega;
+	Acc<V, 2> acc;
+	acc.init();
+	FOR_EACH(i, n) {
+		V ph = PK ? dinv[i] * p[i] : p[i];
+		V sh_ = PK ? dinv[i] * s[i] : s[i];
+		V xi = fma(a, ph, x[i]);
+		xi = fma(om, sh_, xi);
+		x[i] = xi;
+		V ri = fma(-om, t[i], s[i]);
+		res[i] = ri;
+		acc.add_prod(0, ri, ri);
+		acc.add_prod(1, rt[i], ri);
+	}
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double q[2];
+		sum_partials<2>(part, gridDim.x, q, sh);
+		if (threadIdx.x == 0) {
+			double rn = sqrt(q[0]);
+			int it = st->iter;
+			st->res = rn;
+			const int hi = st->nhist;
+			if (hi < st->hist_cap)
+				hist[hi] = rn;
+			st->nhist = hi + 1;
+			if (!isfinite(rn))
+				st->flags |= KF_NONFINITE;
+			if (rn < st->tol) {
+				st->done = 1;
+				st->status = FS_CONVERGED_RTOL;
+				st->info_iters = it + 1;
+			}
+			else if (st->omega == 0.0) {
+				st->done = 1;
+				st->status = FS_DIVERGED_BREAKDOWN;
+				st->info_iters = it + 1;
+			}
+			st->rho_old = st->rho;
+			st->rho = q[1];
+			st->iter = it + 1;
+			if (!st->done) {
+				if (it + 1 >= st->maxiter || (st->flags & KF_NONFINITE)) {
+					st->done = 1;
+					st->status = FS_DIVERGED_ITERS;
+				}
+				else if (sqrt(fabs(q[1])) < 2.220446049250313e-16 * st->r_tilde_norm) {
+					st->flags |= KF_RESTART;
+				}
+			}
+			*counter = 0;
+		}
+	}
+}
+
+// restart set-up after the host recomputed res = b - A x (bicgstab.hh:106-112):
+// r~ = res, p = res, r_tilde_norm = ||res||, rho = r~'res for the next pass
+template<class V>
+__global__ void __launch_bounds__(kThreads)
+k_bi_restart(int64_t n, const V *__restrict__ res, V *__restrict__ rt, V *__restrict__ p,
+             KState *st, double *part, unsigned *counter) {
+	__shared__ double sh[128];
+	Acc<V, 1> acc;
+	acc.init();
+	FOR_EACH(i, n) {
+		V ri = res[i];
+		rt[i] = ri;
+		p[i] = ri;
+		acc.add_prod(0, ri, ri);
+	}
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double s[1];
+		sum_partials<1>(part, gridDim.x, s, sh);
+		if (threadIdx.x == 0) {
+			double rn = sqrt(s[0]);
+			st->res = rn;
+			st->r_tilde_norm = rn;
+			st->rho = s[0];  // recomputed r~'res of the next iteration
+			st->restarts += 1;
+			st->flags &= ~KF_RESTART;
+			*counter = 0;
+		}
+	}
+}
+
+// ------------------------------------------------------- solver core --
+
+const double *Solver::dinv64() const {
+	if (P.kind == FS_PRECOND_JACOBI)
+		return A->dinv;
+	if (P.kind == FS_PRECOND_DIAG)
+		return (const double *)w64[10];
+	return nullptr;
+}
+const float *Solver::dinv32() const {
+	if (P.kind == FS_PRECOND_JACOBI)
+		return A->dinv32;
+	if (P.kind == FS_PRECOND_DIAG)
+		return w32[10];
+	return nullptr;
+}
+
+static int dalloc(Solver *s, void **p, size_t bytes) {
+	cudaError_t e = cudaMalloc(p, bytes);
+	if (e != cudaSuccess) {
+		cudaGetLastError();
+		return set_err(s->ctx, FS_ERR_OUT_OF_MEMORY, "solver work allocation of %zu bytes failed",
+		               bytes);
+	}
+	s->bufs.push_back(*p);
+	return cudaMemsetAsync(*p, 0, bytes, s->ctx->stream) == cudaSuccess ? FS_OK : FS_ERR_CUDA;
+}
+
+int solver_alloc(Solver *s) {
+	if (s->st)
+		return FS_OK;
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	const size_t n64 = (size_t)((n + 31) / 32 * 32 + 32) * 8;
+	const size_t n32 = (size_t)((n + 31) / 32 * 32 + 32) * 4;
+	int nw64 = 0, nw32 = 0;
+	switch (s->method) {
+	case FS_CG: nw64 = 3; break;
+	case FS_BICGSTAB: nw64 = 6; break;
+	case FS_GMRES: nw64 = 3; break;
+	case FS_CG_MIXED: nw64 = 1; nw32 = 5; break;
+	}
+	for (int i = 0; i < nw64; ++i)
+		FS_TRY(dalloc(s, (void **)&s->w64[i], n64));
+	for (int i = 0; i < nw32; ++i)
+		FS_TRY(dalloc(s, (void **)&s->w32[i], n32));
+	FS_TRY(dalloc(s, (void **)&s->st, sizeof(KState)));
+	FS_TRY(dalloc(s, (void **)&s->st_in, sizeof(KState)));
+	FS_TRY(dalloc(s, (void **)&s->part, sizeof(double) * (size_t)ctx->sms * 8 * 4 + 1024));
+	FS_TRY(dalloc(s, (void **)&s->counter, 64));
+	FS_TRY(dalloc(s, (void **)&s->hdev, sizeof(double) * 4096));
+	cudaError_t e = cudaMallocHost(&s->hst, sizeof(KState));
+	if (e != cudaSuccess)
+		return set_err(ctx, FS_ERR_OUT_OF_MEMORY, "pinned state allocation failed");
+	memset(s->hst, 0, sizeof(KState));
+	if (s->P.kind == FS_PRECOND_DIAG) {
+		// keep an FP64 and an FP32 copy of the caller's diagonal
+		FS_TRY(dalloc(s, (void **)&s->w64[10], n64));
+		FS_TRY(dalloc(s, (void **)&s->w32[10], n32));
+	}
+	if (s->P.kind == FS_PRECOND_JACOBI)
+		FS_TRY(ensure_dinv(s->A));
+	if (s->method == FS_CG_MIXED || s->method == FS_GMRES)
+		FS_TRY(ensure_val32(s->A));
+	return FS_OK;
+}
+
+static int ensure_hist(Solver *s, int cap) {
+	if (cap <= s->hist_cap && s->hist)
+		return FS_OK;
+	if (s->hist)
+		cudaFree(s->hist);
+	s->hist = nullptr;
+	FS_CUDA_TRY(s->ctx, cudaMalloc(&s->hist, sizeof(double) * (size_t)(cap + 1)));
+	s->hist_cap = cap;
+	return FS_OK;
+}
+
+int read_state(Solver *s) {
+	FS_CUDA_TRY(s->ctx, cudaMemcpyAsync(s->hst, s->st, sizeof(KState), cudaMemcpyDeviceToHost,
+	                                    s->ctx->stream));
+	FS_CUDA_TRY(s->ctx, cudaStreamSynchronize(s->ctx->stream));
+	return FS_OK;
+}
+
+// Capture `body` (k iterations) once per key, then replay it.
+int graph_run(Solver *s, const GraphKey &key, int (*body)(Solver *, void *), void *arg) {
+	Ctx *ctx = s->ctx;
+	auto it = s->graphs.find(key);
+	if (it == s->graphs.end()) {
+		int64_t before = ctx->launches;
+		FS_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+		int st = body(s, arg);
+		cudaGraph_t g = nullptr;
+		cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+		int nodes = (int)(ctx->launches - before);
+		ctx->launches = before;
+		if (st != FS_OK) {
+			if (g)
+				cudaGraphDestroy(g);
+			return st;
+		}
+		if (e != cudaSuccess)
+			return set_err(ctx, FS_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+		cudaGraphExec_t ge = nullptr;
+		e = cudaGraphInstantiate(&ge, g, 0);
+		cudaGraphDestroy(g);
+		if (e != cudaSuccess)
+			return set_err(ctx, FS_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+		it = s->graphs.emplace(key, std::make_pair(ge, nodes)).first;
+	}
+	FS_CUDA_TRY(ctx, cudaGraphLaunch(it->second.first, ctx->stream));
+	ctx->launches += it->second.second;
+	return FS_OK;
+}
+
+static void clear_graphs(Solver *s) {
+	for (auto &kv : s->graphs)
+		cudaGraphExecDestroy(kv.second.first);
+	s->graphs.clear();
+}
+
+// Common loop driver: launch the captured k-iteration body until the device
+// says done; call the user diagnostic for every new history entry.
+struct LoopSpec {
+	Vec *x;
+	GraphKey key;
+	int (*body)(Solver *, void *);
+	void *arg;
+	int (*on_restart)(Solver *, void *);  // BiCGSTAB restart handler
+};
+
+static int run_loop(Solver *s, const LoopSpec &L, int *user_stop) {
+	*user_stop = 0;
+	int64_t seen = 0;
+	for (;;) {
+		FS_TRY(graph_run(s, L.key, L.body, L.arg));
+		FS_TRY(read_state(s));
+		KState &h = *s->hst;
+		int64_t nh = s->method == FS_BICGSTAB ? (int64_t)h.nhist : h.iter;
+		if (s->diag && nh > seen) {
+			int64_t upto = std::min<int64_t>(nh, s->hist_cap);
+			std::vector<double> hh(upto - seen > 0 ? upto - seen : 0);
+			if (!hh.empty())
+				FS_CUDA_TRY(s->ctx, cudaMemcpy(hh.data(), s->hist + seen, hh.size() * sizeof(double),
+				                               cudaMemcpyDeviceToHost));
+			for (size_t j = 0; j < hh.size(); ++j) {
+				if (s->diag(s->diag_user, reinterpret_cast<fs_vec>(L.x), hh[j])) {
+					*user_stop = (int)(seen + j + 1);
+					return FS_OK;
+				}
+			}
+			seen = nh;
+		}
+		else {
+			seen = nh;
+		}
+		if (h.done)
+			return FS_OK;
+		if ((h.flags & KF_RESTART) && L.on_restart)
+			FS_TRY(L.on_restart(s, L.arg));
+	}
+}
+
+// ---------------------------------------------------- CG apply (FP64) --
+
+struct CgArgs {
+	Vec *b, *x;
+	int k;
+};
+
+template<int PK>
+static int cg_body64(Solver *s, void *a) {
+	CgArgs *g = (CgArgs *)a;
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	double *r = s->w64[0], *p = s->w64[1], *w = s->w64[2];
+	double *x = (double *)g->x->d;
+	const double *dinv = s->dinv64();
+	const int G = red_grid(ctx, n);
+	for (int k = 0; k < g->k; ++k) {
+		FS_TRY(launch_spmv<double, false, false>(
+			ctx, s->A, s->A->val, p, nullptr,
+			EpiCgAp<double>{w, p, s->st, s->part, s->counter}));
+		k_cg_update<double, PK><<<G, kThreads, 0, ctx->stream>>>(n, x, p, r, w, dinv, s->st, s->part,
+		                                                        s->counter, s->hist);
+		FS_TRY(check_launch(ctx, "cg update"));
+		k_cg_dir<double, PK><<<G, kThreads, 0, ctx->stream>>>(n, p, r, dinv, s->st);
+		FS_TRY(check_launch(ctx, "cg direction"));
+	}
+	return FS_OK;
+}
+
+template<int PK>
+static int cg_body32(Solver *s, void *a) {
+	CgArgs *g = (CgArgs *)a;
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	float *r = s->w32[0], *p = s->w32[1], *w = s->w32[2], *x = s->w32[3];
+	const float *dinv = s->dinv32();
+	const int G = red_grid(ctx, n);
+	for (int k = 0; k < g->k; ++k) {
+		FS_TRY(launch_spmv<float, false, false>(
+			ctx, s->A, s->A->val32, p, nullptr,
+			EpiCgAp<float>{w, p, s->st_in, s->part, s->counter}));
+		k_cg_update<float, PK><<<G, kThreads, 0, ctx->stream>>>(n, x, p, r, w, dinv, s->st_in,
+		                                                       s->part, s->counter, s->hist);
+		FS_TRY(check_launch(ctx, "cg update f32"));
+		k_cg_dir<float, PK><<<G, kThreads, 0, ctx->stream>>>(n, p, r, dinv, s->st_in);
+		FS_TRY(check_launch(ctx, "cg direction f32"));
+	}
+	return FS_OK;
+}
+
+static int init_state(Solver *s, KState *dst, double rtol, int maxiter) {
+	KState h{};
+	h.rtol = rtol;
+	h.maxiter = maxiter;
+	h.status = FS_STATUS_UNKNOWN;
+	h.hist_cap = s->hist_cap;
+	FS_CUDA_TRY(s->ctx, cudaMemcpyAsync(dst, &h, sizeof(KState), cudaMemcpyHostToDevice, s->ctx->stream));
+	// the pageable source is consumed before the call returns
+	return FS_OK;
+}
+
+static int norms(Solver *s, Vec *b, Vec *x, bool with_x, int gmres_rule) {
+	Ctx *ctx = s->ctx;
+	const int G = red_grid(ctx, s->n);
+	k_norms<double><<<G, kThreads, 0, ctx->stream>>>(s->n, (const double *)b->d,
+	                                                 with_x ? (const double *)x->d : nullptr,
+	                                                 s->st, s->part, s->counter, gmres_rule);
+	return check_launch(ctx, "norms");
+}
+
+static int sol_norm(Solver *s, Vec *x, double *out) {
+	return fs_vec_l2norm(reinterpret_cast<fs_vec>(x), out);
+}
+
+static int k_default(const Solver *s) {
+	int k = s->set.k_readback;
+	if (k <= 0)
+		k = 32;
+	if (s->diag)
+		k = 1;
+	return k;
+}
+
+static int cg_apply64(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	const int G = red_grid(ctx, n);
+	const bool zg = s->set.base.use_zero_guess != 0;
+	const int PK = s->dinv64() ? 1 : 0;
+	double *r = s->w64[0], *p = s->w64[1];
+	FS_TRY(ensure_hist(s, std::max(1, s->set.base.maxiter)));
+	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, s->set.base.maxiter));
+	FS_TRY(norms(s, b, x, !zg, 0));
+	if (zg) {
+		k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
+		FS_TRY(check_launch(ctx, "fill"));
+		k_copy<double><<<G, kThreads, 0, ctx->stream>>>(n, (const double *)b->d, r);
+		FS_TRY(check_launch(ctx, "copy"));
+	}
+	else {
+		FS_TRY(launch_spmv<double, false, false>(ctx, s->A, s->A->val, (const double *)x->d, nullptr,
+		                                         EpiResidual<double>{(const double *)b->d, r}));
+	}
+	if (PK)
+		k_cg_start<double, 1><<<G, kThreads, 0, ctx->stream>>>(n, r, s->dinv64(), p, s->st, s->part, s->counter);
+	else
+		k_cg_start<double, 0><<<G, kThreads, 0, ctx->stream>>>(n, r, nullptr, p, s->st, s->part, s->counter);
+	FS_TRY(check_launch(ctx, "cg start"));
+	FS_TRY(read_state(s));
+	int user_stop = 0;
+	if (!s->hst->done) {
+		CgArgs args{b, x, k_default(s)};
+		LoopSpec L{x, {b->d, x->d, args.k * 2 + PK}, PK ? cg_body64<1> : cg_body64<0>, &args, nullptr};
+		FS_TRY(run_loop(s, L, &user_stop));
+	}
+	KState &h = *s->hst;
+	s->hhist_count = std::min<int64_t>(h.iter, s->hist_cap);
+	double xn = 0;
+	FS_TRY(sol_norm(s, x, &xn));
+	memset(info, 0, sizeof(*info));
+	info->rhs_norm = (float)h.rhs_norm;
+	info->sol_norm_initial = zg ? 0.f : (float)h.sol0;
+	info->res_norm_initial = (float)h.res0;
+	info->sol_norm_final = (float)xn;
+	info->res_norm_final = (float)h.res;
+	if (user_stop) {
+		info->status = FS_CONVERGED_USER;
+		info->iters = user_stop;
+	}
+	else {
+		info->status = h.status;
+		info->iters = h.info_iters;
+		if (h.iter > 0 && info->iters == 0)
+			info->status = FS_DIVERGED_ITERS;  // cg.hh:135-136
+	}
+	if (h.flags & KF_NONFINITE)
+		return set_err(ctx, FS_ERR_NON_FINITE, "CG: non-finite residual norm");
+	return FS_OK;
+}
+
+// ------------------------------------------- mixed precision refined CG --
+
+// Classic iterative refinement: the residual, the update and the stopping
+// test are FP64 (r = b - A x with the FP64 values), each correction
+// A d = r is solved by FP32 Jacobi-PCG (FP32 values and vectors,
+// compensated dots) to inner_rtol, and x += d in FP64.
+static int cg_apply_mixed(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	const int G = red_grid(ctx, n);
+	const bool zg = s->set.base.use_zero_guess != 0;
+	const int PK = s->dinv32() ? 1 : 0;
+	double *r64 = s->w64[0];
+	float *r32 = s->w32[0], *p32 = s->w32[1], *d32 = s->w32[3];
+	const int maxiter = s->set.base.maxiter;
+	FS_TRY(ensure_hist(s, std::max(1, maxiter)));
+	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, maxiter));
+	FS_TRY(norms(s, b, x, !zg, 0));
+	if (zg) {
+		k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
+		FS_TRY(check_launch(ctx, "fill"));
+	}
+	auto residual = [&]() -> int {
+		return launch_spmv<double, false, false>(
+			ctx, s->A, s->A->val, (const double *)x->d, nullptr,
+			EpiIrResidual{(const double *)b->d, r64, r32, s->st, s->part, s->counter});
+	};
+	FS_TRY(residual());
+	FS_TRY(read_state(s));
+	const double tol = s->hst->tol;
+	const double res0 = s->hst->res;
+	double res = res0;
+	int total = 0, outer = 0;
+	int status = FS_DIVERGED_ITERS;
+	const double inner_rtol = s->set.inner_rtol > 0 ? s->set.inner_rtol : 1e-4;
+	const int max_outer = s->set.max_outer > 0 ? s->set.max_outer : 64;
+	const int k = k_default(s) > 1 ? k_default(s) : 32;
+	std::vector<double> host_hist;
+	while (true) {
+		if (res < tol) {
+			status = FS_CONVERGED_RTOL;
+			break;
+		}
+		if (total >= maxiter || outer >= max_outer || !std::isfinite(res))
+			break;
+		// inner FP32 PCG on A d = r32, d0 = 0
+		k_inner_init<<<1, 1, 0, ctx->stream>>>(s->st_in, s->st, inner_rtol, maxiter - total);
+		FS_TRY(check_launch(ctx, "inner init"));
+		k_fill<float><<<G, kThreads, 0, ctx->stream>>>(n, d32, 0.f);
+		FS_TRY(check_launch(ctx, "fill"));
+		if (PK)
+			k_cg_start<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, r32, s->dinv32(), p32, s->st_in, s->part, s->counter);
+		else
+			k_cg_start<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, p32, s->st_in, s->part, s->counter);
+		FS_TRY(check_launch(ctx, "inner start"));
+		// the inner tolerance refers to ||r32||: k_cg_start sets res0 only
+		CgArgs args{b, x, k};
+		GraphKey key{b->d, x->d, 1000 + k * 2 + PK};
+		int inner_iters = 0;
+		for (int prev = -1;;) {
+			FS_CUDA_TRY(ctx, cudaMemcpyAsync(s->hst, s->st_in, sizeof(KState), cudaMemcpyDeviceToHost, ctx->stream));
+			FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+			if (s->hst->done || s->hst->iter == prev)
+				break;
+			prev = s->hst->iter;
+			FS_TRY(graph_run(s, key, PK ? cg_body32<1> : cg_body32<0>, &args));
+		}
+		inner_iters = s->hst->iter;
+		if (inner_iters == 0 && !s->hst->done)
+			break;
+		total += inner_iters;
+		outer += 1;
+		k_ir_update<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, d32);
+		FS_TRY(check_launch(ctx, "refinement update"));
+		FS_TRY(residual());
+		FS_TRY(read_state(s));
+		res = s->hst->res;
+		host_hist.push_back(res);
+		if (s->diag && s->diag(s->diag_user, reinterpret_cast<fs_vec>(x), res)) {
+			status = FS_CONVERGED_USER;
+			break;
+		}
+		if (inner_iters == 0)
+			break;
+	}
+	s->mixed_outer = outer;
+	s->mixed_inner = total;
+	// history: outer residuals (FP64) after each refinement step
+	s->hhist.assign(host_hist.begin(), host_hist.end());
+	s->hhist_count = -1;
+	double xn = 0;
+	FS_TRY(sol_norm(s, x, &xn));
+	memset(info, 0, sizeof(*info));
+	FS_TRY(read_state(s));
+	info->rhs_norm = (float)s->hst->rhs_norm;
+	info->sol_norm_initial = zg ? 0.f : (float)s->hst->sol0;
+	info->res_norm_initial = (float)res0;
+	info->res_norm_final = (float)res;
+	info->sol_norm_final = (float)xn;
+	info->status = status;
+	info->iters = status == FS_DIVERGED_ITERS ? 0 : total;
+	info->restarts = outer;
+	if (!std::isfinite(res))
+		return set_err(ctx, FS_ERR_NON_FINITE, "mixed CG: non-finite residual norm");
+	return FS_OK;
+}
+
+// ------------------------------------------------------ BiCGSTAB apply --
+
+struct BiArgs {
+	Vec *b, *x;
+	int k;
+};
+
+template<int PK>
+static int bi_body64(Solver *s, void *a) {
+	BiArgs *g = (BiArgs *)a;
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	double *res = s->w64[0], *rt = s->w64[1], *p = s->w64[2], *v = s->w64[3],
+	       *sv = s->w64[4], *t = s->w64[5];
+	double *x = (double *)g->x->d;
+	const double *dinv = s->dinv64();
+	const int G = red_grid(ctx, n);
+	for (int k = 0; k < g->k; ++k) {
+		k_bi_p<double><<<G, kThreads, 0, ctx->stream>>>(n, p, v, res, s->st);
+		FS_TRY(check_launch(ctx, "bicgstab p"));
+		if (PK)
+			FS_TRY((launch_spmv<double, false, true>(ctx, s->A, s->A->val, p, dinv,
+			                                         EpiBiV<double>{v, rt, s->st, s->part, s->counter})));
+		else
+			FS_TRY((launch_spmv<double, false, false>(ctx, s->A, s->A->val, p, nullptr,
+			                                          EpiBiV<double>{v, rt, s->st, s->part, s->counter})));
+		k_bi_s<double><<<G, kThreads, 0, ctx->stream>>>(n, sv, v, res, s->st, s->part, s->counter);
+		FS_TRY(check_launch(ctx, "bicgstab s"));
+		if (PK)
+			FS_TRY((launch_spmv<double, false, true>(ctx, s->A, s->A->val, sv, dinv,
+			                                         EpiBiT<double>{t, sv, s->st, s->part, s->counter})));
+		else
+			FS_TRY((launch_spmv<double, false, false>(ctx, s->A, s->A->val, sv, nullptr,
+			                                          EpiBiT<double>{t, sv, s->st, s->part, s->counter})));
+		k_bi_x<double, PK><<<G, kThreads, 0, ctx->stream>>>(n, x, p, sv, t, res, rt, dinv, s->st,
+		                                                   s->part, s->counter, s->hist);
+		FS_TRY(check_launch(ctx, "bicgstab x"));
+	}
+	return FS_OK;
+}
+
+static int bi_restart(Solver *s, void *a) {
+	BiArgs *g = (BiArgs *)a;
+	Ctx *ctx = s->ctx;
+	double *res = s->w64[0], *rt = s->w64[1], *p = s->w64[2];
+	FS_TRY(launch_spmv<double, false, false>(ctx, s->A, s->A->val, (const double *)g->x->d, nullptr,
+	                                         EpiResidual<double>{(const double *)g->b->d, res}));
+	k_bi_restart<double><<<red_grid(ctx, s->n), kThreads, 0, ctx->stream>>>(s->n, res, rt, p, s->st,
+	                                                                       s->part, s->counter);
+	return check_launch(ctx, "bicgstab restart");
+}
+
+static int bicgstab_apply64(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	const int G = red_grid(ctx, n);
+	const bool zg = s->set.base.use_zero_guess != 0;
+	const int PK = s->dinv64() ? 1 : 0;
+	double *res = s->w64[0], *rt = s->w64[1], *p = s->w64[2], *v = s->w64[3];
+	FS_TRY(ensure_hist(s, std::max(1, s->set.base.maxiter)));
+	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, s->set.base.maxiter));
+	FS_TRY(norms(s, b, x, !zg, 0));
+	if (zg) {
+		k_copy<double><<<G, kThreads, 0, ctx->stream>>>(n, (const double *)b->d, res);
+		FS_TRY(check_launch(ctx, "copy"));
+		k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
+		FS_TRY(check_launch(ctx, "fill"));
+	}
+	else {
+		FS_TRY(launch_spmv<double, false, false>(ctx, s->A, s->A->val, (const double *)x->d, nullptr,
+		                                         EpiResidual<double>{(const double *)b->d, res}));
+	}
+	k_bi_start<double><<<G, kThreads, 0, ctx->stream>>>(n, res, rt, p, v, s->st, s->part, s->counter);
+	FS_TRY(check_launch(ctx, "bicgstab start"));
+	FS_TRY(read_state(s));
+	int user_stop = 0;
+	if (!s->hst->done) {
+		BiArgs args{b, x, k_default(s)};
+		LoopSpec L{x, {b->d, x->d, 100 + args.k * 2 + PK}, PK ? bi_body64<1> : bi_body64<0>, &args,
+		           bi_restart};
+		FS_TRY(run_loop(s, L, &user_stop));
+	}
+	KState &h = *s->hst;
+	s->hhist_count = std::min<int64_t>((int64_t)h.nhist, s->hist_cap);
+	double xn = 0;
+	FS_TRY(sol_norm(s, x, &xn));
+	memset(info, 0, sizeof(*info));
+	info->rhs_norm = (float)h.rhs_norm;
+	info->sol_norm_initial = zg ? 0.f : (float)h.sol0;
+	info->res_norm_initial = (float)h.res0;
+	info->sol_norm_final = (float)xn;
+	info->res_norm_final = (float)h.res;
+	info->restarts = h.restarts;
+	if (user_stop) {
+		info->status = FS_CONVERGED_USER;
+		info->iters = user_stop;
+	}
+	else {
+		info->status = h.status;
+		info->iters = h.info_iters;
+		if (h.res0 >= h.tol && info->iters == 0)
+			info->status = FS_DIVERGED_ITERS;  // bicgstab.hh:183-184
+	}
+	if (h.flags & KF_ALPHA_ZERO)
+		return set_err(ctx, FS_ERR_BREAKDOWN, "BiCGSTAB: encountered alpha = 0 (bicgstab.hh:129)");
+	if (h.flags & KF_NONFINITE)
+		return set_err(ctx, FS_ERR_NON_FINITE, "BiCGSTAB: non-finite residual norm");
+	return FS_OK;
+}
+
+int gmres_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info);
+
+}  // namespace fsg
+
+using namespace fsg;
+
+// ================================================================ C ABI ==
+
+extern "C" {
+
+FS_API int fs_krylov_settings_default(fs_krylov_settings *s) {
+	if (!s)
+		return FS_ERR_INVALID_ARG;
+	memset(s, 0, sizeof(*s));
+	s->base.maxiter = 1000;
+	s->base.rtol = 0.f;
+	s->base.atol = 0.f;
+	s->base.use_zero_guess = 1;
+	s->max_krylov_dim = -1;
+	s->pre_side = FS_RIGHT;
+	s->restart = 0;
+	s->ortho = FS_ORTHO_CGS2;
+	s->k_readback = 0;
+	s->refine = FS_REFINE_RESTART;
+	s->inner_rtol = 1e-4;
+	s->max_outer = 64;
+	return FS_OK;
+}
+
+FS_API int fs_krylov_create(fs_ctx h, int method, const fs_krylov_settings *set, fs_csr Ah,
+                            const fs_precond *P, fs_solver *out) {
+	Ctx *ctx = reinterpret_cast<Ctx *>(h);
+	Csr *A = reinterpret_cast<Csr *>(Ah);
+	if (!ok_ctx(ctx) || !ok_csr(A) || !out || !set)
+		return FS_ERR_BAD_HANDLE;
+	*out = nullptr;
+	if (method < FS_CG || method > FS_CG_MIXED)
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_krylov_create: unknown method %d", method);
+	if (A->nrows != A->ncols)
+		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_krylov_create: operator must be square");
+	Solver *s = new Solver();
+	s->ctx = ctx;
+	s->method = method;
+	s->set = *set;
+	s->A = A;
+	s->n = A->nrows;
+	if (P) {
+		s->P.kind = P->kind;
+		if (P->kind == FS_PRECOND_DIAG) {
+			Vec *d = reinterpret_cast<Vec *>(P->diag);
+			if (!ok_vec(d) || d->n != A->nrows) {
+				delete s;
+				return set_err(ctx, FS_ERR_BAD_HANDLE, "fs_krylov_create: bad diagonal preconditioner");
+			}
+			s->P.diag = d;
+		}
+		else if (P->kind == FS_PRECOND_CSR) {
+			// a CSR preconditioner is accepted when it is diagonal (the D^-1
+			// operator of util/test/mesh.hh:123-140) and turned into a vector
+			Csr *M = reinterpret_cast<Csr *>(P->op);
+			if (!ok_csr(M) || M->nrows != A->nrows) {
+				delete s;
+				return set_err(ctx, FS_ERR_BAD_HANDLE, "fs_krylov_create: bad CSR preconditioner");
+			}
+			std::vector<int> hc(M->nnz);
+			if (M->nnz)
+				cudaMemcpy(hc.data(), M->col, M->nnz * sizeof(int), cudaMemcpyDeviceToHost);
+			bool diagonal = true;
+			for (int64_t i = 0; i < M->nrows && diagonal; ++i)
+				for (int k = M->h_rowptr[i]; k < M->h_rowptr[i + 1]; ++k)
+					if (hc[k] != i)
+						diagonal = false;
+			if (!diagonal) {
+				delete s;
+				return set_err(ctx, FS_ERR_UNSUPPORTED,
+				               "fs_krylov_create: only diagonal CSR preconditioners are supported");
+			}
+			s->P.kind = FS_PRECOND_CSR;
+			s->P.op = M;
+		}
+		else if (P->kind != FS_PRECOND_NONE && P->kind != FS_PRECOND_JACOBI) {
+			delete s;
+			return set_err(ctx, FS_ERR_INVALID_ARG, "fs_krylov_create: unknown preconditioner kind");
+		}
+	}
+	if (method == FS_GMRES) {
+		int m = set->max_krylov_dim < 0 ? set->base.maxiter : set->max_krylov_dim;
+		if (m > 100 || (!set->restart && set->base.maxiter > m)) {
+			delete s;
+			return set_err(ctx, FS_ERR_BREAKDOWN,
+			               "GMRES settings fail the reference's validate() (gmres.hh:394-404)");
+		}
+	}
+	int st = solver_alloc(s);
+	if (st == FS_OK && (s->P.kind == FS_PRECOND_DIAG || s->P.kind == FS_PRECOND_CSR)) {
+		// copy the diagonal into the solver (FP64 + FP32)
+		if (s->P.kind == FS_PRECOND_CSR) {
+			Csr *M = s->P.op;
+			// diagonal entries in row order: the values array itself, with
+			// zeros where a row has no entry
+			std::vector<double> hv(M->nnz), dv(s->n, 0.0);
+			if (M->nnz)
+				cudaMemcpy(hv.data(), M->val, M->nnz * sizeof(double), cudaMemcpyDeviceToHost);
+			for (int64_t i = 0; i < s->n; ++i)
+				for (int k = M->h_rowptr[i]; k < M->h_rowptr[i + 1]; ++k)
+					dv[i] = hv[k];
+			if (s->n)
+				cudaMemcpy(s->w64[10], dv.data(), s->n * sizeof(double), cudaMemcpyHostToDevice);
+			s->P.kind = FS_PRECOND_DIAG;
+		}
+		else {
+			Vec *d = s->P.diag;
+			if (d->dtype == FS_F64)
+				cudaMemcpyAsync(s->w64[10], d->d, s->n * 8, cudaMemcpyDeviceToDevice, ctx->stream);
+			else {
+				std::vector<float> hf(s->n);
+				std::vector<double> hd(s->n);
+				cudaMemcpy(hf.data(), d->d, s->n * 4, cudaMemcpyDeviceToHost);
+				for (int64_t i = 0; i < s->n; ++i)
+					hd[i] = hf[i];
+				cudaMemcpy(s->w64[10], hd.data(), s->n * 8, cudaMemcpyHostToDevice);
+			}
+		}
+		std::vector<double> hd(s->n);
+		std::vector<float> hf(s->n);
+		cudaStreamSynchronize(ctx->stream);
+		if (s->n)
+			cudaMemcpy(hd.data(), s->w64[10], s->n * 8, cudaMemcpyDeviceToHost);
+		for (int64_t i = 0; i < s->n; ++i)
+			hf[i] = (float)hd[i];
+		if (s->n)
+			cudaMemcpy(s->w32[10], hf.data(), s->n * 4, cudaMemcpyHostToDevice);
+		if (cudaGetLastError() != cudaSuccess)
+			st = set_err(ctx, FS_ERR_CUDA, "fs_krylov_create: preconditioner copy failed");
+	}
+	if (st != FS_OK) {
+		for (void *p : s->bufs)
+			cudaFree(p);
+		if (s->hst)
+			cudaFreeHost(s->hst);
+		delete s;
+		return st;
+	}
+	*out = reinterpret_cast<fs_solver>(s);
+	return FS_OK;
+}
+
+FS_API int fs_krylov_destroy(fs_solver h) {
+	Solver *s = reinterpret_cast<Solver *>(h);
+	if (!ok_slv(s))
+		return FS_ERR_BAD_HANDLE;
+	cudaStreamSynchronize(s->ctx->stream);
+	clear_graphs(s);
+	for (void *p : s->bufs)
+		cudaFree(p);
+	if (s->basis)
+		cudaFree(s->basis);
+	if (s->hist)
+		cudaFree(s->hist);
+	if (s->hst)
+		cudaFreeHost(s->hst);
+	s->magic = 0;
+	delete s;
+	return FS_OK;
+}
+
+FS_API int fs_krylov_set_diagnostic(fs_solver h, fs_diag_fn fn, void *user) {
+	Solver *s = reinterpret_cast<Solver *>(h);
+	if (!ok_slv(s))
+		return FS_ERR_BAD_HANDLE;
+	s->diag = fn;
+	s->diag_user = user;
+	return FS_OK;
+}
+
+FS_API int fs_krylov_settings_get(fs_solver h, fs_krylov_settings *out) {
+	Solver *s = reinterpret_cast<Solver *>(h);
+	if (!ok_slv(s) || !out)
+		return FS_ERR_BAD_HANDLE;
+	*out = s->set;
+	return FS_OK;
+}
+
+FS_API int fs_krylov_settings_set(fs_solver h, const fs_krylov_settings *in) {
+	Solver *s = reinterpret_cast<Solver *>(h);
+	if (!ok_slv(s) || !in)
+		return FS_ERR_BAD_HANDLE;
+	if (s->method == FS_GMRES) {
+		int m = in->max_krylov_dim < 0 ? in->base.maxiter : in->max_krylov_dim;
+		if (m > 100 || (!in->restart && in->base.maxiter > m))
+			return set_err(s->ctx, FS_ERR_BREAKDOWN,
+			               "GMRES settings fail the reference's validate() (gmres.hh:394-404)");
+	}
+	cudaStreamSynchronize(s->ctx->stream);
+	clear_graphs(s);
+	s->set = *in;
+	return FS_OK;
+}
+
+FS_API int fs_krylov_apply(fs_solver h, fs_vec bh, fs_vec xh, fs_solve_info *info) {
+	Solver *s = reinterpret_cast<Solver *>(h);
+	Vec *b = reinterpret_cast<Vec *>(bh), *x = reinterpret_cast<Vec *>(xh);
+	if (!ok_slv(s) || !ok_vec(b) || !ok_vec(x) || !info)
+		return FS_ERR_BAD_HANDLE;
+	Ctx *ctx = s->ctx;
+	if (b->n != s->n || x->n != s->n)
+		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_krylov_apply: vector size %lld/%lld != %lld",
+		               (long long)b->n, (long long)x->n, (long long)s->n);
+	if (b->dtype != FS_F64 || x->dtype != FS_F64)
+		return set_err(ctx, FS_ERR_UNSUPPORTED, "fs_krylov_apply: b and x must be FP64");
+	if (b == x)
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_krylov_apply: b and x must differ");
+	cudaSetDevice(ctx->device);
+	s->mixed_outer = s->mixed_inner = 0;
+	switch (s->method) {
+	case FS_CG: return cg_apply64(s, b, x, info);
+	case FS_BICGSTAB: return bicgstab_apply64(s, b, x, info);
+	case FS_GMRES: return gmres_apply(s, b, x, info);
+	case FS_CG_MIXED: return cg_apply_mixed(s, b, x, info);
+	}
+	return FS_ERR_INVALID_ARG;
+}
+
+FS_API int fs_krylov_history(fs_solver h, double *hist, int64_t *n) {
+	Solver *s = reinterpret_cast<Solver *>(h);
+	if (!ok_slv(s) || !n)
+		return FS_ERR_BAD_HANDLE;
+	if (s->hhist_count < 0) {
+		int64_t m = std::min<int64_t>(*n, (int64_t)s->hhist.size());
+		if (hist && m > 0)
+			memcpy(hist, s->hhist.data(), m * sizeof(double));
+		*n = m;
+		return FS_OK;
+	}
+	int64_t m = std::min<int64_t>(*n, s->hhist_count);
+	if (hist && m > 0)
+		FS_CUDA_TRY(s->ctx, cudaMemcpy(hist, s->hist, m * sizeof(double), cudaMemcpyDeviceToHost));
+	*n = m;
+	return FS_OK;
+}
+
+FS_API int fs_krylov_mixed_stats(fs_solver h, int *outer, int *inner) {
+	Solver *s = reinterpret_cast<Solver *>(h);
+	if (!ok_slv(s))
+		return FS_ERR_BAD_HANDLE;
+	if (outer) *outer = s->mixed_outer;
+	if (inner) *inner = s->mixed_inner;
+	return FS_OK;
+}
+
+}  // extern "C"

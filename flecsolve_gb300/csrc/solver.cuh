@@ -1,0 +1,106 @@
+// Bound Krylov solver object shared by krylov.cu and gmres.cu.
+//
+// One fs_solver is the device counterpart of an op::core<op::cg<params>>
+// (flecsolve/solvers/krylov_parameters.hh:94-126): settings, work vectors,
+// operator, preconditioner and diagnostic, plus the device-resident scalar
+// state of the running solve and the CUDA graphs of its iteration body.
+#pragma once
+
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "spmv_kernel.cuh"
+
+namespace fsg {
+
+// flags
+constexpr int KF_NEG_CURVATURE = 1;   // CG: p'Ap <= 0 (cg.hh:101-104 logs it)
+constexpr int KF_ALPHA_ZERO = 2;      // BiCGSTAB: r~'v == 0 (bicgstab.hh:129)
+constexpr int KF_RESTART = 4;         // BiCGSTAB: restart requested (bicgstab.hh:103)
+constexpr int KF_EARLY = 8;           // BiCGSTAB: ||s|| < rtol early exit (bicgstab.hh:136)
+constexpr int KF_NONFINITE = 16;      // a reduction produced NaN/Inf
+
+// Device-resident scalars of one solve.  Written only by the last block of a
+// reduction kernel (thread 0); read by every kernel that follows.
+struct KState {
+	double bnorm, tol, rtol;          // rhs norm (after the zero fix-up), terminate_tol
+	double rhs_norm;                  // info.rhs_norm as the reference reports it
+	double sol0, res0;                // initial solution / residual norms
+	double res;                       // current residual norm
+	double rho, rho_old, alpha, beta, omega, pAp;
+	double r_tilde_norm, s_norm, t_sq, t_s;
+	double aux[4];
+	int iter;                         // iterations completed (loop counter)
+	int done;                         // nonzero: stop
+	int status;                       // fs_stop_reason
+	int info_iters;                   // info.iters as the reference sets it
+	int flags;
+	int maxiter;
+	int restarts;
+	int hist_cap;
+	int nhist;                        // history entries written
+	int pad_;
+};
+
+struct Precond {
+	int kind = FS_PRECOND_NONE;
+	Vec *diag = nullptr;
+	Csr *op = nullptr;
+};
+
+struct GraphKey {
+	const void *b, *x;
+	int k;
+	bool operator<(const GraphKey &o) const {
+		return std::tie(b, x, k) < std::tie(o.b, o.x, o.k);
+	}
+};
+
+struct Solver {
+	int magic = kMagicSlv;
+	Ctx *ctx = nullptr;
+	int method = FS_CG;
+	fs_krylov_settings set{};
+	Csr *A = nullptr;
+	Precond P;
+	fs_diag_fn diag = nullptr;
+	void *diag_user = nullptr;
+
+	int64_t n = 0;
+	// work storage (FP64 and FP32 blocks, allocated on first apply)
+	std::vector<void *> bufs;
+	double *w64[12] = {};
+	float *w32[12] = {};
+	double *basis = nullptr;          // GMRES: (m + 1) x n, column j contiguous
+	double *hdev = nullptr;           // GMRES: dot results scratch
+	KState *st = nullptr;             // device
+	KState *hst = nullptr;            // pinned mirror
+	KState *st_in = nullptr;          // device state of an inner solve
+	double *hist = nullptr;           // device, residual norm per iteration
+	int hist_cap = 0;
+	double *part = nullptr;           // reduction partials
+	unsigned *counter = nullptr;
+	std::map<GraphKey, std::pair<cudaGraphExec_t, int>> graphs;
+	std::vector<double> hhist;        // host copy of the last history
+	int64_t hhist_count = 0;
+	int mixed_outer = 0, mixed_inner = 0;
+	int graph_nodes_launched = 0;
+
+	const double *dinv64() const;
+	const float *dinv32() const;
+};
+
+inline bool ok_slv(const Solver *s) { return s && s->magic == kMagicSlv && ok_ctx(s->ctx); }
+
+// largest grid of the elementwise/reduction kernels of a solver
+inline int red_grid(Ctx *ctx, int64_t n) { return grid_for(ctx, n, 256, 8); }
+
+// shared helpers (krylov.cu)
+int solver_alloc(Solver *s);
+int graph_run(Solver *s, const GraphKey &key, int (*body)(Solver *, void *), void *arg);
+int read_state(Solver *s);
+int ensure_val32(Csr *A);
+int ensure_dinv(Csr *A);
+
+}  // namespace fsg

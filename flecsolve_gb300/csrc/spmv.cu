@@ -1,0 +1,455 @@
+// Device CSR operator: creation, row-block binning, SpMV, residual, D^-1,
+// the row-block distributed (parcsr) SpMV and the CSC transpose view.
+//
+// Reference: mat::sparse / mat::compressed_ops (flecsolve/matrices/seq.hh:
+// 35-63, 177-193), op::core::residual (operators/core.hh:129-142), the D^-1
+// test operator (flecsolve/util/test/mesh.hh:123-140) and mat::parcsr
+// (matrices/parcsr.hh:60-91, topo/csr.hh:413-632).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "spmv_kernel.cuh"
+
+namespace fsg {
+
+int spmv_grid(Ctx *ctx, int nblk) {
+	int cap = ctx->sms * 6;
+	return std::max(1, std::min(nblk, cap));
+}
+
+// Row blocks of at most kBlkRows rows / kBlkNnz nonzeros; a row longer than
+// kBlkNnz is a block of its own.
+static std::vector<int> row_blocks(const std::vector<int> &rp) {
+	const int n = (int)rp.size() - 1;
+	std::vector<int> blk;
+	blk.reserve(n / 64 + 2);
+	blk.push_back(0);
+	int r = 0;
+	while (r < n) {
+		const int start = r;
+		if (rp[r + 1] - rp[r] > kBlkNnz) {
+			r += 1;
+		}
+		else {
+			const int base = rp[r];
+			while (r < n && r - start < kBlkRows && rp[r + 1] - base <= kBlkNnz)
+				++r;
+		}
+		blk.push_back(r);
+	}
+	return blk;
+}
+
+__global__ void to_f32_kernel(int64_t n, const double *__restrict__ a, float *__restrict__ b) {
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+	     i += (int64_t)gridDim.x * blockDim.x)
+		b[i] = (float)a[i];
+}
+
+// dinv_i = 1 / a_ii (0 when the row has no diagonal entry, as the reference's
+// D^-1 builder leaves such a value unset -> zero-initialised)
+__global__ void dinv_kernel(int n, const int *__restrict__ rp, const int *__restrict__ col,
+                            const double *__restrict__ val, double *__restrict__ d,
+                            float *__restrict__ d32) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		double v = 0.0;
+		for (int k = rp[i]; k < rp[i + 1]; ++k)
+			if (col[k] == i)
+				v = 1.0 / val[k];
+		d[i] = v;
+		d32[i] = (float)v;
+	}
+}
+
+int ensure_val32(Csr *A) {
+	if (A->val32_valid)
+		return FS_OK;
+	Ctx *ctx = A->ctx;
+	if (!A->val32) {
+		size_t padded = (size_t)((A->nnz + 15) / 16 * 16 + 16);
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->val32, padded * sizeof(float)));
+		FS_CUDA_TRY(ctx, cudaMemsetAsync(A->val32, 0, padded * sizeof(float), ctx->stream));
+	}
+	if (A->nnz > 0) {
+		to_f32_kernel<<<grid_for(ctx, A->nnz, 256, 8), 256, 0, ctx->stream>>>(A->nnz, A->val, A->val32);
+		FS_TRY(check_launch(ctx, "to_f32"));
+	}
+	A->val32_valid = true;
+	return FS_OK;
+}
+
+int ensure_dinv(Csr *A) {
+	if (A->dinv_valid)
+		return FS_OK;
+	Ctx *ctx = A->ctx;
+	if (!A->dinv) {
+		size_t padded = (size_t)((A->nrows + 31) / 32 * 32 + 32);
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->dinv, padded * sizeof(double)));
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->dinv32, padded * sizeof(float)));
+		FS_CUDA_TRY(ctx, cudaMemsetAsync(A->dinv, 0, padded * sizeof(double), ctx->stream));
+		FS_CUDA_TRY(ctx, cudaMemsetAsync(A->dinv32, 0, padded * sizeof(float), ctx->stream));
+	}
+	if (A->nrows > 0) {
+		dinv_kernel<<<grid_for(ctx, A->nrows, 256, 4), 256, 0, ctx->stream>>>(
+			(int)A->nrows, A->rowptr, A->col, A->val, A->dinv, A->dinv32);
+		FS_TRY(check_launch(ctx, "dinv"));
+	}
+	A->dinv_valid = true;
+	return FS_OK;
+}
+
+static void invalidate_values(Csr *A) {
+	A->val32_valid = false;
+	A->dinv_valid = false;
+	A->t_vals_valid = false;
+}
+
+// ------------------------------------------------------ parcsr split --
+
+// y_i = (sum over owned columns) + (sum over ghost columns), each summed in
+// CSR order, row blocks [floor(N c / P), floor(N (c+1) / P)).
+template<bool EXACT>
+__global__ void parcsr_kernel(int n, int parts, const int *__restrict__ rp,
+                              const int *__restrict__ col, const double *__restrict__ val,
+                              const double *__restrict__ x, double *__restrict__ y) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		// colour of row i: the largest c with floor(n c / P) <= i
+		long long c = ((long long)i * parts + parts - 1) / n;
+		while (c > 0 && ((long long)n * c) / parts > i)
+			--c;
+		while (c + 1 < parts && ((long long)n * (c + 1)) / parts <= i)
+			++c;
+		const int lo = (int)(((long long)n * c) / parts);
+		const int hi = (int)(((long long)n * (c + 1)) / parts);
+		double yd = 0.0, yo = 0.0;
+		for (int k = rp[i]; k < rp[i + 1]; ++k) {
+			const int j = col[k];
+			if (EXACT) {
+				double p = val[k] * x[j];
+				if (j >= lo && j < hi)
+					yd = yd + p;
+				else
+					yo = yo + p;
+			}
+			else {
+				if (j >= lo && j < hi)
+					yd = fma(val[k], x[j], yd);
+				else
+					yo = fma(val[k], x[j], yo);
+			}
+		}
+		y[i] = yd + yo;
+	}
+}
+
+// ------------------------------------------------- transpose (CSC) view --
+
+// counting sort of the CSR entries by column, stable in row order, built on
+// the host once per pattern; values gathered through the permutation
+__global__ void gather_kernel(int64_t n, const int *__restrict__ perm,
+                              const double *__restrict__ src, double *__restrict__ dst) {
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+	     i += (int64_t)gridDim.x * blockDim.x)
+		dst[i] = src[perm[i]];
+}
+
+int ensure_transpose(Csr *A) {
+	Ctx *ctx = A->ctx;
+	if (!A->t_valid) {
+		const int64_t n = A->nrows, m = A->ncols, nnz = A->nnz;
+		std::vector<int> hcol(nnz);
+		FS_CUDA_TRY(ctx, cudaMemcpy(hcol.data(), A->col, nnz * sizeof(int), cudaMemcpyDeviceToHost));
+		std::vector<int> cp(m + 1, 0), trow(nnz), perm(nnz);
+		for (int64_t k = 0; k < nnz; ++k)
+			cp[hcol[k] + 1]++;
+		for (int64_t j = 0; j < m; ++j)
+			cp[j + 1] += cp[j];
+		std::vector<int> fill(cp.begin(), cp.end() - 1);
+		for (int64_t i = 0; i < n; ++i)
+			for (int k = A->h_rowptr[i]; k < A->h_rowptr[i + 1]; ++k) {
+				int slot = fill[hcol[k]]++;
+				trow[slot] = (int)i;
+				perm[slot] = k;
+			}
+		std::vector<int> tb = row_blocks(cp);
+		size_t padded = (size_t)((nnz + 15) / 16 * 16 + 16);
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_colptr, (m + 1) * sizeof(int)));
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_row, padded * sizeof(int)));
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_perm, padded * sizeof(int)));
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_val, padded * sizeof(double)));
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_blk, tb.size() * sizeof(int)));
+		FS_CUDA_TRY(ctx, cudaMemset(A->t_row, 0, padded * sizeof(int)));
+		FS_CUDA_TRY(ctx, cudaMemset(A->t_val, 0, padded * sizeof(double)));
+		FS_CUDA_TRY(ctx, cudaMemcpy(A->t_colptr, cp.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
+		FS_CUDA_TRY(ctx, cudaMemcpy(A->t_row, trow.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
+		FS_CUDA_TRY(ctx, cudaMemcpy(A->t_perm, perm.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
+		FS_CUDA_TRY(ctx, cudaMemcpy(A->t_blk, tb.data(), tb.size() * sizeof(int), cudaMemcpyHostToDevice));
+		A->t_nblk = (int)tb.size() - 1;
+		A->t_valid = true;
+		A->t_vals_valid = false;
+	}
+	if (!A->t_vals_valid) {
+		if (A->nnz > 0) {
+			gather_kernel<<<grid_for(ctx, A->nnz, 256, 8), 256, 0, ctx->stream>>>(
+				A->nnz, A->t_perm, A->val, A->t_val);
+			FS_TRY(check_launch(ctx, "csc gather"));
+		}
+		A->t_vals_valid = true;
+	}
+	return FS_OK;
+}
+
+int transpose_spmv(Csr *A, const double *x, double *y) {
+	FS_TRY(ensure_transpose(A));
+	Csr T;  // a view sharing the CSC arrays
+	T.ctx = A->ctx;
+	T.nrows = A->ncols;
+	T.ncols = A->nrows;
+	T.nnz = A->nnz;
+	T.rowptr = A->t_colptr;
+	T.col = A->t_row;
+	T.val = A->t_val;
+	T.blk = A->t_blk;
+	T.nblk = A->t_nblk;
+	int st = launch_spmv<double, false, false>(A->ctx, &T, A->t_val, x, nullptr,
+	                                           EpiStore<double>{y});
+	T.magic = 0;
+	T.rowptr = nullptr;
+	T.col = nullptr;
+	T.val = nullptr;
+	T.blk = nullptr;
+	return st;
+}
+
+}  // namespace fsg
+
+using namespace fsg;
+
+extern "C" {
+
+FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
+                         const int64_t *rowptr, const void *col, int index_bytes,
+                         const double *val, fs_csr *out) {
+	Ctx *ctx = reinterpret_cast<Ctx *>(h);
+	if (!ok_ctx(ctx) || !out)
+		return FS_ERR_BAD_HANDLE;
+	*out = nullptr;
+	if (nrows < 0 || ncols < 0 || nnz < 0 || !rowptr || (nnz > 0 && (!col || !val)))
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_create: bad arguments");
+	if (index_bytes != 4 && index_bytes != 8)
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_create: index_bytes must be 4 or 8");
+	if (nnz >= (int64_t)1 << 31 || nrows >= (int64_t)1 << 31 || ncols >= (int64_t)1 << 31)
+		return set_err(ctx, FS_ERR_UNSUPPORTED,
+		               "fs_csr_create: this build stores 32-bit offsets (nnz, rows < 2^31)");
+	if (rowptr[0] != 0 || rowptr[nrows] != nnz)
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_create: rowptr[0] must be 0 and rowptr[n] = nnz");
+	std::vector<int> rp(nrows + 1);
+	for (int64_t i = 0; i <= nrows; ++i) {
+		if (i > 0 && rowptr[i] < rowptr[i - 1])
+			return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_create: rowptr not monotone at %lld", (long long)i);
+		rp[i] = (int)rowptr[i];
+	}
+	size_t padded = (size_t)((nnz + 15) / 16 * 16 + 16);
+	std::vector<int> ci(padded, 0);
+	for (int64_t k = 0; k < nnz; ++k) {
+		int64_t c = index_bytes == 4 ? (int64_t)((const int32_t *)col)[k] : ((const int64_t *)col)[k];
+		if (c < 0 || c >= ncols)
+			return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_create: column %lld out of range at %lld",
+			               (long long)c, (long long)k);
+		ci[k] = (int)c;
+	}
+	std::vector<int> blk = row_blocks(rp);
+
+	Csr *A = new Csr();
+	A->ctx = ctx;
+	A->nrows = nrows;
+	A->ncols = ncols;
+	A->nnz = nnz;
+	A->nblk = (int)blk.size() - 1;
+	A->h_rowptr = rp;
+	auto fail = [&](int st) {
+		cudaFree(A->rowptr);
+		cudaFree(A->col);
+		cudaFree(A->val);
+		cudaFree(A->blk);
+		delete A;
+		cudaGetLastError();
+		return set_err(ctx, st, "fs_csr_create: device allocation or copy failed");
+	};
+	if (cudaMalloc(&A->rowptr, (nrows + 1) * sizeof(int)) != cudaSuccess ||
+	    cudaMalloc(&A->col, padded * sizeof(int)) != cudaSuccess ||
+	    cudaMalloc(&A->val, padded * sizeof(double)) != cudaSuccess ||
+	    cudaMalloc(&A->blk, blk.size() * sizeof(int)) != cudaSuccess)
+		return fail(FS_ERR_OUT_OF_MEMORY);
+	if (cudaMemcpy(A->rowptr, rp.data(), (nrows + 1) * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemcpy(A->col, ci.data(), padded * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemset(A->val, 0, padded * sizeof(double)) != cudaSuccess ||
+	    (nnz > 0 && cudaMemcpy(A->val, val, nnz * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) ||
+	    cudaMemcpy(A->blk, blk.data(), blk.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+		return fail(FS_ERR_CUDA);
+	*out = reinterpret_cast<fs_csr>(A);
+	return FS_OK;
+}
+
+FS_API int fs_csr_destroy(fs_csr h) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	if (!ok_csr(A))
+		return FS_ERR_BAD_HANDLE;
+	cudaStreamSynchronize(A->ctx->stream);
+	for (void *p : {(void *)A->rowptr, (void *)A->col, (void *)A->val, (void *)A->val32,
+	                (void *)A->blk, (void *)A->dinv, (void *)A->dinv32, (void *)A->t_colptr,
+	                (void *)A->t_row, (void *)A->t_perm, (void *)A->t_val, (void *)A->t_blk})
+		if (p)
+			cudaFree(p);
+	A->magic = 0;
+	delete A;
+	return FS_OK;
+}
+
+FS_API int fs_csr_shape(fs_csr h, int64_t *nrows, int64_t *ncols, int64_t *nnz) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	if (!ok_csr(A))
+		return FS_ERR_BAD_HANDLE;
+	if (nrows) *nrows = A->nrows;
+	if (ncols) *ncols = A->ncols;
+	if (nnz) *nnz = A->nnz;
+	return FS_OK;
+}
+
+FS_API int fs_csr_update_values(fs_csr h, const double *val) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	if (!ok_csr(A))
+		return FS_ERR_BAD_HANDLE;
+	if (A->nnz > 0 && !val)
+		return FS_ERR_INVALID_ARG;
+	if (A->nnz > 0)
+		FS_CUDA_TRY(A->ctx, cudaMemcpyAsync(A->val, val, A->nnz * sizeof(double),
+		                                    cudaMemcpyHostToDevice, A->ctx->stream));
+	FS_CUDA_TRY(A->ctx, cudaStreamSynchronize(A->ctx->stream));
+	invalidate_values(A);
+	return FS_OK;
+}
+
+FS_API int fs_csr_update_values_device(fs_csr h, const double *dval) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	if (!ok_csr(A))
+		return FS_ERR_BAD_HANDLE;
+	if (A->nnz > 0 && !dval)
+		return FS_ERR_INVALID_ARG;
+	if (A->nnz > 0 && dval != A->val)
+		FS_CUDA_TRY(A->ctx, cudaMemcpyAsync(A->val, dval, A->nnz * sizeof(double),
+		                                    cudaMemcpyDeviceToDevice, A->ctx->stream));
+	invalidate_values(A);
+	return FS_OK;
+}
+
+FS_API int fs_csr_values_device_ptr(fs_csr h, double **dval) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	if (!ok_csr(A) || !dval)
+		return FS_ERR_BAD_HANDLE;
+	*dval = A->val;
+	// the caller may write through the pointer: derived data is rebuilt
+	invalidate_values(A);
+	return FS_OK;
+}
+
+FS_API int fs_csr_spmv(fs_csr h, fs_vec xh, fs_vec yh, int mode) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	Vec *x = reinterpret_cast<Vec *>(xh), *y = reinterpret_cast<Vec *>(yh);
+	if (!ok_csr(A) || !ok_vec(x) || !ok_vec(y))
+		return FS_ERR_BAD_HANDLE;
+	Ctx *ctx = A->ctx;
+	if (x->n != A->ncols || y->n != A->nrows || x->dtype != y->dtype)
+		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_csr_spmv: shapes/dtypes do not match");
+	if (x == y)
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_spmv: x and y must differ");
+	if (mode != FS_SPMV_FMA && mode != FS_SPMV_EXACT)
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_spmv: bad mode");
+	if (A->nrows == 0)
+		return FS_OK;
+	if (x->dtype == FS_F64) {
+		EpiStore<double> e{(double *)y->d};
+		if (mode == FS_SPMV_EXACT)
+			return launch_spmv<double, true, false>(ctx, A, A->val, (const double *)x->d, nullptr, e);
+		return launch_spmv<double, false, false>(ctx, A, A->val, (const double *)x->d, nullptr, e);
+	}
+	FS_TRY(ensure_val32(A));
+	EpiStore<float> e{(float *)y->d};
+	if (mode == FS_SPMV_EXACT)
+		return launch_spmv<float, true, false>(ctx, A, A->val32, (const float *)x->d, nullptr, e);
+	return launch_spmv<float, false, false>(ctx, A, A->val32, (const float *)x->d, nullptr, e);
+}
+
+FS_API int fs_csr_residual(fs_csr h, fs_vec bh, fs_vec xh, fs_vec rh) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	Vec *b = reinterpret_cast<Vec *>(bh), *x = reinterpret_cast<Vec *>(xh),
+	    *r = reinterpret_cast<Vec *>(rh);
+	if (!ok_csr(A) || !ok_vec(b) || !ok_vec(x) || !ok_vec(r))
+		return FS_ERR_BAD_HANDLE;
+	Ctx *ctx = A->ctx;
+	if (x->n != A->ncols || r->n != A->nrows || b->n != A->nrows ||
+	    x->dtype != r->dtype || b->dtype != r->dtype)
+		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_csr_residual: shapes/dtypes do not match");
+	if (x == r)
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_residual: x and r must differ");
+	if (A->nrows == 0)
+		return FS_OK;
+	if (x->dtype == FS_F64)
+		return launch_spmv<double, false, false>(
+			ctx, A, A->val, (const double *)x->d, nullptr,
+			EpiResidual<double>{(const double *)b->d, (double *)r->d});
+	FS_TRY(ensure_val32(A));
+	return launch_spmv<float, false, false>(
+		ctx, A, A->val32, (const float *)x->d, nullptr,
+		EpiResidual<float>{(const float *)b->d, (float *)r->d});
+}
+
+FS_API int fs_csr_diag_inv(fs_csr h, fs_vec dh) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	Vec *d = reinterpret_cast<Vec *>(dh);
+	if (!ok_csr(A) || !ok_vec(d))
+		return FS_ERR_BAD_HANDLE;
+	if (d->n != A->nrows)
+		return set_err(A->ctx, FS_ERR_SIZE_MISMATCH, "fs_csr_diag_inv: size mismatch");
+	FS_TRY(ensure_dinv(A));
+	if (A->nrows == 0)
+		return FS_OK;
+	FS_CUDA_TRY(A->ctx, cudaMemcpyAsync(d->d, d->dtype == FS_F64 ? (void *)A->dinv : (void *)A->dinv32,
+	                                    d->bytes(), cudaMemcpyDeviceToDevice, A->ctx->stream));
+	return FS_OK;
+}
+
+FS_API int fs_parcsr_spmv(fs_csr h, int parts, fs_vec xh, fs_vec yh) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	Vec *x = reinterpret_cast<Vec *>(xh), *y = reinterpret_cast<Vec *>(yh);
+	if (!ok_csr(A) || !ok_vec(x) || !ok_vec(y))
+		return FS_ERR_BAD_HANDLE;
+	Ctx *ctx = A->ctx;
+	if (parts < 1 || parts > A->nrows)
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_parcsr_spmv: parts must be in [1, nrows]");
+	if (x->n != A->ncols || y->n != A->nrows || x->dtype != FS_F64 || y->dtype != FS_F64 ||
+	    A->nrows != A->ncols)
+		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_parcsr_spmv: square FP64 operator and vectors required");
+	if (x == y)
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_parcsr_spmv: x and y must differ");
+	parcsr_kernel<true><<<grid_for(ctx, A->nrows, 256, 1), 256, 0, ctx->stream>>>(
+		(int)A->nrows, parts, A->rowptr, A->col, A->val, (const double *)x->d, (double *)y->d);
+	return check_launch(ctx, "parcsr spmv");
+}
+
+FS_API int fs_csr_spmv_transpose(fs_csr h, fs_vec xh, fs_vec yh) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	Vec *x = reinterpret_cast<Vec *>(xh), *y = reinterpret_cast<Vec *>(yh);
+	if (!ok_csr(A) || !ok_vec(x) || !ok_vec(y))
+		return FS_ERR_BAD_HANDLE;
+	if (x->n != A->nrows || y->n != A->ncols || x->dtype != FS_F64 || y->dtype != FS_F64)
+		return set_err(A->ctx, FS_ERR_SIZE_MISMATCH, "fs_csr_spmv_transpose: FP64 vectors of A^T shape required");
+	if (x == y)
+		return set_err(A->ctx, FS_ERR_INVALID_ARG, "fs_csr_spmv_transpose: x and y must differ");
+	if (A->ncols == 0)
+		return FS_OK;
+	return transpose_spmv(A, (const double *)x->d, (double *)y->d);
+}
+
+}  // extern "C"

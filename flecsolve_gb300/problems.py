@@ -1,0 +1,202 @@
+"""Seeded synthetic problems (thin ctypes layer over ``libfsproblems.so``).
+
+The generators themselves are in ``csrc/problems.c``; this module only
+allocates numpy arrays and names the workloads:
+
+* ``poisson2d(n)``            5-point Laplacian, diagonal 4, off-diagonals -1
+* ``diffusion(dim, n, ...)``  variable-coefficient finite-volume diffusion
+                              with log-normal cells and harmonic faces
+* ``convdiff3d(n, ...)``      7-point upwind convection-diffusion
+* ``uniform(seed, n)``        right-hand sides U[-1, 1]
+
+A problem is a :class:`CSR` with int64 row offsets, int32 column ids and
+float64 values (the reference's ``mat::csr<double>`` holds ``std::size_t``
+indices, flecsolve/matrices/seq.hh:257-261; the C ABI accepts either width).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from functools import lru_cache
+
+import numpy as np
+
+from . import build as _build
+
+_i64 = C.c_int64
+_dp = C.POINTER(C.c_double)
+_i64p = C.POINTER(C.c_int64)
+_i32p = C.POINTER(C.c_int32)
+
+
+@lru_cache(maxsize=1)
+def lib() -> C.CDLL:
+    path = _build.build_problems()
+    L = C.CDLL(str(path))
+    L.fsp_grid_rows.restype = _i64
+    L.fsp_grid_rows.argtypes = [C.c_int, _i64]
+    L.fsp_grid_nnz.restype = _i64
+    L.fsp_grid_nnz.argtypes = [C.c_int, _i64]
+    L.fsp_grid_faces.restype = _i64
+    L.fsp_grid_faces.argtypes = [C.c_int, _i64]
+    L.fsp_uniform.argtypes = [C.c_uint64, _i64, C.c_double, C.c_double, _dp]
+    L.fsp_normal.argtypes = [C.c_uint64, _i64, C.c_double, C.c_double, _dp]
+    L.fsp_randint.argtypes = [C.c_uint64, _i64, _i64, _i64, _i64p]
+    L.fsp_faces_const.argtypes = [C.c_int, _i64, C.c_double, _dp]
+    L.fsp_faces_lognormal.argtypes = [C.c_int, _i64, C.c_double, C.c_double,
+                                      C.c_uint64, _dp, _dp]
+    L.fsp_assemble_diffusion.argtypes = [C.c_int, _i64, _dp, _i64p, _i32p, _dp]
+    L.fsp_assemble_convdiff3d.argtypes = [_i64, C.c_double, C.c_uint64, _i64p,
+                                          _i32p, _dp, _dp]
+    L.fsp_exp_.restype = C.c_double
+    L.fsp_exp_.argtypes = [C.c_double]
+    L.fsp_log_.restype = C.c_double
+    L.fsp_log_.argtypes = [C.c_double]
+    return L
+
+
+def _p(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+@dataclass
+class CSR:
+    """Host CSR matrix: int64 ``rowptr``, int32 ``col``, float64 ``val``."""
+    nrows: int
+    ncols: int
+    rowptr: np.ndarray
+    col: np.ndarray
+    val: np.ndarray
+    name: str = ""
+
+    @property
+    def nnz(self) -> int:
+        return int(self.rowptr[-1])
+
+    def diagonal(self) -> np.ndarray:
+        d = np.zeros(self.nrows)
+        rows = np.repeat(np.arange(self.nrows), np.diff(self.rowptr))
+        m = self.col == rows
+        d[rows[m]] = self.val[m]
+        return d
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.val, self.col, self.rowptr),
+                             shape=(self.nrows, self.ncols))
+
+
+def uniform(seed: int, n: int, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
+    out = np.empty(n)
+    lib().fsp_uniform(seed, n, lo, hi, _p(out, _dp))
+    return out
+
+
+def normal(seed: int, n: int, mu: float = 0.0, sigma: float = 1.0) -> np.ndarray:
+    out = np.empty(n)
+    lib().fsp_normal(seed, n, mu, sigma, _p(out, _dp))
+    return out
+
+
+def randint(seed: int, n: int, lo: int, hi: int) -> np.ndarray:
+    out = np.empty(n, dtype=np.int64)
+    lib().fsp_randint(seed, n, lo, hi, _p(out, _i64p))
+    return out
+
+
+def grid_faces(dim: int, n: int) -> int:
+    return int(lib().fsp_grid_faces(dim, n))
+
+
+def faces_const(dim: int, n: int, c: float = 1.0) -> np.ndarray:
+    f = np.empty(grid_faces(dim, n))
+    lib().fsp_faces_const(dim, n, c, _p(f, _dp))
+    return f
+
+
+def faces_lognormal(dim: int, n: int, seed: int, sigma: float = 1.0,
+                    mu: float = 0.0, return_cells: bool = False):
+    f = np.empty(grid_faces(dim, n))
+    cells = np.empty(int(lib().fsp_grid_rows(dim, n)))
+    lib().fsp_faces_lognormal(dim, n, mu, sigma, seed, _p(f, _dp), _p(cells, _dp))
+    return (f, cells) if return_cells else f
+
+
+def assemble_diffusion(dim: int, n: int, faces: np.ndarray, name: str = "") -> CSR:
+    L = lib()
+    N = int(L.fsp_grid_rows(dim, n))
+    nnz = int(L.fsp_grid_nnz(dim, n))
+    faces = np.ascontiguousarray(faces, dtype=np.float64)
+    assert faces.size == grid_faces(dim, n)
+    rp = np.empty(N + 1, dtype=np.int64)
+    col = np.empty(nnz, dtype=np.int32)
+    val = np.empty(nnz)
+    L.fsp_assemble_diffusion(dim, n, _p(faces, _dp), _p(rp, _i64p),
+                             _p(col, _i32p), _p(val, _dp))
+    return CSR(N, N, rp, col, val, name)
+
+
+def poisson2d(n: int) -> CSR:
+    """5-point Laplacian on an n x n interior grid (diag 4, off -1)."""
+    return assemble_diffusion(2, n, faces_const(2, n, 1.0), f"poisson2d-{n}")
+
+
+def laplace3d(n: int) -> CSR:
+    """7-point Laplacian on an n^3 grid (diag 6, off -1)."""
+    return assemble_diffusion(3, n, faces_const(3, n, 1.0), f"laplace3d-{n}")
+
+
+def diffusion(dim: int, n: int, seed: int, sigma: float = 1.0) -> CSR:
+    """Log-normal variable-coefficient diffusion with harmonic face averages."""
+    return assemble_diffusion(dim, n, faces_lognormal(dim, n, seed, sigma),
+                              f"diffusion{dim}d-{n}-s{seed}")
+
+
+def convdiff3d(n: int, seed: int = 4, pe_max: float = 5.0,
+               return_velocity: bool = False):
+    """Upwind convection-diffusion with a seeded solenoidal vortex."""
+    L = lib()
+    N = n ** 3
+    nnz = int(L.fsp_grid_nnz(3, n))
+    rp = np.empty(N + 1, dtype=np.int64)
+    col = np.empty(nnz, dtype=np.int32)
+    val = np.empty(nnz)
+    vel = np.empty(grid_faces(3, n))
+    L.fsp_assemble_convdiff3d(n, pe_max, seed, _p(rp, _i64p), _p(col, _i32p),
+                              _p(val, _dp), _p(vel, _dp))
+    A = CSR(N, N, rp, col, val, f"convdiff3d-{n}-s{seed}")
+    return (A, vel) if return_velocity else A
+
+
+# Workloads named by what they are (sizes and seeds of the benchmark suite).
+def workload(name: str):
+    """Return (A, b) for a named workload.
+
+    ``poisson2d-128``      2-D Poisson 128^2, RHS U[-1,1] seed 1
+    ``diffusion3d-256``    3-D log-normal diffusion 256^3 (faces seed 2,
+                           RHS U[-1,1] seed 3)
+    ``convdiff3d-192``     3-D upwind convection-diffusion 192^3 (seed 4),
+                           RHS U[-1,1] seed 3
+    Any size suffix works (e.g. ``diffusion3d-48``).
+    """
+    kind, n = name.rsplit("-", 1)
+    n = int(n)
+    if kind == "poisson2d":
+        A = poisson2d(n)
+        b = uniform(1, A.nrows)
+    elif kind == "diffusion3d":
+        A = diffusion(3, n, seed=2)
+        b = uniform(3, A.nrows)
+    elif kind == "diffusion2d":
+        A = diffusion(2, n, seed=2)
+        b = uniform(3, A.nrows)
+    elif kind == "laplace3d":
+        A = laplace3d(n)
+        b = uniform(6, A.nrows)
+    elif kind == "convdiff3d":
+        A = convdiff3d(n, seed=4)
+        b = uniform(3, A.nrows)
+    else:
+        raise ValueError(f"unknown workload {name}")
+    A.name = name
+    return A, b

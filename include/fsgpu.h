@@ -1,0 +1,276 @@
+/*
+ * fsgpu.h -- C ABI of the GB300-native Krylov backend (libfsgpu.so).
+ *
+ * The library is the device replacement for flecsolve's Krylov hot path:
+ * the vector Data/Operations policy (flecsolve/vectors/core.hh:26-353,
+ * vectors/operations/topo_view.hh:26-291), the CSR operator
+ * (flecsolve/matrices/seq.hh:35-63, 177-193; matrices/parcsr.hh:29-177) and the
+ * CG / BiCGSTAB / GMRES loops (flecsolve/solvers/cg.hh:43-139,
+ * bicgstab.hh:39-187, gmres.hh:54-348).  Signatures use plain pointers, sizes
+ * and opaque handles only.
+ *
+ * Conventions
+ *  - Every call returns an int status (FS_OK = 0).  Nothing aborts; the
+ *    message of the last failure on a context is fs_last_error().
+ *  - One fs_ctx = one CUDA device + one CUDA stream.  Calls on a context are
+ *    not thread-safe; different contexts may be driven from different threads.
+ *  - Whoever creates a handle destroys it (fs_*_destroy).  Matrix and vector
+ *    creation copies host data into library-owned device memory.
+ *  - Reductions return their value through a host pointer and synchronise the
+ *    context stream, which is the `.get()` of the reference's futures
+ *    (flecsolve/util/future.hh:23-59).
+ */
+#ifndef FSGPU_H
+#define FSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define FS_API __attribute__((visibility("default")))
+#else
+#define FS_API
+#endif
+
+/* ------------------------------------------------------------ status --- */
+enum fs_status {
+	FS_OK = 0,
+	FS_ERR_BAD_HANDLE = 1,     /* NULL or destroyed handle                  */
+	FS_ERR_SIZE_MISMATCH = 2,  /* vector / matrix sizes disagree            */
+	FS_ERR_OUT_OF_MEMORY = 3,  /* device allocation failed                  */
+	FS_ERR_CUDA = 4,           /* a CUDA runtime call failed                */
+	FS_ERR_NON_FINITE = 5,     /* NaN / Inf met where a finite value is due */
+	FS_ERR_BREAKDOWN = 6,      /* a solver hit a reference flog_assert      */
+	FS_ERR_INVALID_ARG = 7,    /* argument out of range                     */
+	FS_ERR_NO_DEVICE = 8,      /* no usable CUDA device                     */
+	FS_ERR_UNSUPPORTED = 9     /* valid request this build does not handle  */
+};
+
+/* value types of vectors and matrix values */
+enum fs_dtype { FS_F64 = 0, FS_F32 = 1 };
+
+/* solve_info::stop_reason, flecsolve/solvers/solver_settings.hh:64-72 */
+enum fs_stop_reason {
+	FS_CONVERGED_ATOL = 0,
+	FS_CONVERGED_RTOL = 1,
+	FS_CONVERGED_USER = 2,
+	FS_DIVERGED_DTOL = 3,
+	FS_DIVERGED_ITERS = 4,
+	FS_DIVERGED_BREAKDOWN = 5,
+	FS_STATUS_UNKNOWN = 6
+};
+
+typedef struct fs_ctx_s *fs_ctx;
+typedef struct fs_vec_s *fs_vec;
+typedef struct fs_csr_s *fs_csr;
+typedef struct fs_solver_s *fs_solver;
+
+/* ----------------------------------------------------------- context --- */
+/* Replaces the FleCSI runtime/scheduler context the reference's vector ops
+ * run in (flecsolve/vectors/operations/topo_view.hh:38-40). */
+FS_API int fs_ctx_create(int device, fs_ctx *out);
+FS_API int fs_ctx_destroy(fs_ctx ctx);
+FS_API int fs_ctx_sync(fs_ctx ctx);
+/* the context's CUDA stream (a cudaStream_t) for interop */
+FS_API int fs_ctx_stream(fs_ctx ctx, void **stream);
+/* number of SMs of the context device */
+FS_API int fs_ctx_sm_count(fs_ctx ctx, int *sms);
+FS_API const char *fs_last_error(fs_ctx ctx);
+FS_API const char *fs_status_string(int status);
+/* number of kernels this library has launched on the context */
+FS_API int fs_ctx_launch_count(fs_ctx ctx, int64_t *count);
+/* CUDA-event timing on the context stream: record event `slot` (0..15) and
+ * read the time between two recorded slots (synchronises on the later one) */
+FS_API int fs_ctx_event_record(fs_ctx ctx, int slot);
+FS_API int fs_ctx_event_elapsed(fs_ctx ctx, int slot_from, int slot_to, float *ms);
+
+/* ----------------------------------------------------------- vectors --- */
+/* Device Data policy: replaces vec::data::topo_view storage
+ * (flecsolve/vectors/data/topo_view.hh:23-71) and seq_data
+ * (flecsolve/vectors/seq.hh:40-67). */
+FS_API int fs_vec_create(fs_ctx ctx, int64_t n, int dtype, fs_vec *out);
+/* wrap caller-owned device memory (not freed by fs_vec_destroy) */
+FS_API int fs_vec_wrap(fs_ctx ctx, int64_t n, int dtype, void *dptr, fs_vec *out);
+FS_API int fs_vec_destroy(fs_vec v);
+FS_API int fs_vec_size(fs_vec v, int64_t *n);
+FS_API int fs_vec_dtype(fs_vec v, int *dtype);
+FS_API int fs_vec_device_ptr(fs_vec v, void **dptr);
+/* host <-> device copies of the whole vector (host data of the vector's dtype) */
+FS_API int fs_vec_upload(fs_vec v, const void *host, int64_t n);
+FS_API int fs_vec_download(fs_vec v, void *host, int64_t n);
+
+/* Operations policy, flecsolve/vectors/core.hh:59-310 (argument meaning of the
+ * reference: the last vector argument is `this`).  Aliasing of inputs and
+ * output is allowed wherever the reference allows it
+ * (operations/topo_view.hh:78-210). */
+FS_API int fs_vec_copy(fs_vec src, fs_vec dst);                       /* core.hh:59  */
+FS_API int fs_vec_zero(fs_vec x);                                     /* core.hh:67  */
+FS_API int fs_vec_set_scalar(fs_vec x, double val);                   /* core.hh:75  */
+FS_API int fs_vec_scale(double alpha, fs_vec x, fs_vec y);            /* y = alpha x, core.hh:84 */
+FS_API int fs_vec_scale_self(double alpha, fs_vec x);                 /* core.hh:95  */
+FS_API int fs_vec_add(fs_vec x, fs_vec y, fs_vec z);                  /* z = x + y   */
+FS_API int fs_vec_subtract(fs_vec x, fs_vec y, fs_vec z);             /* z = x - y   */
+FS_API int fs_vec_multiply(fs_vec x, fs_vec y, fs_vec z);             /* z = x * y   */
+FS_API int fs_vec_divide(fs_vec x, fs_vec y, fs_vec z);               /* z = x / y   */
+FS_API int fs_vec_reciprocal(fs_vec x, fs_vec y);                     /* y = 1 / x   */
+FS_API int fs_vec_linear_sum(double alpha, fs_vec x, double beta, fs_vec y, fs_vec z);
+FS_API int fs_vec_axpy(double alpha, fs_vec x, fs_vec y, fs_vec z);   /* z = alpha x + y, core.hh:189 */
+FS_API int fs_vec_axpby(double alpha, double beta, fs_vec x, fs_vec z); /* z = alpha x + beta z */
+FS_API int fs_vec_abs(fs_vec x, fs_vec y);                            /* y = |x|     */
+FS_API int fs_vec_add_scalar(fs_vec x, double alpha, fs_vec y);       /* y = x + alpha */
+/* set_random(seed), core.hh:302-310: uniform [0,1) from splitmix64(seed) */
+FS_API int fs_vec_set_random(fs_vec x, uint64_t seed);
+
+/* Reductions (core.hh:229-290).  Deterministic: a fixed-order block tree,
+ * the same bits for the same inputs on the same device.  Single-precision
+ * vectors accumulate with compensated (two-sum / two-product) arithmetic. */
+FS_API int fs_vec_dot(fs_vec x, fs_vec y, double *out);
+FS_API int fs_vec_l1norm(fs_vec x, double *out);
+FS_API int fs_vec_l2norm(fs_vec x, double *out);
+FS_API int fs_vec_inf_norm(fs_vec x, double *out);
+FS_API int fs_vec_min(fs_vec x, double *out);
+FS_API int fs_vec_max(fs_vec x, double *out);
+
+/* --------------------------------------------------------- matrices --- */
+/* Device CSR operator: replaces mat::sparse / compressed_ops::spmv
+ * (flecsolve/matrices/seq.hh:35-63, 177-193).  rowptr has nrows+1 offsets,
+ * col holds column ids of width index_bytes (4 or 8; the reference's
+ * mat::csr<double> uses std::size_t), val holds doubles.  The library stores
+ * int32 column ids and keeps a float copy of the values for mixed precision. */
+FS_API int fs_csr_create(fs_ctx ctx, int64_t nrows, int64_t ncols, int64_t nnz,
+                         const int64_t *rowptr, const void *col, int index_bytes,
+                         const double *val, fs_csr *out);
+FS_API int fs_csr_destroy(fs_csr A);
+FS_API int fs_csr_shape(fs_csr A, int64_t *nrows, int64_t *ncols, int64_t *nnz);
+/* overwrite the values (same pattern) from host memory */
+FS_API int fs_csr_update_values(fs_csr A, const double *val);
+/* overwrite the values from device memory (float64, nnz entries) */
+FS_API int fs_csr_update_values_device(fs_csr A, const double *dval);
+FS_API int fs_csr_values_device_ptr(fs_csr A, double **dval);
+
+/* SpMV modes */
+enum fs_spmv_mode {
+	FS_SPMV_FMA = 0,      /* y_i accumulated with fused multiply-add      */
+	FS_SPMV_EXACT = 1     /* products rounded, then summed left to right:
+	                         the reference's row loop bit for bit         */
+};
+/* y = A x (op::core::apply -> mat::sparse::apply, matrices/seq.hh:50-60).
+ * x and y are both FS_F64 or both FS_F32 (FS_F32 uses the float values). */
+FS_API int fs_csr_spmv(fs_csr A, fs_vec x, fs_vec y, int mode);
+/* r = b - A x (op::core::residual, operators/core.hh:129-142) */
+FS_API int fs_csr_residual(fs_csr A, fs_vec b, fs_vec x, fs_vec r);
+/* y = A^T x through a precomputed CSC view (atomic-free); the view is built
+ * on first use and kept until the values or the matrix change */
+FS_API int fs_csr_spmv_transpose(fs_csr A, fs_vec x, fs_vec y);
+/* dinv_i = 1 / a_ii, the D^-1 operator of flecsolve/util/test/mesh.hh:123-140 */
+FS_API int fs_csr_diag_inv(fs_csr A, fs_vec dinv);
+
+/* Row-block distributed SpMV of mat::parcsr (flecsolve/matrices/parcsr.hh:
+ * 60-91, topo/csr.hh:482-618): rows are split into `parts` contiguous blocks,
+ * each row's owned-column (diag block) and ghost-column (offd block) entries
+ * are summed separately and added, y = y_diag + y_offd.  All parts live on
+ * this device. */
+FS_API int fs_parcsr_spmv(fs_csr A, int parts, fs_vec x, fs_vec y);
+
+/* ---------------------------------------------------------- solvers --- */
+/* solver_settings, flecsolve/solvers/solver_settings.hh:31-36 */
+typedef struct {
+	int maxiter;
+	float rtol;
+	float atol;          /* accepted and unused, as in the reference */
+	int use_zero_guess;
+} fs_solver_settings;
+
+/* solve_info, flecsolve/solvers/solver_settings.hh:61-85 */
+typedef struct {
+	int status;          /* enum fs_stop_reason */
+	int iters;
+	int restarts;
+	float res_norm_initial, res_norm_final;
+	float sol_norm_initial, sol_norm_final;
+	float rhs_norm;
+} fs_solve_info;
+
+enum fs_method {
+	FS_CG = 0,           /* op::cg, cg.hh:43-139                         */
+	FS_BICGSTAB = 1,     /* op::bicgstab, bicgstab.hh:39-187             */
+	FS_GMRES = 2,        /* op::gmres, gmres.hh:78-241                   */
+	FS_CG_MIXED = 3      /* FP32 inner PCG inside FP64 refinement        */
+};
+
+enum fs_precond_kind {
+	FS_PRECOND_NONE = 0,   /* op::I, operators/shell.hh:94-95             */
+	FS_PRECOND_JACOBI = 1, /* D^-1 of A (util/test/mesh.hh:123-140)       */
+	FS_PRECOND_DIAG = 2,   /* caller-given diagonal vector (z_i = d_i r_i) */
+	FS_PRECOND_CSR = 3     /* a CSR operator applied by SpMV               */
+};
+
+typedef struct {
+	int kind;            /* enum fs_precond_kind */
+	fs_vec diag;         /* FS_PRECOND_DIAG      */
+	fs_csr op;           /* FS_PRECOND_CSR       */
+} fs_precond;
+
+enum fs_gmres_side { FS_LEFT = 0, FS_RIGHT = 1 };
+enum fs_gmres_ortho { FS_ORTHO_CGS2 = 0, FS_ORTHO_MGS = 1 };
+
+enum fs_refine_kind {
+	FS_REFINE_RESTART = 0,  /* outer FP64 residual, inner FP32 PCG restarted */
+	FS_REFINE_RELIABLE = 1  /* FP32 recurrences with FP64 residual
+	                           replacement, search direction kept          */
+};
+
+/* Krylov settings: the reference's per-solver settings in one struct
+ * (cg.hh:254, bicgstab.hh:197, gmres.hh:389-405) plus the device controls. */
+typedef struct {
+	fs_solver_settings base;
+	/* GMRES (gmres.hh:389-422) */
+	int max_krylov_dim;  /* -1 = maxiter; bound 100 */
+	int pre_side;        /* enum fs_gmres_side */
+	int restart;
+	int ortho;           /* enum fs_gmres_ortho */
+	/* device loop: iterations per CUDA-graph launch between residual
+	   read-backs (0 = library default) */
+	int k_readback;
+	/* mixed precision (FS_CG_MIXED) */
+	int refine;          /* enum fs_refine_kind */
+	double inner_rtol;   /* restart: inner relative tolerance; reliable:
+	                        residual reduction between replacements        */
+	int max_outer;       /* restart: maximum refinement steps            */
+} fs_krylov_settings;
+
+/* Fill `s` with the reference defaults (gmres.hh:414-418) and device defaults. */
+FS_API int fs_krylov_settings_default(fs_krylov_settings *s);
+
+/* The diagnostic callable bool(const Vec &, double) of the reference
+ * (cg.hh:112, bicgstab.hh:160, gmres.hh:196).  Nonzero return stops the
+ * solve with FS_CONVERGED_USER. */
+typedef int (*fs_diag_fn)(void *user, fs_vec x, double res_norm);
+
+/* Bind a solver: krylov_solver::bind / operator() (krylov_parameters.hh:94-
+ * 126) -- settings, work vectors (make_work, solver_settings.hh:189-200), the
+ * operator and the preconditioner.  The solver owns its work vectors and
+ * its captured CUDA graphs. */
+FS_API int fs_krylov_create(fs_ctx ctx, int method, const fs_krylov_settings *s,
+                            fs_csr A, const fs_precond *P, fs_solver *out);
+FS_API int fs_krylov_destroy(fs_solver s);
+FS_API int fs_krylov_set_diagnostic(fs_solver s, fs_diag_fn fn, void *user);
+FS_API int fs_krylov_settings_get(fs_solver s, fs_krylov_settings *out);
+FS_API int fs_krylov_settings_set(fs_solver s, const fs_krylov_settings *in);
+/* op::core::apply(b, x) of the bound solver (operators/core.hh:107-116) */
+FS_API int fs_krylov_apply(fs_solver s, fs_vec b, fs_vec x, fs_solve_info *info);
+/* per-iteration residual norms of the last apply (the values handed to the
+ * diagnostic); n on input = capacity, on output = count written */
+FS_API int fs_krylov_history(fs_solver s, double *hist, int64_t *n);
+/* number of refinement (outer) steps and total inner iterations of the last
+ * FS_CG_MIXED apply */
+FS_API int fs_krylov_mixed_stats(fs_solver s, int *outer, int *inner_iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,28 @@
+// Stand-in declaration for compiling flecsolve's serial (seq_vec / mat::csr)
+// Krylov path without FleCSI or Boost.  Only the names the reference
+// headers mention are declared; nothing here executes FleCSI behaviour.
+#pragma once
+#include <cstddef>
+#include <array>
+#include <vector>
+namespace flecsi::util {
+using id = std::size_t; using gid = std::size_t;
+template<class T> struct span {
+  using element_type = T; using value_type = std::remove_cv_t<T>;
+  T* p = nullptr; std::size_t n = 0;
+  span() = default; span(T* p, std::size_t n) : p(p), n(n) {}
+  template<class U> span(std::vector<U>& v) : p(v.data()), n(v.size()) {}
+  T* data() const { return p; } std::size_t size() const { return n; }
+  T& operator[](std::size_t i) const { return p[i]; }
+  T* begin() const { return p; } T* end() const { return p + n; }
+  T& front() const { return p[0]; } T& back() const { return p[n-1]; }
+  bool operator==(const span& o) const { return p == o.p && n == o.n; }
+  bool operator!=(const span& o) const { return !(*this == o); }
+};
+template<class T, std::size_t D> struct mdcolex {
+  T* p; std::array<std::size_t, D> s;
+  mdcolex(T* p, std::array<std::size_t, D> s) : p(p), s(s) {}
+  T& operator()(std::size_t i, std::size_t j) const { return p[i + s[0]*j]; }
+};
+template<class T> struct iota_view { T b, e; iota_view(T b, T e):b(b),e(e){} };
+}

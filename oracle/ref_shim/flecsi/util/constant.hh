@@ -1,0 +1,6 @@
+// Stand-in declaration for compiling flecsolve's serial (seq_vec / mat::csr)
+// Krylov path without FleCSI or Boost.  Only the names the reference
+// headers mention are declared; nothing here executes FleCSI behaviour.
+#pragma once
+namespace flecsi::util { template<auto V> struct constant { static constexpr auto value = V; };
+template<auto... V> struct constants {}; }

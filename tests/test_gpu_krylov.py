@@ -1,0 +1,171 @@
+"""Device CG / BiCGSTAB / mixed-precision CG against the reference.
+
+Bars (from the specification of this path): iteration counts within +-2 of
+the reference's, relative residual <= rtol, solution relative error vs the
+FP64 oracle <= 1e-10 for the FP64 path and <= 1e-8 after refinement for the
+mixed path.  The reference numbers come from the golden fixtures produced by
+the reference's own templates (tests/golden/) or from the oracle on the same
+seeded inputs."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import flecsolve_gb300 as fs
+import pyoracle as O
+from flecsolve_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+GOLD = Path(__file__).resolve().parent / "golden"
+META = json.loads((GOLD / "golden.json").read_text())
+ITER_TOL = 2
+X_RTOL_F64 = 1e-10
+X_RTOL_MIXED = 1e-8
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def _true_relres(A, b, x):
+    return np.linalg.norm(O.residual(A, b, x)) / np.linalg.norm(b)
+
+
+def _run(ctx, ns, A, b, x0=None, P_="jacobi", diag=None, **kw):
+    dA = fs.CSR(ctx, A)
+    vb = fs.Vector(ctx, b)
+    vx = fs.Vector(ctx, np.zeros(A.nrows) if x0 is None else x0)
+    s = ns.settings(**kw)
+    prec = fs.op.jacobi if P_ == "jacobi" else fs.op.I
+    slv = ns.solver(s, ns.make_work(vb))(fs.op.ref(dA), prec, diag)
+    info = slv(vb, vx)
+    return info, vx.numpy(), slv
+
+
+GOLD_CASES = [n for n, c in sorted(META["cases"].items()) if c["method"] in ("cg", "bicgstab")]
+
+
+@pytest.mark.parametrize("name", GOLD_CASES)
+def test_against_reference_fixture(ctx, name):
+    c = META["cases"][name]
+    A, b = P.workload(c["workload"])
+    kw = dict(c["kwargs"])
+    x0 = P.uniform(int(c["x0"][1]), A.nrows, 0.0, 1.0) if c["x0"] else None
+    prec = kw.pop("precond", "jacobi")
+    ns = fs.cg if c["method"] == "cg" else fs.bicgstab
+    info, x, _ = _run(ctx, ns, A, b, x0, prec, maxiter=kw.pop("maxiter", 2000),
+                      rtol=kw.pop("rtol", 1e-8), use_zero_guess=kw.pop("use_zero_guess", True))
+    g = np.load(GOLD / f"{name}.npz")
+    assert info.status == c["status"]
+    assert abs(info.iters - c["iters"]) <= ITER_TOL
+    assert _true_relres(A, b, x) <= 1e-8 * 1.01
+    assert _rel(x, g["x"]) <= X_RTOL_F64
+
+
+def test_cg_history_tracks_reference(ctx):
+    A, b = P.workload("poisson2d-128")
+    info, x, slv = _run(ctx, fs.cg, A, b, maxiter=2000, rtol=1e-8)
+    g = np.load(GOLD / "poisson2d-128_cg.npz")
+    h = slv.history()
+    m = min(h.size, g["hist"].size)
+    assert h.size == info.iters
+    # residual norms agree to rounding until the very end of the run
+    assert np.allclose(h[: m - 5], g["hist"][: m - 5], rtol=1e-6)
+
+
+def test_cg_diagnostic_called_every_iteration(ctx):
+    """cg.cc:85-89: the diagnostic runs once per iteration and sees x."""
+    A, b = P.workload("poisson2d-64")
+    calls = []
+
+    def diag(xv, res):
+        calls.append((res, float(xv.l2norm().get())))
+        return False
+
+    info, x, _ = _run(ctx, fs.cg, A, b, diag=diag, maxiter=2000, rtol=1e-8)
+    assert info.iters == len(calls)
+    assert calls[-1][1] == pytest.approx(np.linalg.norm(x), rel=1e-12)
+    # user stop
+    info, _, _ = _run(ctx, fs.cg, A, b, diag=lambda xv, r: True, maxiter=2000, rtol=1e-8)
+    assert info.status == "converged_user" and info.iters == 1
+
+
+def test_cg_edge_cases(ctx):
+    A, b = P.workload("poisson2d-32")
+    info, x, _ = _run(ctx, fs.cg, A, np.zeros_like(b), maxiter=100, rtol=1e-8)
+    assert info.status == "converged_rtol" and info.iters == 0 and not x.any()
+    info, _, _ = _run(ctx, fs.cg, A, b, maxiter=5, rtol=1e-8)
+    assert info.status == "diverged_iters" and info.iters == 0
+    r = O.solve("cg", A, b, maxiter=5)
+    assert (r.status, r.iters) == (info.status, info.iters)
+    bad = b.copy()
+    bad[7] = np.nan
+    with pytest.raises(fs.api._lib.FsError) as ei:
+        _run(ctx, fs.cg, A, bad, maxiter=50, rtol=1e-8)
+    assert ei.value.status == fs.api._lib.ERR_NON_FINITE
+
+
+def test_cg_readback_interval_does_not_change_result(ctx):
+    A, b = P.workload("diffusion3d-24")
+    res = []
+    for k in (1, 7, 32):
+        info, x, _ = _run(ctx, fs.cg, A, b, maxiter=2000, rtol=1e-8, k_readback=k)
+        res.append((info.iters, x))
+    assert res[0][0] == res[1][0] == res[2][0]
+    assert np.array_equal(res[0][1], res[1][1]) and np.array_equal(res[0][1], res[2][1])
+
+
+@pytest.mark.parametrize("wl", ["diffusion3d-40", "diffusion2d-96"])
+def test_cg_vs_oracle(ctx, wl):
+    A, b = P.workload(wl)
+    r = O.solve("cg", A, b, maxiter=4000, rtol=1e-8)
+    info, x, _ = _run(ctx, fs.cg, A, b, maxiter=4000, rtol=1e-8)
+    assert info.status == r.status == "converged_rtol"
+    assert abs(info.iters - r.iters) <= ITER_TOL
+    assert _rel(x, r.x) <= X_RTOL_F64
+
+
+@pytest.mark.parametrize("wl,prec", [("convdiff3d-24", "jacobi"), ("convdiff3d-16", "none"),
+                                     ("diffusion3d-24", "jacobi")])
+def test_bicgstab_vs_oracle(ctx, wl, prec):
+    A, b = P.workload(wl)
+    r = O.solve("bicgstab", A, b, maxiter=4000, rtol=1e-8, precond=prec)
+    info, x, _ = _run(ctx, fs.bicgstab, A, b, P_=prec, maxiter=4000, rtol=1e-8)
+    assert info.status == r.status
+    assert abs(info.iters - r.iters) <= ITER_TOL
+    assert _true_relres(A, b, x) <= 1e-8 * 1.01
+    assert _rel(x, r.x) <= 1e-9
+
+
+def test_bicgstab_early_exit_quirk(ctx):
+    """bicgstab.hh:136-142: ||s|| < rtol (unscaled) exits with iters = iter;
+    with iters == 0 the status becomes diverged_iters (bicgstab.hh:183)."""
+    A, b = P.workload("poisson2d-16")
+    b = b * 1e-12  # tiny rhs: ||s|| below rtol after the first half-step
+    r = O.solve("bicgstab", A, b, maxiter=100, rtol=1e-8)
+    info, x, _ = _run(ctx, fs.bicgstab, A, b, maxiter=100, rtol=1e-8)
+    assert (info.status, info.iters) == (r.status, r.iters)
+    assert _rel(x, r.x) <= 1e-9
+
+
+@pytest.mark.parametrize("wl", ["diffusion3d-40", "poisson2d-128"])
+def test_mixed_cg_refinement(ctx, wl):
+    """FP32-inner / FP64-refined CG reaches the FP64 stopping test, and its
+    error against the FP64 direct solution is <= 1e-8 when the stopping test
+    asks for it (rtol 1e-11 bounds the forward error by cond(A) * 1e-11)."""
+    import scipy.sparse.linalg as spla
+    A, b = P.workload(wl)
+    info, x, slv = _run(ctx, fs.mixed_cg, A, b, maxiter=20000, rtol=1e-8, inner_rtol=1e-4)
+    assert info.status == "converged_rtol"
+    assert _true_relres(A, b, x) <= 1e-8
+    outer, inner = slv.mixed_stats()
+    assert outer >= 1 and inner == info.iters
+    ref64 = O.solve("cg", A, b, maxiter=20000, rtol=1e-8)
+    # both stop at the same residual level: the iteration budgets agree
+    assert info.iters <= 1.5 * ref64.iters + 10
+    xs = spla.spsolve(A.to_scipy().tocsc(), b)
+    info2, x2, _ = _run(ctx, fs.mixed_cg, A, b, maxiter=20000, rtol=1e-11, inner_rtol=1e-4)
+    assert info2.status == "converged_rtol"
+    assert _rel(x2, xs) <= X_RTOL_MIXED

@@ -1,0 +1,127 @@
+"""CSR operator on the GPU against the oracle's reference row loop
+(flecsolve/matrices/seq.hh:177-193): bit-exact in EXACT mode, within a few
+ulps of the row sum in FMA mode; ragged, empty and long rows; FP32 values;
+residual; parcsr split; transpose."""
+import numpy as np
+import pytest
+
+import flecsolve_gb300 as fs
+import pyoracle as O
+from flecsolve_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+def _bound(A, x):
+    # |y_fma - y_exact| <= 2 * nnz_row * eps * sum |a x|
+    S = A.to_scipy()
+    return 2 * 8 * np.finfo(np.float64).eps * (abs(S) @ np.abs(x))
+
+
+@pytest.mark.parametrize("wl", ["poisson2d-128", "diffusion3d-24", "convdiff3d-20"])
+def test_spmv_exact_mode_is_bit_exact(ctx, wl):
+    A, _ = P.workload(wl)
+    x = P.uniform(42, A.ncols)
+    dA = fs.CSR(ctx, A)
+    vx, vy = fs.Vector(ctx, x), fs.Vector(ctx, A.nrows)
+    dA.apply(vx, vy, exact=True)
+    assert np.array_equal(vy.numpy(), O.spmv(A, x))
+    dA.apply(vx, vy)
+    y = vy.numpy()
+    assert (np.abs(y - O.spmv(A, x)) <= _bound(A, x)).all()
+
+
+def _ragged(n, m, seed, long_rows=()):
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(0, 12, n)
+    lens[rng.integers(0, n, 5)] = 0          # empty rows
+    for r in long_rows:
+        lens[r] = 5000                       # longer than a row block
+    rp = np.zeros(n + 1, dtype=np.int64)
+    rp[1:] = np.cumsum(lens)
+    col = np.concatenate([np.sort(rng.choice(m, min(l, m), replace=False)) if l else
+                          np.zeros(0, dtype=np.int64) for l in lens]).astype(np.int32)
+    rp[1:] = np.cumsum([min(l, m) for l in lens])
+    val = rng.standard_normal(rp[-1])
+    return P.CSR(n, m, rp, col, val, "ragged")
+
+
+def test_spmv_ragged_empty_and_long_rows(ctx):
+    A = _ragged(3000, 7000, 3, long_rows=(17, 2999))
+    x = np.random.default_rng(4).standard_normal(A.ncols)
+    dA = fs.CSR(ctx, A)
+    vx, vy = fs.Vector(ctx, x), fs.Vector(ctx, A.nrows)
+    dA.apply(vx, vy, exact=True)
+    assert np.array_equal(vy.numpy(), O.spmv(A, x))
+    dA.apply(vx, vy)
+    assert (np.abs(vy.numpy() - O.spmv(A, x)) <= 2 * 5000 * 1.2e-16 * (abs(A.to_scipy()) @ np.abs(x))).all()
+
+
+def test_spmv_index_widths_and_rectangular(ctx):
+    A = _ragged(500, 1300, 5)
+    A64 = P.CSR(A.nrows, A.ncols, A.rowptr, A.col.astype(np.int64), A.val)
+    x = np.random.default_rng(6).standard_normal(A.ncols)
+    for M in (A, A64):
+        dA = fs.CSR(ctx, M)
+        vx, vy = fs.Vector(ctx, x), fs.Vector(ctx, M.nrows)
+        dA.apply(vx, vy, exact=True)
+        assert np.array_equal(vy.numpy(), O.spmv(A, x))
+
+
+def test_spmv_f32(ctx):
+    A, _ = P.workload("diffusion3d-20")
+    x = P.uniform(8, A.ncols).astype(np.float32)
+    dA = fs.CSR(ctx, A)
+    vx, vy = fs.Vector(ctx, x, "f32"), fs.Vector(ctx, A.nrows, "f32")
+    dA.apply(vx, vy)
+    A32 = A.to_scipy().astype(np.float32).astype(np.float64)
+    ref = A32 @ x.astype(np.float64)
+    assert np.abs(vy.numpy() - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+def test_residual_and_dinv(ctx):
+    A, b = P.workload("convdiff3d-12")
+    x = P.uniform(9, A.nrows)
+    dA = fs.CSR(ctx, A)
+    vb, vx, vr = fs.Vector(ctx, b), fs.Vector(ctx, x), fs.Vector(ctx, A.nrows)
+    dA.residual(vb, vx, vr)
+    r = O.residual(A, b, x)
+    assert np.abs(vr.numpy() - r).max() <= 1e-13 * np.abs(b).max() * 10
+    assert np.array_equal(dA.Dinv().numpy(), O.dinv(A))
+
+
+@pytest.mark.parametrize("parts", [1, 3, 7])
+def test_parcsr_split_is_bit_exact(ctx, parts):
+    A, _ = P.workload("convdiff3d-14")
+    x = P.uniform(10, A.nrows)
+    dA = fs.CSR(ctx, A)
+    vx, vy = fs.Vector(ctx, x), fs.Vector(ctx, A.nrows)
+    dA.parcsr_apply(parts, vx, vy)
+    assert np.array_equal(vy.numpy(), O.parcsr_spmv(A, parts, x))
+
+
+def test_transpose_spmv(ctx):
+    A = _ragged(800, 600, 11, long_rows=(5,))
+    x = np.random.default_rng(12).standard_normal(A.nrows)
+    dA = fs.CSR(ctx, A)
+    vx, vy = fs.Vector(ctx, x), fs.Vector(ctx, A.ncols)
+    dA.apply_transpose(vx, vy)
+    ref = A.to_scipy().T @ x
+    assert np.abs(vy.numpy() - ref).max() <= 1e-12 * (abs(A.to_scipy().T) @ np.abs(x)).max()
+    # values updated -> the CSC view follows
+    A.val *= 2.0
+    dA.update_values(A.val)
+    dA.apply_transpose(vx, vy)
+    assert np.abs(vy.numpy() - 2 * ref).max() <= 2e-12 * (abs(A.to_scipy().T) @ np.abs(x)).max()
+
+
+def test_bad_inputs_are_rejected(ctx):
+    A, _ = P.workload("poisson2d-8")
+    bad = P.CSR(A.nrows, A.ncols, A.rowptr, A.col.copy(), A.val)
+    bad.col[3] = 10_000
+    with pytest.raises(fs.api._lib.FsError) as ei:
+        fs.CSR(ctx, bad)
+    assert ei.value.status == fs.api._lib.ERR_INVALID_ARG
+    dA = fs.CSR(ctx, A)
+    with pytest.raises(fs.api._lib.FsError):
+        dA.apply(fs.Vector(ctx, 5), fs.Vector(ctx, A.nrows))
