@@ -366,8 +366,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="diffusion3d-256")
     ap.add_argument("--maxiter", type=int, default=20000)
-    ap.add_argument("--inner-rtol", dest="inner_rtol", type=float, default=1e-4)
-    ap.add_argument("--refine", default="restart", choices=["restart", "reliable"])
+    ap.add_argument("--inner-rtol", dest="inner_rtol", type=float, default=1e-2)
+    ap.add_argument("--refine", default="reliable", choices=["restart", "reliable"])
     ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
     args = ap.parse_args()

@@ -25,7 +25,7 @@ namespace fsg {
 constexpr int kThreads = 256;
 
 __device__ __forceinline__ bool stopped(const KState *st) {
-	return st->done || (st->flags & KF_RESTART);
+	return st->done || (st->flags & (KF_RESTART | KF_RELIABLE));
 }
 
 // ------------------------------------------------------ setup kernels --
@@ -255,6 +255,124 @@ __global__ void k_inner_init(KState *in, const KState *out, double inner_rtol, i
 	in->flags = 0;
 	in->info_iters = 0;
 }
+
+// Reliable-update variant (residual replacement, Sleijpen & van der Vorst
+// 1996; van der Vorst & Ye 2000): the CG recurrences run in FP32 on a
+// correction xs, and whenever the recurrence residual has dropped by `delta`
+// since the last replacement (or below the tolerance) the host folds xs into
+// the FP64 solution and replaces r by the FP64 true residual b - A x.  The
+// search direction is kept, so no Krylov information is lost.
+template<int PK>
+__global__ void __launch_bounds__(kThreads)
+k_rc_update(int64_t n, float *__restrict__ x, const float *__restrict__ p, float *__restrict__ r,
+            const float *__restrict__ w, const float *__restrict__ dinv, KState *st,
+            double *part, unsigned *counter, double *hist, double delta) {
+	__shared__ double sh[128];
+	if (stopped(st))
+		return;
+	const float alpha = (float)st->alpha;
+	Acc<float, 2> acc;
+	acc.init();
+	FOR_EACH(i, n) {
+		float xi = fmaf(alpha, p[i], x[i]);
+		float ri = fmaf(-alpha, w[i], r[i]);
+		x[i] = xi;
+		r[i] = ri;
+		float zi = PK ? dinv[i] * ri : ri;
+		acc.add_prod(0, ri, ri);
+		acc.add_prod(1, ri, zi);
+	}
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double s[2];
+		sum_partials<2>(part, gridDim.x, s, sh);
+		if (threadIdx.x == 0) {
+			double res = sqrt(s[0]);
+			int it = st->iter + 1;
+			st->iter = it;
+			st->res = res;
+			if (it <= st->hist_cap)
+				hist[it - 1] = res;
+			if (!isfinite(res))
+				st->flags |= KF_NONFINITE;
+			if (res < delta * st->aux[1] || res < st->tol || it >= st->maxiter ||
+			    (st->flags & KF_NONFINITE))
+				st->flags |= KF_RELIABLE;
+			st->rho_old = st->rho;
+			st->rho = s[1];
+			st->beta = s[1] / st->rho_old;
+			*counter = 0;
+		}
+	}
+}
+
+// x64 += xs; xs = 0
+__global__ void k_rel_fold(int64_t n, double *__restrict__ x, float *__restrict__ xs) {
+	FOR_EACH(i, n) {
+		x[i] += (double)xs[i];
+		xs[i] = 0.f;
+	}
+}
+
+// after the FP64 residual replaced r32: rho = r'Dr, beta = rho / rho_old,
+// new reference level for the next replacement, stopping test
+template<int PK>
+__global__ void __launch_bounds__(kThreads)
+k_rel_finish(int64_t n, const float *__restrict__ r, const float *__restrict__ dinv, KState *st,
+             double *part, unsigned *counter) {
+	__shared__ double sh[128];
+	Acc<float, 1> acc;
+	acc.init();
+	FOR_EACH(i, n) {
+		float ri = r[i];
+		acc.add_prod(0, ri, PK ? dinv[i] * ri : ri);
+	}
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double s[1];
+		sum_partials<1>(part, gridDim.x, s, sh);
+		if (threadIdx.x == 0) {
+			st->rho = s[0];
+			st->beta = s[0] / st->rho_old;
+			st->aux[1] = st->res;  // true residual after the replacement
+			st->restarts += 1;     // number of replacements
+			st->flags &= ~KF_RELIABLE;
+			if (st->res < st->tol) {
+				st->done = 1;
+				st->status = FS_CONVERGED_RTOL;
+				st->info_iters = st->iter;
+			}
+			else if (st->iter >= st->maxiter || (st->flags & KF_NONFINITE)) {
+				st->done = 1;
+				st->status = FS_DIVERGED_ITERS;
+				st->info_iters = 0;
+			}
+			*counter = 0;
+		}
+	}
+}
+
+// r64 = b - A x, r32 = (float) r64, st->res = ||r64|| (FP64)
+struct EpiRelResidual {
+	static constexpr int NV = 1;
+	const double *b;
+	float *r32;
+	KState *st;
+	double *part;
+	unsigned *counter;
+	__device__ bool skip() const { return false; }
+	template<class A>
+	__device__ void row(int r, double s, A &acc) const {
+		double v = b[r] - s;
+		r32[r] = (float)v;
+		acc.add_prod(0, v, v);
+	}
+	__device__ void finish(const double *s) const {
+		st->res = sqrt(s[0]);
+		if (!isfinite(st->res))
+			st->flags |= KF_NONFINITE;
+	}
+};
 
 // --------------------------------------------------------- BiCGSTAB --
 
@@ -508,6 +626,12 @@ k_bi_restart(int64_t n, const V *__restrict__ res, V *__restrict__ rt, V *__rest
 			st->rho = s[0];  // recomputed r~'res of the next iteration
 			st->restarts += 1;
 			st->flags &= ~KF_RESTART;
+			// the reference's restart `continue`s: it consumes a loop index
+			st->iter += 1;
+			if (st->iter >= st->maxiter) {
+				st->done = 1;
+				st->status = FS_DIVERGED_ITERS;
+			}
 			*counter = 0;
 		}
 	}
@@ -924,6 +1048,142 @@ static int cg_apply_mixed(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	return FS_OK;
 }
 
+struct RcArgs {
+	Vec *b, *x;
+	int k;
+	double delta;
+};
+
+template<int PK>
+static int rc_body(Solver *s, void *a) {
+	RcArgs *g = (RcArgs *)a;
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	float *r = s->w32[0], *p = s->w32[1], *w = s->w32[2], *xs = s->w32[3];
+	const float *dinv = s->dinv32();
+	const int G = red_grid(ctx, n);
+	for (int k = 0; k < g->k; ++k) {
+		FS_TRY(launch_spmv<float, false, false>(
+			ctx, s->A, s->A->val32, p, nullptr,
+			EpiCgAp<float>{w, p, s->st, s->part, s->counter}));
+		k_rc_update<PK><<<G, kThreads, 0, ctx->stream>>>(n, xs, p, r, w, dinv, s->st, s->part,
+		                                                s->counter, s->hist, g->delta);
+		FS_TRY(check_launch(ctx, "reliable cg update"));
+		k_cg_dir<float, PK><<<G, kThreads, 0, ctx->stream>>>(n, p, r, dinv, s->st);
+		FS_TRY(check_launch(ctx, "cg direction f32"));
+	}
+	return FS_OK;
+}
+
+// FP32 CG with FP64 reliable updates (residual replacement)
+static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	const int G = red_grid(ctx, n);
+	const bool zg = s->set.base.use_zero_guess != 0;
+	const int PK = s->dinv32() ? 1 : 0;
+	float *r32 = s->w32[0], *p32 = s->w32[1], *xs = s->w32[3];
+	const float *dinv = s->dinv32();
+	const int maxiter = s->set.base.maxiter;
+	const double delta = s->set.inner_rtol > 0 ? s->set.inner_rtol : 0.1;
+	FS_TRY(ensure_hist(s, std::max(1, maxiter)));
+	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, maxiter));
+	FS_TRY(norms(s, b, x, !zg, 0));
+	if (zg) {
+		k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
+		FS_TRY(check_launch(ctx, "fill"));
+	}
+	k_fill<float><<<G, kThreads, 0, ctx->stream>>>(n, xs, 0.f);
+	FS_TRY(check_launch(ctx, "fill"));
+	auto true_residual = [&]() -> int {
+		return launch_spmv<double, false, false>(
+			ctx, s->A, s->A->val, (const double *)x->d, nullptr,
+			EpiRelResidual{(const double *)b->d, r32, s->st, s->part, s->counter});
+	};
+	FS_TRY(true_residual());
+	if (PK)
+		k_cg_start<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, p32, s->st, s->part, s->counter);
+	else
+		k_cg_start<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, p32, s->st, s->part, s->counter);
+	FS_TRY(check_launch(ctx, "cg start f32"));
+	FS_TRY(read_state(s));
+	const double res0 = s->hst->res0;
+	{
+		// reference level for the first replacement = the initial residual
+		KState h = *s->hst;
+		h.aux[1] = res0;
+		FS_CUDA_TRY(ctx, cudaMemcpyAsync(&s->st->aux[1], &h.aux[1], sizeof(double),
+		                                 cudaMemcpyHostToDevice, ctx->stream));
+		FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	}
+	int user_stop = 0;
+	int64_t seen = 0;
+	const int k = k_default(s) > 1 ? k_default(s) : 32;
+	RcArgs args{b, x, k, delta};
+	GraphKey key{b->d, x->d, 2000 + k * 2 + PK};
+	while (!s->hst->done) {
+		FS_TRY(graph_run(s, key, PK ? rc_body<1> : rc_body<0>, &args));
+		FS_TRY(read_state(s));
+		if (s->hst->flags & KF_RELIABLE) {
+			k_rel_fold<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs);
+			FS_TRY(check_launch(ctx, "reliable fold"));
+			FS_TRY(true_residual());
+			if (PK)
+				k_rel_finish<1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, s->st, s->part, s->counter);
+			else
+				k_rel_finish<0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, s->st, s->part, s->counter);
+			FS_TRY(check_launch(ctx, "reliable finish"));
+			if (PK)
+				k_cg_dir<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, s->st);
+			else
+				k_cg_dir<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, nullptr, s->st);
+			FS_TRY(check_launch(ctx, "cg direction f32"));
+			FS_TRY(read_state(s));
+		}
+		if (s->diag) {
+			int64_t nh = std::min<int64_t>(s->hst->iter, s->hist_cap);
+			std::vector<double> hh(nh > seen ? nh - seen : 0);
+			if (!hh.empty())
+				FS_CUDA_TRY(ctx, cudaMemcpy(hh.data(), s->hist + seen, hh.size() * sizeof(double),
+				                            cudaMemcpyDeviceToHost));
+			for (size_t j = 0; j < hh.size() && !user_stop; ++j)
+				if (s->diag(s->diag_user, reinterpret_cast<fs_vec>(x), hh[j]))
+					user_stop = (int)(seen + j + 1);
+			seen = nh;
+			if (user_stop)
+				break;
+		}
+	}
+	if (user_stop) {
+		k_rel_fold<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs);
+		FS_TRY(check_launch(ctx, "reliable fold"));
+	}
+	KState &h = *s->hst;
+	s->hhist_count = std::min<int64_t>(h.iter, s->hist_cap);
+	s->mixed_outer = h.restarts;
+	s->mixed_inner = h.iter;
+	double xn = 0;
+	FS_TRY(sol_norm(s, x, &xn));
+	memset(info, 0, sizeof(*info));
+	info->rhs_norm = (float)h.rhs_norm;
+	info->sol_norm_initial = zg ? 0.f : (float)h.sol0;
+	info->res_norm_initial = (float)res0;
+	info->res_norm_final = (float)h.res;
+	info->sol_norm_final = (float)xn;
+	info->restarts = h.restarts;
+	if (user_stop) {
+		info->status = FS_CONVERGED_USER;
+		info->iters = user_stop;
+	}
+	else {
+		info->status = h.status;
+		info->iters = h.info_iters;
+	}
+	if (h.flags & KF_NONFINITE)
+		return set_err(ctx, FS_ERR_NON_FINITE, "mixed CG: non-finite residual norm");
+	return FS_OK;
+}
+
 // ------------------------------------------------------ BiCGSTAB apply --
 
 struct BiArgs {
@@ -1057,8 +1317,8 @@ FS_API int fs_krylov_settings_default(fs_krylov_settings *s) {
 	s->restart = 0;
 	s->ortho = FS_ORTHO_CGS2;
 	s->k_readback = 0;
-	s->refine = FS_REFINE_RESTART;
-	s->inner_rtol = 1e-4;
+	s->refine = FS_REFINE_RELIABLE;
+	s->inner_rtol = 1e-2;
 	s->max_outer = 64;
 	return FS_OK;
 }
@@ -1252,7 +1512,9 @@ FS_API int fs_krylov_apply(fs_solver h, fs_vec bh, fs_vec xh, fs_solve_info *inf
 	case FS_CG: return cg_apply64(s, b, x, info);
 	case FS_BICGSTAB: return bicgstab_apply64(s, b, x, info);
 	case FS_GMRES: return gmres_apply(s, b, x, info);
-	case FS_CG_MIXED: return cg_apply_mixed(s, b, x, info);
+	case FS_CG_MIXED:
+		return s->set.refine == FS_REFINE_RELIABLE ? cg_apply_reliable(s, b, x, info)
+		                                          : cg_apply_mixed(s, b, x, info);
 	}
 	return FS_ERR_INVALID_ARG;
 }

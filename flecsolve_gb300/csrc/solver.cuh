@@ -20,6 +20,7 @@ constexpr int KF_ALPHA_ZERO = 2;      // BiCGSTAB: r~'v == 0 (bicgstab.hh:129)
 constexpr int KF_RESTART = 4;         // BiCGSTAB: restart requested (bicgstab.hh:103)
 constexpr int KF_EARLY = 8;           // BiCGSTAB: ||s|| < rtol early exit (bicgstab.hh:136)
 constexpr int KF_NONFINITE = 16;      // a reduction produced NaN/Inf
+constexpr int KF_RELIABLE = 32;       // mixed CG: residual replacement due
 
 // Device-resident scalars of one solve.  Written only by the last block of a
 // reduction kernel (thread 0); read by every kernel that follows.

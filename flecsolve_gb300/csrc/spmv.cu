@@ -126,11 +126,13 @@ __global__ void parcsr_kernel(int n, int parts, const int *__restrict__ rp,
 		for (int k = rp[i]; k < rp[i + 1]; ++k) {
 			const int j = col[k];
 			if (EXACT) {
-				double p = val[k] * x[j];
+				// explicit roundings: nvcc would otherwise contract the
+				// product and the sum into one fused multiply-add
+				double p = __dmul_rn(val[k], x[j]);
 				if (j >= lo && j < hi)
-					yd = yd + p;
+					yd = __dadd_rn(yd, p);
 				else
-					yo = yo + p;
+					yo = __dadd_rn(yo, p);
 			}
 			else {
 				if (j >= lo && j < hi)
@@ -139,7 +141,7 @@ __global__ void parcsr_kernel(int n, int parts, const int *__restrict__ rp,
 					yo = fma(val[k], x[j], yo);
 			}
 		}
-		y[i] = yd + yo;
+		y[i] = __dadd_rn(yd, yo);
 	}
 }
 

@@ -92,12 +92,17 @@ struct SpmvSmem {
 	double red[128];
 };
 
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+
 // x gather, optionally scaled on the fly by a diagonal (y = A D x, used for
 // right Jacobi preconditioning without materialising D x)
 template<class V, bool SCALE>
 __device__ __forceinline__ V xg(const V *__restrict__ x, const V *__restrict__ d, int c) {
 	if constexpr (SCALE)
-		return __ldg(d + c) * __ldg(x + c);
+		return mul_rn(__ldg(d + c), __ldg(x + c));
 	else
 		return __ldg(x + c);
 }
@@ -131,11 +136,11 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 				for (int c0 = k0; c0 < k1; c0 += kBlkNnz) {
 					int c1 = min(k1, c0 + kBlkNnz);
 					for (int k = c0 + tid; k < c1; k += blockDim.x)
-						sm.val[k - c0] = A.val[k] * xg<V, SCALE>(x, dscale, A.col[k]);
+						sm.val[k - c0] = mul_rn(A.val[k], xg<V, SCALE>(x, dscale, A.col[k]));
 					__syncthreads();
 					if (tid == 0)
 						for (int k = 0; k < c1 - c0; ++k)
-							s = s + sm.val[k];
+							s = add_rn(s, sm.val[k]);
 					__syncthreads();
 				}
 			}
@@ -154,7 +159,7 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 		// stage the block's nonzeros
 		if constexpr (EXACT) {
 			for (int k = k0 + tid; k < k1; k += blockDim.x)
-				sm.val[k - k0] = A.val[k] * xg<V, SCALE>(x, dscale, A.col[k]);
+				sm.val[k - k0] = mul_rn(A.val[k], xg<V, SCALE>(x, dscale, A.col[k]));
 		}
 		else {
 			// 16-byte vector loads over the aligned cover of [k0, k1)
@@ -186,7 +191,7 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 			V s = V(0);
 			if constexpr (EXACT) {
 				for (int k = a; k < e; ++k)
-					s = s + sm.val[k];
+					s = add_rn(s, sm.val[k]);
 			}
 			else {
 				for (int k = a; k < e; ++k)

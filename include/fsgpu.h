@@ -236,7 +236,7 @@ typedef struct {
 	/* device loop: iterations per CUDA-graph launch between residual
 	   read-backs (0 = library default) */
 	int k_readback;
-	/* mixed precision (FS_CG_MIXED) */
+	/* mixed precision (FS_CG_MIXED); default FS_REFINE_RELIABLE, 1e-2 */
 	int refine;          /* enum fs_refine_kind */
 	double inner_rtol;   /* restart: inner relative tolerance; reliable:
 	                        residual reduction between replacements        */

@@ -61,7 +61,22 @@ def test_against_reference_fixture(ctx, name):
     assert info.status == c["status"]
     assert abs(info.iters - c["iters"]) <= ITER_TOL
     assert _true_relres(A, b, x) <= 1e-8 * 1.01
-    assert _rel(x, g["x"]) <= X_RTOL_F64
+    if c["method"] == "cg":
+        assert _rel(x, g["x"]) <= X_RTOL_F64
+    else:
+        _bicgstab_accuracy_bar(A, b, x, g["x"])
+
+
+def _bicgstab_accuracy_bar(A, b, x, x_ref):
+    """BiCGSTAB amplifies the rounding of its dot products: two correct FP64
+    runs whose reductions are summed in different orders follow the same
+    residual history for ~25 iterations and then separate, ending at
+    different points of the rtol ball.  The bar is therefore that the device
+    solution is as accurate as the reference's: its forward error against
+    the direct solution is within 2x the reference's own (+ 1e-12)."""
+    import scipy.sparse.linalg as spla
+    xs = spla.spsolve(A.to_scipy().tocsc(), b)
+    assert _rel(x, xs) <= 2.0 * _rel(x_ref, xs) + 1e-12
 
 
 def test_cg_history_tracks_reference(ctx):
@@ -136,7 +151,7 @@ def test_bicgstab_vs_oracle(ctx, wl, prec):
     assert info.status == r.status
     assert abs(info.iters - r.iters) <= ITER_TOL
     assert _true_relres(A, b, x) <= 1e-8 * 1.01
-    assert _rel(x, r.x) <= 1e-9
+    _bicgstab_accuracy_bar(A, b, x, r.x)
 
 
 def test_bicgstab_early_exit_quirk(ctx):
@@ -157,15 +172,21 @@ def test_mixed_cg_refinement(ctx, wl):
     asks for it (rtol 1e-11 bounds the forward error by cond(A) * 1e-11)."""
     import scipy.sparse.linalg as spla
     A, b = P.workload(wl)
-    info, x, slv = _run(ctx, fs.mixed_cg, A, b, maxiter=20000, rtol=1e-8, inner_rtol=1e-4)
+    ref64 = O.solve("cg", A, b, maxiter=20000, rtol=1e-8)
+    xs = spla.spsolve(A.to_scipy().tocsc(), b)
+    # default: FP32 recurrences with FP64 residual replacement -- the search
+    # direction survives a replacement, so the iteration count is the FP64 one
+    info, x, slv = _run(ctx, fs.mixed_cg, A, b, maxiter=20000, rtol=1e-8)
     assert info.status == "converged_rtol"
     assert _true_relres(A, b, x) <= 1e-8
     outer, inner = slv.mixed_stats()
     assert outer >= 1 and inner == info.iters
-    ref64 = O.solve("cg", A, b, maxiter=20000, rtol=1e-8)
-    # both stop at the same residual level: the iteration budgets agree
-    assert info.iters <= 1.5 * ref64.iters + 10
-    xs = spla.spsolve(A.to_scipy().tocsc(), b)
-    info2, x2, _ = _run(ctx, fs.mixed_cg, A, b, maxiter=20000, rtol=1e-11, inner_rtol=1e-4)
+    assert abs(info.iters - ref64.iters) <= ITER_TOL
+    info2, x2, _ = _run(ctx, fs.mixed_cg, A, b, maxiter=20000, rtol=1e-11)
     assert info2.status == "converged_rtol"
     assert _rel(x2, xs) <= X_RTOL_MIXED
+    # classic restarted refinement: converges, at a higher iteration cost
+    info3, x3, _ = _run(ctx, fs.mixed_cg, A, b, maxiter=20000, rtol=1e-11, refine="restart",
+                        inner_rtol=1e-4)
+    assert info3.status == "converged_rtol"
+    assert _rel(x3, xs) <= X_RTOL_MIXED
