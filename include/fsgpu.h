@@ -270,6 +270,30 @@ FS_API int fs_krylov_history(fs_solver s, double *hist, int64_t *n);
  * FS_CG_MIXED apply */
 FS_API int fs_krylov_mixed_stats(fs_solver s, int *outer, int *inner_iters);
 
+/* ------------------------------------------ allocation-free reduction --- */
+/* No counterpart in the reference.  Dot product sum_i x[i] * y[i] of two
+ * float64 device arrays, written to the device pointer `result`, for callers
+ * that cannot allocate device memory: code whose device memory is owned by
+ * another allocator (a framework's caching allocator or a fixed budget),
+ * code that cannot take the implicit device synchronisation of cudaMalloc /
+ * cudaFree, and code that holds only raw device pointers and a stream (no
+ * fs_ctx, whose creation allocates).  It calls no cudaMalloc, cudaFree or
+ * allocating library routine: its scratch is a 128 KiB static device array
+ * that every GPU loading libfsgpu.so holds until the process exits.
+ *  - n <= FS_DOT_NOALLOC_MAX_N (64 Mi elements, one scratch slot per 4096
+ *    elements); larger n returns FS_ERR_INVALID_ARG and launches nothing.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream) of the current
+ *    device.  The first call on a device looks up the scratch array's device
+ *    address (cudaGetSymbolAddress); make that first call before any stream
+ *    capture.
+ *  - Every call shares the one scratch array, so calls whose kernels can
+ *    overlap on the GPU (different streams without ordering) race.
+ *  - The result is deterministic for a given n and agrees with fs_vec_dot to
+ *    rounding (the two group the partial sums differently). */
+#define FS_DOT_NOALLOC_MAX_N ((int64_t)67108864)
+FS_API int fs_dot_f64_noalloc(const double *x, const double *y, int64_t n,
+                              double *result, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
