@@ -52,7 +52,7 @@ struct Vec {
 // [blk[b], blk[b+1]); a block holds at most kBlkRows rows and kBlkNnz
 // nonzeros unless it is a single row longer than kBlkNnz ("long row").
 constexpr int kBlkRows = 256;
-constexpr int kBlkNnz = 2048;
+constexpr int kBlkNnz = 1792;
 
 struct Csr {
 	int magic = kMagicCsr;

@@ -13,8 +13,8 @@
 
 namespace fsg {
 
-int spmv_grid(Ctx *ctx, int nblk) {
-	int cap = ctx->sms * 6;
+int spmv_grid(Ctx *ctx, int nblk, int per_sm) {
+	int cap = ctx->sms * std::min(per_sm, 8);
 	return std::max(1, std::min(nblk, cap));
 }
 
@@ -176,7 +176,8 @@ int ensure_transpose(Csr *A) {
 			}
 		std::vector<int> tb = row_blocks(cp);
 		size_t padded = (size_t)((nnz + 15) / 16 * 16 + 16);
-		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_colptr, (m + 1) * sizeof(int)));
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_colptr, (m + 1 + 16) * sizeof(int)));
+		FS_CUDA_TRY(ctx, cudaMemset(A->t_colptr, 0, (m + 1 + 16) * sizeof(int)));
 		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_row, padded * sizeof(int)));
 		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_perm, padded * sizeof(int)));
 		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_val, padded * sizeof(double)));
@@ -279,12 +280,13 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 		cudaGetLastError();
 		return set_err(ctx, st, "fs_csr_create: device allocation or copy failed");
 	};
-	if (cudaMalloc(&A->rowptr, (nrows + 1) * sizeof(int)) != cudaSuccess ||
+	if (cudaMalloc(&A->rowptr, (nrows + 1 + 16) * sizeof(int)) != cudaSuccess ||
 	    cudaMalloc(&A->col, padded * sizeof(int)) != cudaSuccess ||
 	    cudaMalloc(&A->val, padded * sizeof(double)) != cudaSuccess ||
 	    cudaMalloc(&A->blk, blk.size() * sizeof(int)) != cudaSuccess)
 		return fail(FS_ERR_OUT_OF_MEMORY);
-	if (cudaMemcpy(A->rowptr, rp.data(), (nrows + 1) * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+	if (cudaMemset(A->rowptr, 0, (nrows + 1 + 16) * sizeof(int)) != cudaSuccess ||
+	    cudaMemcpy(A->rowptr, rp.data(), (nrows + 1) * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
 	    cudaMemcpy(A->col, ci.data(), padded * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
 	    cudaMemset(A->val, 0, padded * sizeof(double)) != cudaSuccess ||
 	    (nnz > 0 && cudaMemcpy(A->val, val, nnz * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) ||

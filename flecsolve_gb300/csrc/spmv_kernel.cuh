@@ -8,14 +8,14 @@
 // stride, so every partial sum has a fixed owner and the reductions fused into
 // the epilogue are deterministic.
 //
-// Per block: the contiguous nonzero span [rowptr[r0], rowptr[r1]) is staged
-// into shared memory with coalesced loads (the values with 16-byte vector
-// loads), then one thread per row accumulates its row from shared memory with
-// x gathered through the read-only path (x of a 7-point stencil is re-used by
-// neighbouring blocks out of L2).
+// Per block: the contiguous nonzero span [rowptr[r0], rowptr[r1]) and the
+// block's row offsets are copied into shared memory with 16-byte cp.async
+// copies of their aligned covers, then one thread per row accumulates its row
+// from shared memory with x gathered through the read-only path (x of a
+// 7-point stencil is re-used by neighbouring blocks out of L2).
 //
-// EXACT mode stages the rounded products a_k * x[c_k] instead and sums them
-// left to right per row, which is the reference's operation order bit for bit.
+// EXACT mode rounds every product a_k * x[c_k] and adds the products left to
+// right per row, which is the reference's operation order bit for bit.
 #pragma once
 
 #include <type_traits>
@@ -84,13 +84,35 @@ struct AccF {
 template<class V, int NV>
 using Acc = std::conditional_t<std::is_same_v<V, double>, AccD<NV>, AccF<NV>>;
 
-// shared staging: values (or products) and column ids of one row block
+// One pipeline stage: the 16-byte aligned cover of a row block's values,
+// column ids and row offsets, plus the block's bounds.
 template<class V>
-struct SpmvSmem {
-	V val[kBlkNnz];
-	int col[kBlkNnz];
-	double red[128];
+struct alignas(16) Stage {
+	V val[kBlkNnz + 16 / sizeof(V)];
+	int col[kBlkNnz + 4];
+	int rp[kBlkRows + 1 + 4];
+	int r0, r1, k0, k1;
 };
+
+template<class V>
+constexpr int kStages = sizeof(V) == 8 ? 2 : 3;  // <= 48 KB of shared memory per CTA
+
+template<class V>
+constexpr size_t spmv_smem_bytes() {
+	return sizeof(Stage<V>) * kStages<V>;
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+	const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+	asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template<int N>
+__device__ __forceinline__ void cp_async_wait() {
+	asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
@@ -107,105 +129,118 @@ __device__ __forceinline__ V xg(const V *__restrict__ x, const V *__restrict__ d
 		return __ldg(x + c);
 }
 
+// Issue the asynchronous copies of row block `b` into stage `st` (every
+// thread commits one group, possibly empty).  All global reads stay inside
+// the padded allocations: covers start at an aligned index <= the first
+// element and end < last element + 4.
+template<class V>
+__device__ __forceinline__ void stage_issue(const CsrDev<V> &A, int b, Stage<V> &st, bool valid) {
+	if (valid) {
+		constexpr int VW = 16 / sizeof(V);
+		const int r0 = A.blk[b], r1 = A.blk[b + 1];
+		const int k0 = A.rowptr[r0], k1 = A.rowptr[r1];
+		if (threadIdx.x == 0) {
+			st.r0 = r0;
+			st.r1 = r1;
+			st.k0 = k0;
+			st.k1 = k1;
+		}
+		if (k1 - k0 <= kBlkNnz) {
+			const int a0 = k0 & ~(VW - 1);
+			const int nv = (k1 - a0 + VW - 1) / VW;
+			for (int c = threadIdx.x; c < nv; c += blockDim.x)
+				cp_async16(st.val + c * VW, A.val + a0 + c * VW);
+			const int c0 = k0 & ~3;
+			const int nc = (k1 - c0 + 3) / 4;
+			for (int c = threadIdx.x; c < nc; c += blockDim.x)
+				cp_async16(st.col + c * 4, A.col + c0 + c * 4);
+			const int p0 = r0 & ~3;
+			const int np = (r1 + 1 - p0 + 3) / 4;
+			for (int c = threadIdx.x; c < np; c += blockDim.x)
+				cp_async16(st.rp + c * 4, A.rowptr + p0 + c * 4);
+		}
+	}
+	cp_async_commit();
+}
+
 // Epilogue concept (struct with):
 //   static constexpr int NV;                        fused reductions
 //   __device__ bool skip() const;                   uniform early exit
 //   __device__ void row(int r, V s, Acc<V,NV>& acc) consume row result
 //   __device__ void finish(const double* sums)      last block, thread 0
 //   double* part; unsigned* counter;                reduction scratch
+//
+// Persistent CTAs walk the row blocks b = blockIdx.x + i * gridDim.x through a
+// kStages-deep cp.async pipeline: the copies of block i + kStages - 1 are in
+// flight while block i is summed out of shared memory.
 template<class V, bool EXACT, bool SCALE, class Epi>
 __global__ void __launch_bounds__(kBlkRows)
-spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscale,
-               Epi epi) {
+spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscale, Epi epi) {
 	constexpr int NV = Epi::NV;
-	__shared__ SpmvSmem<V> sm;
+	constexpr int S = kStages<V>;
+	constexpr int VW = 16 / sizeof(V);
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	Stage<V> *stages = reinterpret_cast<Stage<V> *>(smem_raw);
+	__shared__ double red[128];
 	if (epi.skip())
 		return;
 	Acc<V, NV> acc;
 	acc.init();
 	const int tid = threadIdx.x;
-	for (int b = blockIdx.x; b < A.nblk; b += gridDim.x) {
-		const int r0 = A.blk[b], r1 = A.blk[b + 1];
-		const int k0 = A.rowptr[r0], k1 = A.rowptr[r1];
-		const int span = k1 - k0;
-		if (span > kBlkNnz) {
-			// a single long row: the CTA sums it (fixed strided order + tree)
+	const int nb = A.nblk > (int)blockIdx.x ? (A.nblk - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+#pragma unroll
+	for (int i = 0; i < S - 1; ++i)
+		stage_issue<V>(A, blockIdx.x + i * gridDim.x, stages[i], i < nb);
+	for (int i = 0; i < nb; ++i) {
+		const int ni = i + S - 1;
+		stage_issue<V>(A, blockIdx.x + ni * gridDim.x, stages[ni % S], ni < nb);
+		cp_async_wait<S - 1>();
+		__syncthreads();
+		const Stage<V> &st = stages[i % S];
+		const int r0 = st.r0, r1 = st.r1, k0 = st.k0, k1 = st.k1;
+		if (k1 - k0 > kBlkNnz) {
+			// a single long row: the CTA sums it from global memory
 			V s = V(0);
 			if constexpr (EXACT) {
-				// chunks of products summed left to right by thread 0
-				for (int c0 = k0; c0 < k1; c0 += kBlkNnz) {
-					int c1 = min(k1, c0 + kBlkNnz);
-					for (int k = c0 + tid; k < c1; k += blockDim.x)
-						sm.val[k - c0] = mul_rn(A.val[k], xg<V, SCALE>(x, dscale, A.col[k]));
-					__syncthreads();
-					if (tid == 0)
-						for (int k = 0; k < c1 - c0; ++k)
-							s = add_rn(s, sm.val[k]);
-					__syncthreads();
-				}
+				if (tid == 0)
+					for (int k = k0; k < k1; ++k)
+						s = add_rn(s, mul_rn(A.val[k], xg<V, SCALE>(x, dscale, A.col[k])));
 			}
 			else {
 				double t[1] = {0.0};
 				for (int k = k0 + tid; k < k1; k += blockDim.x)
 					t[0] = fma((double)A.val[k], (double)xg<V, SCALE>(x, dscale, A.col[k]), t[0]);
-				block_sum<1>(t, sm.red);
+				block_sum<1>(t, red);
 				s = (V)t[0];
-				__syncthreads();
 			}
 			if (tid == 0)
 				epi.row(r0, s, acc);
-			continue;
-		}
-		// stage the block's nonzeros
-		if constexpr (EXACT) {
-			for (int k = k0 + tid; k < k1; k += blockDim.x)
-				sm.val[k - k0] = mul_rn(A.val[k], xg<V, SCALE>(x, dscale, A.col[k]));
 		}
 		else {
-			// 16-byte vector loads over the aligned cover of [k0, k1)
-			constexpr int VW = 16 / sizeof(V);
-			using VT = std::conditional_t<std::is_same_v<V, double>, double2, float4>;
-			const int a0 = k0 & ~(VW - 1);
-			for (int k = a0 + tid * VW; k < k1; k += blockDim.x * VW) {
-				VT q = __ldg(reinterpret_cast<const VT *>(A.val + k));
-				const V *qv = reinterpret_cast<const V *>(&q);
-#pragma unroll
-				for (int e = 0; e < VW; ++e)
-					if (k + e >= k0 && k + e < k1)
-						sm.val[k + e - k0] = qv[e];
+			const int r = r0 + tid;
+			if (r < r1) {
+				const int p0 = r0 & ~3, a0 = k0 & ~(VW - 1), c0 = k0 & ~3;
+				const int kb = st.rp[r - p0], ke = st.rp[r + 1 - p0];
+				V s = V(0);
+				for (int k = kb; k < ke; ++k) {
+					const V a = st.val[k - a0];
+					const V xv = xg<V, SCALE>(x, dscale, st.col[k - c0]);
+					if constexpr (EXACT)
+						s = add_rn(s, mul_rn(a, xv));
+					else
+						s = fma(a, xv, s);
+				}
+				epi.row(r, s, acc);
 			}
-			const int c0 = k0 & ~3;
-			for (int k = c0 + tid * 4; k < k1; k += blockDim.x * 4) {
-				int4 q = __ldg(reinterpret_cast<const int4 *>(A.col + k));
-				const int *qc = reinterpret_cast<const int *>(&q);
-#pragma unroll
-				for (int e = 0; e < 4; ++e)
-					if (k + e >= k0 && k + e < k1)
-						sm.col[k + e - k0] = qc[e];
-			}
-		}
-		__syncthreads();
-		const int r = r0 + tid;
-		if (r < r1) {
-			const int a = A.rowptr[r] - k0, e = A.rowptr[r + 1] - k0;
-			V s = V(0);
-			if constexpr (EXACT) {
-				for (int k = a; k < e; ++k)
-					s = add_rn(s, sm.val[k]);
-			}
-			else {
-				for (int k = a; k < e; ++k)
-					s = fma(sm.val[k], xg<V, SCALE>(x, dscale, sm.col[k]), s);
-			}
-			epi.row(r, s, acc);
 		}
 		__syncthreads();
 	}
+	cp_async_wait<0>();
 	if constexpr (NV > 0) {
-		acc.to_part(epi.part, sm.red);
+		acc.to_part(epi.part, red);
 		if (last_block(epi.counter)) {
 			double sums[NV];
-			sum_partials<NV>(epi.part, gridDim.x, sums, sm.red);
+			sum_partials<NV>(epi.part, gridDim.x, sums, red);
 			if (tid == 0) {
 				epi.finish(sums);
 				*epi.counter = 0;
@@ -241,15 +276,25 @@ struct EpiResidual {
 	__device__ void finish(const double *) const {}
 };
 
-// grid size of the persistent SpMV for this matrix
-int spmv_grid(Ctx *ctx, int nblk);
+// persistent grid: resident CTAs per SM (from the occupancy of this
+// instantiation) x SMs, capped by the number of row blocks
+int spmv_grid(Ctx *ctx, int nblk, int per_sm);
 
 template<class V, bool EXACT, bool SCALE, class Epi>
 inline int launch_spmv(Ctx *ctx, const Csr *A, const V *vals, const V *x,
                        const V *dscale, const Epi &epi) {
+	static int per_sm = 0;  // resident CTAs per SM of this instantiation
+	constexpr size_t smem = spmv_smem_bytes<V>();
+	if (per_sm == 0) {
+		int nb = 0;
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_rb_kernel<V, EXACT, SCALE, Epi>,
+		                                                  kBlkRows, smem) != cudaSuccess || nb < 1)
+			nb = 1;
+		per_sm = nb;
+	}
 	CsrDev<V> d{A->rowptr, A->col, vals, A->blk, A->nblk};
-	int g = spmv_grid(ctx, A->nblk);
-	spmv_rb_kernel<V, EXACT, SCALE, Epi><<<g, kBlkRows, 0, ctx->stream>>>(d, x, dscale, epi);
+	int g = spmv_grid(ctx, A->nblk, per_sm);
+	spmv_rb_kernel<V, EXACT, SCALE, Epi><<<g, kBlkRows, smem, ctx->stream>>>(d, x, dscale, epi);
 	return check_launch(ctx, "spmv");
 }
 
