@@ -34,6 +34,8 @@ int check_launch(Ctx *ctx, const char *what) {
 	return FS_OK;
 }
 
+// every elementwise / reduction grid is at most 8 CTAs per SM; the solver
+// partials buffers are sized on that bound
 int grid_for(Ctx *ctx, int64_t n, int threads, int per_thread) {
 	int64_t want = (n + (int64_t)threads * per_thread - 1) / ((int64_t)threads * per_thread);
 	int64_t cap = (int64_t)ctx->sms * 8;

@@ -685,9 +685,11 @@ int solver_alloc(Solver *s) {
 		FS_TRY(dalloc(s, (void **)&s->w32[i], n32));
 	FS_TRY(dalloc(s, (void **)&s->st, sizeof(KState)));
 	FS_TRY(dalloc(s, (void **)&s->st_in, sizeof(KState)));
-	FS_TRY(dalloc(s, (void **)&s->part, sizeof(double) * (size_t)ctx->sms * 8 * 4 + 1024));
+	// reduction partials: up to 8 CTAs per SM, up to 32 values per CTA (the
+	// GMRES multi-dot of gmres.cu); every kernel's grid is <= 8 * SMs
+	FS_TRY(dalloc(s, (void **)&s->part, sizeof(double) * (size_t)ctx->sms * 8 * kPartPerBlock + 1024));
 	FS_TRY(dalloc(s, (void **)&s->counter, 64));
-	FS_TRY(dalloc(s, (void **)&s->hdev, sizeof(double) * 4096));
+	FS_TRY(dalloc(s, (void **)&s->hdev, s->method == FS_GMRES ? sizeof(GmState) : sizeof(double) * 4096));
 	cudaError_t e = cudaMallocHost(&s->hst, sizeof(KState));
 	if (e != cudaSuccess)
 		return set_err(ctx, FS_ERR_OUT_OF_MEMORY, "pinned state allocation failed");
@@ -704,7 +706,7 @@ int solver_alloc(Solver *s) {
 	return FS_OK;
 }
 
-static int ensure_hist(Solver *s, int cap) {
+int solver_hist(Solver *s, int cap) {
 	if (cap <= s->hist_cap && s->hist)
 		return FS_OK;
 	if (s->hist)
@@ -862,7 +864,7 @@ static int init_state(Solver *s, KState *dst, double rtol, int maxiter) {
 	return FS_OK;
 }
 
-static int norms(Solver *s, Vec *b, Vec *x, bool with_x, int gmres_rule) {
+int solver_norms(Solver *s, Vec *b, Vec *x, bool with_x, int gmres_rule) {
 	Ctx *ctx = s->ctx;
 	const int G = red_grid(ctx, s->n);
 	k_norms<double><<<G, kThreads, 0, ctx->stream>>>(s->n, (const double *)b->d,
@@ -891,9 +893,9 @@ static int cg_apply64(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	const bool zg = s->set.base.use_zero_guess != 0;
 	const int PK = s->dinv64() ? 1 : 0;
 	double *r = s->w64[0], *p = s->w64[1];
-	FS_TRY(ensure_hist(s, std::max(1, s->set.base.maxiter)));
+	FS_TRY(solver_hist(s, std::max(1, s->set.base.maxiter)));
 	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, s->set.base.maxiter));
-	FS_TRY(norms(s, b, x, !zg, 0));
+	FS_TRY(solver_norms(s, b, x, !zg, 0));
 	if (zg) {
 		k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
 		FS_TRY(check_launch(ctx, "fill"));
@@ -956,9 +958,9 @@ static int cg_apply_mixed(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	double *r64 = s->w64[0];
 	float *r32 = s->w32[0], *p32 = s->w32[1], *d32 = s->w32[3];
 	const int maxiter = s->set.base.maxiter;
-	FS_TRY(ensure_hist(s, std::max(1, maxiter)));
+	FS_TRY(solver_hist(s, std::max(1, maxiter)));
 	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, maxiter));
-	FS_TRY(norms(s, b, x, !zg, 0));
+	FS_TRY(solver_norms(s, b, x, !zg, 0));
 	if (zg) {
 		k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
 		FS_TRY(check_launch(ctx, "fill"));
@@ -1086,9 +1088,9 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	const float *dinv = s->dinv32();
 	const int maxiter = s->set.base.maxiter;
 	const double delta = s->set.inner_rtol > 0 ? s->set.inner_rtol : 0.1;
-	FS_TRY(ensure_hist(s, std::max(1, maxiter)));
+	FS_TRY(solver_hist(s, std::max(1, maxiter)));
 	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, maxiter));
-	FS_TRY(norms(s, b, x, !zg, 0));
+	FS_TRY(solver_norms(s, b, x, !zg, 0));
 	if (zg) {
 		k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
 		FS_TRY(check_launch(ctx, "fill"));
@@ -1243,9 +1245,9 @@ static int bicgstab_apply64(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	const bool zg = s->set.base.use_zero_guess != 0;
 	const int PK = s->dinv64() ? 1 : 0;
 	double *res = s->w64[0], *rt = s->w64[1], *p = s->w64[2], *v = s->w64[3];
-	FS_TRY(ensure_hist(s, std::max(1, s->set.base.maxiter)));
+	FS_TRY(solver_hist(s, std::max(1, s->set.base.maxiter)));
 	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, s->set.base.maxiter));
-	FS_TRY(norms(s, b, x, !zg, 0));
+	FS_TRY(solver_norms(s, b, x, !zg, 0));
 	if (zg) {
 		k_copy<double><<<G, kThreads, 0, ctx->stream>>>(n, (const double *)b->d, res);
 		FS_TRY(check_launch(ctx, "copy"));

@@ -44,6 +44,21 @@ struct KState {
 	int pad_;
 };
 
+// GMRES least-squares state (gmres.cu): Hessenberg (column-major, ld = m+1),
+// rotations, right-hand side, back-solve result, the projections of the step
+constexpr int kGmMaxDim = 100;  // gmres.hh:31 krylov_dim_bound
+constexpr int kPartPerBlock = 32;  // partial sums per CTA a solver kernel may write
+struct GmState {
+	double H[(kGmMaxDim + 1) * (kGmMaxDim + 1)];
+	double cs[kGmMaxDim + 1], sn[kGmMaxDim + 1], dw[kGmMaxDim + 1], dy[kGmMaxDim + 1];
+	double h1[kGmMaxDim + 1], h2[kGmMaxDim + 1];
+	double vnorm;  // H(k+1,k) before the rotation
+	int k;         // current Krylov dimension
+	int ld;        // Hessenberg leading dimension (min(m, maxiter) + 1)
+	int m;         // max_krylov_dim
+	int pad_;
+};
+
 struct Precond {
 	int kind = FS_PRECOND_NONE;
 	Vec *diag = nullptr;
@@ -74,6 +89,7 @@ struct Solver {
 	double *w64[12] = {};
 	float *w32[12] = {};
 	double *basis = nullptr;          // GMRES: (m + 1) x n, column j contiguous
+	int basis_cols = 0;
 	double *hdev = nullptr;           // GMRES: dot results scratch
 	KState *st = nullptr;             // device
 	KState *hst = nullptr;            // pinned mirror
@@ -101,6 +117,8 @@ inline int red_grid(Ctx *ctx, int64_t n) { return grid_for(ctx, n, 256, 8); }
 int solver_alloc(Solver *s);
 int graph_run(Solver *s, const GraphKey &key, int (*body)(Solver *, void *), void *arg);
 int read_state(Solver *s);
+int solver_norms(Solver *s, Vec *b, Vec *x, bool with_x, int gmres_rule);
+int solver_hist(Solver *s, int cap);
 int ensure_val32(Csr *A);
 int ensure_dinv(Csr *A);
 

@@ -222,13 +222,26 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 				const int p0 = r0 & ~3, a0 = k0 & ~(VW - 1), c0 = k0 & ~3;
 				const int kb = st.rp[r - p0], ke = st.rp[r + 1 - p0];
 				V s = V(0);
-				for (int k = kb; k < ke; ++k) {
-					const V a = st.val[k - a0];
-					const V xv = xg<V, SCALE>(x, dscale, st.col[k - c0]);
-					if constexpr (EXACT)
-						s = add_rn(s, mul_rn(a, xv));
-					else
-						s = fma(a, xv, s);
+				// batches of 8: all gathers of a batch are issued before the
+				// first product, so a 7-point row costs one L2 round trip
+				for (int kc = kb; kc < ke; kc += 8) {
+					V a[8], xv[8];
+#pragma unroll
+					for (int j = 0; j < 8; ++j) {
+						if (kc + j < ke) {
+							a[j] = st.val[kc + j - a0];
+							xv[j] = xg<V, SCALE>(x, dscale, st.col[kc + j - c0]);
+						}
+					}
+#pragma unroll
+					for (int j = 0; j < 8; ++j) {
+						if (kc + j < ke) {
+							if constexpr (EXACT)
+								s = add_rn(s, mul_rn(a[j], xv[j]));
+							else
+								s = fma(a[j], xv[j], s);
+						}
+					}
 				}
 				epi.row(r, s, acc);
 			}

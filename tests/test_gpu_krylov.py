@@ -190,3 +190,91 @@ def test_mixed_cg_refinement(ctx, wl):
                         inner_rtol=1e-4)
     assert info3.status == "converged_rtol"
     assert _rel(x3, xs) <= X_RTOL_MIXED
+
+
+# ------------------------------------------------------------------ GMRES --
+
+GMRES_CASES = [n for n, c in sorted(META["cases"].items()) if c["method"] == "gmres"]
+
+
+def _run_gmres(ctx, A, b, x0=None, prec="jacobi", diag=None, **kw):
+    return _run(ctx, fs.gmres, A, b, x0, prec, diag, **kw)
+
+
+@pytest.mark.parametrize("ortho", ["cgs2", "mgs"])
+@pytest.mark.parametrize("name", GMRES_CASES)
+def test_gmres_against_reference_fixture(ctx, name, ortho):
+    c = META["cases"][name]
+    A, b = P.workload(c["workload"])
+    kw = dict(c["kwargs"])
+    x0 = P.uniform(int(c["x0"][1]), A.nrows, 0.0, 1.0) if c["x0"] else None
+    prec = kw.pop("precond", "jacobi")
+    rtol = kw.pop("rtol", 1e-8)
+    info, x, _ = _run_gmres(ctx, A, b, x0, prec, maxiter=kw.pop("maxiter", 2000), rtol=rtol,
+                            use_zero_guess=x0 is None, max_krylov_dim=kw.pop("krylov_dim", 30),
+                            pre_side=kw.pop("side", "right"), restart=kw.pop("restart", True),
+                            ortho=ortho)
+    g = np.load(GOLD / f"{name}.npz")
+    assert info.status == c["status"]
+    assert abs(info.iters - c["iters"]) <= ITER_TOL
+    if c["status"] == "converged_rtol":
+        assert abs(info.restarts - c["restarts"]) <= 1
+        # GMRES stops on its Arnoldi residual estimate, which for left
+        # preconditioning is the preconditioned residual: the bar is the
+        # reference's own true residual (or rtol, whichever is larger)
+        ref_rr = _true_relres(A, b, g["x"])
+        assert _true_relres(A, b, x) <= 1.5 * max(rtol, ref_rr)
+        _bicgstab_accuracy_bar(A, b, x, g["x"])
+    else:
+        # no convergence: the same number of Krylov steps gives the same
+        # minimal-residual iterate up to rounding
+        assert _rel(x, g["x"]) <= 1e-8
+
+
+def test_gmres_restart_consistency(ctx):
+    """gmres.cc:186-208: a restarted run equals 50 steps + a fresh run
+    started from their result (same iteration total, same final residual)."""
+    A, b = P.workload("convdiff3d-12")  # restarted run converges in 74 (> 50)
+    x0 = P.uniform(1, A.nrows, 0.0, 1.0)
+    dA = fs.CSR(ctx, A)
+    vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, x0)
+    mk = lambda **kw: fs.gmres.solver(fs.gmres.settings(rtol=1e-4, use_zero_guess=False, **kw))(dA, fs.op.I)
+    info_restart = mk(maxiter=100, max_krylov_dim=50, restart=True)(vb, vx)
+    vx.upload(x0)
+    mk(maxiter=50, max_krylov_dim=50, restart=True)(vb, vx)
+    info = mk(maxiter=100, max_krylov_dim=100, restart=False)(vb, vx)
+    assert info_restart.status == "converged_rtol"
+    assert 50 + info.iters == info_restart.iters
+    assert info.res_norm_final == info_restart.res_norm_final
+
+
+def test_gmres_diagnostic_every_iteration(ctx):
+    A, b = P.workload("convdiff3d-12")
+    calls = []
+    info, x, _ = _run_gmres(ctx, A, b, diag=lambda xv, r: calls.append(r) or False,
+                            maxiter=500, rtol=1e-8, max_krylov_dim=10, restart=True)
+    assert info.status == "converged_rtol" and len(calls) == info.iters
+    r = O.solve("gmres", A, b, maxiter=500, rtol=1e-8, krylov_dim=10)
+    assert abs(info.iters - r.iters) <= ITER_TOL
+    info2, _, _ = _run_gmres(ctx, A, b, diag=lambda xv, r: len(calls) > 10**9 or r < 1e3,
+                             maxiter=500, rtol=1e-8, max_krylov_dim=10, restart=True)
+    assert info2.status == "converged_user" and info2.iters >= 1
+
+
+def test_gmres_validate_rejects_reference_asserts(ctx):
+    A, b = P.workload("poisson2d-8")
+    with pytest.raises(fs.api._lib.FsError) as ei:
+        _run_gmres(ctx, A, b, maxiter=10, max_krylov_dim=5, restart=False)
+    assert ei.value.status == fs.api._lib.ERR_BREAKDOWN
+    with pytest.raises(fs.api._lib.FsError):
+        _run_gmres(ctx, A, b, maxiter=1000, max_krylov_dim=101, restart=True)
+
+
+@pytest.mark.parametrize("wl", ["convdiff3d-24", "diffusion3d-20"])
+def test_gmres_cgs2_vs_oracle(ctx, wl):
+    A, b = P.workload(wl)
+    r = O.solve("gmres", A, b, maxiter=5000, rtol=1e-8, krylov_dim=30)
+    info, x, _ = _run_gmres(ctx, A, b, maxiter=5000, rtol=1e-8, max_krylov_dim=30, restart=True)
+    assert info.status == r.status == "converged_rtol"
+    assert abs(info.iters - r.iters) <= ITER_TOL
+    _bicgstab_accuracy_bar(A, b, x, r.x)
