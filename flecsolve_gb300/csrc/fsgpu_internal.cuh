@@ -64,6 +64,7 @@ struct Csr {
 	float *val32 = nullptr;    // float copy, built on first use
 	bool val32_valid = false;
 	int *blk = nullptr;        // row blocks, nblk + 1
+	int4 *blkinfo = nullptr;   // per block {r0, r1, rowptr[r0], rowptr[r1]}
 	int nblk = 0;
 	double *dinv = nullptr;    // 1 / a_ii, built on first use
 	float *dinv32 = nullptr;
@@ -74,6 +75,7 @@ struct Csr {
 	int *t_perm = nullptr;     // nnz: CSC slot -> CSR slot
 	double *t_val = nullptr;   // nnz
 	int *t_blk = nullptr;
+	int4 *t_blkinfo = nullptr;
 	int t_nblk = 0;
 	bool t_valid = false;
 	bool t_vals_valid = false;

@@ -41,6 +41,13 @@ static std::vector<int> row_blocks(const std::vector<int> &rp) {
 	return blk;
 }
 
+static std::vector<int4> block_info(const std::vector<int> &blk, const std::vector<int> &rp) {
+	std::vector<int4> info(blk.size() > 0 ? blk.size() - 1 : 0);
+	for (size_t b = 0; b + 1 < blk.size(); ++b)
+		info[b] = make_int4(blk[b], blk[b + 1], rp[blk[b]], rp[blk[b + 1]]);
+	return info;
+}
+
 __global__ void to_f32_kernel(int64_t n, const double *__restrict__ a, float *__restrict__ b) {
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
 	     i += (int64_t)gridDim.x * blockDim.x)
@@ -175,6 +182,7 @@ int ensure_transpose(Csr *A) {
 				perm[slot] = k;
 			}
 		std::vector<int> tb = row_blocks(cp);
+		std::vector<int4> tinfo = block_info(tb, cp);
 		size_t padded = (size_t)((nnz + 15) / 16 * 16 + 16);
 		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_colptr, (m + 1 + 16) * sizeof(int)));
 		FS_CUDA_TRY(ctx, cudaMemset(A->t_colptr, 0, (m + 1 + 16) * sizeof(int)));
@@ -182,6 +190,10 @@ int ensure_transpose(Csr *A) {
 		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_perm, padded * sizeof(int)));
 		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_val, padded * sizeof(double)));
 		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_blk, tb.size() * sizeof(int)));
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->t_blkinfo, std::max<size_t>(1, tinfo.size()) * sizeof(int4)));
+		if (!tinfo.empty())
+			FS_CUDA_TRY(ctx, cudaMemcpy(A->t_blkinfo, tinfo.data(), tinfo.size() * sizeof(int4),
+			                            cudaMemcpyHostToDevice));
 		FS_CUDA_TRY(ctx, cudaMemset(A->t_row, 0, padded * sizeof(int)));
 		FS_CUDA_TRY(ctx, cudaMemset(A->t_val, 0, padded * sizeof(double)));
 		FS_CUDA_TRY(ctx, cudaMemcpy(A->t_colptr, cp.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
@@ -214,6 +226,7 @@ int transpose_spmv(Csr *A, const double *x, double *y) {
 	T.col = A->t_row;
 	T.val = A->t_val;
 	T.blk = A->t_blk;
+	T.blkinfo = A->t_blkinfo;
 	T.nblk = A->t_nblk;
 	int st = launch_spmv<double, false, false>(A->ctx, &T, A->t_val, x, nullptr,
 	                                           EpiStore<double>{y});
@@ -222,6 +235,7 @@ int transpose_spmv(Csr *A, const double *x, double *y) {
 	T.col = nullptr;
 	T.val = nullptr;
 	T.blk = nullptr;
+	T.blkinfo = nullptr;
 	return st;
 }
 
@@ -263,6 +277,7 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 		ci[k] = (int)c;
 	}
 	std::vector<int> blk = row_blocks(rp);
+	std::vector<int4> binfo = block_info(blk, rp);
 
 	Csr *A = new Csr();
 	A->ctx = ctx;
@@ -276,6 +291,7 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 		cudaFree(A->col);
 		cudaFree(A->val);
 		cudaFree(A->blk);
+		cudaFree(A->blkinfo);
 		delete A;
 		cudaGetLastError();
 		return set_err(ctx, st, "fs_csr_create: device allocation or copy failed");
@@ -283,14 +299,17 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 	if (cudaMalloc(&A->rowptr, (nrows + 1 + 16) * sizeof(int)) != cudaSuccess ||
 	    cudaMalloc(&A->col, padded * sizeof(int)) != cudaSuccess ||
 	    cudaMalloc(&A->val, padded * sizeof(double)) != cudaSuccess ||
-	    cudaMalloc(&A->blk, blk.size() * sizeof(int)) != cudaSuccess)
+	    cudaMalloc(&A->blk, blk.size() * sizeof(int)) != cudaSuccess ||
+	    cudaMalloc(&A->blkinfo, std::max<size_t>(1, binfo.size()) * sizeof(int4)) != cudaSuccess)
 		return fail(FS_ERR_OUT_OF_MEMORY);
 	if (cudaMemset(A->rowptr, 0, (nrows + 1 + 16) * sizeof(int)) != cudaSuccess ||
 	    cudaMemcpy(A->rowptr, rp.data(), (nrows + 1) * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
 	    cudaMemcpy(A->col, ci.data(), padded * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
 	    cudaMemset(A->val, 0, padded * sizeof(double)) != cudaSuccess ||
 	    (nnz > 0 && cudaMemcpy(A->val, val, nnz * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) ||
-	    cudaMemcpy(A->blk, blk.data(), blk.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+	    cudaMemcpy(A->blk, blk.data(), blk.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+	    (!binfo.empty() && cudaMemcpy(A->blkinfo, binfo.data(), binfo.size() * sizeof(int4),
+	                                  cudaMemcpyHostToDevice) != cudaSuccess))
 		return fail(FS_ERR_CUDA);
 	*out = reinterpret_cast<fs_csr>(A);
 	return FS_OK;
@@ -302,8 +321,9 @@ FS_API int fs_csr_destroy(fs_csr h) {
 		return FS_ERR_BAD_HANDLE;
 	cudaStreamSynchronize(A->ctx->stream);
 	for (void *p : {(void *)A->rowptr, (void *)A->col, (void *)A->val, (void *)A->val32,
-	                (void *)A->blk, (void *)A->dinv, (void *)A->dinv32, (void *)A->t_colptr,
-	                (void *)A->t_row, (void *)A->t_perm, (void *)A->t_val, (void *)A->t_blk})
+	                (void *)A->blk, (void *)A->blkinfo, (void *)A->dinv, (void *)A->dinv32,
+	                (void *)A->t_colptr, (void *)A->t_row, (void *)A->t_perm, (void *)A->t_val,
+	                (void *)A->t_blk, (void *)A->t_blkinfo})
 		if (p)
 			cudaFree(p);
 	A->magic = 0;

@@ -29,7 +29,7 @@ struct CsrDev {
 	const int *__restrict__ rowptr;
 	const int *__restrict__ col;
 	const V *__restrict__ val;
-	const int *__restrict__ blk;
+	const int4 *__restrict__ info;  // per row block {r0, r1, k0, k1}
 	int nblk;
 };
 
@@ -129,16 +129,15 @@ __device__ __forceinline__ V xg(const V *__restrict__ x, const V *__restrict__ d
 		return __ldg(x + c);
 }
 
-// Issue the asynchronous copies of row block `b` into stage `st` (every
-// thread commits one group, possibly empty).  All global reads stay inside
-// the padded allocations: covers start at an aligned index <= the first
-// element and end < last element + 4.
+// Issue the asynchronous copies of a row block (bounds m = {r0, r1, k0, k1})
+// into stage `st`; every thread commits one group, possibly empty.  All global
+// reads stay inside the padded allocations: covers start at an aligned index
+// <= the first element and end < last element + 4.
 template<class V>
-__device__ __forceinline__ void stage_issue(const CsrDev<V> &A, int b, Stage<V> &st, bool valid) {
+__device__ __forceinline__ void stage_issue(const CsrDev<V> &A, int4 m, Stage<V> &st, bool valid) {
 	if (valid) {
 		constexpr int VW = 16 / sizeof(V);
-		const int r0 = A.blk[b], r1 = A.blk[b + 1];
-		const int k0 = A.rowptr[r0], k1 = A.rowptr[r1];
+		const int r0 = m.x, r1 = m.y, k0 = m.z, k1 = m.w;
 		if (threadIdx.x == 0) {
 			st.r0 = r0;
 			st.r1 = r1;
@@ -161,6 +160,12 @@ __device__ __forceinline__ void stage_issue(const CsrDev<V> &A, int b, Stage<V> 
 		}
 	}
 	cp_async_commit();
+}
+
+// bounds of the i-th row block of this CTA (a dummy past the end)
+template<class V>
+__device__ __forceinline__ int4 block_meta(const CsrDev<V> &A, int i, int nb) {
+	return i < nb ? __ldg(A.info + blockIdx.x + i * gridDim.x) : make_int4(0, 0, 0, 0);
 }
 
 // Epilogue concept (struct with):
@@ -190,10 +195,14 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 	const int nb = A.nblk > (int)blockIdx.x ? (A.nblk - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 #pragma unroll
 	for (int i = 0; i < S - 1; ++i)
-		stage_issue<V>(A, blockIdx.x + i * gridDim.x, stages[i], i < nb);
+		stage_issue<V>(A, block_meta(A, i, nb), stages[i], i < nb);
+	// bounds are loaded one iteration before their copies are issued, so the
+	// issue never waits on a global load
+	int4 mnext = block_meta(A, S - 1, nb);
 	for (int i = 0; i < nb; ++i) {
 		const int ni = i + S - 1;
-		stage_issue<V>(A, blockIdx.x + ni * gridDim.x, stages[ni % S], ni < nb);
+		stage_issue<V>(A, mnext, stages[ni % S], ni < nb);
+		mnext = block_meta(A, ni + 1, nb);
 		cp_async_wait<S - 1>();
 		__syncthreads();
 		const Stage<V> &st = stages[i % S];
@@ -305,7 +314,7 @@ inline int launch_spmv(Ctx *ctx, const Csr *A, const V *vals, const V *x,
 			nb = 1;
 		per_sm = nb;
 	}
-	CsrDev<V> d{A->rowptr, A->col, vals, A->blk, A->nblk};
+	CsrDev<V> d{A->rowptr, A->col, vals, A->blkinfo, A->nblk};
 	int g = spmv_grid(ctx, A->nblk, per_sm);
 	spmv_rb_kernel<V, EXACT, SCALE, Epi><<<g, kBlkRows, smem, ctx->stream>>>(d, x, dscale, epi);
 	return check_launch(ctx, "spmv");
