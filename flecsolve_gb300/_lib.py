@@ -23,10 +23,10 @@ ERR_BAD_HANDLE, ERR_SIZE_MISMATCH, ERR_OUT_OF_MEMORY, ERR_CUDA = 1, 2, 3, 4
 ERR_NON_FINITE, ERR_BREAKDOWN, ERR_INVALID_ARG, ERR_NO_DEVICE, ERR_UNSUPPORTED = 5, 6, 7, 8, 9
 
 F64, F32 = 0, 1
-CG, BICGSTAB, GMRES, CG_MIXED = 0, 1, 2, 3
+CG, BICGSTAB, GMRES, CG_MIXED, BICGSTAB_MIXED, GMRES_MIXED = 0, 1, 2, 3, 4, 5
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_DIAG, PRECOND_CSR = 0, 1, 2, 3
 LEFT, RIGHT = 0, 1
-ORTHO_CGS2, ORTHO_MGS = 0, 1
+ORTHO_CGS2, ORTHO_MGS, ORTHO_AUTO = 0, 1, 2
 REFINE_RESTART, REFINE_RELIABLE = 0, 1
 SPMV_FMA, SPMV_EXACT = 0, 1
 

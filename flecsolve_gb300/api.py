@@ -31,7 +31,7 @@ from . import _lib
 from ._lib import check, lib
 
 __all__ = ["Context", "Vector", "CSR", "SolveInfo", "Future", "op", "vec", "mat",
-           "cg", "bicgstab", "gmres", "mixed_cg"]
+           "cg", "bicgstab", "gmres", "mixed_cg", "mixed_bicgstab", "mixed_gmres"]
 
 
 class Context:
@@ -353,7 +353,7 @@ def _settings(method, maxiter, rtol, atol, use_zero_guess, **kw):
         if k == "pre_side":
             v = _lib.LEFT if v in ("left", _lib.LEFT) else _lib.RIGHT
         elif k == "ortho":
-            v = _lib.ORTHO_MGS if v in ("mgs", _lib.ORTHO_MGS) else _lib.ORTHO_CGS2
+            v = {"mgs": _lib.ORTHO_MGS, "cgs2": _lib.ORTHO_CGS2, "auto": _lib.ORTHO_AUTO}.get(v, v)
         elif k == "refine":
             v = _lib.REFINE_RELIABLE if v in ("reliable", _lib.REFINE_RELIABLE) else _lib.REFINE_RESTART
         setattr(s, k, v)
@@ -492,3 +492,5 @@ cg = _namespace(_lib.CG, 4)                 # flecsolve/solvers/cg.hh:250-270
 bicgstab = _namespace(_lib.BICGSTAB, 8)     # bicgstab.hh:193-216
 gmres = _namespace(_lib.GMRES, 104, max_krylov_dim=-1, pre_side="right", restart=False)  # gmres.hh:366-438
 mixed_cg = _namespace(_lib.CG_MIXED, 4)     # FP32 inner PCG in FP64 refinement
+mixed_bicgstab = _namespace(_lib.BICGSTAB_MIXED, 8)
+mixed_gmres = _namespace(_lib.GMRES_MIXED, 104, max_krylov_dim=-1, pre_side="right", restart=False)

@@ -24,7 +24,7 @@ namespace fsg {
 namespace {
 
 constexpr int kT = 256;
-constexpr int kChunk = 32;  // basis vectors per orthogonalisation pass
+constexpr int kChunk = 16;  // basis vectors per orthogonalisation pass
 static_assert(kChunk <= kPartPerBlock, "partials buffer holds kPartPerBlock values per CTA");
 
 #define FOR_EACH(i, n)                                                          \
@@ -41,17 +41,22 @@ __device__ __forceinline__ bool restart_pending(const KState *st) {
 // ----------------------------------------------- block multi-reduction --
 
 // Sum nv (<= kChunk) per-thread values over the block into part[b*nv + j].
-__device__ __forceinline__ void block_multi_sum(const double *vals, int nv, double *part,
+// Fully unrolled over kChunk with a predicate, so the values stay in
+// registers (a runtime-bounded loop would move them to local memory).
+__device__ __forceinline__ void block_multi_sum(const double (&vals)[kChunk], int nv, double *part,
                                                 double *sh) {
 	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	const int nw = blockDim.x >> 5;
-	for (int j = 0; j < nv; ++j) {
-		double v = vals[j];
 #pragma unroll
-		for (int o = 16; o > 0; o >>= 1)
-			v += __shfl_down_sync(0xffffffffu, v, o);
-		if (lane == 0)
-			sh[j * 8 + wid] = v;
+	for (int j = 0; j < kChunk; ++j) {
+		if (j < nv) {
+			double v = vals[j];
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1)
+				v += __shfl_down_sync(0xffffffffu, v, o);
+			if (lane == 0)
+				sh[j * 8 + wid] = v;
+		}
 	}
 	__syncthreads();
 	if ((int)threadIdx.x < nv) {
@@ -165,38 +170,50 @@ __device__ void back_solve(GmState *g) {
 // ------------------------------------------------------------- kernels --
 
 // v = A z (right: z = D^-1 V_k gathered on the fly) or v = D^-1 A V_k (left)
+template<class T>
 struct EpiScaleStore {
 	static constexpr int NV = 0;
-	double *y;
-	const double *d;
+	T *y;
+	const T *d;
 	const KState *st;
 	double *part = nullptr;
 	unsigned *counter = nullptr;
 	__device__ bool skip() const { return stopped(st); }
 	template<class A>
-	__device__ void row(int r, double s, A &) const { y[r] = d ? d[r] * s : s; }
+	__device__ void row(int r, T s, A &) const { y[r] = d ? d[r] * s : s; }
 	__device__ void finish(const double *) const {}
 };
 
+// per-thread partial dot products: FP64 fma for a double basis, FP32 fma
+// for a float basis (each thread sums a few dozen terms; the block and grid
+// folds are FP64)
+__device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
+
 // CGS2 pass 1: h1_j = v . V_j, j in [j0, j0 + nj)
+template<class T>
 __global__ void __launch_bounds__(kT)
-k_gm_dots(int64_t n, const double *__restrict__ V, int64_t ld, int j0, int nj,
-          const double *__restrict__ v, GmState *g, KState *st, double *part, unsigned *counter) {
+k_gm_dots(int64_t n, const T *__restrict__ V, int64_t ld, int j0, int nj,
+          const T *__restrict__ v, GmState *g, KState *st, double *part, unsigned *counter) {
 	__shared__ double sh[kChunk * 8];
 	if (stopped(st))
 		return;
-	double acc[kChunk];
+	T acc[kChunk];
 #pragma unroll
 	for (int j = 0; j < kChunk; ++j)
-		acc[j] = 0.0;
+		acc[j] = T(0);
 	FOR_EACH(i, n) {
-		const double vi = v[i];
+		const T vi = v[i];
 #pragma unroll
 		for (int j = 0; j < kChunk; ++j)
 			if (j < nj)
-				acc[j] = fma(vi, V[(size_t)(j0 + j) * ld + i], acc[j]);
+				acc[j] = mad(vi, V[(size_t)(j0 + j) * ld + i], acc[j]);
 	}
-	block_multi_sum(acc, nj, part, sh);
+	double accd[kChunk];
+#pragma unroll
+	for (int j = 0; j < kChunk; ++j)
+		accd[j] = (double)acc[j];
+	block_multi_sum(accd, nj, part, sh);
 	if (last_block(counter)) {
 		fold_multi(part, nj, g->h1 + j0);
 		if (threadIdx.x == 0)
@@ -205,35 +222,61 @@ k_gm_dots(int64_t n, const double *__restrict__ V, int64_t ld, int j0, int nj,
 }
 
 // CGS2 pass 2: (chunk j0 == 0 only) v -= sum_j h1_j V_j over all k + 1
-// vectors, then h2_j = v . V_j for the chunk [j0, j0 + nj)
+// vectors, then h2_j = v . V_j for the chunk [j0, j0 + nj).  When all k + 1
+// vectors fit one chunk, each V_j is loaded once and kept in registers for
+// both the update and the dot.
+template<class T>
 __global__ void __launch_bounds__(kT)
-k_gm_project_dots(int64_t n, const double *__restrict__ V, int64_t ld, int kp1, int j0, int nj,
-                  double *__restrict__ v, GmState *g, KState *st, double *part,
+k_gm_project_dots(int64_t n, const T *__restrict__ V, int64_t ld, int kp1, int j0, int nj,
+                  T *__restrict__ v, GmState *g, KState *st, double *part,
                   unsigned *counter) {
 	__shared__ double sh[kChunk * 8];
-	__shared__ double hs[kGmMaxDim + 1];
+	__shared__ T hs[kGmMaxDim + 1];
 	if (stopped(st))
 		return;
 	for (int j = threadIdx.x; j < kp1; j += blockDim.x)
-		hs[j] = g->h1[j];
+		hs[j] = (T)g->h1[j];
 	__syncthreads();
-	double acc[kChunk];
+	T acc[kChunk];
 #pragma unroll
 	for (int j = 0; j < kChunk; ++j)
-		acc[j] = 0.0;
-	FOR_EACH(i, n) {
-		double vi = v[i];
-		if (j0 == 0) {
-			for (int j = 0; j < kp1; ++j)
-				vi = fma(-hs[j], V[(size_t)j * ld + i], vi);
-			v[i] = vi;
-		}
+		acc[j] = T(0);
+	if (j0 == 0 && kp1 <= kChunk) {
+		FOR_EACH(i, n) {
+			T vr[kChunk];
+			T vi = v[i];
 #pragma unroll
-		for (int j = 0; j < kChunk; ++j)
-			if (j < nj)
-				acc[j] = fma(vi, V[(size_t)(j0 + j) * ld + i], acc[j]);
+			for (int j = 0; j < kChunk; ++j)
+				if (j < kp1) {
+					vr[j] = V[(size_t)j * ld + i];
+					vi = mad(-hs[j], vr[j], vi);
+				}
+			v[i] = vi;
+#pragma unroll
+			for (int j = 0; j < kChunk; ++j)
+				if (j < kp1)
+					acc[j] = mad(vi, vr[j], acc[j]);
+		}
 	}
-	block_multi_sum(acc, nj, part, sh);
+	else {
+		FOR_EACH(i, n) {
+			T vi = v[i];
+			if (j0 == 0) {
+				for (int j = 0; j < kp1; ++j)
+					vi = mad(-hs[j], V[(size_t)j * ld + i], vi);
+				v[i] = vi;
+			}
+#pragma unroll
+			for (int j = 0; j < kChunk; ++j)
+				if (j < nj)
+					acc[j] = mad(vi, V[(size_t)(j0 + j) * ld + i], acc[j]);
+		}
+	}
+	double accd[kChunk];
+#pragma unroll
+	for (int j = 0; j < kChunk; ++j)
+		accd[j] = (double)acc[j];
+	block_multi_sum(accd, nj, part, sh);
 	if (last_block(counter)) {
 		fold_multi(part, nj, g->h2 + j0);
 		if (threadIdx.x == 0)
@@ -243,28 +286,30 @@ k_gm_project_dots(int64_t n, const double *__restrict__ V, int64_t ld, int kp1, 
 
 // CGS2 pass 3: v -= sum_j h2_j V_j and ||v||^2; the last block assembles the
 // Hessenberg column (h1 + h2, ||v||) and finishes the step
+template<class T>
 __global__ void __launch_bounds__(kT)
-k_gm_project_norm(int64_t n, const double *__restrict__ V, int64_t ld, int kp1,
-                  double *__restrict__ v, GmState *g, KState *st, double *part,
+k_gm_project_norm(int64_t n, const T *__restrict__ V, int64_t ld, int kp1,
+                  T *__restrict__ v, GmState *g, KState *st, double *part,
                   unsigned *counter, double *hist) {
 	__shared__ double sh[128];
-	__shared__ double hs[kGmMaxDim + 1];
+	__shared__ T hs[kGmMaxDim + 1];
 	if (stopped(st))
 		return;
 	for (int j = threadIdx.x; j < kp1; j += blockDim.x)
-		hs[j] = g->h2[j];
+		hs[j] = (T)g->h2[j];
 	__syncthreads();
-	double acc[1] = {0.0};
+	T acc = T(0);
 	FOR_EACH(i, n) {
-		double vi = v[i];
+		T vi = v[i];
 		for (int j = 0; j < kp1; ++j)
-			vi = fma(-hs[j], V[(size_t)j * ld + i], vi);
+			vi = mad(-hs[j], V[(size_t)j * ld + i], vi);
 		v[i] = vi;
-		acc[0] = fma(vi, vi, acc[0]);
+		acc = mad(vi, vi, acc);
 	}
-	block_sum<1>(acc, sh);
+	double accd[1] = {(double)acc};
+	block_sum<1>(accd, sh);
 	if (threadIdx.x == 0)
-		part[blockIdx.x] = acc[0];
+		part[blockIdx.x] = accd[0];
 	if (last_block(counter)) {
 		double s[1];
 		sum_partials<1>(part, gridDim.x, s, sh);
@@ -284,29 +329,31 @@ k_gm_project_norm(int64_t n, const double *__restrict__ V, int64_t ld, int kp1,
 // MGS pass j (gmres.hh:270-278): v -= h_{j-1} V_{j-1} (j > 0), then
 // h_j = v . V_j into H(j, k); pass j == kp1 applies the last update, takes
 // ||v|| and finishes the step
+template<class T>
 __global__ void __launch_bounds__(kT)
-k_gm_mgs(int64_t n, const double *__restrict__ V, int64_t ld, int j, int kp1,
-         double *__restrict__ v, GmState *g, KState *st, double *part, unsigned *counter,
+k_gm_mgs(int64_t n, const T *__restrict__ V, int64_t ld, int j, int kp1,
+         T *__restrict__ v, GmState *g, KState *st, double *part, unsigned *counter,
          double *hist) {
 	__shared__ double sh[128];
 	if (stopped(st))
 		return;
 	const int k = g->k, ldh = g->ld;
-	const double hprev = j > 0 ? g->H[(j - 1) + ldh * k] : 0.0;
-	const double *Vp = j > 0 ? V + (size_t)(j - 1) * ld : nullptr;
-	const double *Vj = j < kp1 ? V + (size_t)j * ld : nullptr;
-	double acc[1] = {0.0};
+	const T hprev = j > 0 ? (T)g->H[(j - 1) + ldh * k] : T(0);
+	const T *Vp = j > 0 ? V + (size_t)(j - 1) * ld : nullptr;
+	const T *Vj = j < kp1 ? V + (size_t)j * ld : nullptr;
+	T acc = T(0);
 	FOR_EACH(i, n) {
-		double vi = v[i];
+		T vi = v[i];
 		if (j > 0) {
-			vi = fma(-hprev, Vp[i], vi);
+			vi = mad(-hprev, Vp[i], vi);
 			v[i] = vi;
 		}
-		acc[0] = fma(vi, j < kp1 ? Vj[i] : vi, acc[0]);
+		acc = mad(vi, j < kp1 ? Vj[i] : vi, acc);
 	}
-	block_sum<1>(acc, sh);
+	double accd[1] = {(double)acc};
+	block_sum<1>(accd, sh);
 	if (threadIdx.x == 0)
-		part[blockIdx.x] = acc[0];
+		part[blockIdx.x] = accd[0];
 	if (last_block(counter)) {
 		double s[1];
 		sum_partials<1>(part, gridDim.x, s, sh);
@@ -327,12 +374,13 @@ k_gm_mgs(int64_t n, const double *__restrict__ V, int64_t ld, int j, int kp1,
 
 // basis_{k+1} = v * (1 / vnorm), or v itself when vnorm == 0
 // (gmres.hh:156-162); unused (and skipped) once the step stopped or restarts
-__global__ void k_gm_normalize(int64_t n, const double *__restrict__ v, double *__restrict__ out,
+template<class T>
+__global__ void k_gm_normalize(int64_t n, const T *__restrict__ v, T *__restrict__ out,
                                const GmState *g, const KState *st) {
 	if (stopped(st))
 		return;
 	const double vn = g->vnorm;
-	const double inv = vn != 0.0 ? 1.0 / vn : 1.0;
+	const T inv = (T)(vn != 0.0 ? 1.0 / vn : 1.0);
 	FOR_EACH(i, n) out[i] = vn != 0.0 ? v[i] * inv : v[i];
 }
 
@@ -345,10 +393,11 @@ __global__ void k_gm_backsolve(GmState *g, const KState *st) {
 }
 
 // correct (gmres.hh:244-263) with nr = k - 1: right: z = sum_i dy_i V_i
-// accumulated left to right, x += 1.0 * P z; left: x += dy_i V_i in order
-template<bool GATED>
+// accumulated left to right, x += 1.0 * P z; left: x += dy_i V_i in order.
+// x and the accumulation are FP64 for either basis type.
+template<bool GATED, class T>
 __global__ void __launch_bounds__(kT)
-k_gm_correct(int64_t n, const double *__restrict__ V, int64_t ld, const GmState *g,
+k_gm_correct(int64_t n, const T *__restrict__ V, int64_t ld, const GmState *g,
              const double *__restrict__ dinv, double *__restrict__ x, int right, const KState *st) {
 	if (GATED && !restart_pending(st))
 		return;
@@ -363,14 +412,14 @@ k_gm_correct(int64_t n, const double *__restrict__ V, int64_t ld, const GmState 
 		if (right) {
 			double z = 0.0;
 			for (int j = 0; j <= nr; ++j)
-				z = fma(dy[j], V[(size_t)j * ld + i], z);
+				z = fma(dy[j], (double)V[(size_t)j * ld + i], z);
 			const double pz = dinv ? dinv[i] * z : z;
 			x[i] = fma(1.0, pz, x[i]);
 		}
 		else {
 			double xi = x[i];
 			for (int j = 0; j <= nr; ++j)
-				xi = fma(dy[j], V[(size_t)j * ld + i], xi);
+				xi = fma(dy[j], (double)V[(size_t)j * ld + i], xi);
 			x[i] = xi;
 		}
 	}
@@ -401,15 +450,15 @@ struct EpiGmResidual {
 
 // basis_0 = res * (1 / beta), dw[0] = beta, k = 0 (gmres.hh:134-139,
 // 218-224); the restart variant also counts the restart and clears the flag
-template<bool RESTART>
+template<bool RESTART, class T>
 __global__ void __launch_bounds__(kT)
-k_gm_basis0(int64_t n, const double *__restrict__ res, double *__restrict__ V0, GmState *g,
+k_gm_basis0(int64_t n, const double *__restrict__ res, T *__restrict__ V0, GmState *g,
             KState *st, unsigned *counter) {
 	if (RESTART && !restart_pending(st))
 		return;
 	const double beta = st->aux[2];
 	const double inv = 1.0 / beta;
-	FOR_EACH(i, n) V0[i] = res[i] * inv;
+	FOR_EACH(i, n) V0[i] = (T)(res[i] * inv);
 	if (last_block(counter) && threadIdx.x == 0) {
 		g->dw[0] = beta;
 		g->k = 0;
@@ -439,67 +488,121 @@ __global__ void k_gm_start(GmState *g, KState *st, int m, int ld) {
 	}
 }
 
+// Mixed precision: a cycle ends on the Arnoldi estimate (converged, maxiter
+// or k == m); the stopping decision is then taken on the FP64 true residual
+// that the restart tail computed into aux[2].
+__global__ void k_gm_mixed_decide(KState *st) {
+	if (st->done)
+		return;
+	const double beta = st->aux[2];
+	st->res = beta;
+	if (!isfinite(beta))
+		st->flags |= KF_NONFINITE;
+	if (beta < st->tol) {
+		st->done = 1;
+		st->status = FS_CONVERGED_RTOL;
+		st->info_iters = st->iter;
+	}
+	else if (st->iter >= st->maxiter || (st->flags & KF_NONFINITE)) {
+		st->done = 1;
+		st->status = FS_DIVERGED_ITERS;
+	}
+}
+
+// In mixed mode the step's stop tests become "end the cycle"
+__global__ void k_gm_mixed_cycle_end(KState *st) {
+	if (st->done && st->status == FS_CONVERGED_RTOL) {
+		// the FP32 Arnoldi estimate met the tolerance: verify in FP64
+		st->done = 0;
+		st->status = FS_STATUS_UNKNOWN;
+		st->info_iters = 0;
+		st->flags |= KF_RESTART;
+	}
+	else if (st->done && st->status == FS_DIVERGED_ITERS && !(st->flags & KF_NONFINITE)) {
+		// maxiter: still fold the cycle into x and measure the residual
+		st->done = 0;
+		st->flags |= KF_RESTART;
+	}
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- host --
 
 namespace {
 
+template<class T>
+struct GmBufs {
+	T *V;           // basis, ld x (mdim + 1)
+	T *v;           // new direction
+	const T *dinv;  // Jacobi diagonal in T (or null)
+	const T *vals;  // CSR values in T
+};
+
 struct GmArgs {
 	Vec *b, *x;
 	int first, last;   // steps captured
 	bool with_restart; // the gated restart tail
+	bool mixed;
 };
 
 inline GmState *gm_state(Solver *s) { return reinterpret_cast<GmState *>(s->hdev); }
 inline int64_t gm_ld(const Solver *s) { return (s->n + 31) / 32 * 32; }
 
+template<class T>
+GmBufs<T> gm_bufs(Solver *s) {
+	if constexpr (sizeof(T) == 8)
+		return {(T *)s->basis, (T *)s->w64[2], (const T *)s->dinv64(), (const T *)s->A->val};
+	else
+		return {(T *)s->basis, (T *)s->w32[2], (const T *)s->dinv32(), (const T *)s->A->val32};
+}
+
+template<class T>
 int gm_step(Solver *s, int k) {
 	Ctx *ctx = s->ctx;
 	const int64_t n = s->n, ld = gm_ld(s);
 	const int G = red_grid(ctx, n);
 	const bool right = s->set.pre_side != FS_LEFT;
-	const double *dinv = s->dinv64();
-	double *v = s->w64[2];
-	double *V = s->basis;
+	GmBufs<T> B = gm_bufs<T>(s);
 	GmState *g = gm_state(s);
 	const int kp1 = k + 1;
-	const double *Vk = V + (size_t)k * ld;
-	if (right && dinv)
-		FS_TRY((launch_spmv<double, false, true>(ctx, s->A, s->A->val, Vk, dinv,
-		                                         EpiScaleStore{v, nullptr, s->st})));
+	const T *Vk = B.V + (size_t)k * ld;
+	if (right && B.dinv)
+		FS_TRY((launch_spmv<T, false, true>(ctx, s->A, B.vals, Vk, B.dinv,
+		                                    EpiScaleStore<T>{B.v, nullptr, s->st})));
 	else
-		FS_TRY((launch_spmv<double, false, false>(ctx, s->A, s->A->val, Vk, nullptr,
-		                                          EpiScaleStore{v, right ? nullptr : dinv, s->st})));
-	if (s->set.ortho == FS_ORTHO_MGS) {
+		FS_TRY((launch_spmv<T, false, false>(ctx, s->A, B.vals, Vk, nullptr,
+		                                     EpiScaleStore<T>{B.v, right ? nullptr : B.dinv, s->st})));
+	const bool mgs = s->set.ortho == FS_ORTHO_MGS || (s->set.ortho == FS_ORTHO_AUTO && sizeof(T) == 8);
+	if (mgs) {
 		for (int j = 0; j <= kp1; ++j) {
-			k_gm_mgs<<<G, kT, 0, ctx->stream>>>(n, V, ld, j, kp1, v, g, s->st, s->part, s->counter,
-			                                    s->hist);
+			k_gm_mgs<T><<<G, kT, 0, ctx->stream>>>(n, B.V, ld, j, kp1, B.v, g, s->st, s->part,
+			                                       s->counter, s->hist);
 			FS_TRY(check_launch(ctx, "gmres mgs"));
 		}
 	}
 	else {
 		for (int j0 = 0; j0 < kp1; j0 += kChunk) {
-			k_gm_dots<<<G, kT, 0, ctx->stream>>>(n, V, ld, j0, std::min(kChunk, kp1 - j0), v, g,
-			                                     s->st, s->part, s->counter);
+			k_gm_dots<T><<<G, kT, 0, ctx->stream>>>(n, B.V, ld, j0, std::min(kChunk, kp1 - j0), B.v,
+			                                        g, s->st, s->part, s->counter);
 			FS_TRY(check_launch(ctx, "gmres dots"));
 		}
 		for (int j0 = 0; j0 < kp1; j0 += kChunk) {
-			k_gm_project_dots<<<G, kT, 0, ctx->stream>>>(n, V, ld, kp1, j0,
-			                                             std::min(kChunk, kp1 - j0), v, g, s->st,
-			                                             s->part, s->counter);
+			k_gm_project_dots<T><<<G, kT, 0, ctx->stream>>>(n, B.V, ld, kp1, j0,
+			                                                std::min(kChunk, kp1 - j0), B.v, g,
+			                                                s->st, s->part, s->counter);
 			FS_TRY(check_launch(ctx, "gmres project"));
 		}
-		k_gm_project_norm<<<G, kT, 0, ctx->stream>>>(n, V, ld, kp1, v, g, s->st, s->part,
-		                                             s->counter, s->hist);
+		k_gm_project_norm<T><<<G, kT, 0, ctx->stream>>>(n, B.V, ld, kp1, B.v, g, s->st, s->part,
+		                                                s->counter, s->hist);
 		FS_TRY(check_launch(ctx, "gmres norm"));
 	}
-	k_gm_normalize<<<G, kT, 0, ctx->stream>>>(n, v, V + (size_t)kp1 * ld, g, s->st);
+	k_gm_normalize<T><<<G, kT, 0, ctx->stream>>>(n, B.v, B.V + (size_t)kp1 * ld, g, s->st);
 	return check_launch(ctx, "gmres normalize");
 }
 
-// residual + basis_0 (initial: unconditional; restart: gated by the flag)
-template<bool RESTART>
+// residual (FP64) + basis_0 (initial: unconditional; restart: gated)
+template<bool RESTART, class T>
 int gm_restart(Solver *s, Vec *b, Vec *x) {
 	Ctx *ctx = s->ctx;
 	const int64_t n = s->n;
@@ -509,32 +612,51 @@ int gm_restart(Solver *s, Vec *b, Vec *x) {
 		ctx, s->A, s->A->val, (const double *)x->d, nullptr,
 		EpiGmResidual{(const double *)b->d, res, right ? nullptr : s->dinv64(), s->st, s->part,
 		              s->counter, RESTART})));
-	k_gm_basis0<RESTART><<<red_grid(ctx, n), kT, 0, ctx->stream>>>(n, res, s->basis, gm_state(s),
-	                                                             s->st, s->counter);
+	k_gm_basis0<RESTART, T><<<red_grid(ctx, n), kT, 0, ctx->stream>>>(n, res, (T *)s->basis,
+	                                                                 gm_state(s), s->st, s->counter);
 	return check_launch(ctx, "gmres basis0");
 }
 
+template<class T>
 int gm_body(Solver *s, void *a) {
 	GmArgs *ga = (GmArgs *)a;
 	Ctx *ctx = s->ctx;
 	const int64_t n = s->n;
 	for (int j = ga->first; j <= ga->last; ++j)
-		FS_TRY(gm_step(s, j));
+		FS_TRY(gm_step<T>(s, j));
 	if (ga->with_restart) {
 		const bool right = s->set.pre_side != FS_LEFT;
+		if (ga->mixed) {
+			k_gm_mixed_cycle_end<<<1, 1, 0, ctx->stream>>>(s->st);
+			FS_TRY(check_launch(ctx, "gmres cycle end"));
+		}
 		k_gm_backsolve<true><<<1, 1, 0, ctx->stream>>>(gm_state(s), s->st);
 		FS_TRY(check_launch(ctx, "gmres backsolve"));
-		k_gm_correct<true><<<red_grid(ctx, n), kT, 0, ctx->stream>>>(
-			n, s->basis, gm_ld(s), gm_state(s), s->dinv64(), (double *)ga->x->d, right ? 1 : 0, s->st);
+		k_gm_correct<true, T><<<red_grid(ctx, n), kT, 0, ctx->stream>>>(
+			n, (const T *)s->basis, gm_ld(s), gm_state(s), s->dinv64(), (double *)ga->x->d,
+			right ? 1 : 0, s->st);
 		FS_TRY(check_launch(ctx, "gmres correct"));
-		FS_TRY(gm_restart<true>(s, ga->b, ga->x));
+		if (ga->mixed) {
+			// the true FP64 residual re-anchors the next FP32 cycle
+			FS_TRY((launch_spmv<double, false, false>(
+				ctx, s->A, s->A->val, (const double *)ga->x->d, nullptr,
+				EpiGmResidual{(const double *)ga->b->d, s->w64[0], right ? nullptr : s->dinv64(),
+				              s->st, s->part, s->counter, true})));
+			k_gm_mixed_decide<<<1, 1, 0, ctx->stream>>>(s->st);
+			FS_TRY(check_launch(ctx, "gmres decide"));
+			k_gm_basis0<true, T><<<red_grid(ctx, n), kT, 0, ctx->stream>>>(
+				n, s->w64[0], (T *)s->basis, gm_state(s), s->st, s->counter);
+			FS_TRY(check_launch(ctx, "gmres basis0"));
+		}
+		else {
+			FS_TRY((gm_restart<true, T>(s, ga->b, ga->x)));
+		}
 	}
 	return FS_OK;
 }
 
-}  // namespace
-
-int gmres_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
+template<class T>
+int gmres_run(Solver *s, Vec *b, Vec *x, fs_solve_info *info, bool mixed) {
 	Ctx *ctx = s->ctx;
 	const int64_t n = s->n, ld = gm_ld(s);
 	const bool zg = s->set.base.use_zero_guess != 0;
@@ -546,13 +668,14 @@ int gmres_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 		               "GMRES settings fail the reference's validate() (gmres.hh:394-404)");
 	const int mdim = std::max(1, std::min(m, maxiter));  // gmres.hh:58
 	const int cols = mdim + 1;
-	if (s->basis_cols < cols) {
+	const size_t need = sizeof(T) * (size_t)ld * cols;
+	if (s->basis_bytes < need) {
 		if (s->basis)
 			cudaFree(s->basis);
 		s->basis = nullptr;
-		FS_CUDA_TRY(ctx, cudaMalloc(&s->basis, sizeof(double) * (size_t)ld * cols));
-		FS_CUDA_TRY(ctx, cudaMemsetAsync(s->basis, 0, sizeof(double) * (size_t)ld * cols, ctx->stream));
-		s->basis_cols = cols;
+		FS_CUDA_TRY(ctx, cudaMalloc(&s->basis, need));
+		FS_CUDA_TRY(ctx, cudaMemsetAsync(s->basis, 0, need, ctx->stream));
+		s->basis_bytes = need;
 		// graphs captured with the old basis address are stale
 		for (auto &kv : s->graphs)
 			cudaGraphExecDestroy(kv.second.first);
@@ -574,21 +697,23 @@ int gmres_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 		FS_CUDA_TRY(ctx, cudaMemsetAsync(x->d, 0, x->bytes(), ctx->stream));
 	// initial residual (a zero guess makes b - A x == b exactly, the copy of
 	// gmres.hh:112-120), basis_0 and the start test
-	FS_TRY(gm_restart<false>(s, b, x));
+	FS_TRY((gm_restart<false, T>(s, b, x)));
 	GmState *g = gm_state(s);
 	k_gm_start<<<1, 1, 0, ctx->stream>>>(g, s->st, m, mdim + 1);
 	FS_TRY(check_launch(ctx, "gmres start"));
 	FS_TRY(read_state(s));
 	const int steps = std::min(m, maxiter);
+	const int tag = (mixed ? 1 : 0) + 2 * (int)sizeof(T);
 	int user_stop = 0;
 	int64_t seen = 0;
 	while (!s->hst->done && !user_stop) {
-		if (s->diag) {
+		if (s->diag && !mixed) {
 			// one graph per step so that the diagnostic sees every iteration
 			// (x is constant within a cycle, as in the reference)
 			for (int j = 0; j < steps && !s->hst->done; ++j) {
-				GmArgs a{b, x, j, j, j == steps - 1};
-				FS_TRY(graph_run(s, GraphKey{b->d, x->d, 300000 + 2 * j + (j == steps - 1)}, gm_body, &a));
+				GmArgs a{b, x, j, j, j == steps - 1, mixed};
+				FS_TRY(graph_run(s, GraphKey{b->d, x->d, 300000 + 2 * j + (j == steps - 1) + 1000 * tag},
+				                 gm_body<T>, &a));
 				FS_TRY(read_state(s));
 				if (s->hst->nhist > seen) {
 					double hv = 0;
@@ -603,21 +728,38 @@ int gmres_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 			}
 		}
 		else {
-			GmArgs a{b, x, 0, steps - 1, true};
-			FS_TRY(graph_run(s, GraphKey{b->d, x->d, 200000 + steps}, gm_body, &a));
+			GmArgs a{b, x, 0, steps - 1, true, mixed};
+			FS_TRY(graph_run(s, GraphKey{b->d, x->d, 200000 + steps + 1000 * tag}, gm_body<T>, &a));
 			FS_TRY(read_state(s));
+			if (s->diag && s->hst->nhist > seen) {
+				// mixed: the diagnostic sees each step's estimate after its cycle
+				const int64_t upto = std::min<int64_t>(s->hst->nhist, s->hist_cap);
+				std::vector<double> hh(upto > seen ? upto - seen : 0);
+				if (!hh.empty())
+					FS_CUDA_TRY(ctx, cudaMemcpy(hh.data(), s->hist + seen, hh.size() * sizeof(double),
+					                            cudaMemcpyDeviceToHost));
+				for (size_t j = 0; j < hh.size() && !user_stop; ++j)
+					if (s->diag(s->diag_user, reinterpret_cast<fs_vec>(x), hh[j]))
+						user_stop = (int)(seen + j + 1);
+				seen = upto;
+			}
 		}
 	}
-	// final correction with the current k (gmres.hh:228-233)
 	const int G = red_grid(ctx, n);
-	k_gm_backsolve<false><<<1, 1, 0, ctx->stream>>>(g, s->st);
-	FS_TRY(check_launch(ctx, "gmres backsolve"));
-	k_gm_correct<false><<<G, kT, 0, ctx->stream>>>(n, s->basis, ld, g, s->dinv64(), (double *)x->d,
-	                                              right ? 1 : 0, s->st);
-	FS_TRY(check_launch(ctx, "gmres correct"));
+	if (!mixed || user_stop) {
+		// final correction with the current k (gmres.hh:228-233); in mixed
+		// mode every cycle was already folded into x by its tail
+		k_gm_backsolve<false><<<1, 1, 0, ctx->stream>>>(g, s->st);
+		FS_TRY(check_launch(ctx, "gmres backsolve"));
+		k_gm_correct<false, T><<<G, kT, 0, ctx->stream>>>(n, (const T *)s->basis, ld, g, s->dinv64(),
+		                                                  (double *)x->d, right ? 1 : 0, s->st);
+		FS_TRY(check_launch(ctx, "gmres correct"));
+	}
 	FS_TRY(read_state(s));
 	KState &h = *s->hst;
 	s->hhist_count = std::min<int64_t>(h.nhist, s->hist_cap);
+	s->mixed_outer = mixed ? h.restarts : 0;
+	s->mixed_inner = mixed ? h.iter : 0;
 	double xn = 0;
 	FS_TRY(fs_vec_l2norm(reinterpret_cast<fs_vec>(x), &xn));
 	memset(info, 0, sizeof(*info));
@@ -640,6 +782,16 @@ int gmres_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	if (h.flags & KF_NONFINITE)
 		return set_err(ctx, FS_ERR_NON_FINITE, "GMRES: non-finite residual norm");
 	return FS_OK;
+}
+
+}  // namespace
+
+int gmres_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
+	return gmres_run<double>(s, b, x, info, false);
+}
+
+int gmres_apply_mixed(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
+	return gmres_run<float>(s, b, x, info, true);
 }
 
 }  // namespace fsg

@@ -521,7 +521,13 @@ struct EpiBiT {
 
 // x += alpha P p (+ omega P s); res = s - omega t; ||res||, r~'res; tests
 // (bicgstab.hh:136-178, with the next iteration's rho = r~'res fused in)
-template<class V, int PK>
+//
+// RELY (mixed precision): the FP32 recurrence never stops by itself; every
+// stop condition, and a residual drop by aux[0] since the last replacement,
+// raises KF_RELIABLE with the reason in aux[3] (0 drop, 1 converged, 2 early
+// exit, 3 omega == 0, 4 maxiter) and the host replaces the residual by the
+// FP64 one before deciding.
+template<class V, int PK, bool RELY = false>
 __global__ void __launch_bounds__(kThreads)
 k_bi_x(int64_t n, V *__restrict__ x, const V *__restrict__ p, const V *__restrict__ s,
        const V *__restrict__ t, V *__restrict__ res, const V *__restrict__ rt,
@@ -538,9 +544,15 @@ k_bi_x(int64_t n, V *__restrict__ x, const V *__restrict__ p, const V *__restric
 		}
 		// the state changes only once every block has passed its entry test
 		if (last_block(counter) && threadIdx.x == 0) {
-			st->info_iters = st->iter;
-			st->done = 1;
-			st->status = FS_CONVERGED_RTOL;
+			if (RELY) {
+				st->flags |= KF_RELIABLE;
+				st->aux[3] = 2;
+			}
+			else {
+				st->info_iters = st->iter;
+				st->done = 1;
+				st->status = FS_CONVERGED_RTOL;
+			}
 			*counter = 0;
 		}
 		return;
@@ -573,7 +585,22 @@ k_bi_x(int64_t n, V *__restrict__ x, const V *__restrict__ p, const V *__restric
 			st->nhist = hi + 1;
 			if (!isfinite(rn))
 				st->flags |= KF_NONFINITE;
-			if (rn < st->tol) {
+			if (RELY) {
+				int why = -1;
+				if (rn < st->tol)
+					why = 1;
+				else if (st->omega == 0.0)
+					why = 3;
+				else if (it + 1 >= st->maxiter || (st->flags & KF_NONFINITE))
+					why = 4;
+				else if (rn < st->aux[0] * st->aux[1])
+					why = 0;
+				if (why >= 0) {
+					st->flags |= KF_RELIABLE;
+					st->aux[3] = why;
+				}
+			}
+			else if (rn < st->tol) {
 				st->done = 1;
 				st->status = FS_CONVERGED_RTOL;
 				st->info_iters = it + 1;
@@ -586,7 +613,7 @@ k_bi_x(int64_t n, V *__restrict__ x, const V *__restrict__ p, const V *__restric
 			st->rho_old = st->rho;
 			st->rho = q[1];
 			st->iter = it + 1;
-			if (!st->done) {
+			if (!st->done && !(st->flags & KF_RELIABLE)) {
 				if (it + 1 >= st->maxiter || (st->flags & KF_NONFINITE)) {
 					st->done = 1;
 					st->status = FS_DIVERGED_ITERS;
@@ -595,6 +622,54 @@ k_bi_x(int64_t n, V *__restrict__ x, const V *__restrict__ p, const V *__restric
 					st->flags |= KF_RESTART;
 				}
 			}
+			*counter = 0;
+		}
+	}
+}
+
+// mixed BiCGSTAB: decision after the FP64 residual replaced res (st->res)
+__global__ void k_bi_rel_decide(KState *st) {
+	const int why = (int)st->aux[3];
+	st->flags &= ~(KF_RELIABLE | KF_EARLY);
+	st->aux[3] = 0;
+	if (st->res < st->tol) {
+		st->done = 1;
+		st->status = FS_CONVERGED_RTOL;
+		st->info_iters = st->iter;
+	}
+	else if (why == 3) {
+		st->done = 1;
+		st->status = FS_DIVERGED_BREAKDOWN;
+		st->info_iters = st->iter;
+	}
+	else if (why == 4 || st->iter >= st->maxiter || (st->flags & KF_NONFINITE)) {
+		st->done = 1;
+		st->status = FS_DIVERGED_ITERS;
+	}
+	else {
+		st->aux[1] = st->res;
+		if (why == 2 || why == 1)
+			st->flags |= KF_RESTART;  // the recurrence is spent: restart from r
+	}
+}
+
+// rho = r~ . res after a replacement (the next iteration's rho_1)
+template<class V>
+__global__ void __launch_bounds__(kThreads)
+k_bi_rho(int64_t n, const V *__restrict__ rt, const V *__restrict__ res, KState *st,
+         double *part, unsigned *counter) {
+	__shared__ double sh[128];
+	if (st->done || (st->flags & KF_RESTART))
+		return;
+	Acc<V, 1> acc;
+	acc.init();
+	FOR_EACH(i, n) acc.add_prod(0, rt[i], res[i]);
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double q[1];
+		sum_partials<1>(part, gridDim.x, q, sh);
+		if (threadIdx.x == 0) {
+			st->rho = q[0];
 			*counter = 0;
 		}
 	}
@@ -678,6 +753,8 @@ int solver_alloc(Solver *s) {
 	case FS_BICGSTAB: nw64 = 6; break;
 	case FS_GMRES: nw64 = 3; break;
 	case FS_CG_MIXED: nw64 = 1; nw32 = 5; break;
+	case FS_BICGSTAB_MIXED: nw64 = 1; nw32 = 7; break;
+	case FS_GMRES_MIXED: nw64 = 3; nw32 = 3; break;
 	}
 	for (int i = 0; i < nw64; ++i)
 		FS_TRY(dalloc(s, (void **)&s->w64[i], n64));
@@ -689,7 +766,8 @@ int solver_alloc(Solver *s) {
 	// GMRES multi-dot of gmres.cu); every kernel's grid is <= 8 * SMs
 	FS_TRY(dalloc(s, (void **)&s->part, sizeof(double) * (size_t)ctx->sms * 8 * kPartPerBlock + 1024));
 	FS_TRY(dalloc(s, (void **)&s->counter, 64));
-	FS_TRY(dalloc(s, (void **)&s->hdev, s->method == FS_GMRES ? sizeof(GmState) : sizeof(double) * 4096));
+	const bool gm = s->method == FS_GMRES || s->method == FS_GMRES_MIXED;
+	FS_TRY(dalloc(s, (void **)&s->hdev, gm ? sizeof(GmState) : sizeof(double) * 4096));
 	cudaError_t e = cudaMallocHost(&s->hst, sizeof(KState));
 	if (e != cudaSuccess)
 		return set_err(ctx, FS_ERR_OUT_OF_MEMORY, "pinned state allocation failed");
@@ -701,7 +779,7 @@ int solver_alloc(Solver *s) {
 	}
 	if (s->P.kind == FS_PRECOND_JACOBI)
 		FS_TRY(ensure_dinv(s->A));
-	if (s->method == FS_CG_MIXED || s->method == FS_GMRES)
+	if (s->method == FS_CG_MIXED || s->method == FS_BICGSTAB_MIXED || s->method == FS_GMRES_MIXED)
 		FS_TRY(ensure_val32(s->A));
 	return FS_OK;
 }
@@ -1296,7 +1374,149 @@ static int bicgstab_apply64(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	return FS_OK;
 }
 
+// ------------------------------------------- mixed precision BiCGSTAB --
+
+template<int PK>
+static int bi_body32(Solver *s, void *a) {
+	BiArgs *g = (BiArgs *)a;
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	float *res = s->w32[0], *rt = s->w32[1], *p = s->w32[2], *v = s->w32[3], *sv = s->w32[4],
+	      *t = s->w32[5], *xs = s->w32[6];
+	const float *dinv = s->dinv32();
+	const int G = red_grid(ctx, n);
+	for (int k = 0; k < g->k; ++k) {
+		k_bi_p<float><<<G, kThreads, 0, ctx->stream>>>(n, p, v, res, s->st);
+		FS_TRY(check_launch(ctx, "bicgstab p f32"));
+		if (PK)
+			FS_TRY((launch_spmv<float, false, true>(ctx, s->A, s->A->val32, p, dinv,
+			                                        EpiBiV<float>{v, rt, s->st, s->part, s->counter})));
+		else
+			FS_TRY((launch_spmv<float, false, false>(ctx, s->A, s->A->val32, p, nullptr,
+			                                         EpiBiV<float>{v, rt, s->st, s->part, s->counter})));
+		k_bi_s<float><<<G, kThreads, 0, ctx->stream>>>(n, sv, v, res, s->st, s->part, s->counter);
+		FS_TRY(check_launch(ctx, "bicgstab s f32"));
+		if (PK)
+			FS_TRY((launch_spmv<float, false, true>(ctx, s->A, s->A->val32, sv, dinv,
+			                                        EpiBiT<float>{t, sv, s->st, s->part, s->counter})));
+		else
+			FS_TRY((launch_spmv<float, false, false>(ctx, s->A, s->A->val32, sv, nullptr,
+			                                         EpiBiT<float>{t, sv, s->st, s->part, s->counter})));
+		k_bi_x<float, PK, true><<<G, kThreads, 0, ctx->stream>>>(n, xs, p, sv, t, res, rt, dinv, s->st,
+		                                                        s->part, s->counter, s->hist);
+		FS_TRY(check_launch(ctx, "bicgstab x f32"));
+	}
+	return FS_OK;
+}
+
+// FP32 BiCGSTAB recurrences on a correction xs, with the FP64 residual
+// b - A x replacing the recurrence residual whenever it has dropped by
+// inner_rtol since the last replacement and at every stop, so that the
+// stopping test is the reference's, on the FP64 residual.
+static int bicgstab_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	const int G = red_grid(ctx, n);
+	const bool zg = s->set.base.use_zero_guess != 0;
+	const int PK = s->dinv32() ? 1 : 0;
+	float *res = s->w32[0], *rt = s->w32[1], *p = s->w32[2], *v = s->w32[3], *xs = s->w32[6];
+	const int maxiter = s->set.base.maxiter;
+	const double delta = s->set.inner_rtol > 0 ? s->set.inner_rtol : 1e-2;
+	FS_TRY(solver_hist(s, std::max(1, maxiter)));
+	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, maxiter));
+	FS_TRY(solver_norms(s, b, x, !zg, 0));
+	if (zg) {
+		k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
+		FS_TRY(check_launch(ctx, "fill"));
+	}
+	auto fold_and_residual = [&]() -> int {
+		k_rel_fold<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs);
+		FS_TRY(check_launch(ctx, "fold"));
+		return launch_spmv<double, false, false>(
+			ctx, s->A, s->A->val, (const double *)x->d, nullptr,
+			EpiRelResidual{(const double *)b->d, res, s->st, s->part, s->counter});
+	};
+	k_fill<float><<<G, kThreads, 0, ctx->stream>>>(n, xs, 0.f);
+	FS_TRY(check_launch(ctx, "fill"));
+	FS_TRY(fold_and_residual());
+	k_bi_start<float><<<G, kThreads, 0, ctx->stream>>>(n, res, rt, p, v, s->st, s->part, s->counter);
+	FS_TRY(check_launch(ctx, "bicgstab start f32"));
+	FS_TRY(read_state(s));
+	const double res0 = s->hst->res0;
+	{
+		double a[2] = {delta, res0};  // aux[0] = replacement factor, aux[1] = level
+		FS_CUDA_TRY(ctx, cudaMemcpyAsync(&s->st->aux[0], a, sizeof a, cudaMemcpyHostToDevice, ctx->stream));
+		FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	}
+	int user_stop = 0;
+	int64_t seen = 0;
+	const int k = k_default(s) > 1 ? k_default(s) : 32;
+	BiArgs args{b, x, k};
+	GraphKey key{b->d, x->d, 400 + k * 2 + PK};
+	while (!s->hst->done && !user_stop) {
+		FS_TRY(graph_run(s, key, PK ? bi_body32<1> : bi_body32<0>, &args));
+		FS_TRY(read_state(s));
+		if (s->hst->flags & KF_RELIABLE) {
+			FS_TRY(fold_and_residual());
+			k_bi_rel_decide<<<1, 1, 0, ctx->stream>>>(s->st);
+			FS_TRY(check_launch(ctx, "bicgstab decide"));
+			k_bi_rho<float><<<G, kThreads, 0, ctx->stream>>>(n, rt, res, s->st, s->part, s->counter);
+			FS_TRY(check_launch(ctx, "bicgstab rho"));
+			FS_TRY(read_state(s));
+		}
+		if ((s->hst->flags & KF_RESTART) && !s->hst->done) {
+			// bicgstab.hh:103-113 (also after a spent recurrence): r from the
+			// FP64 residual, r~ = r, p = r
+			FS_TRY(fold_and_residual());
+			k_bi_restart<float><<<G, kThreads, 0, ctx->stream>>>(n, res, rt, p, s->st, s->part, s->counter);
+			FS_TRY(check_launch(ctx, "bicgstab restart f32"));
+			FS_TRY(read_state(s));
+		}
+		if (s->diag) {
+			const int64_t nh = std::min<int64_t>(s->hst->nhist, s->hist_cap);
+			std::vector<double> hh(nh > seen ? nh - seen : 0);
+			if (!hh.empty())
+				FS_CUDA_TRY(ctx, cudaMemcpy(hh.data(), s->hist + seen, hh.size() * sizeof(double),
+				                            cudaMemcpyDeviceToHost));
+			for (size_t j = 0; j < hh.size() && !user_stop; ++j)
+				if (s->diag(s->diag_user, reinterpret_cast<fs_vec>(x), hh[j]))
+					user_stop = (int)(seen + j + 1);
+			seen = nh;
+		}
+	}
+	k_rel_fold<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs);
+	FS_TRY(check_launch(ctx, "fold"));
+	FS_TRY(read_state(s));
+	KState &h = *s->hst;
+	s->hhist_count = std::min<int64_t>(h.nhist, s->hist_cap);
+	s->mixed_outer = h.restarts;
+	s->mixed_inner = h.iter;
+	double xn = 0;
+	FS_TRY(sol_norm(s, x, &xn));
+	memset(info, 0, sizeof(*info));
+	info->rhs_norm = (float)h.rhs_norm;
+	info->sol_norm_initial = zg ? 0.f : (float)h.sol0;
+	info->res_norm_initial = (float)res0;
+	info->res_norm_final = (float)h.res;
+	info->sol_norm_final = (float)xn;
+	info->restarts = h.restarts;
+	if (user_stop) {
+		info->status = FS_CONVERGED_USER;
+		info->iters = user_stop;
+	}
+	else {
+		info->status = h.status;
+		info->iters = h.info_iters;
+		if (res0 >= h.tol && info->iters == 0)
+			info->status = FS_DIVERGED_ITERS;
+	}
+	if (h.flags & KF_NONFINITE)
+		return set_err(ctx, FS_ERR_NON_FINITE, "mixed BiCGSTAB: non-finite residual norm");
+	return FS_OK;
+}
+
 int gmres_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info);
+int gmres_apply_mixed(Solver *s, Vec *b, Vec *x, fs_solve_info *info);
 
 }  // namespace fsg
 
@@ -1317,7 +1537,7 @@ FS_API int fs_krylov_settings_default(fs_krylov_settings *s) {
 	s->max_krylov_dim = -1;
 	s->pre_side = FS_RIGHT;
 	s->restart = 0;
-	s->ortho = FS_ORTHO_CGS2;
+	s->ortho = FS_ORTHO_AUTO;
 	s->k_readback = 0;
 	s->refine = FS_REFINE_RELIABLE;
 	s->inner_rtol = 1e-2;
@@ -1332,7 +1552,7 @@ FS_API int fs_krylov_create(fs_ctx h, int method, const fs_krylov_settings *set,
 	if (!ok_ctx(ctx) || !ok_csr(A) || !out || !set)
 		return FS_ERR_BAD_HANDLE;
 	*out = nullptr;
-	if (method < FS_CG || method > FS_CG_MIXED)
+	if (method < FS_CG || method > FS_GMRES_MIXED)
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_krylov_create: unknown method %d", method);
 	if (A->nrows != A->ncols)
 		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_krylov_create: operator must be square");
@@ -1381,7 +1601,7 @@ FS_API int fs_krylov_create(fs_ctx h, int method, const fs_krylov_settings *set,
 			return set_err(ctx, FS_ERR_INVALID_ARG, "fs_krylov_create: unknown preconditioner kind");
 		}
 	}
-	if (method == FS_GMRES) {
+	if (method == FS_GMRES || method == FS_GMRES_MIXED) {
 		int m = set->max_krylov_dim < 0 ? set->base.maxiter : set->max_krylov_dim;
 		if (m > 100 || (!set->restart && set->base.maxiter > m)) {
 			delete s;
@@ -1483,7 +1703,7 @@ FS_API int fs_krylov_settings_set(fs_solver h, const fs_krylov_settings *in) {
 	Solver *s = reinterpret_cast<Solver *>(h);
 	if (!ok_slv(s) || !in)
 		return FS_ERR_BAD_HANDLE;
-	if (s->method == FS_GMRES) {
+	if (s->method == FS_GMRES || s->method == FS_GMRES_MIXED) {
 		int m = in->max_krylov_dim < 0 ? in->base.maxiter : in->max_krylov_dim;
 		if (m > 100 || (!in->restart && in->base.maxiter > m))
 			return set_err(s->ctx, FS_ERR_BREAKDOWN,
@@ -1517,6 +1737,8 @@ FS_API int fs_krylov_apply(fs_solver h, fs_vec bh, fs_vec xh, fs_solve_info *inf
 	case FS_CG_MIXED:
 		return s->set.refine == FS_REFINE_RELIABLE ? cg_apply_reliable(s, b, x, info)
 		                                          : cg_apply_mixed(s, b, x, info);
+	case FS_BICGSTAB_MIXED: return bicgstab_apply_reliable(s, b, x, info);
+	case FS_GMRES_MIXED: return gmres_apply_mixed(s, b, x, info);
 	}
 	return FS_ERR_INVALID_ARG;
 }

@@ -89,7 +89,7 @@ struct Solver {
 	double *w64[12] = {};
 	float *w32[12] = {};
 	double *basis = nullptr;          // GMRES: (m + 1) x n, column j contiguous
-	int basis_cols = 0;
+	size_t basis_bytes = 0;
 	double *hdev = nullptr;           // GMRES: dot results scratch
 	KState *st = nullptr;             // device
 	KState *hst = nullptr;            // pinned mirror

@@ -199,7 +199,9 @@ enum fs_method {
 	FS_CG = 0,           /* op::cg, cg.hh:43-139                         */
 	FS_BICGSTAB = 1,     /* op::bicgstab, bicgstab.hh:39-187             */
 	FS_GMRES = 2,        /* op::gmres, gmres.hh:78-241                   */
-	FS_CG_MIXED = 3      /* FP32 inner PCG inside FP64 refinement        */
+	FS_CG_MIXED = 3,     /* FP32 inner PCG inside FP64 refinement        */
+	FS_BICGSTAB_MIXED = 4, /* FP32 BiCGSTAB, FP64 residual replacement   */
+	FS_GMRES_MIXED = 5   /* FP32 Arnoldi cycles, FP64 restart residual   */
 };
 
 enum fs_precond_kind {
@@ -216,7 +218,10 @@ typedef struct {
 } fs_precond;
 
 enum fs_gmres_side { FS_LEFT = 0, FS_RIGHT = 1 };
-enum fs_gmres_ortho { FS_ORTHO_CGS2 = 0, FS_ORTHO_MGS = 1 };
+/* GMRES orthogonalisation.  AUTO picks MGS for the FP64 basis (half the FP64
+ * multiply-adds of CGS2, and the reference's order) and CGS2 for the FP32
+ * basis of FS_GMRES_MIXED (3 reductions per step instead of k + 2). */
+enum fs_gmres_ortho { FS_ORTHO_CGS2 = 0, FS_ORTHO_MGS = 1, FS_ORTHO_AUTO = 2 };
 
 enum fs_refine_kind {
 	FS_REFINE_RESTART = 0,  /* outer FP64 residual, inner FP32 PCG restarted */

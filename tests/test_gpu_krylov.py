@@ -278,3 +278,31 @@ def test_gmres_cgs2_vs_oracle(ctx, wl):
     assert info.status == r.status == "converged_rtol"
     assert abs(info.iters - r.iters) <= ITER_TOL
     _bicgstab_accuracy_bar(A, b, x, r.x)
+
+
+# ------------------------------------------------- mixed BiCGSTAB / GMRES --
+
+@pytest.mark.parametrize("wl", ["convdiff3d-24", "diffusion3d-24"])
+def test_mixed_bicgstab(ctx, wl):
+    """FP32 BiCGSTAB with FP64 residual replacement: the stopping test is on
+    the FP64 residual and the iteration count stays near the FP64 one."""
+    A, b = P.workload(wl)
+    r = O.solve("bicgstab", A, b, maxiter=4000, rtol=1e-8)
+    info, x, slv = _run(ctx, fs.mixed_bicgstab, A, b, maxiter=4000, rtol=1e-8)
+    assert info.status == "converged_rtol"
+    assert _true_relres(A, b, x) <= 1e-8
+    assert info.iters <= 1.3 * r.iters + 5
+
+
+@pytest.mark.parametrize("ortho", ["auto", "mgs"])
+@pytest.mark.parametrize("wl", ["convdiff3d-24", "diffusion3d-20"])
+def test_mixed_gmres(ctx, wl, ortho):
+    """FP32 Arnoldi cycles re-anchored on the FP64 residual at every restart:
+    converges on the FP64 residual with the FP64 iteration count +- a few."""
+    A, b = P.workload(wl)
+    r = O.solve("gmres", A, b, maxiter=5000, rtol=1e-8, krylov_dim=30)
+    info, x, slv = _run(ctx, fs.mixed_gmres, A, b, maxiter=5000, rtol=1e-8, max_krylov_dim=30,
+                        restart=True, ortho=ortho)
+    assert info.status == "converged_rtol"
+    assert _true_relres(A, b, x) <= 1e-8
+    assert info.iters <= 1.2 * r.iters + 30
