@@ -95,6 +95,18 @@ def build_gpu(force: bool = False, verbose: bool = False) -> Path:
     return out
 
 
+def build_cpp_tests(force: bool = False) -> Path:
+    """The C++ API test (tests/cpp) against the in-tree libraries."""
+    out = BUILD / "test_krylov_api"
+    src = ROOT / "tests" / "cpp" / "test_krylov_api.cc"
+    deps = [src, INCLUDE / "fsgpu.h", INCLUDE / "flecsolve_gb300" / "flecsolve.hh",
+            BUILD / "libfsgpu.so", BUILD / "libfsproblems.so"]
+    if force or _stale(out, deps):
+        _run(["g++", "-std=c++17", "-O2", "-I", str(INCLUDE), str(src), "-o", str(out),
+              "-L", str(BUILD), "-lfsgpu", "-lfsproblems", f"-Wl,-rpath,{BUILD}"])
+    return out
+
+
 def build_oracle() -> None:
     _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"])
 
@@ -103,6 +115,7 @@ def build_all(force: bool = False, verbose: bool = False) -> None:
     build_problems(force)
     build_oracle()
     build_gpu(force, verbose)
+    build_cpp_tests(force)
 
 
 if __name__ == "__main__":

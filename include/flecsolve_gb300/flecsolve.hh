@@ -1,0 +1,486 @@
+// flecsolve_gb300/flecsolve.hh -- C++ mirror of flecsolve's Krylov-path API
+// over the C ABI of fsgpu.h (header-only; link with -lfsgpu).
+//
+// Names, argument order and semantics follow the reference so that a caller
+// of flecsolve's Krylov path compiles against this header after switching
+// the includes:
+//
+//   vec::device_vec             vec::core<Data, Ops, Config> with the device
+//                               Data/Operations policy (flecsolve/vectors/
+//                               core.hh:26-353)
+//   op::core / op::handle /     flecsolve/operators/{core,handle,shell}.hh
+//   op::ref / op::cref / op::I
+//   mat::device_csr             mat::csr as an op::base policy
+//                               (flecsolve/matrices/seq.hh:35-63)
+//   cg / bicgstab / gmres       settings, make_work, nwork, solver(s, w)(A[, P
+//                               [, diag]]) -> operator, (b, x) -> solve_info
+//                               (flecsolve/solvers/cg.hh:250-270,
+//                               bicgstab.hh:193-216, gmres.hh:366-438,
+//                               krylov_parameters.hh:94-126)
+//   solve_info, solver_settings flecsolve/solvers/solver_settings.hh:31-85
+//
+// Every call goes to libfsgpu.so; errors become fs_error exceptions, and the
+// reference's flog_assert sites (FS_ERR_BREAKDOWN) raise too.
+#pragma once
+
+#include <cstdint>
+#include <functional>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "../fsgpu.h"
+
+namespace flecsolve {
+
+// ------------------------------------------------------------ errors --
+
+struct fs_error : std::runtime_error {
+	int status;
+	fs_error(int s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+inline void check(int s, fs_ctx c = nullptr, const char *what = "") {
+	if (s != FS_OK) {
+		std::string m = std::string(what) + ": " + fs_status_string(s);
+		if (c)
+			m += std::string(" (") + fs_last_error(c) + ")";
+		throw fs_error(s, m);
+	}
+}
+
+// One device + stream; the FleCSI runtime context of the reference.
+class context {
+public:
+	explicit context(int device = 0) { check(fs_ctx_create(device, &h_), nullptr, "fs_ctx_create"); }
+	~context() {
+		if (h_)
+			fs_ctx_destroy(h_);
+	}
+	context(const context &) = delete;
+	context &operator=(const context &) = delete;
+	fs_ctx get() const { return h_; }
+	void sync() const { check(fs_ctx_sync(h_), h_, "sync"); }
+
+private:
+	fs_ctx h_ = nullptr;
+};
+
+// ------------------------------------------------- settings and info ---
+
+// solver_settings.hh:31-36 (float tolerances, as in the reference)
+struct solver_settings {
+	int maxiter;
+	float rtol;
+	float atol;
+	bool use_zero_guess;
+};
+
+// solver_settings.hh:61-85
+struct solve_info {
+	enum class stop_reason {
+		converged_atol,
+		converged_rtol,
+		converged_user,
+		diverged_dtol,
+		diverged_iters,
+		diverged_breakdown,
+		unknown
+	};
+	stop_reason status = stop_reason::unknown;
+	int iters = 0;
+	int restarts = 0;
+	float res_norm_initial = 0, res_norm_final = 0;
+	float sol_norm_initial = 0, sol_norm_final = 0;
+	float rhs_norm = 0;
+	bool success() const {
+		return status == stop_reason::converged_atol || status == stop_reason::converged_rtol ||
+		       status == stop_reason::converged_user;
+	}
+	static solve_info from(const fs_solve_info &i) {
+		solve_info o;
+		o.status = static_cast<stop_reason>(i.status);
+		o.iters = i.iters;
+		o.restarts = i.restarts;
+		o.res_norm_initial = i.res_norm_initial;
+		o.res_norm_final = i.res_norm_final;
+		o.sol_norm_initial = i.sol_norm_initial;
+		o.sol_norm_final = i.sol_norm_final;
+		o.rhs_norm = i.rhs_norm;
+		return o;
+	}
+};
+
+// ----------------------------------------------------------- vectors ---
+
+namespace vec {
+
+// the `.get()` futures of the reference's reductions (util/future.hh)
+template<class T>
+struct future {
+	T val;
+	T get() const { return val; }
+};
+
+// vec::core over the device Data/Operations policy.  Methods and argument
+// order follow flecsolve/vectors/core.hh:59-310 (`this` is the output).
+class device_vec {
+public:
+	using scalar = double;
+	using real = double;
+	using len_t = std::size_t;
+
+	device_vec(const context &c, std::size_t n) : ctx_(c.get()), owns_(true) {
+		check(fs_vec_create(ctx_, (int64_t)n, FS_F64, &h_), ctx_, "fs_vec_create");
+	}
+	device_vec(const context &c, const std::vector<double> &host) : device_vec(c, host.size()) {
+		upload(host);
+	}
+	// non-owning view of a library vector (the diagnostic's argument)
+	static device_vec view(fs_ctx c, fs_vec h) { return device_vec(c, h); }
+	device_vec(device_vec &&o) noexcept : ctx_(o.ctx_), h_(o.h_), owns_(o.owns_) { o.h_ = nullptr; }
+	device_vec &operator=(device_vec &&o) noexcept {
+		std::swap(ctx_, o.ctx_);
+		std::swap(h_, o.h_);
+		std::swap(owns_, o.owns_);
+		return *this;
+	}
+	device_vec(const device_vec &) = delete;
+	~device_vec() {
+		if (h_ && owns_)
+			fs_vec_destroy(h_);
+	}
+
+	fs_vec handle() const { return h_; }
+	fs_ctx ctx() const { return ctx_; }
+
+	void upload(const std::vector<double> &host) {
+		check(fs_vec_upload(h_, host.data(), (int64_t)host.size()), ctx_, "upload");
+	}
+	std::vector<double> download() const {
+		std::vector<double> out(local_size());
+		check(fs_vec_download(h_, out.data(), (int64_t)out.size()), ctx_, "download");
+		return out;
+	}
+
+	void copy(const device_vec &src) { check(fs_vec_copy(src.h_, h_), ctx_, "copy"); }
+	void zero() { check(fs_vec_zero(h_), ctx_, "zero"); }
+	void set_scalar(double v) { check(fs_vec_set_scalar(h_, v), ctx_, "set_scalar"); }
+	void scale(double a, const device_vec &x) { check(fs_vec_scale(a, x.h_, h_), ctx_, "scale"); }
+	void scale(double a) { check(fs_vec_scale_self(a, h_), ctx_, "scale"); }
+	void add(const device_vec &x, const device_vec &y) { check(fs_vec_add(x.h_, y.h_, h_), ctx_, "add"); }
+	void subtract(const device_vec &x, const device_vec &y) {
+		check(fs_vec_subtract(x.h_, y.h_, h_), ctx_, "subtract");
+	}
+	void multiply(const device_vec &x, const device_vec &y) {
+		check(fs_vec_multiply(x.h_, y.h_, h_), ctx_, "multiply");
+	}
+	void divide(const device_vec &x, const device_vec &y) {
+		check(fs_vec_divide(x.h_, y.h_, h_), ctx_, "divide");
+	}
+	void reciprocal(const device_vec &x) { check(fs_vec_reciprocal(x.h_, h_), ctx_, "reciprocal"); }
+	void linear_sum(double a, const device_vec &x, double b, const device_vec &y) {
+		check(fs_vec_linear_sum(a, x.h_, b, y.h_, h_), ctx_, "linear_sum");
+	}
+	void axpy(double a, const device_vec &x, const device_vec &y) {
+		check(fs_vec_axpy(a, x.h_, y.h_, h_), ctx_, "axpy");
+	}
+	void axpby(double a, double b, const device_vec &x) {
+		check(fs_vec_axpby(a, b, x.h_, h_), ctx_, "axpby");
+	}
+	void abs(const device_vec &x) { check(fs_vec_abs(x.h_, h_), ctx_, "abs"); }
+	void add_scalar(const device_vec &x, double a) {
+		check(fs_vec_add_scalar(x.h_, a, h_), ctx_, "add_scalar");
+	}
+	void set_random(unsigned seed) { check(fs_vec_set_random(h_, seed), ctx_, "set_random"); }
+
+	future<double> min() const { return red(fs_vec_min); }
+	future<double> max() const { return red(fs_vec_max); }
+	future<double> l1norm() const { return red(fs_vec_l1norm); }
+	future<double> l2norm() const { return red(fs_vec_l2norm); }
+	future<double> inf_norm() const { return red(fs_vec_inf_norm); }
+	future<double> dot(const device_vec &x) const {
+		double r;
+		check(fs_vec_dot(h_, x.h_, &r), ctx_, "dot");
+		return {r};
+	}
+	future<std::size_t> global_size() const { return {local_size()}; }
+	std::size_t local_size() const {
+		int64_t n;
+		check(fs_vec_size(h_, &n), ctx_, "size");
+		return (std::size_t)n;
+	}
+
+private:
+	device_vec(fs_ctx c, fs_vec h) : ctx_(c), h_(h), owns_(false) {}
+	future<double> red(int (*f)(fs_vec, double *)) const {
+		double r;
+		check(f(h_, &r), ctx_, "reduction");
+		return {r};
+	}
+	fs_ctx ctx_ = nullptr;
+	fs_vec h_ = nullptr;
+	bool owns_ = true;
+};
+
+}  // namespace vec
+
+// ---------------------------------------------------------- operators --
+
+namespace op {
+
+// op::base (operators/core.hh:29-78), parameterless form
+struct base {};
+
+// op::core<P>: apply / operator() / residual (operators/core.hh:80-143)
+template<class P>
+struct core : P {
+	using P::P;
+	core(P p) : P(std::move(p)) {}
+	void apply(const vec::device_vec &x, vec::device_vec &y) const { P::apply(x, y); }
+	void operator()(const vec::device_vec &x, vec::device_vec &y) const { P::apply(x, y); }
+	// r = b - A x
+	void residual(const vec::device_vec &b, const vec::device_vec &x, vec::device_vec &r) const {
+		P::residual(b, x, r);
+	}
+};
+
+// op::handle: reference or shared ownership (operators/handle.hh:10-56)
+template<class T>
+struct handle {
+	using type = T;
+	std::shared_ptr<T> own;
+	T *ptr = nullptr;
+	T &get() const { return *ptr; }
+};
+template<class T>
+handle<T> ref(T &o) { return {nullptr, &o}; }
+template<class T>
+handle<const T> cref(const T &o) { return {nullptr, &o}; }
+template<class T, class... A>
+handle<T> make_shared(A &&...a) {
+	auto p = std::make_shared<T>(std::forward<A>(a)...);
+	return {p, p.get()};
+}
+
+// op::I, the identity operator (operators/shell.hh:317-318)
+struct identity_t {};
+inline constexpr identity_t I{};
+
+}  // namespace op
+
+// ------------------------------------------------------------ matrices --
+
+namespace mat {
+
+// The CSR operator on the device.  Constructed from the reference's host CSR
+// arrays (std::size_t or int32 column ids, double values).
+class device_csr {
+public:
+	device_csr(const context &c, std::size_t nrows, std::size_t ncols,
+	           const std::vector<int64_t> &rowptr, const std::vector<int32_t> &col,
+	           const std::vector<double> &val)
+		: ctx_(c.get()) {
+		check(fs_csr_create(ctx_, (int64_t)nrows, (int64_t)ncols, (int64_t)val.size(), rowptr.data(),
+		                    col.data(), 4, val.data(), &h_),
+		      ctx_, "fs_csr_create");
+	}
+	device_csr(const context &c, std::size_t nrows, std::size_t ncols,
+	           const std::vector<int64_t> &rowptr, const std::vector<std::size_t> &col,
+	           const std::vector<double> &val)
+		: ctx_(c.get()) {
+		check(fs_csr_create(ctx_, (int64_t)nrows, (int64_t)ncols, (int64_t)val.size(), rowptr.data(),
+		                    col.data(), (int)sizeof(std::size_t), val.data(), &h_),
+		      ctx_, "fs_csr_create");
+	}
+	device_csr(device_csr &&o) noexcept : ctx_(o.ctx_), h_(o.h_) { o.h_ = nullptr; }
+	device_csr(const device_csr &) = delete;
+	~device_csr() {
+		if (h_)
+			fs_csr_destroy(h_);
+	}
+	fs_csr handle() const { return h_; }
+	fs_ctx ctx() const { return ctx_; }
+	std::size_t rows() const { return shape().first; }
+	std::size_t cols() const { return shape().second; }
+
+	// y = A x (mat::sparse::apply -> compressed_ops::spmv)
+	void apply(const vec::device_vec &x, vec::device_vec &y) const {
+		check(fs_csr_spmv(h_, x.handle(), y.handle(), FS_SPMV_FMA), ctx_, "spmv");
+	}
+	void residual(const vec::device_vec &b, const vec::device_vec &x, vec::device_vec &r) const {
+		check(fs_csr_residual(h_, b.handle(), x.handle(), r.handle()), ctx_, "residual");
+	}
+	// the D^-1 operator of the reference's tests (util/test/mesh.hh:123-140)
+	// as a diagonal vector usable as a preconditioner
+	vec::device_vec Dinv(const context &c) const {
+		vec::device_vec d(c, rows());
+		check(fs_csr_diag_inv(h_, d.handle()), ctx_, "diag_inv");
+		return d;
+	}
+
+private:
+	std::pair<std::size_t, std::size_t> shape() const {
+		int64_t r, c;
+		check(fs_csr_shape(h_, &r, &c, nullptr), ctx_, "shape");
+		return {(std::size_t)r, (std::size_t)c};
+	}
+	fs_ctx ctx_;
+	fs_csr h_ = nullptr;
+};
+
+using csr = op::core<device_csr>;
+
+}  // namespace mat
+
+// --------------------------------------------------------- solvers ----
+
+// default diagnostic (krylov_parameters.hh:29-31)
+inline const auto default_diagnostic = [](const vec::device_vec &, double) { return false; };
+
+namespace detail {
+
+struct jacobi_t {};
+
+template<class D>
+int diag_trampoline(void *user, fs_vec x, double res) {
+	auto *p = static_cast<std::pair<D *, fs_ctx> *>(user);
+	auto v = vec::device_vec::view(p->second, x);
+	return (*p->first)(v, res) ? 1 : 0;
+}
+
+// op::X<krylov_parameters<...>> bound by krylov_solver::operator()
+// (krylov_parameters.hh:94-126): owns the device solver and its work.
+template<class Diag>
+class bound_solver {
+public:
+	bound_solver(int method, const fs_krylov_settings &s, const mat::csr &A, fs_precond P,
+	             Diag diag)
+		: ctx_(A.ctx()), diag_(std::make_unique<Diag>(std::move(diag))) {
+		check(fs_krylov_create(ctx_, method, &s, A.handle(), &P, &h_), ctx_, "fs_krylov_create");
+		if constexpr (!std::is_same_v<std::decay_t<Diag>, std::decay_t<decltype(default_diagnostic)>>) {
+			user_ = std::make_unique<std::pair<Diag *, fs_ctx>>(diag_.get(), ctx_);
+			check(fs_krylov_set_diagnostic(h_, &diag_trampoline<Diag>, user_.get()), ctx_,
+			      "set_diagnostic");
+		}
+	}
+	bound_solver(bound_solver &&) = default;
+	~bound_solver() {
+		if (h_)
+			fs_krylov_destroy(h_);
+	}
+	// op::core::apply(b, x) -> solve_info
+	solve_info apply(const vec::device_vec &b, vec::device_vec &x) const {
+		fs_solve_info i{};
+		check(fs_krylov_apply(h_, b.handle(), x.handle(), &i), ctx_, "fs_krylov_apply");
+		return solve_info::from(i);
+	}
+	solve_info operator()(const vec::device_vec &b, vec::device_vec &x) const { return apply(b, x); }
+
+private:
+	fs_ctx ctx_;
+	fs_solver h_ = nullptr;
+	std::unique_ptr<Diag> diag_;
+	std::unique_ptr<std::pair<Diag *, fs_ctx>> user_;
+};
+
+inline fs_precond to_precond(op::identity_t) { return {FS_PRECOND_NONE, nullptr, nullptr}; }
+inline fs_precond to_precond(jacobi_t) { return {FS_PRECOND_JACOBI, nullptr, nullptr}; }
+inline fs_precond to_precond(const vec::device_vec &d) { return {FS_PRECOND_DIAG, d.handle(), nullptr}; }
+template<class T>
+fs_precond to_precond(const op::handle<T> &h) { return to_precond(h.get()); }
+
+// settings beyond solver_settings (GMRES)
+inline void fill_extra(const solver_settings &, fs_krylov_settings &) {}
+
+template<class Settings>
+fs_krylov_settings to_c(const Settings &s) {
+	fs_krylov_settings k;
+	fs_krylov_settings_default(&k);
+	k.base.maxiter = s.maxiter;
+	k.base.rtol = s.rtol;
+	k.base.atol = s.atol;
+	k.base.use_zero_guess = s.use_zero_guess ? 1 : 0;
+	fill_extra(s, k);
+	return k;
+}
+
+// work description returned by make_work: the device solver allocates its
+// own work vectors from the exemplar's size (solver_settings.hh:189-200)
+struct work {
+	std::size_t n;
+};
+
+// krylov_solver<OpType, Settings, Work> (krylov_parameters.hh:94-126)
+template<class Settings, int Method>
+struct krylov_solver {
+	Settings settings;
+	work workspace;
+
+	krylov_solver(Settings s, work w) : settings(std::move(s)), workspace(w) {}
+
+	template<class P = op::identity_t, class D = std::decay_t<decltype(default_diagnostic)>>
+	auto operator()(const op::handle<mat::csr> &A, const P &precond = op::I,
+	                D diag = default_diagnostic) const {
+		return bound_solver<D>(Method, to_c(settings), A.get(), to_precond(precond), std::move(diag));
+	}
+	template<class P, class D>
+	auto operator()(const op::handle<mat::csr> &A, const P &precond,
+	                std::reference_wrapper<D> diag) const {
+		return bound_solver<std::reference_wrapper<D>>(Method, to_c(settings), A.get(),
+		                                               to_precond(precond), diag);
+	}
+};
+
+}  // namespace detail
+
+// the Jacobi (D^-1) preconditioner computed from A on the device
+inline constexpr detail::jacobi_t jacobi{};
+
+namespace cg {
+static constexpr std::size_t nwork = 4;  // cg.hh:252
+using settings = solver_settings;        // cg.hh:254
+inline detail::work make_work(const vec::device_vec &b) { return {b.local_size()}; }
+using solver = detail::krylov_solver<settings, FS_CG>;
+}  // namespace cg
+
+namespace bicgstab {
+static constexpr std::size_t nwork = 8;  // bicgstab.hh:195
+struct settings : solver_settings {};    // bicgstab.hh:197
+inline detail::work make_work(const vec::device_vec &b) { return {b.local_size()}; }
+using solver = detail::krylov_solver<settings, FS_BICGSTAB>;
+}  // namespace bicgstab
+
+namespace gmres {
+static constexpr int krylov_dim_bound = 100;                       // gmres.hh:31
+static constexpr std::size_t nwork = (krylov_dim_bound + 1) + 3;   // gmres.hh:32
+enum class precond_side { left, right };                           // gmres.hh:33
+struct settings : solver_settings {                                // gmres.hh:389-405
+	int max_krylov_dim;
+	precond_side pre_side;
+	bool restart;
+};
+inline detail::work make_work(const vec::device_vec &b) { return {b.local_size()}; }
+using solver = detail::krylov_solver<settings, FS_GMRES>;
+}  // namespace gmres
+
+namespace gmres {
+// found by argument-dependent lookup from detail::to_c
+inline void fill_extra(const settings &s, fs_krylov_settings &k) {
+	k.max_krylov_dim = s.max_krylov_dim;
+	k.pre_side = s.pre_side == precond_side::left ? FS_LEFT : FS_RIGHT;
+	k.restart = s.restart ? 1 : 0;
+}
+}  // namespace gmres
+
+// FP32-inner / FP64-refined variants (no counterpart in the reference)
+namespace mixed {
+using cg_solver = detail::krylov_solver<cg::settings, FS_CG_MIXED>;
+using bicgstab_solver = detail::krylov_solver<bicgstab::settings, FS_BICGSTAB_MIXED>;
+using gmres_solver = detail::krylov_solver<gmres::settings, FS_GMRES_MIXED>;
+}  // namespace mixed
+
+}  // namespace flecsolve

@@ -1,0 +1,201 @@
+// The C++ mirror of flecsolve's Krylov API (include/flecsolve_gb300/
+// flecsolve.hh) driving the device solvers, written the way the reference's
+// own tests are (flecsolve/solvers/test/cg.cc, gmres.cc, bicgstab.cc,
+// flecsolve/vectors/test/flecsi_vector.cc).  Prints one PASS/FAIL line per
+// check; the exit status is the number of failures.
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "flecsolve_gb300/flecsolve.hh"
+
+// seeded problem generators of libfsproblems.so
+extern "C" {
+int64_t fsp_grid_rows(int dim, int64_t n);
+int64_t fsp_grid_nnz(int dim, int64_t n);
+int64_t fsp_grid_faces(int dim, int64_t n);
+void fsp_faces_const(int dim, int64_t n, double c, double *faces);
+void fsp_faces_lognormal(int dim, int64_t n, double mu, double sigma, uint64_t seed, double *faces,
+                         double *cells);
+void fsp_assemble_diffusion(int dim, int64_t n, const double *faces, int64_t *rowptr, int32_t *col,
+                            double *val);
+void fsp_assemble_convdiff3d(int64_t n, double pe_max, uint64_t seed, int64_t *rowptr, int32_t *col,
+                             double *val, double *vel);
+void fsp_uniform(uint64_t seed, int64_t n, double lo, double hi, double *out);
+}
+
+using namespace flecsolve;
+
+static int failures = 0;
+static void expect(bool ok, const char *what) {
+	std::printf("%s %s\n", ok ? "PASS" : "FAIL", what);
+	if (!ok)
+		++failures;
+}
+
+struct host_csr {
+	std::size_t n;
+	std::vector<int64_t> rp;
+	std::vector<int32_t> col;
+	std::vector<double> val;
+};
+
+static host_csr diffusion(int dim, int64_t n, bool lognormal) {
+	host_csr A;
+	A.n = fsp_grid_rows(dim, n);
+	std::vector<double> faces(fsp_grid_faces(dim, n));
+	if (lognormal)
+		fsp_faces_lognormal(dim, n, 0.0, 1.0, 2, faces.data(), nullptr);
+	else
+		fsp_faces_const(dim, n, 1.0, faces.data());
+	A.rp.resize(A.n + 1);
+	A.col.resize(fsp_grid_nnz(dim, n));
+	A.val.resize(A.col.size());
+	fsp_assemble_diffusion(dim, n, faces.data(), A.rp.data(), A.col.data(), A.val.data());
+	return A;
+}
+
+static host_csr convdiff(int64_t n) {
+	host_csr A;
+	A.n = n * n * n;
+	A.rp.resize(A.n + 1);
+	A.col.resize(fsp_grid_nnz(3, n));
+	A.val.resize(A.col.size());
+	fsp_assemble_convdiff3d(n, 5.0, 4, A.rp.data(), A.col.data(), A.val.data(), nullptr);
+	return A;
+}
+
+// cg.cc:16-54: with b = 0 the error is x itself; CG must decrease its A-norm
+// monotonically, and the diagnostic runs once per iteration
+struct anorm_diagnostic {
+	anorm_diagnostic(const mat::csr &A, const vec::device_vec &x0, const context &c)
+		: A(A), Ax(c, x0.local_size()) {
+		A.apply(x0, Ax);
+		e_prev = std::sqrt(x0.dot(Ax).get());
+	}
+	bool operator()(const vec::device_vec &x, double) {
+		A.apply(x, Ax);
+		double e = std::sqrt(x.dot(Ax).get());
+		monotonic_fail = monotonic_fail || (e > e_prev);
+		e_prev = e;
+		++iter;
+		return false;
+	}
+	const mat::csr &A;
+	vec::device_vec Ax;
+	double e_prev = 0;
+	int iter = 0;
+	bool monotonic_fail = false;
+};
+
+int main() {
+	context ctx;
+
+	// ------------------------------------------- vector closed forms --
+	{
+		// flecsi_vector.cc:21-57, 309-401 on 32 dofs
+		std::vector<double> gx(32), gy(32), gz(32);
+		for (int i = 0; i < 32; ++i) {
+			gx[i] = i;
+			gy[i] = 2.0 * i;
+			gz[i] = 3.0 * i;
+		}
+		vec::device_vec x(ctx, gx), y(ctx, gy), z(ctx, gz), tmp(ctx, 32);
+		tmp.add(x, z);
+		auto h = tmp.download();
+		bool ok = true;
+		for (int i = 0; i < 32; ++i)
+			ok = ok && h[i] == 4.0 * i;
+		expect(ok, "vec add");
+		tmp.add_scalar(y, -7);
+		expect(tmp.min().get() == -7, "vec min == -7");
+		expect(z.max().get() == 93, "vec max == 93");
+		x.set_scalar(1.5);
+		y.set_scalar(3.8);
+		expect(std::fabs(x.dot(y).get() - 32 * 1.5 * 3.8) < 1e-8, "vec dot");
+		x.set_scalar(-3.141719);
+		expect(std::fabs(x.l1norm().get() - 32 * 3.141719) < 1e-8, "vec l1norm");
+		expect(std::fabs(x.l2norm().get() - std::sqrt(32.0) * 3.141719) < 1e-8, "vec l2norm");
+	}
+
+	// ------------------------------------------- CG (cg.cc style) --------
+	{
+		host_csr H = diffusion(2, 64, false);
+		mat::csr A(ctx, H.n, H.n, H.rp, H.col, H.val);
+		vec::device_vec b(ctx, H.n), x(ctx, H.n);
+		b.set_scalar(0.0);
+		x.set_random(7);
+		anorm_diagnostic diag{A, x, ctx};
+		cg::settings s{2000, 1e-9f, 1e-9f, false};  // cg.cfg
+		auto slv_op = cg::solver(s, cg::make_work(b))(op::ref(A), op::I, std::ref(diag));
+		auto info = slv_op(b, x);
+		expect(info.status == solve_info::stop_reason::converged_rtol, "cg converged (b = 0, x0 random)");
+		expect(!diag.monotonic_fail, "cg A-norm error monotone");
+		expect(info.iters == diag.iter, "cg diagnostic called once per iteration");
+	}
+	{
+		// the reference's iteration count on the 128^2 Poisson problem
+		// (tests/golden: 389 with Jacobi, rtol 1e-8, zero guess)
+		host_csr H = diffusion(2, 128, false);
+		mat::csr A(ctx, H.n, H.n, H.rp, H.col, H.val);
+		std::vector<double> hb(H.n);
+		fsp_uniform(1, (int64_t)H.n, -1.0, 1.0, hb.data());
+		vec::device_vec b(ctx, hb), x(ctx, H.n);
+		auto info = cg::solver(cg::settings{2000, 1e-8f, 0.f, true}, cg::make_work(b))(op::ref(A), jacobi)(b, x);
+		expect(info.success() && std::abs(info.iters - 389) <= 2, "cg jacobi poisson2d-128: 389 +- 2 iterations");
+		vec::device_vec d = A.Dinv(ctx);
+		auto info2 = cg::solver(cg::settings{2000, 1e-8f, 0.f, true}, cg::make_work(b))(op::ref(A), d)(b, x);
+		expect(info2.iters == info.iters, "cg with the D^-1 vector == cg with jacobi");
+		auto info3 = mixed::cg_solver(cg::settings{2000, 1e-8f, 0.f, true}, cg::make_work(b))(op::ref(A), jacobi)(b, x);
+		expect(info3.success() && std::abs(info3.iters - info.iters) <= 2, "mixed cg: same iteration count");
+	}
+
+	// ------------------------------------------- BiCGSTAB ----------------
+	{
+		host_csr H = convdiff(16);
+		mat::csr A(ctx, H.n, H.n, H.rp, H.col, H.val);
+		vec::device_vec b(ctx, H.n), x(ctx, H.n);
+		b.set_random(0);
+		x.set_random(1);
+		bicgstab::settings s{{200, 1e-9f, 0.f, false}};  // bicgstab.cfg
+		bicgstab::solver slv(s, bicgstab::make_work(b));
+		auto info = slv(op::ref(A))(b, x);
+		expect(info.status == solve_info::stop_reason::converged_rtol, "bicgstab converged_rtol");
+	}
+
+	// ------------------------------------------- GMRES (gmres.cc style) --
+	{
+		host_csr H = convdiff(12);
+		mat::csr A(ctx, H.n, H.n, H.rp, H.col, H.val);
+		vec::device_vec b(ctx, H.n), x(ctx, H.n);
+		std::vector<double> hx(H.n);
+		fsp_uniform(1, (int64_t)H.n, 0.0, 1.0, hx.data());
+		b.set_random(0);
+		x.upload(hx);
+		gmres::settings sr{{100, 1e-4f, 0.f, false}, 50, gmres::precond_side::right, true};
+		gmres::solver slv(sr, gmres::make_work(b));
+		auto info_restart = slv(op::ref(A))(b, x);
+		x.upload(hx);
+		slv.settings.maxiter = 50;
+		slv(op::ref(A))(b, x);
+		slv.settings.maxiter = 100;
+		slv.settings.max_krylov_dim = 100;
+		slv.settings.restart = false;
+		auto slv1 = slv(op::ref(A));
+		auto info = slv1.apply(b, x);
+		expect(info_restart.success(), "gmres restarted run converged");
+		expect(50 + info.iters == info_restart.iters, "gmres restart consistency: iterations");
+		expect(info.res_norm_final == info_restart.res_norm_final, "gmres restart consistency: residual");
+		gmres::settings bad{{10, 1e-4f, 0.f, false}, 5, gmres::precond_side::right, false};
+		bool threw = false;
+		try {
+			gmres::solver(bad, gmres::make_work(b))(op::ref(A));
+		}
+		catch (const fs_error &e) {
+			threw = e.status == FS_ERR_BREAKDOWN;
+		}
+		expect(threw, "gmres validate(): restart = false with maxiter > max_krylov_dim rejected");
+	}
+	std::printf("%d failure(s)\n", failures);
+	return failures;
+}

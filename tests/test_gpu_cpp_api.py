@@ -1,0 +1,20 @@
+"""The C++ mirror of the reference's API, exercised by tests/cpp/
+test_krylov_api.cc (written like the reference's own cg.cc / gmres.cc /
+bicgstab.cc / flecsi_vector.cc tests) against the device library."""
+import subprocess
+
+import pytest
+
+from flecsolve_gb300 import build
+
+pytestmark = pytest.mark.gpu
+
+
+def test_cpp_api_program():
+    exe = build.build_cpp_tests()
+    r = subprocess.run([str(exe)], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       timeout=600)
+    print(r.stdout)
+    assert "FAIL" not in r.stdout
+    assert r.returncode == 0, r.stdout
+    assert r.stdout.count("PASS") >= 15

@@ -101,3 +101,10 @@ def test_lognormal_statistics():
     f, cells = P.faces_lognormal(3, 20, seed=2, return_cells=True)
     lg = np.log(cells)
     assert abs(lg.mean()) < 0.05 and abs(lg.std() - 1.0) < 0.05
+
+
+def test_cpp_api_header_compiles_and_links():
+    """The C++ mirror of the reference's API builds against the C ABI
+    (running it needs a GPU: tests/test_gpu_cpp_api.py)."""
+    exe = build.build_cpp_tests()
+    assert exe.exists()
