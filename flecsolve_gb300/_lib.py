@@ -127,6 +127,11 @@ _PROTOS = {
     "fs_krylov_apply": [_vp, _vp, _vp, C.POINTER(SolveInfo)],
     "fs_krylov_history": [_vp, _dp, C.POINTER(_i64)],
     "fs_krylov_mixed_stats": [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "fs_batch_cg_solve": [_vp, C.POINTER(KrylovSettings), _vp, C.c_int, C.POINTER(_i64), _vp, _vp,
+                          C.c_int, C.c_int, C.POINTER(SolveInfo)],
+    "fs_batch_tuning": [_vp, _vp, C.c_int, C.POINTER(_i64), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "fs_block_cg_solve": [_vp, C.POINTER(KrylovSettings), _vp, C.POINTER(Precond), C.c_int, _vp, _vp,
+                          C.POINTER(SolveInfo)],
 }
 
 # entry points that exist in the header but are optional for older builds

@@ -30,7 +30,8 @@ import numpy as np
 from . import _lib
 from ._lib import check, lib
 
-__all__ = ["Context", "Vector", "CSR", "SolveInfo", "Future", "op", "vec", "mat",
+__all__ = ["Context", "Vector", "Multi", "CSR", "SolveInfo", "Future", "op", "vec", "mat",
+           "batch_cg", "batch_tuning", "block_cg",
            "cg", "bicgstab", "gmres", "mixed_cg", "mixed_bicgstab", "mixed_gmres"]
 
 
@@ -243,10 +244,14 @@ class Vector:
 
 
 class CSR:
-    """Device CSR operator (``op::core<mat::csr<double>>``)."""
+    """Device CSR operator (``op::core<mat::csr<double>>``).  ``var`` is the
+    operator's input/output variable (``op::base<Params, ivar, ovar>``,
+    operators/core.hh:29-34): applied to a :class:`Multi` the operator acts on
+    that component (``op::core::apply`` subsets, core.hh:107-116)."""
 
-    def __init__(self, ctx: Context, A):
+    def __init__(self, ctx: Context, A, var=None):
         self.ctx = ctx
+        self.var = var
         self.nrows, self.ncols = int(A.nrows), int(A.ncols)
         rp = np.ascontiguousarray(A.rowptr, dtype=np.int64)
         col = np.ascontiguousarray(A.col)
@@ -280,8 +285,12 @@ class CSR:
         check(lib().fs_csr_shape(self.h, None, None, C.byref(n)), self.ctx.h)
         return n.value
 
+    def _sub(self, v):
+        return v.subset(self.var) if isinstance(v, Multi) else v
+
     def apply(self, x: Vector, y: Vector, exact: bool = False):
         """y = A x (op::core::apply, operators/core.hh:107-116)."""
+        x, y = self._sub(x), self._sub(y)
         check(lib().fs_csr_spmv(self.h, x.h, y.h, _lib.SPMV_EXACT if exact else _lib.SPMV_FMA),
               self.ctx.h, "spmv")
 
@@ -289,6 +298,7 @@ class CSR:
 
     def residual(self, b: Vector, x: Vector, r: Vector):
         """r = b - A x (op::core::residual, operators/core.hh:129-142)."""
+        b, x, r = self._sub(b), self._sub(x), self._sub(r)
         check(lib().fs_csr_residual(self.h, b.h, x.h, r.h), self.ctx.h, "residual")
 
     def apply_transpose(self, x: Vector, y: Vector):
@@ -308,6 +318,88 @@ class CSR:
         return d
 
 
+class Multi:
+    """``vec::multi``: a tuple of component vectors tagged with variables
+    (flecsolve/vectors/multi.hh:74-160, operations/multi.hh:27-277).
+
+    The components are views into one contiguous device allocation, so the
+    multivector is also one :class:`Vector` (``whole``) for solvers bound to
+    an operator on all components.  Elementwise operations act on every
+    component; reductions combine the per-component reductions the way the
+    reference's multi ops do (sum of dots, sqrt of the summed squares, max /
+    min over components, in component order)."""
+
+    def __init__(self, ctx: Context, parts, vars=None, dtype: str = "f64"):
+        arrays = [np.asarray(p) if not isinstance(p, (int, np.integer)) else None for p in parts]
+        sizes = [int(p) if a is None else int(a.size) for p, a in zip(parts, arrays)]
+        self.ctx = ctx
+        self.vars = list(vars) if vars is not None else list(range(len(sizes)))
+        self.whole = Vector(ctx, sum(sizes), dtype)
+        es = 4 if dtype == "f32" else 8
+        base = self.whole.device_ptr
+        self.components, off = [], 0
+        for n, a in zip(sizes, arrays):
+            c = Vector.wrap(ctx, n, base + off * es, dtype)
+            c._owner = self.whole  # keep the allocation alive
+            if a is not None:
+                c.upload(a)
+            self.components.append(c)
+            off += n
+
+    # -- access (multi.hh:94-159)
+    def get(self, i: int) -> Vector:
+        return self.components[i]
+
+    def subset(self, var) -> Vector:
+        return self.components[self.vars.index(var)]
+
+    def __len__(self):
+        return len(self.whole)
+
+    def numpy(self):
+        return [c.numpy() for c in self.components]
+
+    # -- elementwise: the same operation on each component
+    def _each(self, name, *args):
+        for i, c in enumerate(self.components):
+            a = [x.components[i] if isinstance(x, Multi) else x for x in args]
+            getattr(c, name)(*a)
+
+    def copy(self, src): self._each("copy", src)
+    def zero(self): self._each("zero")
+    def set_scalar(self, v): self._each("set_scalar", v)
+    def scale(self, a, x=None): self._each("scale", a) if x is None else self._each("scale", a, x)
+    def add(self, x, y): self._each("add", x, y)
+    def subtract(self, x, y): self._each("subtract", x, y)
+    def multiply(self, x, y): self._each("multiply", x, y)
+    def divide(self, x, y): self._each("divide", x, y)
+    def reciprocal(self, x): self._each("reciprocal", x)
+    def linear_sum(self, a, x, b, y): self._each("linear_sum", a, x, b, y)
+    def axpy(self, a, x, y): self._each("axpy", a, x, y)
+    def axpby(self, a, b, x): self._each("axpby", a, b, x)
+    def abs(self, x): self._each("abs", x)
+    def add_scalar(self, x, a): self._each("add_scalar", x, a)
+
+    # -- reductions combined over components (operations/multi.hh:179-253)
+    def dot(self, x):
+        return Future(sum(c.dot(xc).get() for c, xc in zip(self.components, x.components)))
+
+    def l1norm(self):
+        return Future(sum(c.l1norm().get() for c in self.components))
+
+    def l2norm(self):
+        return Future(float(np.sqrt(sum(c.dot(c).get() for c in self.components))))
+
+    def inf_norm(self):
+        return Future(max(c.inf_norm().get() for c in self.components))
+
+    def min(self):
+        return Future(min(c.min().get() for c in self.components))
+
+    def max(self):
+        return Future(max(c.max().get() for c in self.components))
+
+
 # ------------------------------------------------------------- op:: ----
 
 class _Identity:
@@ -320,7 +412,8 @@ class _Jacobi:
 
 op = SimpleNamespace(I=_Identity(), jacobi=_Jacobi(), ref=lambda A: A, cref=lambda A: A,
                      make_shared=lambda A: A)
-vec = SimpleNamespace(make=lambda ctx, a, dtype="f64": Vector(ctx, a, dtype), Vector=Vector)
+vec = SimpleNamespace(make=lambda ctx, a, dtype="f64": Vector(ctx, a, dtype), Vector=Vector,
+                      multi=Multi)
 mat = SimpleNamespace(csr=CSR)
 
 
@@ -424,6 +517,11 @@ class BoundSolver:
         check(lib().fs_krylov_settings_set(self.h, C.byref(s)), self.ctx.h)
 
     def apply(self, b: Vector, x: Vector) -> SolveInfo:
+        # op::core::apply subsets by the operator's variables (core.hh:107-116)
+        if isinstance(b, Multi):
+            b = b.subset(self.A.var) if self.A.var is not None else b.whole
+        if isinstance(x, Multi):
+            x = x.subset(self.A.var) if self.A.var is not None else x.whole
         info = _lib.SolveInfo()
         st = lib().fs_krylov_apply(self.h, b.h, x.h, C.byref(info))
         out = SolveInfo(_lib.STOP_REASONS.get(info.status, str(info.status)), info.iters,
@@ -457,6 +555,49 @@ class BoundSolver:
                 self.h = None
         except Exception:
             pass
+
+
+def _info(i) -> "SolveInfo":
+    return SolveInfo(_lib.STOP_REASONS.get(i.status, str(i.status)), i.iters, i.restarts,
+                     i.res_norm_initial, i.res_norm_final, i.sol_norm_initial, i.sol_norm_final,
+                     i.rhs_norm)
+
+
+def batch_cg(A: CSR, offsets, b: Vector, x: Vector, maxiter: int, rtol: float,
+             use_zero_guess: bool = True, delta: float = 1e-2, cluster: int = 0,
+             threads: int = 0):
+    """Solve the independent systems on the diagonal blocks of ``A`` (system
+    s = rows offsets[s]:offsets[s+1]) in one persistent launch, one thread-
+    block cluster per system; returns one :class:`SolveInfo` per system.
+    ``cluster``/``threads`` = 0 lets the autotuner choose."""
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    nsys = off.size - 1
+    st = _settings(_lib.CG_MIXED, maxiter, rtol, 0.0, use_zero_guess, inner_rtol=delta)
+    infos = (_lib.SolveInfo * nsys)()
+    check(lib().fs_batch_cg_solve(A.ctx.h, C.byref(st), A.h, nsys,
+                                  off.ctypes.data_as(C.POINTER(C.c_int64)), b.h, x.h, int(cluster),
+                                  int(threads), infos), A.ctx.h, "fs_batch_cg_solve")
+    return [_info(i) for i in infos]
+
+
+def block_cg(A: CSR, B: Vector, X: Vector, nrhs: int, maxiter: int, rtol: float,
+             use_zero_guess: bool = True, jacobi: bool = True, k_readback: int = 16):
+    """Block Jacobi-PCG on ``nrhs`` right-hand sides stored N x nrhs row-major
+    in ``B`` / ``X``; returns one :class:`SolveInfo` per column."""
+    st = _settings(_lib.CG, maxiter, rtol, 0.0, use_zero_guess, k_readback=k_readback)
+    pc = _lib.Precond(_lib.PRECOND_JACOBI if jacobi else _lib.PRECOND_NONE, None, None)
+    infos = (_lib.SolveInfo * nrhs)()
+    check(lib().fs_block_cg_solve(A.ctx.h, C.byref(st), A.h, C.byref(pc), nrhs, B.h, X.h, infos),
+          A.ctx.h, "fs_block_cg_solve")
+    return [_info(i) for i in infos]
+
+
+def batch_tuning(A: CSR, offsets):
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    c, t = C.c_int(), C.c_int()
+    check(lib().fs_batch_tuning(A.ctx.h, A.h, off.size - 1, off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                C.byref(c), C.byref(t)), A.ctx.h, "fs_batch_tuning")
+    return c.value, t.value
 
 
 class _SolverFactory:

@@ -1,0 +1,854 @@
+// Batched solves: many independent systems of uneven size in one persistent
+// launch.
+//
+// The systems are the diagonal blocks of one block-diagonal CSR matrix
+// (rows [off[s], off[s+1]) couple only among themselves).  One thread-block
+// cluster owns one system and runs its whole Jacobi-PCG loop without leaving
+// the kernel: each CTA of the cluster owns a contiguous slice of the
+// system's rows, the per-iteration reductions are folded through distributed
+// shared memory (every CTA reads the cluster's partials in rank order, so all
+// CTAs obtain the same bits), and hardware cluster barriers order the phases.
+// A system stops on its own convergence test; the rest of the grid keeps
+// working (per-system convergence masks without any host round trip).
+//
+// Arithmetic (the reference's cg.hh:43-139 recurrences): FP32 values and
+// vectors, dots accumulated in FP64; the residual is replaced by the FP64 one,
+// b - A x with the FP64 values, whenever it has dropped by `delta` and at
+// every stop, and the stopping test is on that FP64 residual.
+//
+// Block CG (several right-hand sides of one operator) lives at the end of the
+// file.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <vector>
+
+#include "solver.cuh"
+
+namespace cgrp = cooperative_groups;
+
+namespace fsg {
+
+namespace {
+
+struct BatchArgs {
+	int nsys;
+	const int *order;        // system processed by cluster c (largest first)
+	const int64_t *off;      // row offsets, nsys + 1
+	const int *rowptr;
+	const int *col;
+	const float *val32;
+	const double *val64;
+	const float *dinv32;
+	const double *dinv64;
+	const double *b;
+	double *x;               // FP64 solution
+	float *x32, *r32, *p32, *w32;  // FP32 work (correction, residual, direction, A p)
+	fs_solve_info *info;     // per system
+	int maxiter;
+	float rtol;
+	double delta;
+	int zero_guess;
+};
+
+// sum of NV doubles over the cluster: every CTA block-reduces its values,
+// publishes them in its shared slot for phase `ph`, and after the cluster
+// barrier reads all CTAs' slots in rank order
+template<int NV>
+__device__ __forceinline__ void cluster_sum(double (&v)[NV], double *sh_tree,
+                                            double (*slots)[4], int ph, cgrp::cluster_group &cl) {
+	block_sum<NV>(v, sh_tree);
+	if (threadIdx.x == 0)
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			slots[ph & 1][k] = v[k];
+	__threadfence();
+	cl.sync();
+	double t[NV];
+#pragma unroll
+	for (int k = 0; k < NV; ++k)
+		t[k] = 0.0;
+	for (unsigned r = 0; r < cl.num_blocks(); ++r) {
+		double(*rs)[4] = cl.map_shared_rank(slots, r);
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			t[k] += rs[ph & 1][k];
+	}
+#pragma unroll
+	for (int k = 0; k < NV; ++k)
+		v[k] = t[k];
+}
+
+__global__ void __launch_bounds__(1024)
+k_batch_cg(BatchArgs a) {
+	cgrp::cluster_group cl = cgrp::this_cluster();
+	const int crank = (int)cl.block_rank();
+	const int csize = (int)cl.num_blocks();
+	const int cidx = (int)(blockIdx.x / csize);
+	if (cidx >= a.nsys)
+		return;  // uniform across the cluster
+	const int sys = a.order[cidx];
+	const int64_t R0 = a.off[sys], R1 = a.off[sys + 1];
+	const int64_t nrow = R1 - R0;
+	const int64_t chunk = (nrow + csize - 1) / csize;
+	const int64_t lo = chunk * crank, hi = chunk * (crank + 1);
+	const int64_t r0 = R0 + (lo < nrow ? lo : nrow);
+	const int64_t r1 = R0 + (hi < nrow ? hi : nrow);
+	__shared__ double sh_tree[4 * 32];
+	__shared__ double slots[2][4];
+	int ph = 0;
+	const int tid = threadIdx.x, nt = blockDim.x;
+
+	// ||b|| and the initial residual (FP64): r = b - A x (or b), x32 = 0
+	double v2[2] = {0.0, 0.0};
+	for (int64_t i = r0 + tid; i < r1; i += nt) {
+		const double bi = a.b[i];
+		v2[0] = fma(bi, bi, v2[0]);
+		if (a.zero_guess)
+			a.x[i] = 0.0;
+		v2[1] = fma(a.x[i], a.x[i], v2[1]);
+		a.x32[i] = 0.f;
+	}
+	cluster_sum<2>(v2, sh_tree, slots, ph++, cl);
+	double bnorm = sqrt(v2[0]);
+	const double rhs_norm = bnorm;
+	if (bnorm == 0.0)
+		bnorm = 1.0;
+	const double tol = (double)a.rtol * bnorm;
+	const double sol0 = sqrt(v2[1]);
+
+	// FP64 residual replacement: r64 = b - A64 x, r32 = (float) r64; returns
+	// ||r64|| and r32 . D^-1 r32 (all CTAs of the cluster get the same)
+	auto replace = [&](double &res, double &rz) {
+		double t[2] = {0.0, 0.0};
+		for (int64_t i = r0 + tid; i < r1; i += nt) {
+			double s = 0.0;
+			for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k)
+				s = fma(a.val64[k], a.x[a.col[k]], s);
+			const double ri = a.b[i] - s;
+			const float r32 = (float)ri;
+			a.r32[i] = r32;
+			t[0] = fma(ri, ri, t[0]);
+			t[1] = fma((double)r32, (double)(a.dinv32[i] * r32), t[1]);
+		}
+		cluster_sum<2>(t, sh_tree, slots, ph++, cl);
+		res = sqrt(t[0]);
+		rz = t[1];
+	};
+	double res = 0.0, rz = 0.0;
+	replace(res, rz);
+	const double res0 = res;
+	double rmax = res;
+	int status = FS_DIVERGED_ITERS;
+	int iters = 0, outer = 0;
+	if (res < tol) {
+		status = FS_CONVERGED_RTOL;
+	}
+	else {
+		// p = D^-1 r, rho = r . z
+		for (int64_t i = r0 + tid; i < r1; i += nt)
+			a.p32[i] = a.dinv32[i] * a.r32[i];
+		double rho = rz;
+		__threadfence();
+		cl.sync();
+		for (int it = 0; it < a.maxiter; ++it) {
+			// w = A p, p . w
+			double q[1] = {0.0};
+			for (int64_t i = r0 + tid; i < r1; i += nt) {
+				float s = 0.f;
+				for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k)
+					s = fmaf(a.val32[k], a.p32[a.col[k]], s);
+				a.w32[i] = s;
+				q[0] = fma((double)s, (double)a.p32[i], q[0]);
+			}
+			cluster_sum<1>(q, sh_tree, slots, ph++, cl);
+			const double alpha = rho / q[0];
+			const float af = (float)alpha;
+			// x32 += alpha p, r -= alpha w, ||r||^2, r . z
+			double u[2] = {0.0, 0.0};
+			for (int64_t i = r0 + tid; i < r1; i += nt) {
+				a.x32[i] = fmaf(af, a.p32[i], a.x32[i]);
+				const float ri = fmaf(-af, a.w32[i], a.r32[i]);
+				a.r32[i] = ri;
+				u[0] = fma((double)ri, (double)ri, u[0]);
+				u[1] = fma((double)ri, (double)(a.dinv32[i] * ri), u[1]);
+			}
+			cluster_sum<2>(u, sh_tree, slots, ph++, cl);
+			iters = it + 1;
+			double est = sqrt(u[0]);
+			double rz_new = u[1];
+			const bool last = iters >= a.maxiter;
+			if (est < a.delta * rmax || est < tol || last || !isfinite(est)) {
+				// fold the correction and replace r by the FP64 residual
+				for (int64_t i = r0 + tid; i < r1; i += nt) {
+					a.x[i] += (double)a.x32[i];
+					a.x32[i] = 0.f;
+				}
+				__threadfence();
+				cl.sync();
+				replace(res, rz_new);
+				++outer;
+				rmax = res;
+				if (res < tol) {
+					status = FS_CONVERGED_RTOL;
+					break;
+				}
+				if (last || !isfinite(res))
+					break;
+			}
+			else {
+				res = est;
+			}
+			const double beta = rz_new / rho;
+			rho = rz_new;
+			const float bf = (float)beta;
+			for (int64_t i = r0 + tid; i < r1; i += nt)
+				a.p32[i] = fmaf(bf, a.p32[i], a.dinv32[i] * a.r32[i]);
+			__threadfence();
+			cl.sync();
+		}
+	}
+	double xn[1] = {0.0};
+	for (int64_t i = r0 + tid; i < r1; i += nt)
+		xn[0] = fma(a.x[i], a.x[i], xn[0]);
+	cluster_sum<1>(xn, sh_tree, slots, ph++, cl);
+	if (crank == 0 && tid == 0) {
+		fs_solve_info inf;
+		inf.status = status;
+		inf.iters = status == FS_CONVERGED_RTOL ? iters : 0;
+		inf.restarts = outer;
+		inf.res_norm_initial = (float)res0;
+		inf.res_norm_final = (float)res;
+		inf.sol_norm_initial = a.zero_guess ? 0.f : (float)sol0;
+		inf.sol_norm_final = (float)sqrt(xn[0]);
+		inf.rhs_norm = (float)rhs_norm;
+		a.info[sys] = inf;
+	}
+	// no CTA may leave while a peer can still read its shared slots
+	cl.sync();
+}
+
+struct BatchPlan {
+	std::vector<int64_t> off;
+	int64_t *d_off = nullptr;
+	int *d_order = nullptr;
+	fs_solve_info *d_info = nullptr;
+	float *work = nullptr;  // x32, r32, p32, w32
+	int nsys = 0;
+	int tuned_cluster = 0, tuned_threads = 0;
+};
+
+// one plan per (matrix, partition); freed with the context process
+std::map<std::pair<const Csr *, std::vector<int64_t>>, BatchPlan> g_plans;
+
+int launch_batch(Ctx *ctx, const BatchArgs &a, int nsys, int cluster, int threads) {
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3((unsigned)(nsys * cluster), 1, 1);
+	cfg.blockDim = dim3((unsigned)threads, 1, 1);
+	cfg.dynamicSmemBytes = 0;
+	cfg.stream = ctx->stream;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeClusterDimension;
+	attr[0].val.clusterDim.x = (unsigned)cluster;
+	attr[0].val.clusterDim.y = 1;
+	attr[0].val.clusterDim.z = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	cudaError_t e = cudaLaunchKernelEx(&cfg, k_batch_cg, a);
+	if (e != cudaSuccess)
+		return set_err(ctx, FS_ERR_CUDA, "batched CG launch (cluster %d, %d threads): %s", cluster,
+		               threads, cudaGetErrorString(e));
+	ctx->launches++;
+	return FS_OK;
+}
+
+}  // namespace
+
+}  // namespace fsg
+
+using namespace fsg;
+
+extern "C" FS_API int fs_batch_cg_solve(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah, int nsys,
+                                        const int64_t *sys_offsets, fs_vec bh, fs_vec xh,
+                                        int cluster_size, int threads, fs_solve_info *infos) {
+	Ctx *ctx = reinterpret_cast<Ctx *>(h);
+	Csr *A = reinterpret_cast<Csr *>(Ah);
+	Vec *b = reinterpret_cast<Vec *>(bh), *x = reinterpret_cast<Vec *>(xh);
+	if (!ok_ctx(ctx) || !ok_csr(A) || !ok_vec(b) || !ok_vec(x) || !s || !sys_offsets || !infos)
+		return FS_ERR_BAD_HANDLE;
+	if (nsys < 1 || sys_offsets[0] != 0 || sys_offsets[nsys] != A->nrows || A->nrows != A->ncols ||
+	    b->n != A->nrows || x->n != A->nrows || b->dtype != FS_F64 || x->dtype != FS_F64)
+		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_batch_cg_solve: offsets/sizes do not match");
+	if (cluster_size != 0 && (cluster_size < 1 || cluster_size > 8 ||
+	                          (cluster_size & (cluster_size - 1))))
+		return set_err(ctx, FS_ERR_INVALID_ARG, "cluster_size must be 0 (autotune), 1, 2, 4 or 8");
+	if (threads != 0 && (threads < 64 || threads > 1024 || threads % 32))
+		return set_err(ctx, FS_ERR_INVALID_ARG, "threads must be 0 (autotune) or 64..1024, a multiple of 32");
+	cudaSetDevice(ctx->device);
+	std::vector<int64_t> off(sys_offsets, sys_offsets + nsys + 1);
+	for (int k = 0; k < nsys; ++k)
+		if (off[k + 1] < off[k])
+			return set_err(ctx, FS_ERR_INVALID_ARG, "fs_batch_cg_solve: offsets not monotone");
+	auto key = std::make_pair((const Csr *)A, off);
+	auto it = g_plans.find(key);
+	if (it == g_plans.end()) {
+		// check block-diagonality once per partition
+		std::vector<int> hc(A->nnz);
+		FS_CUDA_TRY(ctx, cudaMemcpy(hc.data(), A->col, A->nnz * sizeof(int), cudaMemcpyDeviceToHost));
+		for (int k = 0; k < nsys; ++k)
+			for (int64_t r = off[k]; r < off[k + 1]; ++r)
+				for (int q = A->h_rowptr[r]; q < A->h_rowptr[r + 1]; ++q)
+					if (hc[q] < off[k] || hc[q] >= off[k + 1])
+						return set_err(ctx, FS_ERR_INVALID_ARG,
+						               "fs_batch_cg_solve: row %lld couples outside system %d",
+						               (long long)r, k);
+		BatchPlan p;
+		p.off = off;
+		p.nsys = nsys;
+		// largest systems first (longest-processing-time order)
+		std::vector<int> order(nsys);
+		std::iota(order.begin(), order.end(), 0);
+		std::stable_sort(order.begin(), order.end(), [&](int i, int j) {
+			return off[i + 1] - off[i] > off[j + 1] - off[j];
+		});
+		const size_t n = (size_t)A->nrows;
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.d_off, sizeof(int64_t) * (nsys + 1)));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.d_order, sizeof(int) * nsys));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.d_info, sizeof(fs_solve_info) * nsys));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.work, sizeof(float) * 4 * (n + 32)));
+		FS_CUDA_TRY(ctx, cudaMemcpy(p.d_off, off.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice));
+		FS_CUDA_TRY(ctx, cudaMemcpy(p.d_order, order.data(), sizeof(int) * nsys, cudaMemcpyHostToDevice));
+		it = g_plans.emplace(key, p).first;
+	}
+	BatchPlan &p = it->second;
+	FS_TRY(ensure_val32(A));
+	FS_TRY(ensure_dinv(A));
+	const size_t n = (size_t)A->nrows;
+	BatchArgs a;
+	a.nsys = nsys;
+	a.order = p.d_order;
+	a.off = p.d_off;
+	a.rowptr = A->rowptr;
+	a.col = A->col;
+	a.val32 = A->val32;
+	a.val64 = A->val;
+	a.dinv32 = A->dinv32;
+	a.dinv64 = A->dinv;
+	a.b = (const double *)b->d;
+	a.x = (double *)x->d;
+	a.x32 = p.work;
+	a.r32 = p.work + (n + 32);
+	a.p32 = p.work + 2 * (n + 32);
+	a.w32 = p.work + 3 * (n + 32);
+	a.info = p.d_info;
+	a.maxiter = s->base.maxiter;
+	a.rtol = s->base.rtol;
+	a.delta = s->inner_rtol > 0 ? s->inner_rtol : 1e-2;
+	a.zero_guess = s->base.use_zero_guess ? 1 : 0;
+
+	int cl = cluster_size, th = threads;
+	if (cl == 0 || th == 0) {
+		if (p.tuned_cluster == 0) {
+			// autotuner: time a short capped run of each candidate on this
+			// batch (the solution is restored afterwards) and keep the fastest
+			std::vector<double> xsave(n);
+			FS_CUDA_TRY(ctx, cudaMemcpy(xsave.data(), x->d, n * 8, cudaMemcpyDeviceToHost));
+			BatchArgs t = a;
+			t.maxiter = std::min(a.maxiter, 40);
+			t.zero_guess = 1;
+			float best = 1e30f;
+			cudaEvent_t e0, e1;
+			cudaEventCreate(&e0);
+			cudaEventCreate(&e1);
+			for (int c : {1, 2, 4, 8})
+				for (int tt : {256, 512, 1024}) {
+					if (cluster_size && c != cluster_size)
+						continue;
+					if (threads && tt != threads)
+						continue;
+					cudaEventRecord(e0, ctx->stream);
+					int st = launch_batch(ctx, t, nsys, c, tt);
+					cudaEventRecord(e1, ctx->stream);
+					if (st != FS_OK) {
+						cudaGetLastError();
+						continue;
+					}
+					cudaEventSynchronize(e1);
+					float ms = 0;
+					cudaEventElapsedTime(&ms, e0, e1);
+					if (ms < best) {
+						best = ms;
+						p.tuned_cluster = c;
+						p.tuned_threads = tt;
+					}
+				}
+			cudaEventDestroy(e0);
+			cudaEventDestroy(e1);
+			FS_CUDA_TRY(ctx, cudaMemcpy(x->d, xsave.data(), n * 8, cudaMemcpyHostToDevice));
+			if (p.tuned_cluster == 0)
+				return set_err(ctx, FS_ERR_CUDA, "batched CG: no launch configuration ran");
+		}
+		if (!cl)
+			cl = p.tuned_cluster;
+		if (!th)
+			th = p.tuned_threads;
+	}
+	FS_TRY(launch_batch(ctx, a, nsys, cl, th));
+	FS_CUDA_TRY(ctx, cudaMemcpyAsync(infos, p.d_info, sizeof(fs_solve_info) * nsys, cudaMemcpyDeviceToHost,
+	                                 ctx->stream));
+	FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	return FS_OK;
+}
+
+extern "C" FS_API int fs_batch_tuning(fs_ctx h, fs_csr Ah, int nsys, const int64_t *sys_offsets,
+                                      int *cluster_size, int *threads) {
+	Ctx *ctx = reinterpret_cast<Ctx *>(h);
+	Csr *A = reinterpret_cast<Csr *>(Ah);
+	if (!ok_ctx(ctx) || !ok_csr(A) || !sys_offsets || !cluster_size || !threads)
+		return FS_ERR_BAD_HANDLE;
+	std::vector<int64_t> off(sys_offsets, sys_offsets + nsys + 1);
+	auto it = g_plans.find(std::make_pair((const Csr *)A, off));
+	if (it == g_plans.end())
+		return set_err(ctx, FS_ERR_INVALID_ARG, "no batched solve has run on this partition");
+	*cluster_size = it->second.tuned_cluster;
+	*threads = it->second.tuned_threads;
+	return FS_OK;
+}
+
+// ======================================================== block CG ======
+//
+// Block Jacobi-PCG (O'Leary, "The block conjugate gradient algorithm and
+// related methods", LAA 29, 1980) for S right-hand sides of one operator,
+// FP64.  X, R, P, Q are N x S row-major (the S values of a row contiguous),
+// so the SpMM reads A once for all S columns and gathers one 8*S-byte row of
+// P per nonzero.  Per iteration:
+//   Q = A P,  M = P^T Q                 (SpMM with the Gram product fused)
+//   alpha = M^-1 G
+//   X += P alpha,  R -= Q alpha,  Z = D^-1 R,  G' = Z^T R, ||R_j||
+//   beta = G^-1 G',  P = Z + P beta,  G = G'
+// Gram products: each CTA walks 16-row tiles; thread (i, j) of the 256 sums
+// P[r][i] Q[r][j] over the tile rows and keeps its running sum, the per-CTA
+// sums are folded in CTA order by the last CTA (deterministic).  Columns that
+// reach rtol * ||B_j|| record their iteration count; the block iterates
+// until every column has.
+namespace fsg {
+namespace {
+
+constexpr int kS = 16;           // right-hand sides per block
+constexpr int kTile = 16;        // rows per tile (kTile * kS = 256 threads)
+
+struct BcgState {
+	double G[kS * kS], Gn[kS * kS], M[kS * kS], alpha[kS * kS], beta[kS * kS];
+	double bnorm[kS], rnorm[kS], res0[kS];
+	int conv_iter[kS];
+	int iter, done, status, flags;
+};
+
+// x = A^-1 B for the s x s matrix A (row-major), s right-hand sides in B
+// (row-major, overwritten with the solution): Gaussian elimination with
+// partial pivoting.  Returns false on a zero pivot.  Single thread.
+__device__ bool small_solve(double *A, double *B) {
+	int piv[kS];
+	for (int i = 0; i < kS; ++i)
+		piv[i] = i;
+	for (int k = 0; k < kS; ++k) {
+		int p = k;
+		double m = fabs(A[k * kS + k]);
+		for (int i = k + 1; i < kS; ++i)
+			if (fabs(A[i * kS + k]) > m) {
+				m = fabs(A[i * kS + k]);
+				p = i;
+			}
+		if (!(m > 0.0))
+			return false;
+		if (p != k) {
+			for (int j = 0; j < kS; ++j) {
+				double t = A[k * kS + j];
+				A[k * kS + j] = A[p * kS + j];
+				A[p * kS + j] = t;
+				t = B[k * kS + j];
+				B[k * kS + j] = B[p * kS + j];
+				B[p * kS + j] = t;
+			}
+		}
+		for (int i = k + 1; i < kS; ++i) {
+			const double f = A[i * kS + k] / A[k * kS + k];
+			for (int j = k; j < kS; ++j)
+				A[i * kS + j] -= f * A[k * kS + j];
+			for (int j = 0; j < kS; ++j)
+				B[i * kS + j] -= f * B[k * kS + j];
+		}
+	}
+	for (int k = kS - 1; k >= 0; --k)
+		for (int j = 0; j < kS; ++j) {
+			double s = B[k * kS + j];
+			for (int i = k + 1; i < kS; ++i)
+				s -= A[k * kS + i] * B[i * kS + j];
+			B[k * kS + j] = s / A[k * kS + k];
+		}
+	return true;
+}
+
+// Q = A P and the CTA's part of M = P^T Q
+__global__ void __launch_bounds__(256)
+k_bcg_spmm(int n, const int *__restrict__ rp, const int *__restrict__ col,
+           const double *__restrict__ val, const double *__restrict__ P, double *__restrict__ Q,
+           BcgState *st, double *part, unsigned *counter) {
+	__shared__ double sp[kTile][kS], sq[kTile][kS];
+	if (st->done)
+		return;
+	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
+	const int ntiles = (n + kTile - 1) / kTile;
+	double m = 0.0;
+	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+		const int r = t * kTile + tr;
+		double q = 0.0, p = 0.0;
+		if (r < n) {
+			for (int k = rp[r]; k < rp[r + 1]; ++k)
+				q = fma(val[k], P[(size_t)col[k] * kS + tj], q);
+			Q[(size_t)r * kS + tj] = q;
+			p = P[(size_t)r * kS + tj];
+		}
+		sp[tr][tj] = p;
+		sq[tr][tj] = q;
+		__syncthreads();
+		// thread (i = tr, j = tj) of the Gram tile
+#pragma unroll
+		for (int rr = 0; rr < kTile; ++rr)
+			m = fma(sp[rr][tr], sq[rr][tj], m);
+		__syncthreads();
+	}
+	part[(size_t)blockIdx.x * 256 + threadIdx.x] = m;
+	if (last_block(counter)) {
+		double s = 0.0;
+		for (unsigned b = 0; b < gridDim.x; ++b)
+			s += __ldcg(part + (size_t)b * 256 + threadIdx.x);
+		st->M[threadIdx.x] = s;
+		__syncthreads();
+		if (threadIdx.x == 0) {
+			// alpha = M^-1 G
+			double Mc[kS * kS];
+			for (int i = 0; i < kS * kS; ++i) {
+				Mc[i] = st->M[i];
+				st->alpha[i] = st->G[i];
+			}
+			if (!small_solve(Mc, st->alpha)) {
+				st->done = 1;
+				st->status = FS_DIVERGED_BREAKDOWN;
+			}
+			*counter = 0;
+		}
+	}
+}
+
+// X += P alpha, R -= Q alpha, Z = D^-1 R; G' = Z^T R and ||R_j||^2 parts;
+// the last CTA tests every column and forms beta = G^-1 G'
+__global__ void __launch_bounds__(256)
+k_bcg_update(int n, double *__restrict__ X, const double *__restrict__ P, double *__restrict__ R,
+             const double *__restrict__ Q, const double *__restrict__ dinv, BcgState *st,
+             double *part, double *part2, unsigned *counter, double tolf, int maxiter) {
+	__shared__ double sa[kS * kS], sp[kTile][kS], sq[kTile][kS], sr[kTile][kS], sz[kTile][kS];
+	if (st->done)
+		return;
+	sa[threadIdx.x] = st->alpha[threadIdx.x];
+	__syncthreads();
+	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
+	const int ntiles = (n + kTile - 1) / kTile;
+	double g = 0.0, nr = 0.0;
+	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+		const int r = t * kTile + tr;
+		sp[tr][tj] = r < n ? P[(size_t)r * kS + tj] : 0.0;
+		sq[tr][tj] = r < n ? Q[(size_t)r * kS + tj] : 0.0;
+		__syncthreads();
+		double x = 0.0, rv = 0.0, z = 0.0;
+		if (r < n) {
+			x = X[(size_t)r * kS + tj];
+			rv = R[(size_t)r * kS + tj];
+#pragma unroll
+			for (int i = 0; i < kS; ++i) {
+				x = fma(sp[tr][i], sa[i * kS + tj], x);
+				rv = fma(-sq[tr][i], sa[i * kS + tj], rv);
+			}
+			X[(size_t)r * kS + tj] = x;
+			R[(size_t)r * kS + tj] = rv;
+			z = dinv ? dinv[r] * rv : rv;
+			nr = fma(rv, rv, nr);
+		}
+		sr[tr][tj] = rv;
+		sz[tr][tj] = z;
+		__syncthreads();
+#pragma unroll
+		for (int rr = 0; rr < kTile; ++rr)
+			g = fma(sz[rr][tr], sr[rr][tj], g);
+		__syncthreads();
+	}
+	part[(size_t)blockIdx.x * 256 + threadIdx.x] = g;
+	// column norms: thread (tr, tj) summed rows of column tj; fold the 16
+	// row-threads of each column in the block first
+	__shared__ double cn[kTile][kS];
+	cn[tr][tj] = nr;
+	__syncthreads();
+	if (threadIdx.x < kS) {
+		double c = 0.0;
+		for (int rr = 0; rr < kTile; ++rr)
+			c += cn[rr][threadIdx.x];
+		part2[(size_t)blockIdx.x * kS + threadIdx.x] = c;
+	}
+	if (last_block(counter)) {
+		double s = 0.0;
+		for (unsigned b = 0; b < gridDim.x; ++b)
+			s += __ldcg(part + (size_t)b * 256 + threadIdx.x);
+		st->Gn[threadIdx.x] = s;
+		if (threadIdx.x < kS) {
+			double c = 0.0;
+			for (unsigned b = 0; b < gridDim.x; ++b)
+				c += __ldcg(part2 + (size_t)b * kS + threadIdx.x);
+			st->rnorm[threadIdx.x] = sqrt(c);
+		}
+		__syncthreads();
+		if (threadIdx.x == 0) {
+			const int it = st->iter + 1;
+			st->iter = it;
+			bool all = true;
+			for (int j = 0; j < kS; ++j) {
+				if (st->conv_iter[j] == 0 && st->rnorm[j] < tolf * st->bnorm[j])
+					st->conv_iter[j] = it;
+				all = all && st->conv_iter[j] != 0;
+			}
+			if (all) {
+				st->done = 1;
+				st->status = FS_CONVERGED_RTOL;
+			}
+			else if (it >= maxiter) {
+				st->done = 1;
+				st->status = FS_DIVERGED_ITERS;
+			}
+			else {
+				// beta = G^-1 G'
+				double Gc[kS * kS];
+				for (int i = 0; i < kS * kS; ++i) {
+					Gc[i] = st->G[i];
+					st->beta[i] = st->Gn[i];
+				}
+				if (!small_solve(Gc, st->beta)) {
+					st->done = 1;
+					st->status = FS_DIVERGED_BREAKDOWN;
+				}
+				for (int i = 0; i < kS * kS; ++i)
+					st->G[i] = st->Gn[i];
+			}
+			*counter = 0;
+		}
+	}
+}
+
+// P = Z + P beta (Z = D^-1 R)
+__global__ void __launch_bounds__(256)
+k_bcg_dir(int n, double *__restrict__ P, const double *__restrict__ R,
+          const double *__restrict__ dinv, const BcgState *st) {
+	__shared__ double sb[kS * kS], sp[kTile][kS];
+	if (st->done)
+		return;
+	sb[threadIdx.x] = st->beta[threadIdx.x];
+	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
+	const int ntiles = (n + kTile - 1) / kTile;
+	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+		const int r = t * kTile + tr;
+		__syncthreads();
+		sp[tr][tj] = r < n ? P[(size_t)r * kS + tj] : 0.0;
+		__syncthreads();
+		if (r < n) {
+			double p = (dinv ? dinv[r] : 1.0) * R[(size_t)r * kS + tj];
+#pragma unroll
+			for (int i = 0; i < kS; ++i)
+				p = fma(sp[tr][i], sb[i * kS + tj], p);
+			P[(size_t)r * kS + tj] = p;
+		}
+	}
+}
+
+// R = B - A X (or B with X = 0), P = Z = D^-1 R, G = Z^T R, ||B_j||, ||R_j||
+__global__ void __launch_bounds__(256)
+k_bcg_start(int n, const int *__restrict__ rp, const int *__restrict__ col,
+            const double *__restrict__ val, const double *__restrict__ B, double *__restrict__ X,
+            double *__restrict__ R, double *__restrict__ P, const double *__restrict__ dinv,
+            int zero_guess, BcgState *st, double *part, double *part2, unsigned *counter) {
+	__shared__ double sr[kTile][kS], sz[kTile][kS], cb[kTile][kS], cr[kTile][kS];
+	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
+	const int ntiles = (n + kTile - 1) / kTile;
+	double g = 0.0, nb = 0.0, nr = 0.0;
+	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+		const int r = t * kTile + tr;
+		double rv = 0.0, z = 0.0;
+		if (r < n) {
+			const double bv = B[(size_t)r * kS + tj];
+			double ax = 0.0;
+			if (zero_guess)
+				X[(size_t)r * kS + tj] = 0.0;
+			else
+				for (int k = rp[r]; k < rp[r + 1]; ++k)
+					ax = fma(val[k], X[(size_t)col[k] * kS + tj], ax);
+			rv = bv - ax;
+			R[(size_t)r * kS + tj] = rv;
+			z = dinv ? dinv[r] * rv : rv;
+			P[(size_t)r * kS + tj] = z;
+			nb = fma(bv, bv, nb);
+			nr = fma(rv, rv, nr);
+		}
+		sr[tr][tj] = rv;
+		sz[tr][tj] = z;
+		__syncthreads();
+#pragma unroll
+		for (int rr = 0; rr < kTile; ++rr)
+			g = fma(sz[rr][tr], sr[rr][tj], g);
+		__syncthreads();
+	}
+	part[(size_t)blockIdx.x * 256 + threadIdx.x] = g;
+	cb[tr][tj] = nb;
+	cr[tr][tj] = nr;
+	__syncthreads();
+	if (threadIdx.x < kS) {
+		double c1 = 0.0, c2 = 0.0;
+		for (int rr = 0; rr < kTile; ++rr) {
+			c1 += cb[rr][threadIdx.x];
+			c2 += cr[rr][threadIdx.x];
+		}
+		part2[(size_t)blockIdx.x * 2 * kS + threadIdx.x] = c1;
+		part2[(size_t)blockIdx.x * 2 * kS + kS + threadIdx.x] = c2;
+	}
+	if (last_block(counter)) {
+		double s = 0.0;
+		for (unsigned b = 0; b < gridDim.x; ++b)
+			s += __ldcg(part + (size_t)b * 256 + threadIdx.x);
+		st->G[threadIdx.x] = s;
+		if (threadIdx.x < kS) {
+			double c1 = 0.0, c2 = 0.0;
+			for (unsigned b = 0; b < gridDim.x; ++b) {
+				c1 += __ldcg(part2 + (size_t)b * 2 * kS + threadIdx.x);
+				c2 += __ldcg(part2 + (size_t)b * 2 * kS + kS + threadIdx.x);
+			}
+			const double bn = sqrt(c1);
+			st->bnorm[threadIdx.x] = bn == 0.0 ? 1.0 : bn;
+			st->rnorm[threadIdx.x] = sqrt(c2);
+			st->res0[threadIdx.x] = sqrt(c2);
+			st->conv_iter[threadIdx.x] = 0;
+		}
+		if (threadIdx.x == 0) {
+			st->iter = 0;
+			st->done = 0;
+			st->status = FS_STATUS_UNKNOWN;
+			st->flags = 0;
+			*counter = 0;
+		}
+	}
+}
+
+struct BcgPlan {
+	BcgState *st = nullptr, *hst = nullptr;
+	double *work = nullptr;     // P, Q (N x S each)
+	double *part = nullptr;     // G partials (grid x 256) + norm partials
+	unsigned *counter = nullptr;
+	int64_t n = 0;
+};
+std::map<const Csr *, BcgPlan> g_bcg;
+
+}  // namespace
+}  // namespace fsg
+
+extern "C" FS_API int fs_block_cg_solve(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah,
+                                        const fs_precond *Pc, int nrhs, fs_vec bh, fs_vec xh,
+                                        fs_solve_info *infos) {
+	using namespace fsg;
+	Ctx *ctx = reinterpret_cast<Ctx *>(h);
+	Csr *A = reinterpret_cast<Csr *>(Ah);
+	Vec *B = reinterpret_cast<Vec *>(bh), *X = reinterpret_cast<Vec *>(xh);
+	if (!ok_ctx(ctx) || !ok_csr(A) || !ok_vec(B) || !ok_vec(X) || !s || !infos)
+		return FS_ERR_BAD_HANDLE;
+	if (nrhs != kS)
+		return set_err(ctx, FS_ERR_UNSUPPORTED, "fs_block_cg_solve: this build takes %d right-hand sides", kS);
+	const int64_t n = A->nrows;
+	if (A->nrows != A->ncols || B->n != n * kS || X->n != n * kS || B->dtype != FS_F64 ||
+	    X->dtype != FS_F64)
+		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_block_cg_solve: B and X hold N x %d FP64 row-major", kS);
+	const bool jac = Pc && Pc->kind == FS_PRECOND_JACOBI;
+	if (Pc && Pc->kind != FS_PRECOND_NONE && !jac)
+		return set_err(ctx, FS_ERR_UNSUPPORTED, "fs_block_cg_solve: identity or Jacobi preconditioner");
+	cudaSetDevice(ctx->device);
+	if (jac)
+		FS_TRY(ensure_dinv(A));
+	BcgPlan &p = g_bcg[A];
+	const int G = std::max(1, std::min(ctx->sms * 8, (int)((n + kTile - 1) / kTile)));
+	if (p.n != n) {
+		if (p.work) {
+			cudaFree(p.work);
+			cudaFree(p.part);
+			cudaFree(p.counter);
+			cudaFree(p.st);
+			cudaFreeHost(p.hst);
+		}
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.work, sizeof(double) * 3 * (size_t)n * kS));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.part, sizeof(double) * (size_t)ctx->sms * 8 * (256 + 2 * kS)));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.counter, 64));
+		FS_CUDA_TRY(ctx, cudaMemset(p.counter, 0, 64));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.st, sizeof(BcgState)));
+		FS_CUDA_TRY(ctx, cudaMallocHost(&p.hst, sizeof(BcgState)));
+		p.n = n;
+	}
+	double *Pm = p.work, *Qm = p.work + (size_t)n * kS;
+	double *part = p.part, *part2 = p.part + (size_t)ctx->sms * 8 * 256;
+	const double *dinv = jac ? A->dinv : nullptr;
+	const double *b = (const double *)B->d;
+	double *x = (double *)X->d;
+	double *R = p.work + 2 * (size_t)n * kS;
+	k_bcg_start<<<G, 256, 0, ctx->stream>>>((int)n, A->rowptr, A->col, A->val, b, x, R, Pm, dinv,
+	                                        s->base.use_zero_guess ? 1 : 0, p.st, part, part2, p.counter);
+	int st = check_launch(ctx, "block cg start");
+	const double tolf = (double)s->base.rtol;
+	const int maxiter = s->base.maxiter;
+	const int k = s->k_readback > 0 ? s->k_readback : 16;
+	int it = 0;
+	while (st == FS_OK) {
+		for (int j = 0; j < k && st == FS_OK; ++j) {
+			k_bcg_spmm<<<G, 256, 0, ctx->stream>>>((int)n, A->rowptr, A->col, A->val, Pm, Qm, p.st,
+			                                       part, p.counter);
+			st = check_launch(ctx, "block cg spmm");
+			k_bcg_update<<<G, 256, 0, ctx->stream>>>((int)n, x, Pm, R, Qm, dinv, p.st, part, part2,
+			                                         p.counter, tolf, maxiter);
+			if (st == FS_OK)
+				st = check_launch(ctx, "block cg update");
+			k_bcg_dir<<<G, 256, 0, ctx->stream>>>((int)n, Pm, R, dinv, p.st);
+			if (st == FS_OK)
+				st = check_launch(ctx, "block cg direction");
+		}
+		it += k;
+		if (st != FS_OK)
+			break;
+		if (cudaMemcpyAsync(p.hst, p.st, sizeof(BcgState), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+		    cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+			st = set_err(ctx, FS_ERR_CUDA, "block cg: state read-back failed");
+			break;
+		}
+		if (p.hst->done || p.hst->iter >= maxiter)
+			break;
+	}
+	if (st != FS_OK)
+		return st;
+	const BcgState &hs = *p.hst;
+	for (int j = 0; j < kS; ++j) {
+		fs_solve_info &inf = infos[j];
+		memset(&inf, 0, sizeof inf);
+		inf.status = hs.conv_iter[j] ? FS_CONVERGED_RTOL
+		                             : (hs.status == FS_DIVERGED_BREAKDOWN ? FS_DIVERGED_BREAKDOWN
+		                                                                   : FS_DIVERGED_ITERS);
+		inf.iters = hs.conv_iter[j];
+		inf.restarts = hs.iter;  // block iterations run
+		inf.res_norm_initial = (float)hs.res0[j];
+		inf.res_norm_final = (float)hs.rnorm[j];
+		inf.rhs_norm = (float)hs.bnorm[j];
+	}
+	return FS_OK;
+}

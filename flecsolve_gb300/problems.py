@@ -200,3 +200,35 @@ def workload(name: str):
         raise ValueError(f"unknown workload {name}")
     A.name = name
     return A, b
+
+
+def block_diagonal(mats):
+    """Concatenate square CSR matrices into one block-diagonal CSR; returns
+    (CSR, row offsets)."""
+    sizes = [m.nrows for m in mats]
+    off = np.zeros(len(mats) + 1, dtype=np.int64)
+    off[1:] = np.cumsum(sizes)
+    nnz = [m.nnz for m in mats]
+    noff = np.zeros(len(mats) + 1, dtype=np.int64)
+    noff[1:] = np.cumsum(nnz)
+    rp = np.empty(off[-1] + 1, dtype=np.int64)
+    col = np.empty(noff[-1], dtype=np.int32)
+    val = np.empty(noff[-1])
+    rp[-1] = noff[-1]
+    for k, m in enumerate(mats):
+        rp[off[k]:off[k + 1]] = m.rowptr[:-1] + noff[k]
+        col[noff[k]:noff[k + 1]] = m.col + off[k]
+        val[noff[k]:noff[k + 1]] = m.val
+    return CSR(int(off[-1]), int(off[-1]), rp, col, val, "block-diagonal"), off
+
+
+def batch_diffusion2d(nsys: int = 512, side_lo: int = 32, side_hi: int = 256, seed: int = 5):
+    """Independent 2-D log-normal diffusion systems with sides drawn uniformly
+    from [side_lo, side_hi] (seed), system s with face seed 1000 + s and RHS
+    U[-1,1] seed 2000 + s.  Returns (block-diagonal CSR, offsets, rhs, sides)."""
+    sides = randint(seed, nsys, side_lo, side_hi)
+    mats = [diffusion(2, int(n), seed=1000 + k) for k, n in enumerate(sides)]
+    A, off = block_diagonal(mats)
+    b = np.concatenate([uniform(2000 + k, m.nrows) for k, m in enumerate(mats)])
+    A.name = f"batch{nsys}-diffusion2d-{side_lo}-{side_hi}"
+    return A, off, b, sides

@@ -23,6 +23,7 @@
 // reference's flog_assert sites (FS_ERR_BREAKDOWN) raise too.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <functional>
 #include <memory>
@@ -141,6 +142,20 @@ public:
 	}
 	// non-owning view of a library vector (the diagnostic's argument)
 	static device_vec view(fs_ctx c, fs_vec h) { return device_vec(c, h); }
+	// view of n doubles of caller-owned device memory (the handle is freed
+	// with the view, the memory is not)
+	static device_vec wrap(fs_ctx c, std::size_t n, double *dptr) {
+		fs_vec h = nullptr;
+		check(fs_vec_wrap(c, (int64_t)n, FS_F64, dptr, &h), c, "fs_vec_wrap");
+		device_vec v(c, h);
+		v.owns_ = true;
+		return v;
+	}
+	double *device_ptr() const {
+		void *p = nullptr;
+		check(fs_vec_device_ptr(h_, &p), ctx_, "device_ptr");
+		return static_cast<double *>(p);
+	}
 	device_vec(device_vec &&o) noexcept : ctx_(o.ctx_), h_(o.h_), owns_(o.owns_) { o.h_ = nullptr; }
 	device_vec &operator=(device_vec &&o) noexcept {
 		std::swap(ctx_, o.ctx_);
@@ -224,6 +239,89 @@ private:
 	fs_ctx ctx_ = nullptr;
 	fs_vec h_ = nullptr;
 	bool owns_ = true;
+};
+
+// vec::multi (flecsolve/vectors/multi.hh:74-160): components tagged by
+// index, stored as views into one contiguous device allocation (`whole()`),
+// elementwise ops per component, reductions combined over components the way
+// operations/multi.hh:179-253 does (sum of dots, sqrt of summed squares,
+// max/min over components, in component order).
+class multi {
+public:
+	multi(const context &c, const std::vector<std::size_t> &sizes)
+		: whole_(c, total(sizes)) {
+		double *base = whole_.device_ptr();
+		std::size_t off = 0;
+		for (std::size_t n : sizes) {
+			comps_.push_back(device_vec::wrap(c.get(), n, base + off));
+			off += n;
+		}
+	}
+	std::size_t size() const { return comps_.size(); }
+	device_vec &get(std::size_t i) { return comps_[i]; }
+	const device_vec &get(std::size_t i) const { return comps_[i]; }
+	device_vec &subset(std::size_t i) { return comps_[i]; }
+	device_vec &whole() { return whole_; }
+	const device_vec &whole() const { return whole_; }
+
+	template<class F>
+	void each(F &&f) {
+		for (auto &c : comps_)
+			f(c);
+	}
+	void copy(const multi &s) { zip(s, [](device_vec &a, const device_vec &b) { a.copy(b); }); }
+	void zero() { each([](device_vec &c) { c.zero(); }); }
+	void set_scalar(double v) { each([v](device_vec &c) { c.set_scalar(v); }); }
+	void scale(double a) { each([a](device_vec &c) { c.scale(a); }); }
+	void axpy(double a, const multi &x, const multi &y) {
+		for (std::size_t i = 0; i < comps_.size(); ++i)
+			comps_[i].axpy(a, x.comps_[i], y.comps_[i]);
+	}
+	future<double> dot(const multi &x) const {
+		double s = 0;
+		for (std::size_t i = 0; i < comps_.size(); ++i)
+			s += comps_[i].dot(x.comps_[i]).get();
+		return {s};
+	}
+	future<double> l2norm() const {
+		double s = 0;
+		for (auto &c : comps_)
+			s += c.dot(c).get();
+		return {std::sqrt(s)};
+	}
+	future<double> l1norm() const {
+		double s = 0;
+		for (auto &c : comps_)
+			s += c.l1norm().get();
+		return {s};
+	}
+	future<double> inf_norm() const { return fold([](const device_vec &c) { return c.inf_norm().get(); }, true); }
+	future<double> max() const { return fold([](const device_vec &c) { return c.max().get(); }, true); }
+	future<double> min() const { return fold([](const device_vec &c) { return c.min().get(); }, false); }
+
+private:
+	static std::size_t total(const std::vector<std::size_t> &s) {
+		std::size_t t = 0;
+		for (auto n : s)
+			t += n;
+		return t;
+	}
+	template<class F>
+	void zip(const multi &o, F f) {
+		for (std::size_t i = 0; i < comps_.size(); ++i)
+			f(comps_[i], o.comps_[i]);
+	}
+	template<class F>
+	future<double> fold(F f, bool is_max) const {
+		double r = f(comps_[0]);
+		for (std::size_t i = 1; i < comps_.size(); ++i) {
+			double v = f(comps_[i]);
+			r = is_max ? (v > r ? v : r) : (v < r ? v : r);
+		}
+		return {r};
+	}
+	device_vec whole_;
+	std::vector<device_vec> comps_;
 };
 
 }  // namespace vec

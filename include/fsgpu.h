@@ -275,6 +275,32 @@ FS_API int fs_krylov_history(fs_solver s, double *hist, int64_t *n);
  * FS_CG_MIXED apply */
 FS_API int fs_krylov_mixed_stats(fs_solver s, int *outer, int *inner_iters);
 
+/* --------------------------------------------------- batched solves --- */
+/* Many independent systems in one persistent launch (no counterpart in the
+ * reference, whose solvers take one system per call: this batches calls of
+ * cg.hh:43-139).  A is block diagonal: system s owns rows and columns
+ * [sys_offsets[s], sys_offsets[s+1]).  One thread-block cluster per system
+ * runs Jacobi-PCG with FP32 values/vectors and FP64 residual replacement
+ * (settings->inner_rtol = replacement factor), stopping per system on the
+ * FP64 residual (rtol * ||b_s||).  cluster_size (1, 2, 4, 8) and threads per
+ * CTA may be 0: an autotuner times the candidates on the first call for this
+ * partition and keeps the fastest (fs_batch_tuning reports it).  infos[s]
+ * receives system s's solve_info. */
+FS_API int fs_batch_cg_solve(fs_ctx ctx, const fs_krylov_settings *s, fs_csr A, int nsys,
+                             const int64_t *sys_offsets, fs_vec b, fs_vec x, int cluster_size,
+                             int threads, fs_solve_info *infos);
+FS_API int fs_batch_tuning(fs_ctx ctx, fs_csr A, int nsys, const int64_t *sys_offsets,
+                           int *cluster_size, int *threads);
+
+/* Block Jacobi-PCG for nrhs = 16 right-hand sides of one operator (FP64).
+ * B and X hold N x 16 values row-major (the 16 values of row r contiguous).
+ * P: NULL/FS_PRECOND_NONE or FS_PRECOND_JACOBI.  Column j converges when
+ * ||R_j|| < rtol ||B_j||; infos[j].iters is the block iteration at which it
+ * did, infos[j].restarts the block iterations run. */
+FS_API int fs_block_cg_solve(fs_ctx ctx, const fs_krylov_settings *s, fs_csr A,
+                             const fs_precond *P, int nrhs, fs_vec B, fs_vec X,
+                             fs_solve_info *infos);
+
 /* ------------------------------------------ allocation-free reduction --- */
 /* No counterpart in the reference.  Dot product sum_i x[i] * y[i] of two
  * float64 device arrays, written to the device pointer `result`, for callers

@@ -118,6 +118,19 @@ int main() {
 		expect(std::fabs(x.l2norm().get() - std::sqrt(32.0) * 3.141719) < 1e-8, "vec l2norm");
 	}
 
+	// ------------------------------------------- vec::multi --------------
+	{
+		vec::multi m(ctx, {100, 7, 33});
+		m.get(0).set_scalar(1.0);
+		m.get(1).set_scalar(-2.0);
+		m.get(2).set_scalar(0.5);
+		expect(std::fabs(m.dot(m).get() - (100 + 7 * 4 + 33 * 0.25)) < 1e-12, "multi dot = sum of component dots");
+		expect(std::fabs(m.l2norm().get() - std::sqrt(100 + 7 * 4 + 33 * 0.25)) < 1e-12, "multi l2norm");
+		expect(m.min().get() == -2.0 && m.max().get() == 1.0, "multi min/max over components");
+		auto w = m.whole().download();
+		expect(w.size() == 140 && w[100] == -2.0 && w[139] == 0.5, "multi components are views of one vector");
+	}
+
 	// ------------------------------------------- CG (cg.cc style) --------
 	{
 		host_csr H = diffusion(2, 64, false);

@@ -1,0 +1,72 @@
+"""Batched solves in one persistent launch (one thread-block cluster per
+system) against the oracle's CG on every system separately."""
+import numpy as np
+import pytest
+
+import flecsolve_gb300 as fs
+import pyoracle as O
+from flecsolve_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def batch():
+    return P.batch_diffusion2d(nsys=24, side_lo=6, side_hi=48, seed=11)
+
+
+@pytest.mark.parametrize("cluster,threads", [(0, 0), (1, 256), (2, 512), (8, 1024)])
+def test_batch_cg_each_system(ctx, batch, cluster, threads):
+    A, off, b, sides = batch
+    dA = fs.CSR(ctx, A)
+    vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
+    infos = fs.batch_cg(dA, off, vb, vx, maxiter=4000, rtol=1e-8, cluster=cluster,
+                        threads=threads)
+    x = vx.numpy()
+    S = A.to_scipy()
+    for k, inf in enumerate(infos):
+        lo, hi = off[k], off[k + 1]
+        Ak = P.CSR(hi - lo, hi - lo, A.rowptr[lo:hi + 1] - A.rowptr[lo],
+                   A.col[A.rowptr[lo]:A.rowptr[hi]] - lo, A.val[A.rowptr[lo]:A.rowptr[hi]])
+        ref = O.solve("cg", Ak, b[lo:hi], maxiter=4000, rtol=1e-8)
+        assert inf.status == "converged_rtol", (k, inf)
+        rr = np.linalg.norm(b[lo:hi] - S[lo:hi] @ x) / np.linalg.norm(b[lo:hi])
+        assert rr <= 1e-8, (k, rr)
+        # FP32 recurrences with FP64 residual replacement keep the FP64 count
+        assert abs(inf.iters - ref.iters) <= 3, (k, inf.iters, ref.iters)
+    if cluster == 0:
+        c, t = fs.batch_tuning(dA, off)
+        assert c in (1, 2, 4, 8) and t in (256, 512, 1024)
+
+
+def test_batch_rejects_coupled_systems(ctx):
+    A, _ = P.workload("poisson2d-10")
+    dA = fs.CSR(ctx, A)
+    vb, vx = fs.Vector(ctx, np.ones(A.nrows)), fs.Vector(ctx, A.nrows)
+    with pytest.raises(fs.api._lib.FsError) as ei:
+        fs.batch_cg(dA, [0, 50, 100], vb, vx, maxiter=10, rtol=1e-8, cluster=1, threads=256)
+    assert ei.value.status == fs.api._lib.ERR_INVALID_ARG
+
+
+def test_block_cg_16_rhs(ctx):
+    """Block CG on 16 right-hand sides: every column converges to rtol on its
+    own true residual, no later than single-vector PCG on that column, and
+    matches the direct solve."""
+    import scipy.sparse.linalg as spla
+    A, _ = P.workload("laplace3d-24")
+    n = A.nrows
+    B = np.stack([P.uniform(6 + j, n) for j in range(16)], axis=1)  # N x 16
+    dA = fs.CSR(ctx, A)
+    vB, vX = fs.Vector(ctx, B.ravel()), fs.Vector(ctx, n * 16)
+    infos = fs.block_cg(dA, vB, vX, 16, maxiter=2000, rtol=1e-8)
+    X = vX.numpy().reshape(n, 16)
+    S = A.to_scipy()
+    lu = spla.splu(S.tocsc())
+    for j, inf in enumerate(infos):
+        assert inf.status == "converged_rtol", (j, inf)
+        rr = np.linalg.norm(B[:, j] - S @ X[:, j]) / np.linalg.norm(B[:, j])
+        assert rr <= 1e-8 * 1.5, (j, rr)
+        single = O.solve("cg", A, B[:, j], maxiter=2000, rtol=1e-8)
+        assert inf.iters <= single.iters + 2, (j, inf.iters, single.iters)
+        xs = lu.solve(B[:, j])
+        assert np.linalg.norm(X[:, j] - xs) / np.linalg.norm(xs) <= 1e-6
