@@ -118,9 +118,10 @@ class _DinvMat:
     """D^-1 as a 1-nnz-per-row CSR (flecsolve/util/test/mesh.hh:123-140)."""
 
     def __init__(self, A):
-        n = A.nrows
+        n = int(A.nrows)
         d = np.zeros(n)
-        lib().or_diag_inv(C.byref(_Mat(A).s), _dp(d))
+        m = _Mat(A)  # keeps the converted arrays alive during the call
+        lib().or_diag_inv(C.byref(m.s), _dp(d))
         self.rp = np.arange(n + 1, dtype=np.int64)
         self.col = np.arange(n, dtype=np.int32)
         self.val = d
