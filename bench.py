@@ -292,7 +292,7 @@ def run_ours(args, ws, rank, local):
         "mixed_pcg": {"s": ms_mx * 1e-3, "iters": info_mx.iters, "outer": info_mx.restarts,
                       "status": info_mx.status, "true_relres": relres_mx,
                       "rel_err_vs_fp64_gpu": err_vs_fp64, "refine": args.refine,
-                      "inner_rtol": args.inner_rtol},
+                      "inner_rtol": args.inner_rtol or ("library default (0.1)" if args.refine == "reliable" else "library default (1e-4)")},
         "speedup_mixed_vs_fp64": ms_64 / ms_mx,
         "spmv_hbm_gbs": {"f64": gbs64, "f32": gbs32, "f64_ms": spmv64_ms, "f32_ms": spmv32_ms},
         "roofline": {"bound": "hbm", "kernel": "spmv_rb_kernel<float> (FP32 CSR SpMV)",
@@ -366,7 +366,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="diffusion3d-256")
     ap.add_argument("--maxiter", type=int, default=20000)
-    ap.add_argument("--inner-rtol", dest="inner_rtol", type=float, default=1e-2)
+    ap.add_argument("--inner-rtol", dest="inner_rtol", type=float, default=0.0,
+                    help="replacement factor (reliable) / inner tolerance (restart); 0 = library default")
     ap.add_argument("--refine", default="reliable", choices=["restart", "reliable"])
     ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")

@@ -130,6 +130,11 @@ _PROTOS = {
     "fs_batch_cg_solve": [_vp, C.POINTER(KrylovSettings), _vp, C.c_int, C.POINTER(_i64), _vp, _vp,
                           C.c_int, C.c_int, C.POINTER(SolveInfo)],
     "fs_batch_tuning": [_vp, _vp, C.c_int, C.POINTER(_i64), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "fs_krylov_apply_transpose": [_vp, _vp, _vp, C.POINTER(SolveInfo)],
+    "fs_csr_transpose": [_vp, C.POINTER(_vp)],
+    "fs_csr_value_grad": [_vp, _vp, _vp, _vp],
+    "fs_fv_assemble": [_vp, C.c_int, _i64, _vp, C.c_double, C.c_double],
+    "fs_fv_face_grad": [_vp, C.c_int, _i64, _vp, _vp, C.c_double, C.c_int, _vp],
     "fs_block_cg_solve": [_vp, C.POINTER(KrylovSettings), _vp, C.POINTER(Precond), C.c_int, _vp, _vp,
                           C.POINTER(SolveInfo)],
 }

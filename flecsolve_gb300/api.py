@@ -249,9 +249,14 @@ class CSR:
     operators/core.hh:29-34): applied to a :class:`Multi` the operator acts on
     that component (``op::core::apply`` subsets, core.hh:107-116)."""
 
-    def __init__(self, ctx: Context, A, var=None):
+    def __init__(self, ctx: Context, A, var=None, *, _handle=None):
         self.ctx = ctx
         self.var = var
+        if _handle is not None:
+            r, c = C.c_int64(), C.c_int64()
+            check(lib().fs_csr_shape(_handle, C.byref(r), C.byref(c), None), ctx.h)
+            self.nrows, self.ncols, self.h = r.value, c.value, _handle
+            return
         self.nrows, self.ncols = int(A.nrows), int(A.ncols)
         rp = np.ascontiguousarray(A.rowptr, dtype=np.int64)
         col = np.ascontiguousarray(A.col)
@@ -310,6 +315,31 @@ class CSR:
     def update_values(self, val: np.ndarray):
         v = np.ascontiguousarray(val, dtype=np.float64)
         check(lib().fs_csr_update_values(self.h, v.ctypes.data_as(C.c_void_p)), self.ctx.h)
+
+    def values(self) -> np.ndarray:
+        """The current values (row order) copied to the host."""
+        p = C.c_void_p()
+        check(lib().fs_csr_values_device_ptr(self.h, C.byref(p)), self.ctx.h)
+        v = Vector.wrap(self.ctx, self.nnz(), p.value)
+        return v.numpy()
+
+    def transpose(self) -> "CSR":
+        """A^T materialised as a new device CSR matrix."""
+        h = C.c_void_p()
+        check(lib().fs_csr_transpose(self.h, C.byref(h)), self.ctx.h, "fs_csr_transpose")
+        return CSR(self.ctx, None, _handle=h)
+
+    def value_grad(self, lam: Vector, x: Vector, g: Vector):
+        """g = dL/dA on the pattern for x = A^-1 b and lam = A^-T dL/dx:
+        g_k = -lam_i x_j for entry k = (i, j)."""
+        check(lib().fs_csr_value_grad(self.h, lam.h, x.h, g.h), self.ctx.h, "value grad")
+
+    def fv_assemble(self, dim: int, n: int, faces: Vector, scale: float = 1.0,
+                    shift: float = 0.0):
+        """Values = scale K(faces) + shift I for the finite-volume diffusion
+        pattern of an n^dim grid (the generator's face layout and row order)."""
+        check(lib().fs_fv_assemble(self.h, dim, n, faces.h, scale, shift), self.ctx.h,
+              "fs_fv_assemble")
 
     def Dinv(self) -> Vector:
         """Diagonal inverse as a vector (util/test/mesh.hh:123-140)."""
@@ -516,14 +546,14 @@ class BoundSolver:
     def settings(self, s):
         check(lib().fs_krylov_settings_set(self.h, C.byref(s)), self.ctx.h)
 
-    def apply(self, b: Vector, x: Vector) -> SolveInfo:
+    def apply(self, b: Vector, x: Vector, _fn="fs_krylov_apply") -> SolveInfo:
         # op::core::apply subsets by the operator's variables (core.hh:107-116)
         if isinstance(b, Multi):
             b = b.subset(self.A.var) if self.A.var is not None else b.whole
         if isinstance(x, Multi):
             x = x.subset(self.A.var) if self.A.var is not None else x.whole
         info = _lib.SolveInfo()
-        st = lib().fs_krylov_apply(self.h, b.h, x.h, C.byref(info))
+        st = getattr(lib(), _fn)(self.h, b.h, x.h, C.byref(info))
         out = SolveInfo(_lib.STOP_REASONS.get(info.status, str(info.status)), info.iters,
                         info.restarts, info.res_norm_initial, info.res_norm_final,
                         info.sol_norm_initial, info.sol_norm_final, info.rhs_norm)
@@ -534,6 +564,11 @@ class BoundSolver:
         return out
 
     __call__ = apply
+
+    def apply_transpose(self, b: Vector, x: Vector) -> SolveInfo:
+        """Solve A^T x = b with the same method, settings and preconditioner
+        (the adjoint solve; A^T is a device view of A's current values)."""
+        return self.apply(b, x, _fn="fs_krylov_apply_transpose")
 
     def history(self) -> np.ndarray:
         n = C.c_int64(1 << 30)
@@ -564,7 +599,7 @@ def _info(i) -> "SolveInfo":
 
 
 def batch_cg(A: CSR, offsets, b: Vector, x: Vector, maxiter: int, rtol: float,
-             use_zero_guess: bool = True, delta: float = 1e-2, cluster: int = 0,
+             use_zero_guess: bool = True, delta: float = 0.0, cluster: int = 0,
              threads: int = 0):
     """Solve the independent systems on the diagonal blocks of ``A`` (system
     s = rows offsets[s]:offsets[s+1]) in one persistent launch, one thread-

@@ -322,6 +322,7 @@ extern "C" FS_API int fs_batch_cg_solve(fs_ctx h, const fs_krylov_settings *s, f
 		FS_CUDA_TRY(ctx, cudaMalloc(&p.work, sizeof(float) * 4 * (n + 32)));
 		FS_CUDA_TRY(ctx, cudaMemcpy(p.d_off, off.data(), sizeof(int64_t) * (nsys + 1), cudaMemcpyHostToDevice));
 		FS_CUDA_TRY(ctx, cudaMemcpy(p.d_order, order.data(), sizeof(int) * nsys, cudaMemcpyHostToDevice));
+		FS_CUDA_TRY(ctx, fence_setup_copies());
 		it = g_plans.emplace(key, p).first;
 	}
 	BatchPlan &p = it->second;
@@ -347,7 +348,7 @@ extern "C" FS_API int fs_batch_cg_solve(fs_ctx h, const fs_krylov_settings *s, f
 	a.info = p.d_info;
 	a.maxiter = s->base.maxiter;
 	a.rtol = s->base.rtol;
-	a.delta = s->inner_rtol > 0 ? s->inner_rtol : 1e-2;
+	a.delta = s->inner_rtol > 0 ? s->inner_rtol : 0.1;
 	a.zero_guess = s->base.use_zero_guess ? 1 : 0;
 
 	int cl = cluster_size, th = threads;
@@ -389,6 +390,7 @@ extern "C" FS_API int fs_batch_cg_solve(fs_ctx h, const fs_krylov_settings *s, f
 			cudaEventDestroy(e0);
 			cudaEventDestroy(e1);
 			FS_CUDA_TRY(ctx, cudaMemcpy(x->d, xsave.data(), n * 8, cudaMemcpyHostToDevice));
+			FS_CUDA_TRY(ctx, fence_setup_copies());
 			if (p.tuned_cluster == 0)
 				return set_err(ctx, FS_ERR_CUDA, "batched CG: no launch configuration ran");
 		}
@@ -794,6 +796,7 @@ extern "C" FS_API int fs_block_cg_solve(fs_ctx h, const fs_krylov_settings *s, f
 		FS_CUDA_TRY(ctx, cudaMalloc(&p.part, sizeof(double) * (size_t)ctx->sms * 8 * (256 + 2 * kS)));
 		FS_CUDA_TRY(ctx, cudaMalloc(&p.counter, 64));
 		FS_CUDA_TRY(ctx, cudaMemset(p.counter, 0, 64));
+		FS_CUDA_TRY(ctx, fence_setup_copies());
 		FS_CUDA_TRY(ctx, cudaMalloc(&p.st, sizeof(BcgState)));
 		FS_CUDA_TRY(ctx, cudaMallocHost(&p.hst, sizeof(BcgState)));
 		p.n = n;

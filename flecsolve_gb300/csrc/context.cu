@@ -322,7 +322,8 @@ FS_API int fs_ctx_create(int device, fs_ctx *out) {
 	    cudaMalloc(&c->red_count, sizeof(unsigned) * 8) != cudaSuccess ||
 	    cudaMallocHost(&c->host_out, sizeof(double) * 8) != cudaSuccess)
 		return fail(FS_ERR_OUT_OF_MEMORY);
-	if (cudaMemset(c->red_count, 0, sizeof(unsigned) * 8) != cudaSuccess)
+	if (cudaMemset(c->red_count, 0, sizeof(unsigned) * 8) != cudaSuccess ||
+	    fence_setup_copies() != cudaSuccess)
 		return fail(FS_ERR_CUDA);
 	*out = reinterpret_cast<fs_ctx>(c);
 	return FS_OK;

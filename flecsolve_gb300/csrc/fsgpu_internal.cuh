@@ -107,6 +107,12 @@ int set_err(Ctx *ctx, int status, const char *fmt, ...);
 int check_launch(Ctx *ctx, const char *what);
 
 inline bool ok_ctx(const Ctx *c) { return c && c->magic == kMagicCtx; }
+
+// Setup copies and memsets go through the legacy default stream; a pageable
+// host-to-device copy may still be in flight when cudaMemcpy returns, and the
+// context's stream is non-blocking, so setup paths fence the legacy stream
+// before the context's stream reads what they wrote.
+inline cudaError_t fence_setup_copies() { return cudaStreamSynchronize(cudaStreamLegacy); }
 inline bool ok_vec(const Vec *v) { return v && v->magic == kMagicVec && ok_ctx(v->ctx); }
 inline bool ok_csr(const Csr *a) { return a && a->magic == kMagicCsr && ok_ctx(a->ctx); }
 

@@ -678,7 +678,7 @@ int gmres_run(Solver *s, Vec *b, Vec *x, fs_solve_info *info, bool mixed) {
 		s->basis_bytes = need;
 		// graphs captured with the old basis address are stale
 		for (auto &kv : s->graphs)
-			cudaGraphExecDestroy(kv.second.first);
+			cudaGraphExecDestroy(kv.second.exec);
 		s->graphs.clear();
 	}
 	FS_CUDA_TRY(ctx, cudaMemsetAsync(s->hdev, 0, sizeof(GmState), ctx->stream));

@@ -805,7 +805,8 @@ int read_state(Solver *s) {
 // Capture `body` (k iterations) once per key, then replay it.
 int graph_run(Solver *s, const GraphKey &key, int (*body)(Solver *, void *), void *arg) {
 	Ctx *ctx = s->ctx;
-	auto it = s->graphs.find(key);
+	const auto gkey = std::make_pair((const Csr *)s->A, key);
+	auto it = s->graphs.find(gkey);
 	if (it == s->graphs.end()) {
 		int64_t before = ctx->launches;
 		FS_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -826,16 +827,28 @@ int graph_run(Solver *s, const GraphKey &key, int (*body)(Solver *, void *), voi
 		cudaGraphDestroy(g);
 		if (e != cudaSuccess)
 			return set_err(ctx, FS_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
-		it = s->graphs.emplace(key, std::make_pair(ge, nodes)).first;
+		if (s->graphs.size() >= Solver::kMaxGraphs) {
+			// evict the least recently launched graph once the stream has
+			// drained (it may be the one still running)
+			auto lru = s->graphs.begin();
+			for (auto jt = s->graphs.begin(); jt != s->graphs.end(); ++jt)
+				if (jt->second.last_use < lru->second.last_use)
+					lru = jt;
+			FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+			cudaGraphExecDestroy(lru->second.exec);
+			s->graphs.erase(lru);
+		}
+		it = s->graphs.emplace(gkey, Solver::GraphEntry{ge, nodes, 0}).first;
 	}
-	FS_CUDA_TRY(ctx, cudaGraphLaunch(it->second.first, ctx->stream));
-	ctx->launches += it->second.second;
+	it->second.last_use = ++s->graph_tick;
+	FS_CUDA_TRY(ctx, cudaGraphLaunch(it->second.exec, ctx->stream));
+	ctx->launches += it->second.nodes;
 	return FS_OK;
 }
 
 static void clear_graphs(Solver *s) {
 	for (auto &kv : s->graphs)
-		cudaGraphExecDestroy(kv.second.first);
+		cudaGraphExecDestroy(kv.second.exec);
 	s->graphs.clear();
 }
 
@@ -1515,6 +1528,7 @@ static int bicgstab_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *inf
 	return FS_OK;
 }
 
+int ensure_transpose(Csr *A);
 int gmres_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info);
 int gmres_apply_mixed(Solver *s, Vec *b, Vec *x, fs_solve_info *info);
 
@@ -1540,7 +1554,7 @@ FS_API int fs_krylov_settings_default(fs_krylov_settings *s) {
 	s->ortho = FS_ORTHO_AUTO;
 	s->k_readback = 0;
 	s->refine = FS_REFINE_RELIABLE;
-	s->inner_rtol = 1e-2;
+	s->inner_rtol = 0.0;  // per-method default
 	s->max_outer = 64;
 	return FS_OK;
 }
@@ -1648,6 +1662,7 @@ FS_API int fs_krylov_create(fs_ctx h, int method, const fs_krylov_settings *set,
 			hf[i] = (float)hd[i];
 		if (s->n)
 			cudaMemcpy(s->w32[10], hf.data(), s->n * 4, cudaMemcpyHostToDevice);
+		fence_setup_copies();
 		if (cudaGetLastError() != cudaSuccess)
 			st = set_err(ctx, FS_ERR_CUDA, "fs_krylov_create: preconditioner copy failed");
 	}
@@ -1671,6 +1686,12 @@ FS_API int fs_krylov_destroy(fs_solver h) {
 	clear_graphs(s);
 	for (void *p : s->bufs)
 		cudaFree(p);
+	if (s->AT) {
+		if (s->AT->val32)
+			cudaFree(s->AT->val32);  // the only array the view owns
+		s->AT->magic = 0;
+		delete s->AT;
+	}
 	if (s->basis)
 		cudaFree(s->basis);
 	if (s->hist)
@@ -1730,6 +1751,13 @@ FS_API int fs_krylov_apply(fs_solver h, fs_vec bh, fs_vec xh, fs_solve_info *inf
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_krylov_apply: b and x must differ");
 	cudaSetDevice(ctx->device);
 	s->mixed_outer = s->mixed_inner = 0;
+	// the operator's values may have changed since the last apply
+	// (fs_csr_update_values, fs_fv_assemble): derived arrays are rebuilt in
+	// place, so captured graphs stay valid
+	if (s->P.kind == FS_PRECOND_JACOBI)
+		FS_TRY(ensure_dinv(s->A));
+	if (s->method == FS_CG_MIXED || s->method == FS_BICGSTAB_MIXED || s->method == FS_GMRES_MIXED)
+		FS_TRY(ensure_val32(s->A));
 	switch (s->method) {
 	case FS_CG: return cg_apply64(s, b, x, info);
 	case FS_BICGSTAB: return bicgstab_apply64(s, b, x, info);
@@ -1741,6 +1769,42 @@ FS_API int fs_krylov_apply(fs_solver h, fs_vec bh, fs_vec xh, fs_solve_info *inf
 	case FS_GMRES_MIXED: return gmres_apply_mixed(s, b, x, info);
 	}
 	return FS_ERR_INVALID_ARG;
+}
+
+// A^T x = b with the bound solver's method, settings and preconditioner
+// (the Jacobi diagonal of A^T is A's).  The transposed operator is a view of
+// A's CSC arrays, refreshed from A's current values on every call.
+FS_API int fs_krylov_apply_transpose(fs_solver h, fs_vec bh, fs_vec xh, fs_solve_info *info) {
+	Solver *s = reinterpret_cast<Solver *>(h);
+	if (!ok_slv(s))
+		return FS_ERR_BAD_HANDLE;
+	Csr *A = s->A;
+	FS_TRY(ensure_transpose(A));
+	FS_TRY(ensure_dinv(A));
+	if (!s->AT) {
+		s->AT = new Csr();
+		s->AT->ctx = A->ctx;
+	}
+	Csr *T = s->AT;
+	T->nrows = A->ncols;
+	T->ncols = A->nrows;
+	T->nnz = A->nnz;
+	T->rowptr = A->t_colptr;
+	T->col = A->t_row;
+	T->val = A->t_val;
+	T->blk = A->t_blk;
+	T->blkinfo = A->t_blkinfo;
+	T->nblk = A->t_nblk;
+	T->dinv = A->dinv;
+	T->dinv32 = A->dinv32;
+	T->dinv_valid = true;
+	T->val32_valid = false;  // rebuilt from the current values when needed
+	if (s->method == FS_CG_MIXED || s->method == FS_BICGSTAB_MIXED || s->method == FS_GMRES_MIXED)
+		FS_TRY(ensure_val32(T));
+	s->A = T;
+	int st = fs_krylov_apply(h, bh, xh, info);
+	s->A = A;
+	return st;
 }
 
 FS_API int fs_krylov_history(fs_solver h, double *hist, int64_t *n) {

@@ -98,7 +98,18 @@ struct Solver {
 	int hist_cap = 0;
 	double *part = nullptr;           // reduction partials
 	unsigned *counter = nullptr;
-	std::map<GraphKey, std::pair<cudaGraphExec_t, int>> graphs;
+	// captured graphs, keyed by the operator they were captured with and the
+	// vectors / body they run; at most kMaxGraphs are kept (least recently
+	// launched evicted first)
+	struct GraphEntry {
+		cudaGraphExec_t exec;
+		int nodes;
+		uint64_t last_use;
+	};
+	static constexpr size_t kMaxGraphs = 48;
+	std::map<std::pair<const Csr *, GraphKey>, GraphEntry> graphs;
+	uint64_t graph_tick = 0;
+	Csr *AT = nullptr;                // transpose view for the adjoint solve
 	std::vector<double> hhist;        // host copy of the last history
 	int64_t hhist_count = 0;
 	int mixed_outer = 0, mixed_inner = 0;

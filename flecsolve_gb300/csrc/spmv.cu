@@ -200,6 +200,7 @@ int ensure_transpose(Csr *A) {
 		FS_CUDA_TRY(ctx, cudaMemcpy(A->t_row, trow.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
 		FS_CUDA_TRY(ctx, cudaMemcpy(A->t_perm, perm.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
 		FS_CUDA_TRY(ctx, cudaMemcpy(A->t_blk, tb.data(), tb.size() * sizeof(int), cudaMemcpyHostToDevice));
+		FS_CUDA_TRY(ctx, fence_setup_copies());
 		A->t_nblk = (int)tb.size() - 1;
 		A->t_valid = true;
 		A->t_vals_valid = false;
@@ -309,7 +310,8 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 	    (nnz > 0 && cudaMemcpy(A->val, val, nnz * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) ||
 	    cudaMemcpy(A->blk, blk.data(), blk.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
 	    (!binfo.empty() && cudaMemcpy(A->blkinfo, binfo.data(), binfo.size() * sizeof(int4),
-	                                  cudaMemcpyHostToDevice) != cudaSuccess))
+	                                  cudaMemcpyHostToDevice) != cudaSuccess) ||
+	    fence_setup_copies() != cudaSuccess)
 		return fail(FS_ERR_CUDA);
 	*out = reinterpret_cast<fs_csr>(A);
 	return FS_OK;

@@ -241,10 +241,12 @@ typedef struct {
 	/* device loop: iterations per CUDA-graph launch between residual
 	   read-backs (0 = library default) */
 	int k_readback;
-	/* mixed precision (FS_CG_MIXED); default FS_REFINE_RELIABLE, 1e-2 */
+	/* mixed precision (FS_*_MIXED); default FS_REFINE_RELIABLE */
 	int refine;          /* enum fs_refine_kind */
-	double inner_rtol;   /* restart: inner relative tolerance; reliable:
-	                        residual reduction between replacements        */
+	double inner_rtol;   /* restart: inner relative tolerance (0 = 1e-4);
+	                        reliable: residual reduction between FP64
+	                        replacements (0 = 0.1 for CG and batched CG,
+	                        1e-2 for BiCGSTAB)                              */
 	int max_outer;       /* restart: maximum refinement steps            */
 } fs_krylov_settings;
 
@@ -274,6 +276,23 @@ FS_API int fs_krylov_history(fs_solver s, double *hist, int64_t *n);
 /* number of refinement (outer) steps and total inner iterations of the last
  * FS_CG_MIXED apply */
 FS_API int fs_krylov_mixed_stats(fs_solver s, int *outer, int *inner_iters);
+
+/* ------------------------------------------------------------ adjoint --- */
+/* No counterpart in the reference (it has no adjoint).  For a loss L(x) of
+ * x = A^-1 b:  A^T lambda = dL/dx (fs_krylov_apply_transpose: the bound
+ * solver on the transposed operator, a CSC view of A built once per pattern),
+ * dL/db = lambda, dL/dA_ij = -lambda_i x_j (fs_csr_value_grad), and for the
+ * finite-volume diffusion operator assembled from face coefficients
+ * (fs_fv_assemble, same face layout and row order as the seeded generators)
+ * dL/dc_f = -(lambda_i - lambda_j)(x_i - x_j), or -lambda_i x_i on the
+ * boundary (fs_fv_face_grad; `scale` multiplies, `accumulate` adds to g). */
+FS_API int fs_krylov_apply_transpose(fs_solver s, fs_vec b, fs_vec x, fs_solve_info *info);
+FS_API int fs_csr_transpose(fs_csr A, fs_csr *AT);
+FS_API int fs_csr_value_grad(fs_csr A, fs_vec lambda, fs_vec x, fs_vec grad_values);
+/* A.values = scale * K(faces) + shift * I for an n^dim grid (dim 2 or 3) */
+FS_API int fs_fv_assemble(fs_csr A, int dim, int64_t n, fs_vec faces, double scale, double shift);
+FS_API int fs_fv_face_grad(fs_ctx ctx, int dim, int64_t n, fs_vec lambda, fs_vec x, double scale,
+                           int accumulate, fs_vec grad_faces);
 
 /* --------------------------------------------------- batched solves --- */
 /* Many independent systems in one persistent launch (no counterpart in the

@@ -170,10 +170,12 @@ def test_mixed_cg_refinement(ctx, wl):
     """FP32-inner / FP64-refined CG reaches the FP64 stopping test, and its
     error against the FP64 direct solution is <= 1e-8 when the stopping test
     asks for it (rtol 1e-11 bounds the forward error by cond(A) * 1e-11)."""
-    import scipy.sparse.linalg as spla
     A, b = P.workload(wl)
     ref64 = O.solve("cg", A, b, maxiter=20000, rtol=1e-8)
-    xs = spla.spsolve(A.to_scipy().tocsc(), b)
+    # FP64 solution to rtol 1e-14 by the oracle (a sparse LU of the 3-D
+    # operator takes half a minute on the test host); its forward error is
+    # <= cond(A) * 1e-14, far inside the 1e-8 bar
+    xs = O.solve("cg", A, b, maxiter=20000, rtol=1e-14).x
     # default: FP32 recurrences with FP64 residual replacement -- the search
     # direction survives a replacement, so the iteration count is the FP64 one
     info, x, slv = _run(ctx, fs.mixed_cg, A, b, maxiter=20000, rtol=1e-8)
