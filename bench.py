@@ -164,6 +164,43 @@ def cpu_sample(A, b, seconds_target=15.0, max_iters=60):
 
 # ------------------------------------------------------------ GPU side --
 
+def spmv_events_ms(fs, ctx, dA, n, dtype, reps=20):
+    """Average duration of one CSR SpMV launch (CUDA events on the library's
+    stream around `reps` back-to-back launches, after 3 warm-up launches)."""
+    xv = fs.Vector(ctx, n, dtype)
+    yv = fs.Vector(ctx, n, dtype)
+    xv.set_random(5)
+    for _ in range(3):
+        dA.apply(xv, yv)
+    ctx.sync()
+    ctx.record(2)
+    for _ in range(reps):
+        dA.apply(xv, yv)
+    ctx.record(3)
+    return ctx.elapsed_ms(2, 3) / reps
+
+
+def run_spmv_only(args):
+    """`--mode spmv`: the SpMV kernel alone on the workload, FP64 then FP32
+    (`--steps` timed launches each after `--warmup` ones); the command that
+    the ncu summaries of the SpMV kernel are captured from."""
+    import flecsolve_gb300 as fs
+    from flecsolve_gb300 import problems as P
+    A, _ = P.workload(args.workload)
+    n, nnz = A.nrows, A.nnz
+    ctx = fs.Context(0)
+    dA = fs.CSR(ctx, A)
+    peak, peak_kind = _peaks()
+    out = {"mode": "spmv", "workload": args.workload, "rows": n, "nnz": nnz}
+    for dt, vb in (("f64", 8), ("f32", 4)):
+        ms = spmv_events_ms(fs, ctx, dA, n, dt, reps=max(1, args.steps))
+        gbs = spmv_bytes(n, nnz, vb) / (ms * 1e-3) / 1e9
+        out[dt] = {"ms": ms, "gbs": gbs, "frac": gbs / peak, "peak": peak,
+                   "peak_source": f"hbm_gbs of {peak_kind}",
+                   "algorithmic_bytes": spmv_bytes(n, nnz, vb)}
+    return out
+
+
 def run_ours(args, ws, rank, local):
     import flecsolve_gb300 as fs
     from flecsolve_gb300 import problems as P
@@ -220,21 +257,8 @@ def run_ours(args, ws, rank, local):
         ms_mx, ms_64 = float(t[0]), float(t[1])
 
     # SpMV kernel alone (the dominant kernel), CUDA events on the same stream
-    def spmv_time(dtype, reps=20):
-        xv = fs.Vector(ctx, n, dtype)
-        yv = fs.Vector(ctx, n, dtype)
-        xv.set_random(5)
-        for _ in range(3):
-            dA.apply(xv, yv)
-        ctx.sync()
-        ctx.record(2)
-        for _ in range(reps):
-            dA.apply(xv, yv)
-        ctx.record(3)
-        return ctx.elapsed_ms(2, 3) / reps
-
-    spmv64_ms = spmv_time("f64")
-    spmv32_ms = spmv_time("f32")
+    spmv64_ms = spmv_events_ms(fs, ctx, dA, n, "f64")
+    spmv32_ms = spmv_events_ms(fs, ctx, dA, n, "f32")
     peak, peak_kind = _peaks()
     b64 = spmv_bytes(n, nnz, 8)
     b32 = spmv_bytes(n, nnz, 4)
@@ -371,7 +395,12 @@ def main():
     ap.add_argument("--refine", default="reliable", choices=["restart", "reliable"])
     ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
+    ap.add_argument("--mode", default="solve", choices=["solve", "spmv"],
+                    help="spmv: time only the SpMV kernel on the workload (profiling)")
     args = ap.parse_args()
+    if args.mode == "spmv":
+        print(json.dumps(run_spmv_only(args)))
+        return
     ws, rank, local = _dist()
     if ws > 1:
         import torch
