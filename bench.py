@@ -112,10 +112,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def spmv_bytes(nrows, nnz, val_bytes):
-    """Algorithmic bytes of one CSR SpMV: values + int32 columns, int32 row
-    offsets, x read once, y written once."""
-    return nnz * (val_bytes + 4) + 4 * (nrows + 1) + 2 * nrows * val_bytes
+def spmv_bytes(nrows, nnz, val_bytes, coded=False, nblk=0):
+    """Algorithmic bytes of one CSR SpMV: values + int32 columns (or 4-bit
+    column-offset codes and a 16-entry int32 offset table per row block),
+    int32 row offsets, x read once, y written once."""
+    idx = (nnz + 1) // 2 + 64 * nblk if coded else 4 * nnz
+    return nnz * val_bytes + idx + 4 * (nrows + 1) + 2 * nrows * val_bytes
 
 
 def pcg_iter_bytes(nrows, nnz, val_bytes):
@@ -191,13 +193,202 @@ def run_spmv_only(args):
     ctx = fs.Context(0)
     dA = fs.CSR(ctx, A)
     peak, peak_kind = _peaks()
-    out = {"mode": "spmv", "workload": args.workload, "rows": n, "nnz": nnz}
-    for dt, vb in (("f64", 8), ("f32", 4)):
-        ms = spmv_events_ms(fs, ctx, dA, n, dt, reps=max(1, args.steps))
-        gbs = spmv_bytes(n, nnz, vb) / (ms * 1e-3) / 1e9
-        out[dt] = {"ms": ms, "gbs": gbs, "frac": gbs / peak, "peak": peak,
-                   "peak_source": f"hbm_gbs of {peak_kind}",
-                   "algorithmic_bytes": spmv_bytes(n, nnz, vb)}
+    coded = dA.index_coding()
+    out = {"mode": "spmv", "workload": args.workload, "rows": n, "nnz": nnz,
+           "index_coding": coded}
+    for use in ([True, False] if coded else [False]):
+        dA.index_coding(use)
+        for dt, vb in (("f64", 8), ("f32", 4)):
+            ms = spmv_events_ms(fs, ctx, dA, n, dt, reps=max(1, args.steps))
+            nbytes = spmv_bytes(n, nnz, vb, coded=use, nblk=dA.nblk())
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            out[dt + ("_coded" if use else "_colids")] = {
+                "ms": ms, "gbs": gbs, "frac": gbs / peak, "peak": peak,
+                "peak_source": f"hbm_gbs of {peak_kind}", "algorithmic_bytes": nbytes}
+    dA.index_coding(True)
+    return out
+
+
+def _timed_solve(ctx, slv, vb, vx):
+    """One warm solve, then one timed with CUDA events on the library stream."""
+    slv(vb, vx)
+    ctx.sync()
+    ctx.record(6)
+    info = slv(vb, vx)
+    ctx.record(7)
+    return ctx.elapsed_ms(6, 7) * 1e-3, info
+
+
+def _relres(S, b, x):
+    return float(np.linalg.norm(b - S @ x) / np.linalg.norm(b))
+
+
+def run_suite(args):
+    """`--mode suite`: the secondary configurations, one solve each after a
+    warm-up (CUDA events), with iteration counts and true FP64 residuals:
+    2-D Poisson 128^2 (CG, BiCGSTAB, GMRES(30)); convection-diffusion 192^3
+    (BiCGSTAB and GMRES(30), FP64 and mixed); 512 independent 2-D diffusion
+    systems in one batched launch against the same solver run system by
+    system on a sample; block CG on 16 right-hand sides of the 128^3
+    Laplacian against 16 separate solves; the adjoint gradient of
+    ||x - x_target||^2 at 128^3 and backward-Euler heat 64^3 x 200 steps
+    differentiated with checkpoints every 20."""
+    import flecsolve_gb300 as fs
+    from flecsolve_gb300 import adjoint as ad
+    from flecsolve_gb300 import problems as P
+    ctx = fs.Context(0)
+    out = {"mode": "suite"}
+    only = set(args.suite.split(",")) if args.suite else None
+
+    def want(k):
+        return only is None or k in only
+
+    def krylov(tag, A, b, cases):
+        dA = fs.CSR(ctx, A)
+        vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
+        S = A.to_scipy()
+        res = {"rows": A.nrows, "nnz": A.nnz}
+        for name, ns, kw in cases:
+            slv = ns.solver(ns.settings(maxiter=30000, rtol=1e-8, **kw))(dA, fs.op.jacobi)
+            s, info = _timed_solve(ctx, slv, vb, vx)
+            res[name] = {"s": s, "iters": info.iters, "restarts": info.restarts,
+                         "status": info.status, "true_relres": _relres(S, b, vx.numpy())}
+        out[tag] = res
+
+    g30 = dict(max_krylov_dim=30, restart=True)
+    if want("poisson2d"):
+        A, b = P.workload("poisson2d-128")
+        krylov("poisson2d-128", A, b, [("cg", fs.cg, {}), ("bicgstab", fs.bicgstab, {}),
+                                       ("gmres30", fs.gmres, g30)])
+    if want("convdiff3d"):
+        A, b = P.workload("convdiff3d-192")
+        krylov("convdiff3d-192", A, b, [
+            ("bicgstab", fs.bicgstab, {}), ("bicgstab_mixed", fs.mixed_bicgstab, {}),
+            ("gmres30_mgs", fs.gmres, dict(g30, ortho="mgs")),
+            ("gmres30_cgs2", fs.gmres, dict(g30, ortho="cgs2")),
+            ("gmres30_mixed", fs.mixed_gmres, g30)])
+        ref = json.loads((ROOT / "tests" / "golden" / "full_size.json").read_text()).get("convdiff3d-192", {})
+        out["convdiff3d-192"]["reference_iters"] = {k: v["iters"] for k, v in ref.items()}
+    if want("batched"):
+        A, off, b, sides = P.batch_diffusion2d()
+        dA = fs.CSR(ctx, A)
+        vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
+        fs.batch_cg(dA, off, vb, vx, maxiter=20000, rtol=1e-8)  # autotune + warm
+        cl, th = fs.batch_tuning(dA, off)
+        ctx.sync()
+        ctx.record(6)
+        infos = fs.batch_cg(dA, off, vb, vx, maxiter=20000, rtol=1e-8)
+        ctx.record(7)
+        t = ctx.elapsed_ms(6, 7) * 1e-3
+        x = vx.numpy()
+        S = A.to_scipy()
+        rr = max(_relres(S[off[k]:off[k + 1]], b[off[k]:off[k + 1]], x) for k in range(len(infos)))
+        its = [i.iters for i in infos]
+        # the same solver system by system on every 32nd system, scaled to all
+        seq, sample = 0.0, list(range(0, len(infos), 32))
+        for k in sample:
+            lo, hi = off[k], off[k + 1]
+            Ak = P.CSR(int(hi - lo), int(hi - lo), A.rowptr[lo:hi + 1] - A.rowptr[lo],
+                       A.col[A.rowptr[lo]:A.rowptr[hi]] - lo, A.val[A.rowptr[lo]:A.rowptr[hi]])
+            slv = fs.mixed_cg.solver(fs.mixed_cg.settings(maxiter=20000, rtol=1e-8))(
+                fs.CSR(ctx, Ak), fs.op.jacobi)
+            seq += _timed_solve(ctx, slv, fs.Vector(ctx, b[lo:hi]), fs.Vector(ctx, int(hi - lo)))[0]
+        out["batch512-diffusion2d"] = {
+            "systems": len(infos), "rows": A.nrows, "nnz": A.nnz, "s": t, "cluster": cl,
+            "threads": th, "all_converged": all(i.status == "converged_rtol" for i in infos),
+            "max_true_relres": rr, "iters_min": min(its), "iters_max": max(its),
+            "iters_sum": int(sum(its)),
+            "one_by_one_s_estimate": seq * len(infos) / len(sample),
+            "one_by_one_sample": f"{len(sample)} systems (every 32nd), mixed CG one solve each"}
+    if want("blockcg-mixed"):
+        # the mixed block solve alone (profiling): 16 right-hand sides of the
+        # 96^3 Laplacian, one warm-up and one timed solve
+        A, _ = P.workload("laplace3d-96")
+        n = A.nrows
+        B = np.stack([P.uniform(6 + j, n) for j in range(16)], axis=1)
+        dA = fs.CSR(ctx, A)
+        vB, vX = fs.Vector(ctx, B.ravel()), fs.Vector(ctx, n * 16)
+        fs.block_cg(dA, vB, vX, 16, maxiter=5000, rtol=1e-8, mixed=True)
+        ctx.sync()
+        ctx.record(6)
+        infos = fs.block_cg(dA, vB, vX, 16, maxiter=5000, rtol=1e-8, mixed=True)
+        ctx.record(7)
+        out["laplace3d-96x16-mixed"] = {"s": ctx.elapsed_ms(6, 7) * 1e-3,
+                                        "block_iters": infos[0].restarts}
+    if want("blockcg"):
+        A, _ = P.workload("laplace3d-128")
+        n = A.nrows
+        B = np.stack([P.uniform(6 + j, n) for j in range(16)], axis=1)
+        dA = fs.CSR(ctx, A)
+        S = A.to_scipy()
+        res = {"rows": n, "nnz": A.nnz, "rhs": 16}
+        vB, vX = fs.Vector(ctx, B.ravel()), fs.Vector(ctx, n * 16)
+        fs.block_cg(dA, vB, vX, 16, maxiter=5000, rtol=1e-8)
+        ctx.sync()
+        ctx.record(6)
+        infos = fs.block_cg(dA, vB, vX, 16, maxiter=5000, rtol=1e-8)
+        ctx.record(7)
+        X = vX.numpy().reshape(n, 16)
+        res["block_cg_fp64"] = {"s": ctx.elapsed_ms(6, 7) * 1e-3, "block_iters": infos[0].restarts,
+                                "max_true_relres": max(_relres(S, B[:, j], X[:, j]) for j in range(16))}
+        fs.block_cg(dA, vB, vX, 16, maxiter=5000, rtol=1e-8, mixed=True)
+        ctx.sync()
+        ctx.record(6)
+        infos = fs.block_cg(dA, vB, vX, 16, maxiter=5000, rtol=1e-8, mixed=True)
+        ctx.record(7)
+        X = vX.numpy().reshape(n, 16)
+        res["block_cg_mixed"] = {"s": ctx.elapsed_ms(6, 7) * 1e-3, "block_iters": infos[0].restarts,
+                                 "all_converged": all(i.status == "converged_rtol" for i in infos),
+                                 "max_true_relres": max(_relres(S, B[:, j], X[:, j]) for j in range(16))}
+        for name, ns in (("16x_pcg_fp64", fs.cg), ("16x_pcg_mixed", fs.mixed_cg)):
+            vb, vx = fs.Vector(ctx, n), fs.Vector(ctx, n)
+            slv = ns.solver(ns.settings(maxiter=5000, rtol=1e-8))(dA, fs.op.jacobi)
+            tot, its = 0.0, []
+            for j in range(16):
+                vb.upload(B[:, j])
+                s, info = _timed_solve(ctx, slv, vb, vx)
+                tot += s
+                its.append(info.iters)
+            res[name] = {"s": tot, "iters_max": max(its), "iters_sum": sum(its)}
+        out["laplace3d-128x16"] = res
+    if want("adjoint"):
+        n = 128
+        system = ad.DiffusionSolve(ctx, 3, n, rtol=1e-8)
+        c = P.faces_lognormal(3, n, seed=2)
+        b = P.uniform(3, n ** 3)
+        system.set_faces(P.faces_lognormal(3, n, seed=7))
+        vb, xt = fs.Vector(ctx, b), fs.Vector(ctx, n ** 3)
+        system.solve(vb, xt)
+        t_h = xt.numpy()
+        x = fs.Vector(ctx, n ** 3)
+        system.set_faces(c)
+        g = fs.Vector(ctx, n ** 3)
+        for rep in range(2):
+            ctx.sync()
+            ctx.record(6)
+            system.solve(vb, x)                     # forward
+            g.linear_sum(2.0, x, -2.0, xt)          # dL/dx
+            system.adjoint(g, x)                    # A^T lam = dL/dx, dL/dc
+            ctx.record(7)
+        out["adjoint-diffusion3d-128"] = {
+            "s_forward_plus_gradient": ctx.elapsed_ms(6, 7) * 1e-3,
+            "gradient_entries": system.nfaces + n ** 3}
+        n, dt, steps = 64, 1e-3, 200
+        heat = ad.DiffusionSolve(ctx, 3, n, rtol=1e-8, scale=dt, shift=1.0)
+        u0 = P.uniform(9, n ** 3)
+        heat.set_faces(P.faces_lognormal(3, n, seed=7))
+        target = ad.heat_forward(heat, u0, steps)[0].numpy()
+        cf = P.faces_lognormal(3, n, seed=2)
+        t0 = time.perf_counter()
+        heat.set_faces(cf)
+        ad.heat_forward(heat, u0, steps)
+        ctx.sync()
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ad.heat_loss_and_grad(heat, cf, u0, target, steps, checkpoint=20)
+        ctx.sync()
+        out["heat-be-64x200"] = {"s_forward": t_fwd, "s_loss_and_gradient": time.perf_counter() - t0,
+                                 "checkpoint_every": 20, "states_held": 20 + 1 + steps // 20}
     return out
 
 
@@ -260,8 +451,9 @@ def run_ours(args, ws, rank, local):
     spmv64_ms = spmv_events_ms(fs, ctx, dA, n, "f64")
     spmv32_ms = spmv_events_ms(fs, ctx, dA, n, "f32")
     peak, peak_kind = _peaks()
-    b64 = spmv_bytes(n, nnz, 8)
-    b32 = spmv_bytes(n, nnz, 4)
+    coded = dA.index_coding()
+    b64 = spmv_bytes(n, nnz, 8, coded=coded, nblk=dA.nblk())
+    b32 = spmv_bytes(n, nnz, 4, coded=coded, nblk=dA.nblk())
     gbs64 = b64 / (spmv64_ms * 1e-3) / 1e9
     gbs32 = b32 / (spmv32_ms * 1e-3) / 1e9
 
@@ -319,14 +511,16 @@ def run_ours(args, ws, rank, local):
                       "inner_rtol": args.inner_rtol or ("library default (0.1)" if args.refine == "reliable" else "library default (1e-4)")},
         "speedup_mixed_vs_fp64": ms_64 / ms_mx,
         "spmv_hbm_gbs": {"f64": gbs64, "f32": gbs32, "f64_ms": spmv64_ms, "f32_ms": spmv32_ms},
-        "roofline": {"bound": "hbm", "kernel": "spmv_rb_kernel<float> (FP32 CSR SpMV)",
+        "roofline": {"bound": "hbm",
+                     "kernel": "spmv_rb_kernel<float> (FP32 CSR SpMV, "
+                               + ("4-bit column-offset codes)" if coded else "int32 column ids)"),
                      "achieved": gbs32, "peak": peak, "unit": "GB/s", "frac": gbs32 / peak,
                      "peak_source": f"hbm_gbs of {peak_kind}",
                      "algorithmic_bytes_per_launch": b32,
-                     "traffic": _traffic_from_profiles("spmv_f32")},
+                     "traffic": _traffic_from_profiles("spmv_f32" + ("_coded" if coded else ""))},
         "roofline_fp64_spmv": {"achieved": gbs64, "peak": peak, "frac": gbs64 / peak,
                                "algorithmic_bytes_per_launch": b64,
-                               "traffic": _traffic_from_profiles("spmv_f64")},
+                               "traffic": _traffic_from_profiles("spmv_f64" + ("_coded" if coded else ""))},
         "e2e": {"value": e2e_ms * 1e-3, "unit": "s", "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 8 * n},
         "gpu_launches": launches_mx,
@@ -395,11 +589,16 @@ def main():
     ap.add_argument("--refine", default="reliable", choices=["restart", "reliable"])
     ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
-    ap.add_argument("--mode", default="solve", choices=["solve", "spmv"],
-                    help="spmv: time only the SpMV kernel on the workload (profiling)")
+    ap.add_argument("--mode", default="solve", choices=["solve", "spmv", "suite"],
+                    help="spmv: time only the SpMV kernel on the workload (profiling); "
+                         "suite: the secondary configurations")
+    ap.add_argument("--suite", default="", help="comma list of suite parts (default: all)")
     args = ap.parse_args()
     if args.mode == "spmv":
         print(json.dumps(run_spmv_only(args)))
+        return
+    if args.mode == "suite":
+        print(json.dumps(run_suite(args)))
         return
     ws, rank, local = _dist()
     if ws > 1:

@@ -112,6 +112,8 @@ _PROTOS = {
     "fs_csr_update_values": [_vp, _vp],
     "fs_csr_update_values_device": [_vp, _vp],
     "fs_csr_values_device_ptr": [_vp, C.POINTER(_vp)],
+    "fs_csr_index_coding": [_vp, C.c_int, C.POINTER(C.c_int)],
+    "fs_csr_row_blocks": [_vp, C.POINTER(_i64)],
     "fs_csr_spmv": [_vp, _vp, _vp, C.c_int],
     "fs_csr_residual": [_vp, _vp, _vp, _vp],
     "fs_csr_spmv_transpose": [_vp, _vp, _vp],
@@ -137,6 +139,8 @@ _PROTOS = {
     "fs_fv_face_grad": [_vp, C.c_int, _i64, _vp, _vp, C.c_double, C.c_int, _vp],
     "fs_block_cg_solve": [_vp, C.POINTER(KrylovSettings), _vp, C.POINTER(Precond), C.c_int, _vp, _vp,
                           C.POINTER(SolveInfo)],
+    "fs_block_cg_solve_mixed": [_vp, C.POINTER(KrylovSettings), _vp, C.POINTER(Precond), C.c_int,
+                                _vp, _vp, C.POINTER(SolveInfo)],
 }
 
 # entry points that exist in the header but are optional for older builds

@@ -316,6 +316,20 @@ class CSR:
         v = np.ascontiguousarray(val, dtype=np.float64)
         check(lib().fs_csr_update_values(self.h, v.ctypes.data_as(C.c_void_p)), self.ctx.h)
 
+    def nblk(self) -> int:
+        """Number of SpMV row blocks."""
+        n = C.c_int64()
+        check(lib().fs_csr_row_blocks(self.h, C.byref(n)), self.ctx.h)
+        return n.value
+
+    def index_coding(self, enable=None) -> bool:
+        """Whether the SpMV reads 4-bit column-offset codes (stencil
+        patterns) instead of column ids; `enable` switches it (True/False)."""
+        a = C.c_int()
+        check(lib().fs_csr_index_coding(self.h, -1 if enable is None else int(bool(enable)),
+                                        C.byref(a)), self.ctx.h)
+        return bool(a.value)
+
     def values(self) -> np.ndarray:
         """The current values (row order) copied to the host."""
         p = C.c_void_p()
@@ -616,13 +630,18 @@ def batch_cg(A: CSR, offsets, b: Vector, x: Vector, maxiter: int, rtol: float,
 
 
 def block_cg(A: CSR, B: Vector, X: Vector, nrhs: int, maxiter: int, rtol: float,
-             use_zero_guess: bool = True, jacobi: bool = True, k_readback: int = 16):
+             use_zero_guess: bool = True, jacobi: bool = True, k_readback: int = 16,
+             mixed: bool = False, delta: float = 0.0):
     """Block Jacobi-PCG on ``nrhs`` right-hand sides stored N x nrhs row-major
-    in ``B`` / ``X``; returns one :class:`SolveInfo` per column."""
-    st = _settings(_lib.CG, maxiter, rtol, 0.0, use_zero_guess, k_readback=k_readback)
+    in ``B`` / ``X``; returns one :class:`SolveInfo` per column.  ``mixed``:
+    FP32 block recurrences with FP64 residual replacement every ``delta``
+    reduction (0 = library default)."""
+    st = _settings(_lib.CG, maxiter, rtol, 0.0, use_zero_guess, k_readback=k_readback,
+                   inner_rtol=delta)
     pc = _lib.Precond(_lib.PRECOND_JACOBI if jacobi else _lib.PRECOND_NONE, None, None)
     infos = (_lib.SolveInfo * nrhs)()
-    check(lib().fs_block_cg_solve(A.ctx.h, C.byref(st), A.h, C.byref(pc), nrhs, B.h, X.h, infos),
+    fn = lib().fs_block_cg_solve_mixed if mixed else lib().fs_block_cg_solve
+    check(fn(A.ctx.h, C.byref(st), A.h, C.byref(pc), nrhs, B.h, X.h, infos),
           A.ctx.h, "fs_block_cg_solve")
     return [_info(i) for i in infos]
 

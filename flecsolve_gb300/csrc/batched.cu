@@ -16,8 +16,6 @@
 // b - A x with the FP64 values, whenever it has dropped by `delta` and at
 // every stop, and the stopping test is on that FP64 residual.
 //
-// Block CG (several right-hand sides of one operator) lives at the end of the
-// file.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -418,440 +416,5 @@ extern "C" FS_API int fs_batch_tuning(fs_ctx h, fs_csr Ah, int nsys, const int64
 		return set_err(ctx, FS_ERR_INVALID_ARG, "no batched solve has run on this partition");
 	*cluster_size = it->second.tuned_cluster;
 	*threads = it->second.tuned_threads;
-	return FS_OK;
-}
-
-// ======================================================== block CG ======
-//
-// Block Jacobi-PCG (O'Leary, "The block conjugate gradient algorithm and
-// related methods", LAA 29, 1980) for S right-hand sides of one operator,
-// FP64.  X, R, P, Q are N x S row-major (the S values of a row contiguous),
-// so the SpMM reads A once for all S columns and gathers one 8*S-byte row of
-// P per nonzero.  Per iteration:
-//   Q = A P,  M = P^T Q                 (SpMM with the Gram product fused)
-//   alpha = M^-1 G
-//   X += P alpha,  R -= Q alpha,  Z = D^-1 R,  G' = Z^T R, ||R_j||
-//   beta = G^-1 G',  P = Z + P beta,  G = G'
-// Gram products: each CTA walks 16-row tiles; thread (i, j) of the 256 sums
-// P[r][i] Q[r][j] over the tile rows and keeps its running sum, the per-CTA
-// sums are folded in CTA order by the last CTA (deterministic).  Columns that
-// reach rtol * ||B_j|| record their iteration count; the block iterates
-// until every column has.
-namespace fsg {
-namespace {
-
-constexpr int kS = 16;           // right-hand sides per block
-constexpr int kTile = 16;        // rows per tile (kTile * kS = 256 threads)
-
-struct BcgState {
-	double G[kS * kS], Gn[kS * kS], M[kS * kS], alpha[kS * kS], beta[kS * kS];
-	double bnorm[kS], rnorm[kS], res0[kS];
-	int conv_iter[kS];
-	int iter, done, status, flags;
-};
-
-// x = A^-1 B for the s x s matrix A (row-major), s right-hand sides in B
-// (row-major, overwritten with the solution): Gaussian elimination with
-// partial pivoting.  Returns false on a zero pivot.  Single thread.
-__device__ bool small_solve(double *A, double *B) {
-	int piv[kS];
-	for (int i = 0; i < kS; ++i)
-		piv[i] = i;
-	for (int k = 0; k < kS; ++k) {
-		int p = k;
-		double m = fabs(A[k * kS + k]);
-		for (int i = k + 1; i < kS; ++i)
-			if (fabs(A[i * kS + k]) > m) {
-				m = fabs(A[i * kS + k]);
-				p = i;
-			}
-		if (!(m > 0.0))
-			return false;
-		if (p != k) {
-			for (int j = 0; j < kS; ++j) {
-				double t = A[k * kS + j];
-				A[k * kS + j] = A[p * kS + j];
-				A[p * kS + j] = t;
-				t = B[k * kS + j];
-				B[k * kS + j] = B[p * kS + j];
-				B[p * kS + j] = t;
-			}
-		}
-		for (int i = k + 1; i < kS; ++i) {
-			const double f = A[i * kS + k] / A[k * kS + k];
-			for (int j = k; j < kS; ++j)
-				A[i * kS + j] -= f * A[k * kS + j];
-			for (int j = 0; j < kS; ++j)
-				B[i * kS + j] -= f * B[k * kS + j];
-		}
-	}
-	for (int k = kS - 1; k >= 0; --k)
-		for (int j = 0; j < kS; ++j) {
-			double s = B[k * kS + j];
-			for (int i = k + 1; i < kS; ++i)
-				s -= A[k * kS + i] * B[i * kS + j];
-			B[k * kS + j] = s / A[k * kS + k];
-		}
-	return true;
-}
-
-// Q = A P and the CTA's part of M = P^T Q
-__global__ void __launch_bounds__(256)
-k_bcg_spmm(int n, const int *__restrict__ rp, const int *__restrict__ col,
-           const double *__restrict__ val, const double *__restrict__ P, double *__restrict__ Q,
-           BcgState *st, double *part, unsigned *counter) {
-	__shared__ double sp[kTile][kS], sq[kTile][kS];
-	if (st->done)
-		return;
-	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
-	const int ntiles = (n + kTile - 1) / kTile;
-	double m = 0.0;
-	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const int r = t * kTile + tr;
-		double q = 0.0, p = 0.0;
-		if (r < n) {
-			for (int k = rp[r]; k < rp[r + 1]; ++k)
-				q = fma(val[k], P[(size_t)col[k] * kS + tj], q);
-			Q[(size_t)r * kS + tj] = q;
-			p = P[(size_t)r * kS + tj];
-		}
-		sp[tr][tj] = p;
-		sq[tr][tj] = q;
-		__syncthreads();
-		// thread (i = tr, j = tj) of the Gram tile
-#pragma unroll
-		for (int rr = 0; rr < kTile; ++rr)
-			m = fma(sp[rr][tr], sq[rr][tj], m);
-		__syncthreads();
-	}
-	part[(size_t)blockIdx.x * 256 + threadIdx.x] = m;
-	if (last_block(counter)) {
-		double s = 0.0;
-		for (unsigned b = 0; b < gridDim.x; ++b)
-			s += __ldcg(part + (size_t)b * 256 + threadIdx.x);
-		st->M[threadIdx.x] = s;
-		__syncthreads();
-		if (threadIdx.x == 0) {
-			// alpha = M^-1 G
-			double Mc[kS * kS];
-			for (int i = 0; i < kS * kS; ++i) {
-				Mc[i] = st->M[i];
-				st->alpha[i] = st->G[i];
-			}
-			if (!small_solve(Mc, st->alpha)) {
-				st->done = 1;
-				st->status = FS_DIVERGED_BREAKDOWN;
-			}
-			*counter = 0;
-		}
-	}
-}
-
-// X += P alpha, R -= Q alpha, Z = D^-1 R; G' = Z^T R and ||R_j||^2 parts;
-// the last CTA tests every column and forms beta = G^-1 G'
-__global__ void __launch_bounds__(256)
-k_bcg_update(int n, double *__restrict__ X, const double *__restrict__ P, double *__restrict__ R,
-             const double *__restrict__ Q, const double *__restrict__ dinv, BcgState *st,
-             double *part, double *part2, unsigned *counter, double tolf, int maxiter) {
-	__shared__ double sa[kS * kS], sp[kTile][kS], sq[kTile][kS], sr[kTile][kS], sz[kTile][kS];
-	if (st->done)
-		return;
-	sa[threadIdx.x] = st->alpha[threadIdx.x];
-	__syncthreads();
-	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
-	const int ntiles = (n + kTile - 1) / kTile;
-	double g = 0.0, nr = 0.0;
-	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const int r = t * kTile + tr;
-		sp[tr][tj] = r < n ? P[(size_t)r * kS + tj] : 0.0;
-		sq[tr][tj] = r < n ? Q[(size_t)r * kS + tj] : 0.0;
-		__syncthreads();
-		double x = 0.0, rv = 0.0, z = 0.0;
-		if (r < n) {
-			x = X[(size_t)r * kS + tj];
-			rv = R[(size_t)r * kS + tj];
-#pragma unroll
-			for (int i = 0; i < kS; ++i) {
-				x = fma(sp[tr][i], sa[i * kS + tj], x);
-				rv = fma(-sq[tr][i], sa[i * kS + tj], rv);
-			}
-			X[(size_t)r * kS + tj] = x;
-			R[(size_t)r * kS + tj] = rv;
-			z = dinv ? dinv[r] * rv : rv;
-			nr = fma(rv, rv, nr);
-		}
-		sr[tr][tj] = rv;
-		sz[tr][tj] = z;
-		__syncthreads();
-#pragma unroll
-		for (int rr = 0; rr < kTile; ++rr)
-			g = fma(sz[rr][tr], sr[rr][tj], g);
-		__syncthreads();
-	}
-	part[(size_t)blockIdx.x * 256 + threadIdx.x] = g;
-	// column norms: thread (tr, tj) summed rows of column tj; fold the 16
-	// row-threads of each column in the block first
-	__shared__ double cn[kTile][kS];
-	cn[tr][tj] = nr;
-	__syncthreads();
-	if (threadIdx.x < kS) {
-		double c = 0.0;
-		for (int rr = 0; rr < kTile; ++rr)
-			c += cn[rr][threadIdx.x];
-		part2[(size_t)blockIdx.x * kS + threadIdx.x] = c;
-	}
-	if (last_block(counter)) {
-		double s = 0.0;
-		for (unsigned b = 0; b < gridDim.x; ++b)
-			s += __ldcg(part + (size_t)b * 256 + threadIdx.x);
-		st->Gn[threadIdx.x] = s;
-		if (threadIdx.x < kS) {
-			double c = 0.0;
-			for (unsigned b = 0; b < gridDim.x; ++b)
-				c += __ldcg(part2 + (size_t)b * kS + threadIdx.x);
-			st->rnorm[threadIdx.x] = sqrt(c);
-		}
-		__syncthreads();
-		if (threadIdx.x == 0) {
-			const int it = st->iter + 1;
-			st->iter = it;
-			bool all = true;
-			for (int j = 0; j < kS; ++j) {
-				if (st->conv_iter[j] == 0 && st->rnorm[j] < tolf * st->bnorm[j])
-					st->conv_iter[j] = it;
-				all = all && st->conv_iter[j] != 0;
-			}
-			if (all) {
-				st->done = 1;
-				st->status = FS_CONVERGED_RTOL;
-			}
-			else if (it >= maxiter) {
-				st->done = 1;
-				st->status = FS_DIVERGED_ITERS;
-			}
-			else {
-				// beta = G^-1 G'
-				double Gc[kS * kS];
-				for (int i = 0; i < kS * kS; ++i) {
-					Gc[i] = st->G[i];
-					st->beta[i] = st->Gn[i];
-				}
-				if (!small_solve(Gc, st->beta)) {
-					st->done = 1;
-					st->status = FS_DIVERGED_BREAKDOWN;
-				}
-				for (int i = 0; i < kS * kS; ++i)
-					st->G[i] = st->Gn[i];
-			}
-			*counter = 0;
-		}
-	}
-}
-
-// P = Z + P beta (Z = D^-1 R)
-__global__ void __launch_bounds__(256)
-k_bcg_dir(int n, double *__restrict__ P, const double *__restrict__ R,
-          const double *__restrict__ dinv, const BcgState *st) {
-	__shared__ double sb[kS * kS], sp[kTile][kS];
-	if (st->done)
-		return;
-	sb[threadIdx.x] = st->beta[threadIdx.x];
-	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
-	const int ntiles = (n + kTile - 1) / kTile;
-	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const int r = t * kTile + tr;
-		__syncthreads();
-		sp[tr][tj] = r < n ? P[(size_t)r * kS + tj] : 0.0;
-		__syncthreads();
-		if (r < n) {
-			double p = (dinv ? dinv[r] : 1.0) * R[(size_t)r * kS + tj];
-#pragma unroll
-			for (int i = 0; i < kS; ++i)
-				p = fma(sp[tr][i], sb[i * kS + tj], p);
-			P[(size_t)r * kS + tj] = p;
-		}
-	}
-}
-
-// R = B - A X (or B with X = 0), P = Z = D^-1 R, G = Z^T R, ||B_j||, ||R_j||
-__global__ void __launch_bounds__(256)
-k_bcg_start(int n, const int *__restrict__ rp, const int *__restrict__ col,
-            const double *__restrict__ val, const double *__restrict__ B, double *__restrict__ X,
-            double *__restrict__ R, double *__restrict__ P, const double *__restrict__ dinv,
-            int zero_guess, BcgState *st, double *part, double *part2, unsigned *counter) {
-	__shared__ double sr[kTile][kS], sz[kTile][kS], cb[kTile][kS], cr[kTile][kS];
-	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
-	const int ntiles = (n + kTile - 1) / kTile;
-	double g = 0.0, nb = 0.0, nr = 0.0;
-	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const int r = t * kTile + tr;
-		double rv = 0.0, z = 0.0;
-		if (r < n) {
-			const double bv = B[(size_t)r * kS + tj];
-			double ax = 0.0;
-			if (zero_guess)
-				X[(size_t)r * kS + tj] = 0.0;
-			else
-				for (int k = rp[r]; k < rp[r + 1]; ++k)
-					ax = fma(val[k], X[(size_t)col[k] * kS + tj], ax);
-			rv = bv - ax;
-			R[(size_t)r * kS + tj] = rv;
-			z = dinv ? dinv[r] * rv : rv;
-			P[(size_t)r * kS + tj] = z;
-			nb = fma(bv, bv, nb);
-			nr = fma(rv, rv, nr);
-		}
-		sr[tr][tj] = rv;
-		sz[tr][tj] = z;
-		__syncthreads();
-#pragma unroll
-		for (int rr = 0; rr < kTile; ++rr)
-			g = fma(sz[rr][tr], sr[rr][tj], g);
-		__syncthreads();
-	}
-	part[(size_t)blockIdx.x * 256 + threadIdx.x] = g;
-	cb[tr][tj] = nb;
-	cr[tr][tj] = nr;
-	__syncthreads();
-	if (threadIdx.x < kS) {
-		double c1 = 0.0, c2 = 0.0;
-		for (int rr = 0; rr < kTile; ++rr) {
-			c1 += cb[rr][threadIdx.x];
-			c2 += cr[rr][threadIdx.x];
-		}
-		part2[(size_t)blockIdx.x * 2 * kS + threadIdx.x] = c1;
-		part2[(size_t)blockIdx.x * 2 * kS + kS + threadIdx.x] = c2;
-	}
-	if (last_block(counter)) {
-		double s = 0.0;
-		for (unsigned b = 0; b < gridDim.x; ++b)
-			s += __ldcg(part + (size_t)b * 256 + threadIdx.x);
-		st->G[threadIdx.x] = s;
-		if (threadIdx.x < kS) {
-			double c1 = 0.0, c2 = 0.0;
-			for (unsigned b = 0; b < gridDim.x; ++b) {
-				c1 += __ldcg(part2 + (size_t)b * 2 * kS + threadIdx.x);
-				c2 += __ldcg(part2 + (size_t)b * 2 * kS + kS + threadIdx.x);
-			}
-			const double bn = sqrt(c1);
-			st->bnorm[threadIdx.x] = bn == 0.0 ? 1.0 : bn;
-			st->rnorm[threadIdx.x] = sqrt(c2);
-			st->res0[threadIdx.x] = sqrt(c2);
-			st->conv_iter[threadIdx.x] = 0;
-		}
-		if (threadIdx.x == 0) {
-			st->iter = 0;
-			st->done = 0;
-			st->status = FS_STATUS_UNKNOWN;
-			st->flags = 0;
-			*counter = 0;
-		}
-	}
-}
-
-struct BcgPlan {
-	BcgState *st = nullptr, *hst = nullptr;
-	double *work = nullptr;     // P, Q (N x S each)
-	double *part = nullptr;     // G partials (grid x 256) + norm partials
-	unsigned *counter = nullptr;
-	int64_t n = 0;
-};
-std::map<const Csr *, BcgPlan> g_bcg;
-
-}  // namespace
-}  // namespace fsg
-
-extern "C" FS_API int fs_block_cg_solve(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah,
-                                        const fs_precond *Pc, int nrhs, fs_vec bh, fs_vec xh,
-                                        fs_solve_info *infos) {
-	using namespace fsg;
-	Ctx *ctx = reinterpret_cast<Ctx *>(h);
-	Csr *A = reinterpret_cast<Csr *>(Ah);
-	Vec *B = reinterpret_cast<Vec *>(bh), *X = reinterpret_cast<Vec *>(xh);
-	if (!ok_ctx(ctx) || !ok_csr(A) || !ok_vec(B) || !ok_vec(X) || !s || !infos)
-		return FS_ERR_BAD_HANDLE;
-	if (nrhs != kS)
-		return set_err(ctx, FS_ERR_UNSUPPORTED, "fs_block_cg_solve: this build takes %d right-hand sides", kS);
-	const int64_t n = A->nrows;
-	if (A->nrows != A->ncols || B->n != n * kS || X->n != n * kS || B->dtype != FS_F64 ||
-	    X->dtype != FS_F64)
-		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_block_cg_solve: B and X hold N x %d FP64 row-major", kS);
-	const bool jac = Pc && Pc->kind == FS_PRECOND_JACOBI;
-	if (Pc && Pc->kind != FS_PRECOND_NONE && !jac)
-		return set_err(ctx, FS_ERR_UNSUPPORTED, "fs_block_cg_solve: identity or Jacobi preconditioner");
-	cudaSetDevice(ctx->device);
-	if (jac)
-		FS_TRY(ensure_dinv(A));
-	BcgPlan &p = g_bcg[A];
-	const int G = std::max(1, std::min(ctx->sms * 8, (int)((n + kTile - 1) / kTile)));
-	if (p.n != n) {
-		if (p.work) {
-			cudaFree(p.work);
-			cudaFree(p.part);
-			cudaFree(p.counter);
-			cudaFree(p.st);
-			cudaFreeHost(p.hst);
-		}
-		FS_CUDA_TRY(ctx, cudaMalloc(&p.work, sizeof(double) * 3 * (size_t)n * kS));
-		FS_CUDA_TRY(ctx, cudaMalloc(&p.part, sizeof(double) * (size_t)ctx->sms * 8 * (256 + 2 * kS)));
-		FS_CUDA_TRY(ctx, cudaMalloc(&p.counter, 64));
-		FS_CUDA_TRY(ctx, cudaMemset(p.counter, 0, 64));
-		FS_CUDA_TRY(ctx, fence_setup_copies());
-		FS_CUDA_TRY(ctx, cudaMalloc(&p.st, sizeof(BcgState)));
-		FS_CUDA_TRY(ctx, cudaMallocHost(&p.hst, sizeof(BcgState)));
-		p.n = n;
-	}
-	double *Pm = p.work, *Qm = p.work + (size_t)n * kS;
-	double *part = p.part, *part2 = p.part + (size_t)ctx->sms * 8 * 256;
-	const double *dinv = jac ? A->dinv : nullptr;
-	const double *b = (const double *)B->d;
-	double *x = (double *)X->d;
-	double *R = p.work + 2 * (size_t)n * kS;
-	k_bcg_start<<<G, 256, 0, ctx->stream>>>((int)n, A->rowptr, A->col, A->val, b, x, R, Pm, dinv,
-	                                        s->base.use_zero_guess ? 1 : 0, p.st, part, part2, p.counter);
-	int st = check_launch(ctx, "block cg start");
-	const double tolf = (double)s->base.rtol;
-	const int maxiter = s->base.maxiter;
-	const int k = s->k_readback > 0 ? s->k_readback : 16;
-	int it = 0;
-	while (st == FS_OK) {
-		for (int j = 0; j < k && st == FS_OK; ++j) {
-			k_bcg_spmm<<<G, 256, 0, ctx->stream>>>((int)n, A->rowptr, A->col, A->val, Pm, Qm, p.st,
-			                                       part, p.counter);
-			st = check_launch(ctx, "block cg spmm");
-			k_bcg_update<<<G, 256, 0, ctx->stream>>>((int)n, x, Pm, R, Qm, dinv, p.st, part, part2,
-			                                         p.counter, tolf, maxiter);
-			if (st == FS_OK)
-				st = check_launch(ctx, "block cg update");
-			k_bcg_dir<<<G, 256, 0, ctx->stream>>>((int)n, Pm, R, dinv, p.st);
-			if (st == FS_OK)
-				st = check_launch(ctx, "block cg direction");
-		}
-		it += k;
-		if (st != FS_OK)
-			break;
-		if (cudaMemcpyAsync(p.hst, p.st, sizeof(BcgState), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
-		    cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
-			st = set_err(ctx, FS_ERR_CUDA, "block cg: state read-back failed");
-			break;
-		}
-		if (p.hst->done || p.hst->iter >= maxiter)
-			break;
-	}
-	if (st != FS_OK)
-		return st;
-	const BcgState &hs = *p.hst;
-	for (int j = 0; j < kS; ++j) {
-		fs_solve_info &inf = infos[j];
-		memset(&inf, 0, sizeof inf);
-		inf.status = hs.conv_iter[j] ? FS_CONVERGED_RTOL
-		                             : (hs.status == FS_DIVERGED_BREAKDOWN ? FS_DIVERGED_BREAKDOWN
-		                                                                   : FS_DIVERGED_ITERS);
-		inf.iters = hs.conv_iter[j];
-		inf.restarts = hs.iter;  // block iterations run
-		inf.res_norm_initial = (float)hs.res0[j];
-		inf.res_norm_final = (float)hs.rnorm[j];
-		inf.rhs_norm = (float)hs.bnorm[j];
-	}
 	return FS_OK;
 }

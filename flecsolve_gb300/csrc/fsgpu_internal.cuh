@@ -53,6 +53,8 @@ struct Vec {
 // nonzeros unless it is a single row longer than kBlkNnz ("long row").
 constexpr int kBlkRows = 256;
 constexpr int kBlkNnz = 1792;
+// column-offset coding: at most kOffTab distinct offsets c - r per row block
+constexpr int kOffTab = 16;
 
 struct Csr {
 	int magic = kMagicCsr;
@@ -66,6 +68,12 @@ struct Csr {
 	int *blk = nullptr;        // row blocks, nblk + 1
 	int4 *blkinfo = nullptr;   // per block {r0, r1, rowptr[r0], rowptr[r1]}
 	int nblk = 0;
+	// column-offset coding (null when some row block has more than kOffTab
+	// distinct offsets c - r): 4-bit code per nonzero, two per byte, and
+	// kOffTab offsets per row block
+	unsigned char *code = nullptr;
+	int *tab = nullptr;
+	bool use_codes = true;
 	double *dinv = nullptr;    // 1 / a_ii, built on first use
 	float *dinv32 = nullptr;
 	bool dinv_valid = false;

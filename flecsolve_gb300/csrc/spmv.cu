@@ -41,6 +41,37 @@ static std::vector<int> row_blocks(const std::vector<int> &rp) {
 	return blk;
 }
 
+// Column-offset codes of a row-blocked pattern: per block the distinct
+// offsets c - r (at most kOffTab, in order of first use) and per nonzero the
+// 4-bit index of its offset, two per byte (even k in the low nibble).  False
+// when some block needs more offsets; the plain column ids are used then.
+static bool offset_codes(const std::vector<int> &rp, const std::vector<int> &ci,
+                         const std::vector<int> &blk, std::vector<unsigned char> &code,
+                         std::vector<int> &tab) {
+	const int64_t nnz = rp.back();
+	const size_t nb = blk.size() - 1;
+	code.assign((size_t)(nnz + 1) / 2 + 32, 0);
+	tab.assign(nb * kOffTab, 0);
+	for (size_t b = 0; b < nb; ++b) {
+		int *t = tab.data() + b * kOffTab;
+		int cnt = 0;
+		for (int r = blk[b]; r < blk[b + 1]; ++r)
+			for (int k = rp[r]; k < rp[r + 1]; ++k) {
+				const int d = ci[k] - r;
+				int j = 0;
+				while (j < cnt && t[j] != d)
+					++j;
+				if (j == cnt) {
+					if (cnt == kOffTab)
+						return false;
+					t[cnt++] = d;
+				}
+				code[(size_t)k >> 1] |= (unsigned char)(j << ((k & 1) * 4));
+			}
+	}
+	return true;
+}
+
 static std::vector<int4> block_info(const std::vector<int> &blk, const std::vector<int> &rp) {
 	std::vector<int4> info(blk.size() > 0 ? blk.size() - 1 : 0);
 	for (size_t b = 0; b + 1 < blk.size(); ++b)
@@ -313,7 +344,40 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 	                                  cudaMemcpyHostToDevice) != cudaSuccess) ||
 	    fence_setup_copies() != cudaSuccess)
 		return fail(FS_ERR_CUDA);
+	std::vector<unsigned char> code;
+	std::vector<int> tab;
+	if (nnz > 0 && offset_codes(rp, ci, blk, code, tab)) {
+		if (cudaMalloc(&A->code, code.size()) != cudaSuccess ||
+		    cudaMalloc(&A->tab, tab.size() * sizeof(int)) != cudaSuccess ||
+		    cudaMemcpy(A->code, code.data(), code.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+		    cudaMemcpy(A->tab, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice) !=
+		        cudaSuccess ||
+		    fence_setup_copies() != cudaSuccess) {
+			cudaFree(A->code);
+			cudaFree(A->tab);
+			return fail(FS_ERR_OUT_OF_MEMORY);
+		}
+	}
 	*out = reinterpret_cast<fs_csr>(A);
+	return FS_OK;
+}
+
+FS_API int fs_csr_index_coding(fs_csr h, int enable, int *active) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	if (!ok_csr(A))
+		return FS_ERR_BAD_HANDLE;
+	if (enable >= 0)
+		A->use_codes = enable != 0;
+	if (active)
+		*active = A->code && A->use_codes ? 1 : 0;
+	return FS_OK;
+}
+
+FS_API int fs_csr_row_blocks(fs_csr h, int64_t *nblk) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	if (!ok_csr(A) || !nblk)
+		return FS_ERR_BAD_HANDLE;
+	*nblk = A->nblk;
 	return FS_OK;
 }
 
@@ -324,6 +388,7 @@ FS_API int fs_csr_destroy(fs_csr h) {
 	cudaStreamSynchronize(A->ctx->stream);
 	for (void *p : {(void *)A->rowptr, (void *)A->col, (void *)A->val, (void *)A->val32,
 	                (void *)A->blk, (void *)A->blkinfo, (void *)A->dinv, (void *)A->dinv32,
+	                (void *)A->code, (void *)A->tab,
 	                (void *)A->t_colptr, (void *)A->t_row, (void *)A->t_perm, (void *)A->t_val,
 	                (void *)A->t_blk, (void *)A->t_blkinfo})
 		if (p)

@@ -151,6 +151,17 @@ FS_API int fs_csr_update_values(fs_csr A, const double *val);
 /* overwrite the values from device memory (float64, nnz entries) */
 FS_API int fs_csr_update_values_device(fs_csr A, const double *dval);
 FS_API int fs_csr_values_device_ptr(fs_csr A, double **dval);
+/* Index coding (no counterpart in the reference; a storage choice of this
+ * library).  When every block of up to 256 rows uses at most 16 distinct
+ * column offsets c - r (stencil patterns), fs_csr_create also stores a 4-bit
+ * offset code per nonzero and the SpMV reads those instead of the 32-bit
+ * column ids; the results are identical.  enable: 1 use the codes when
+ * present (the default), 0 read the column ids, -1 leave unchanged;
+ * *active (may be NULL) = 1 when the coded SpMV is in use. */
+FS_API int fs_csr_index_coding(fs_csr A, int enable, int *active);
+/* number of SpMV row blocks (at most 256 rows and 1792 nonzeros each, a
+ * longer row alone); no counterpart in the reference */
+FS_API int fs_csr_row_blocks(fs_csr A, int64_t *nblk);
 
 /* SpMV modes */
 enum fs_spmv_mode {
@@ -312,13 +323,24 @@ FS_API int fs_batch_tuning(fs_ctx ctx, fs_csr A, int nsys, const int64_t *sys_of
                            int *cluster_size, int *threads);
 
 /* Block Jacobi-PCG for nrhs = 16 right-hand sides of one operator (FP64).
- * B and X hold N x 16 values row-major (the 16 values of row r contiguous).
- * P: NULL/FS_PRECOND_NONE or FS_PRECOND_JACOBI.  Column j converges when
- * ||R_j|| < rtol ||B_j||; infos[j].iters is the block iteration at which it
- * did, infos[j].restarts the block iterations run. */
+ * No counterpart in the reference (its CG, cg.hh:43-139, takes one
+ * right-hand side per call).  B and X hold N x 16 values row-major (the 16
+ * values of row r contiguous).  P: NULL/FS_PRECOND_NONE or
+ * FS_PRECOND_JACOBI.  Column j converges when ||R_j|| < rtol ||B_j||;
+ * infos[j].iters is the block iteration at which it did, infos[j].restarts
+ * the block iterations run. */
 FS_API int fs_block_cg_solve(fs_ctx ctx, const fs_krylov_settings *s, fs_csr A,
                              const fs_precond *P, int nrhs, fs_vec B, fs_vec X,
                              fs_solve_info *infos);
+/* The same with FP32 block recurrences (FP32 matrix values and vectors,
+ * compensated FP32 Gram sums) and FP64 residual replacement: the FP64 X is
+ * updated and R replaced by B - A X in FP64 whenever every unconverged
+ * column's residual has dropped by s->inner_rtol (0 = 0.1) since the last
+ * replacement, or a column may have converged; columns converge on the FP64
+ * residual only.  B and X are FP64 as above. */
+FS_API int fs_block_cg_solve_mixed(fs_ctx ctx, const fs_krylov_settings *s, fs_csr A,
+                                   const fs_precond *P, int nrhs, fs_vec B, fs_vec X,
+                                   fs_solve_info *infos);
 
 /* ------------------------------------------ allocation-free reduction --- */
 /* No counterpart in the reference.  Dot product sum_i x[i] * y[i] of two

@@ -70,3 +70,56 @@ def test_block_cg_16_rhs(ctx):
         assert inf.iters <= single.iters + 2, (j, inf.iters, single.iters)
         xs = lu.solve(B[:, j])
         assert np.linalg.norm(X[:, j] - xs) / np.linalg.norm(xs) <= 1e-6
+
+
+@pytest.mark.parametrize("wl,jacobi", [("laplace3d-24", True), ("diffusion3d-20", True),
+                                       ("poisson2d-40", False)])
+def test_block_cg_16_rhs_mixed(ctx, wl, jacobi):
+    """FP32 block recurrences with FP64 residual replacement: every column
+    converges on its own FP64 residual (checked here on the host) and a
+    tighter rtol gives the direct solution to the forward-error bound.  On
+    the 3-D operators the block iteration count is the FP64 one; on the small
+    2-D system the 16-column block Krylov space reaches half the dimension
+    (49 FP64 block iterations x 16 columns of 1600 unknowns), where FP64 block
+    CG gains from near-finite termination that FP32 recurrences lose (60)."""
+    import scipy.sparse.linalg as spla
+    A, _ = P.workload(wl)
+    n = A.nrows
+    B = np.stack([P.uniform(60 + j, n) for j in range(16)], axis=1)
+    dA = fs.CSR(ctx, A)
+    S = A.to_scipy()
+    vB = fs.Vector(ctx, B.ravel())
+    vX64, vXm = fs.Vector(ctx, n * 16), fs.Vector(ctx, n * 16)
+    i64 = fs.block_cg(dA, vB, vX64, 16, maxiter=4000, rtol=1e-8, jacobi=jacobi)
+    imx = fs.block_cg(dA, vB, vXm, 16, maxiter=4000, rtol=1e-8, jacobi=jacobi, mixed=True)
+    X = vXm.numpy().reshape(n, 16)
+
+    def slack(it):
+        return 3 if wl.startswith(("laplace3d", "diffusion3d")) else 0.25 * it + 3
+
+    for j, inf in enumerate(imx):
+        assert inf.status == "converged_rtol", (j, inf)
+        rr = np.linalg.norm(B[:, j] - S @ X[:, j]) / np.linalg.norm(B[:, j])
+        assert rr < 1e-8, (j, rr)
+        assert inf.iters <= i64[j].iters + slack(i64[j].iters), (j, inf.iters, i64[j].iters)
+    assert imx[0].restarts <= i64[0].restarts + slack(i64[0].restarts)
+    imx2 = fs.block_cg(dA, vB, vXm, 16, maxiter=4000, rtol=1e-12, jacobi=jacobi, mixed=True)
+    assert all(i.status == "converged_rtol" for i in imx2)
+    X = vXm.numpy().reshape(n, 16)
+    lu = spla.splu(S.tocsc())
+    for j in range(16):
+        xs = lu.solve(B[:, j])
+        assert np.linalg.norm(X[:, j] - xs) / np.linalg.norm(xs) <= 1e-8
+
+
+def test_block_cg_rejects_bad_arguments(ctx):
+    A, _ = P.workload("poisson2d-10")
+    dA = fs.CSR(ctx, A)
+    vB, vX = fs.Vector(ctx, A.nrows * 16), fs.Vector(ctx, A.nrows * 8)
+    for mixed in (False, True):
+        with pytest.raises(fs.api._lib.FsError) as ei:
+            fs.block_cg(dA, vB, vX, 16, maxiter=10, rtol=1e-8, mixed=mixed)
+        assert ei.value.status == fs.api._lib.ERR_SIZE_MISMATCH
+        with pytest.raises(fs.api._lib.FsError) as ei:
+            fs.block_cg(dA, vB, vB, 8, maxiter=10, rtol=1e-8, mixed=mixed)
+        assert ei.value.status == fs.api._lib.ERR_UNSUPPORTED

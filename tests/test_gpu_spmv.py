@@ -31,6 +31,39 @@ def test_spmv_exact_mode_is_bit_exact(ctx, wl):
     assert (np.abs(y - O.spmv(A, x)) <= _bound(A, x)).all()
 
 
+@pytest.mark.parametrize("wl", ["poisson2d-128", "diffusion3d-24", "convdiff3d-20"])
+def test_offset_coded_spmv_matches_column_ids(ctx, wl):
+    """Stencil patterns get 4-bit column-offset codes; the coded SpMV gives
+    the same bits as the one reading column ids, in every mode and type."""
+    A, _ = P.workload(wl)
+    x = P.uniform(43, A.ncols)
+    dA = fs.CSR(ctx, A)
+    assert dA.index_coding()
+    out = {}
+    for coded in (True, False):
+        assert dA.index_coding(coded) == coded
+        for dt in ("f64", "f32"):
+            vx, vy = fs.Vector(ctx, x.astype(np.float32) if dt == "f32" else x, dt), fs.Vector(ctx, A.nrows, dt)
+            for exact in (True, False):
+                dA.apply(vx, vy, exact=exact)
+                out[coded, dt, exact] = vy.numpy()
+            r = fs.Vector(ctx, A.nrows)
+        b = fs.Vector(ctx, P.uniform(44, A.nrows))
+        r = fs.Vector(ctx, A.nrows)
+        dA.residual(b, fs.Vector(ctx, x), r)
+        out[coded, "res"] = r.numpy()
+    for key in [k for k in out if k[0]]:
+        assert np.array_equal(out[key], out[(False,) + key[1:]]), key
+    assert np.array_equal(out[True, "f64", True], O.spmv(A, x))
+
+
+def test_offset_coding_falls_back_on_irregular_patterns(ctx):
+    A = _ragged(3000, 7000, 5)
+    dA = fs.CSR(ctx, A)
+    assert not dA.index_coding()
+    assert not dA.index_coding(True)
+
+
 def _ragged(n, m, seed, long_rows=()):
     rng = np.random.default_rng(seed)
     lens = rng.integers(0, 12, n)
