@@ -113,10 +113,11 @@ class ClockSampler:
 
 
 def spmv_bytes(nrows, nnz, val_bytes, coded=False, nblk=0):
-    """Algorithmic bytes of one CSR SpMV: values + int32 columns (or 4-bit
-    column-offset codes and a 16-entry int32 offset table per row block),
-    int32 row offsets, x read once, y written once."""
-    idx = (nnz + 1) // 2 + 64 * nblk if coded else 4 * nnz
+    """Algorithmic bytes of one CSR SpMV: values + int32 columns (or, with
+    row patterns, one pattern-id byte per row; the <= 8 KB pattern table is
+    read once per CTA out of L2 and not counted), int32 row offsets, x read
+    once, y written once."""
+    idx = nrows if coded else 4 * nnz
     return nnz * val_bytes + idx + 4 * (nrows + 1) + 2 * nrows * val_bytes
 
 
@@ -513,7 +514,7 @@ def run_ours(args, ws, rank, local):
         "spmv_hbm_gbs": {"f64": gbs64, "f32": gbs32, "f64_ms": spmv64_ms, "f32_ms": spmv32_ms},
         "roofline": {"bound": "hbm",
                      "kernel": "spmv_rb_kernel<float> (FP32 CSR SpMV, "
-                               + ("4-bit column-offset codes)" if coded else "int32 column ids)"),
+                               + ("row-pattern ids)" if coded else "int32 column ids)"),
                      "achieved": gbs32, "peak": peak, "unit": "GB/s", "frac": gbs32 / peak,
                      "peak_source": f"hbm_gbs of {peak_kind}",
                      "algorithmic_bytes_per_launch": b32,

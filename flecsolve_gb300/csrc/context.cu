@@ -25,6 +25,20 @@ int set_err(Ctx *ctx, int status, const char *fmt, ...) {
 	return status;
 }
 
+int check_device_error(Ctx *ctx) {
+	unsigned *h = reinterpret_cast<unsigned *>(ctx->host_out + 15);
+	FS_CUDA_TRY(ctx, cudaMemcpyAsync(h, ctx->dev_err, sizeof(unsigned), cudaMemcpyDeviceToHost,
+	                                 ctx->stream));
+	FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	if (*h) {
+		const unsigned e = *h;
+		*h = 0;
+		FS_CUDA_TRY(ctx, cudaMemsetAsync(ctx->dev_err, 0, sizeof(unsigned), ctx->stream));
+		return set_err(ctx, FS_ERR_CUDA, "a device-side wait ran out of its iteration limit (code %u)", e);
+	}
+	return FS_OK;
+}
+
 int check_launch(Ctx *ctx, const char *what) {
 	ctx->launches++;
 	cudaError_t e = cudaGetLastError();
@@ -319,10 +333,11 @@ FS_API int fs_ctx_create(int device, fs_ctx *out) {
 		return fail(FS_ERR_CUDA);
 	if (cudaMalloc(&c->red_part, sizeof(double) * kMaxRedBlocks * 4) != cudaSuccess ||
 	    cudaMalloc(&c->red_out, sizeof(double) * 8) != cudaSuccess ||
-	    cudaMalloc(&c->red_count, sizeof(unsigned) * 8) != cudaSuccess ||
-	    cudaMallocHost(&c->host_out, sizeof(double) * 8) != cudaSuccess)
+	    cudaMalloc(&c->red_count, sizeof(unsigned) * 16) != cudaSuccess ||
+	    cudaMallocHost(&c->host_out, sizeof(double) * 16) != cudaSuccess)
 		return fail(FS_ERR_OUT_OF_MEMORY);
-	if (cudaMemset(c->red_count, 0, sizeof(unsigned) * 8) != cudaSuccess ||
+	c->dev_err = c->red_count + 15;
+	if (cudaMemset(c->red_count, 0, sizeof(unsigned) * 16) != cudaSuccess ||
 	    fence_setup_copies() != cudaSuccess)
 		return fail(FS_ERR_CUDA);
 	*out = reinterpret_cast<fs_ctx>(c);
@@ -353,7 +368,7 @@ FS_API int fs_ctx_sync(fs_ctx h) {
 	if (!ok_ctx(c))
 		return FS_ERR_BAD_HANDLE;
 	FS_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-	return FS_OK;
+	return check_device_error(c);
 }
 
 FS_API int fs_ctx_stream(fs_ctx h, void **stream) {

@@ -36,7 +36,12 @@ struct Ctx {
 	unsigned *red_count = nullptr;  // completion counters (device)
 	double *host_out = nullptr;     // pinned
 	cudaEvent_t ev[16] = {};        // timing events (fs_ctx_event_*)
+	// device error word (bounded waits that ran out); inside red_count
+	unsigned *dev_err = nullptr;
 };
+
+// reads and clears the device error word (synchronises the stream)
+int check_device_error(Ctx *ctx);
 
 struct Vec {
 	int magic = kMagicVec;
@@ -53,8 +58,10 @@ struct Vec {
 // nonzeros unless it is a single row longer than kBlkNnz ("long row").
 constexpr int kBlkRows = 256;
 constexpr int kBlkNnz = 1792;
-// column-offset coding: at most kOffTab distinct offsets c - r per row block
-constexpr int kOffTab = 16;
+// row patterns: rows of at most kPatW nonzeros, at most kMaxPat distinct
+// sequences of column offsets c - r per matrix
+constexpr int kPatW = 8;
+constexpr int kMaxPat = 256;
 
 struct Csr {
 	int magic = kMagicCsr;
@@ -68,11 +75,12 @@ struct Csr {
 	int *blk = nullptr;        // row blocks, nblk + 1
 	int4 *blkinfo = nullptr;   // per block {r0, r1, rowptr[r0], rowptr[r1]}
 	int nblk = 0;
-	// column-offset coding (null when some row block has more than kOffTab
-	// distinct offsets c - r): 4-bit code per nonzero, two per byte, and
-	// kOffTab offsets per row block
-	unsigned char *code = nullptr;
-	int *tab = nullptr;
+	// row patterns (null when some row is longer than kPatW or the matrix
+	// has more than kMaxPat offset sequences): pattern id per row, kPatW
+	// offsets c - r per pattern
+	unsigned char *pid = nullptr;
+	int *ptab = nullptr;
+	int npat = 0;
 	bool use_codes = true;
 	double *dinv = nullptr;    // 1 / a_ii, built on first use
 	float *dinv32 = nullptr;

@@ -798,8 +798,7 @@ int solver_hist(Solver *s, int cap) {
 int read_state(Solver *s) {
 	FS_CUDA_TRY(s->ctx, cudaMemcpyAsync(s->hst, s->st, sizeof(KState), cudaMemcpyDeviceToHost,
 	                                    s->ctx->stream));
-	FS_CUDA_TRY(s->ctx, cudaStreamSynchronize(s->ctx->stream));
-	return FS_OK;
+	return check_device_error(s->ctx);  // synchronises the stream
 }
 
 // Capture `body` (k iterations) once per key, then replay it.

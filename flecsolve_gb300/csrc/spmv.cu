@@ -6,7 +6,9 @@
 // test operator (flecsolve/util/test/mesh.hh:123-140) and mat::parcsr
 // (matrices/parcsr.hh:60-91, topo/csr.hh:413-632).
 #include <algorithm>
+#include <array>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "spmv_kernel.cuh"
@@ -41,34 +43,47 @@ static std::vector<int> row_blocks(const std::vector<int> &rp) {
 	return blk;
 }
 
-// Column-offset codes of a row-blocked pattern: per block the distinct
-// offsets c - r (at most kOffTab, in order of first use) and per nonzero the
-// 4-bit index of its offset, two per byte (even k in the low nibble).  False
-// when some block needs more offsets; the plain column ids are used then.
-static bool offset_codes(const std::vector<int> &rp, const std::vector<int> &ci,
-                         const std::vector<int> &blk, std::vector<unsigned char> &code,
-                         std::vector<int> &tab) {
-	const int64_t nnz = rp.back();
-	const size_t nb = blk.size() - 1;
-	code.assign((size_t)(nnz + 1) / 2 + 32, 0);
-	tab.assign(nb * kOffTab, 0);
-	for (size_t b = 0; b < nb; ++b) {
-		int *t = tab.data() + b * kOffTab;
-		int cnt = 0;
-		for (int r = blk[b]; r < blk[b + 1]; ++r)
-			for (int k = rp[r]; k < rp[r + 1]; ++k) {
-				const int d = ci[k] - r;
-				int j = 0;
-				while (j < cnt && t[j] != d)
-					++j;
-				if (j == cnt) {
-					if (cnt == kOffTab)
-						return false;
-					t[cnt++] = d;
-				}
-				code[(size_t)k >> 1] |= (unsigned char)(j << ((k & 1) * 4));
+// Row patterns: the sequence of column offsets c - r of every row, numbered
+// in order of first appearance.  False when a row is longer than kPatW or
+// the matrix has more than kMaxPat distinct sequences; the column ids are
+// used then.  Consecutive rows usually share a sequence, which is checked
+// first.
+static bool row_patterns(const std::vector<int> &rp, const std::vector<int> &ci,
+                         std::vector<unsigned char> &pid, std::vector<int> &ptab, int &npat) {
+	const int64_t n = (int64_t)rp.size() - 1;
+	pid.assign((size_t)n + 32, 0);
+	ptab.clear();
+	std::map<std::array<int, kPatW + 1>, int> ids;
+	std::array<int, kPatW + 1> key{}, last{};
+	int last_id = -1;
+	for (int64_t r = 0; r < n; ++r) {
+		const int len = rp[r + 1] - rp[r];
+		if (len > kPatW)
+			return false;
+		key.fill(0);
+		key[kPatW] = len;
+		for (int j = 0; j < len; ++j)
+			key[j] = ci[rp[r] + j] - (int)r;
+		int id;
+		if (last_id >= 0 && key == last)
+			id = last_id;
+		else {
+			auto it = ids.find(key);
+			if (it == ids.end()) {
+				if ((int)ids.size() == kMaxPat)
+					return false;
+				id = (int)ids.size();
+				ids.emplace(key, id);
+				ptab.insert(ptab.end(), key.begin(), key.begin() + kPatW);
 			}
+			else
+				id = it->second;
+			last = key;
+			last_id = id;
+		}
+		pid[r] = (unsigned char)id;
 	}
+	npat = (int)ids.size();
 	return true;
 }
 
@@ -344,19 +359,21 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 	                                  cudaMemcpyHostToDevice) != cudaSuccess) ||
 	    fence_setup_copies() != cudaSuccess)
 		return fail(FS_ERR_CUDA);
-	std::vector<unsigned char> code;
-	std::vector<int> tab;
-	if (nnz > 0 && offset_codes(rp, ci, blk, code, tab)) {
-		if (cudaMalloc(&A->code, code.size()) != cudaSuccess ||
-		    cudaMalloc(&A->tab, tab.size() * sizeof(int)) != cudaSuccess ||
-		    cudaMemcpy(A->code, code.data(), code.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-		    cudaMemcpy(A->tab, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice) !=
+	std::vector<unsigned char> pid;
+	std::vector<int> ptab;
+	int npat = 0;
+	if (nnz > 0 && nrows > 0 && row_patterns(rp, ci, pid, ptab, npat)) {
+		if (cudaMalloc(&A->pid, pid.size()) != cudaSuccess ||
+		    cudaMalloc(&A->ptab, ptab.size() * sizeof(int)) != cudaSuccess ||
+		    cudaMemcpy(A->pid, pid.data(), pid.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+		    cudaMemcpy(A->ptab, ptab.data(), ptab.size() * sizeof(int), cudaMemcpyHostToDevice) !=
 		        cudaSuccess ||
 		    fence_setup_copies() != cudaSuccess) {
-			cudaFree(A->code);
-			cudaFree(A->tab);
+			cudaFree(A->pid);
+			cudaFree(A->ptab);
 			return fail(FS_ERR_OUT_OF_MEMORY);
 		}
+		A->npat = npat;
 	}
 	*out = reinterpret_cast<fs_csr>(A);
 	return FS_OK;
@@ -369,7 +386,7 @@ FS_API int fs_csr_index_coding(fs_csr h, int enable, int *active) {
 	if (enable >= 0)
 		A->use_codes = enable != 0;
 	if (active)
-		*active = A->code && A->use_codes ? 1 : 0;
+		*active = A->pid && A->use_codes ? 1 : 0;
 	return FS_OK;
 }
 
@@ -388,7 +405,7 @@ FS_API int fs_csr_destroy(fs_csr h) {
 	cudaStreamSynchronize(A->ctx->stream);
 	for (void *p : {(void *)A->rowptr, (void *)A->col, (void *)A->val, (void *)A->val32,
 	                (void *)A->blk, (void *)A->blkinfo, (void *)A->dinv, (void *)A->dinv32,
-	                (void *)A->code, (void *)A->tab,
+	                (void *)A->pid, (void *)A->ptab,
 	                (void *)A->t_colptr, (void *)A->t_row, (void *)A->t_perm, (void *)A->t_val,
 	                (void *)A->t_blk, (void *)A->t_blkinfo})
 		if (p)

@@ -8,19 +8,25 @@
 // stride, so every partial sum has a fixed owner and the reductions fused into
 // the epilogue are deterministic.
 //
-// Per block: the contiguous nonzero span [rowptr[r0], rowptr[r1]) and the
-// block's row offsets are copied into shared memory with 16-byte cp.async
-// copies of their aligned covers, then one thread per row accumulates its row
-// from shared memory with x gathered through the read-only path (x of a
-// 7-point stencil is re-used by neighbouring blocks out of L2).
+// Staging: one thread of the CTA copies a row block's contiguous nonzero
+// span, its indices and its row offsets into a ring of shared-memory stages
+// with bulk asynchronous copies (cp.async.bulk, completed on one mbarrier per
+// stage) while the CTA sums an earlier block; one thread per row then
+// accumulates its row out of shared memory, with x gathered through the
+// read-only path (x of a stencil operator is re-used by neighbouring blocks
+// out of L2).  Every wait on an mbarrier is bounded: past the limit the CTA
+// records an error in the context's device error word, waits (again bounded)
+// for the copies it issued, and finishes without summing further blocks.
 //
-// Column-offset coding: when every row block's nonzeros use at most kOffTab
-// distinct column offsets c - r (a stencil pattern: 7 for a 7-point
-// operator), the matrix also carries a per-block table of those offsets and a
-// 4-bit code per nonzero (two per byte), and the kernel reads the codes
-// instead of the 32-bit column ids: index traffic 0.5 instead of 4 bytes per
-// nonzero.  The columns, the products and their order are the same, so the
-// result is the same bit for bit.
+// Index formats:
+//  * column ids: 32-bit column id per nonzero;
+//  * row patterns: when every row has at most kPatW nonzeros and the matrix
+//    has at most kMaxPat distinct sequences of column offsets c - r (a
+//    stencil operator: 27 for a 7-point 3-D one), each row stores the 8-bit id
+//    of its sequence and the kernel keeps the sequences in shared memory:
+//    index traffic one byte per row instead of four per nonzero.  The columns,
+//    the products and their order are the same, so the result is the same bit
+//    for bit.
 //
 // EXACT mode rounds every product a_k * x[c_k] and adds the products left to
 // right per row, which is the reference's operation order bit for bit.
@@ -39,8 +45,10 @@ struct CsrDev {
 	const V *__restrict__ val;
 	const int4 *__restrict__ info;  // per row block {r0, r1, k0, k1}
 	int nblk;
-	const unsigned char *__restrict__ code;  // coded: 4-bit offset code per nonzero
-	const int *__restrict__ tab;             // coded: kOffTab offsets per row block
+	const unsigned char *__restrict__ pid;  // row patterns: pattern id per row
+	const int *__restrict__ ptab;           // row patterns: kPatW offsets per pattern
+	int npat;
+	unsigned *err;                          // device error word of the context
 };
 
 // Per-thread accumulators for fused reductions: plain FP64 fma for double
@@ -94,39 +102,70 @@ struct AccF {
 template<class V, int NV>
 using Acc = std::conditional_t<std::is_same_v<V, double>, AccD<NV>, AccF<NV>>;
 
-// One pipeline stage: the 16-byte aligned cover of a row block's values,
-// column ids (or offset codes and the block's offset table) and row offsets,
-// plus the block's bounds.
-template<class V, bool CODED>
+// One pipeline stage: the 16-byte aligned covers of a row block's values,
+// indices (column ids, or pattern ids) and row offsets, plus the block's
+// bounds.  Every array starts on a 16-byte boundary.
+template<class V, bool PAT>
 struct alignas(16) Stage {
 	V val[kBlkNnz + 16 / sizeof(V)];
-	int col[CODED ? 4 : kBlkNnz + 4];
-	unsigned char code[CODED ? kBlkNnz / 2 + 32 : 16];
-	int tab[kOffTab];
-	int rp[kBlkRows + 1 + 4];
+	int col[PAT ? 4 : kBlkNnz + 4];
+	unsigned char pid[PAT ? kBlkRows + 32 : 16];
+	int rp[kBlkRows + 1 + 7];
 	int r0, r1, k0, k1;
 };
 
-// pipeline depth: plain FP64 2 and FP32 3 (<= 48 KB per CTA); the smaller
-// coded stages allow one more
-template<class V, bool CODED>
-constexpr int kStages = (sizeof(V) == 8 ? 2 : 3) + (CODED ? 1 : 0);
+// pipeline depth: <= 48 KB of stages per CTA with column ids; pattern stages
+// are about half as large
+template<class V, bool PAT>
+constexpr int kStages = PAT ? (sizeof(V) == 8 ? 3 : 4) : (sizeof(V) == 8 ? 2 : 3);
 
-template<class V, bool CODED>
+template<class V, bool PAT>
 constexpr size_t spmv_smem_bytes() {
-	return sizeof(Stage<V, CODED>) * kStages<V, CODED>;
+	return sizeof(Stage<V, PAT>) * kStages<V, PAT> + (PAT ? sizeof(int) * kMaxPat * kPatW : 0);
 }
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-	const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+// ------------------------------------------------- mbarrier / bulk copy --
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+	return (unsigned)__cvta_generic_to_shared(p);
 }
-__device__ __forceinline__ void cp_async_commit() {
-	asm volatile("cp.async.commit_group;\n" ::: "memory");
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count)
+	             : "memory");
 }
-template<int N>
-__device__ __forceinline__ void cp_async_wait() {
-	asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+__device__ __forceinline__ void mbar_init_fence() {
+	asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)),
+	             "r"(bytes)
+	             : "memory");
+}
+// bounded wait for the phase with the given parity; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+	const unsigned a = smem_addr(bar);
+	for (int it = 0; it < (1 << 22); ++it) {
+		unsigned done;
+		asm volatile(
+			"{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+			" selp.u32 %0, 1, 0, p;\n}\n"
+			: "=r"(done)
+			: "r"(a), "r"(parity)
+			: "memory");
+		if (done)
+			return true;
+	}
+	return false;
+}
+// global -> shared bulk copy of `bytes` (a multiple of 16, both addresses
+// 16-byte aligned), completing on `bar`
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         unsigned long long *bar) {
+	asm volatile(
+		"cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+			smem_addr(dst)),
+		"l"(src), "r"(bytes), "r"(smem_addr(bar))
+		: "memory");
 }
 
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
@@ -144,48 +183,38 @@ __device__ __forceinline__ V xg(const V *__restrict__ x, const V *__restrict__ d
 		return __ldg(x + c);
 }
 
-// Issue the asynchronous copies of row block `b` (bounds m = {r0, r1, k0,
-// k1}) into stage `st`; every thread commits one group, possibly empty.  All
-// global reads stay inside the padded allocations: covers start at an aligned
-// index <= the first element and end < last element + 4 (codes: + 16 bytes).
-template<class V, bool CODED>
-__device__ __forceinline__ void stage_issue(const CsrDev<V> &A, int b, int4 m, Stage<V, CODED> &st,
-                                            bool valid) {
-	if (valid) {
-		constexpr int VW = 16 / sizeof(V);
-		const int r0 = m.x, r1 = m.y, k0 = m.z, k1 = m.w;
-		if (threadIdx.x == 0) {
-			st.r0 = r0;
-			st.r1 = r1;
-			st.k0 = k0;
-			st.k1 = k1;
-		}
-		if (k1 - k0 <= kBlkNnz) {
-			const int a0 = k0 & ~(VW - 1);
-			const int nv = (k1 - a0 + VW - 1) / VW;
-			for (int c = threadIdx.x; c < nv; c += blockDim.x)
-				cp_async16(st.val + c * VW, A.val + a0 + c * VW);
-			if constexpr (CODED) {
-				const int ab = (k0 >> 1) & ~15;
-				const int nb16 = (((k1 + 1) >> 1) - ab + 15) / 16;
-				for (int c = threadIdx.x; c < nb16; c += blockDim.x)
-					cp_async16(st.code + c * 16, A.code + ab + c * 16);
-				if (threadIdx.x < kOffTab / 4)
-					cp_async16(st.tab + threadIdx.x * 4, A.tab + (size_t)b * kOffTab + threadIdx.x * 4);
-			}
-			else {
-				const int c0 = k0 & ~3;
-				const int nc = (k1 - c0 + 3) / 4;
-				for (int c = threadIdx.x; c < nc; c += blockDim.x)
-					cp_async16(st.col + c * 4, A.col + c0 + c * 4);
-			}
-			const int p0 = r0 & ~3;
-			const int np = (r1 + 1 - p0 + 3) / 4;
-			for (int c = threadIdx.x; c < np; c += blockDim.x)
-				cp_async16(st.rp + c * 4, A.rowptr + p0 + c * 4);
-		}
+// Issue the bulk copies of a row block (bounds m = {r0, r1, k0, k1}) into
+// stage `st`; thread 0 only.  Each cover starts at an aligned index <= the
+// first element and ends within 16 bytes past the last, inside the padded
+// allocations.  A long row copies nothing (it is summed from global memory).
+template<class V, bool PAT>
+__device__ __forceinline__ void stage_issue(const CsrDev<V> &A, int4 m, Stage<V, PAT> &st,
+                                            unsigned long long *bar) {
+	constexpr int VW = 16 / sizeof(V);
+	const int r0 = m.x, r1 = m.y, k0 = m.z, k1 = m.w;
+	st.r0 = r0;
+	st.r1 = r1;
+	st.k0 = k0;
+	st.k1 = k1;
+	unsigned bv = 0, bc = 0, bp = 0, br = 0;
+	const int a0 = k0 & ~(VW - 1), c0 = k0 & ~3, q0 = r0 & ~15, p0 = r0 & ~3;
+	if (k1 - k0 <= kBlkNnz) {
+		bv = k1 > k0 ? (unsigned)(((k1 - a0 + VW - 1) / VW) * 16) : 0u;
+		if constexpr (PAT)
+			bp = (unsigned)(((r1 - q0 + 15) / 16) * 16);
+		else
+			bc = k1 > k0 ? (unsigned)(((k1 - c0 + 3) / 4) * 16) : 0u;
+		br = (unsigned)(((r1 + 1 - p0 + 3) / 4) * 16);
 	}
-	cp_async_commit();
+	mbar_arrive_expect_tx(bar, bv + bc + bp + br);
+	if (bv)
+		bulk_g2s(st.val, A.val + a0, bv, bar);
+	if (bc)
+		bulk_g2s(st.col, A.col + c0, bc, bar);
+	if (bp)
+		bulk_g2s(st.pid, A.pid + q0, bp, bar);
+	if (br)
+		bulk_g2s(st.rp, A.rowptr + p0, br, bar);
 }
 
 // bounds of the i-th row block of this CTA (a dummy past the end)
@@ -202,36 +231,60 @@ __device__ __forceinline__ int4 block_meta(const CsrDev<V> &A, int i, int nb) {
 //   double* part; unsigned* counter;                reduction scratch
 //
 // Persistent CTAs walk the row blocks b = blockIdx.x + i * gridDim.x through a
-// kStages-deep cp.async pipeline: the copies of block i + kStages - 1 are in
-// flight while block i is summed out of shared memory.
-template<class V, bool EXACT, bool SCALE, class Epi, bool CODED = false>
+// kStages-deep ring: the copies of block i + kStages - 1 are in flight while
+// block i is summed out of shared memory.
+template<class V, bool EXACT, bool SCALE, class Epi, bool PAT = false>
 __global__ void __launch_bounds__(kBlkRows)
 spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscale, Epi epi) {
 	constexpr int NV = Epi::NV;
-	constexpr int S = kStages<V, CODED>;
+	constexpr int S = kStages<V, PAT>;
 	constexpr int VW = 16 / sizeof(V);
+	using St = Stage<V, PAT>;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	using St = Stage<V, CODED>;
 	St *stages = reinterpret_cast<St *>(smem_raw);
+	int *ptab = reinterpret_cast<int *>(smem_raw + sizeof(St) * S);
 	__shared__ double red[128];
+	__shared__ unsigned long long bars[S];
+	__shared__ int abort_flag;
 	if (epi.skip())
 		return;
 	Acc<V, NV> acc;
 	acc.init();
 	const int tid = threadIdx.x;
 	const int nb = A.nblk > (int)blockIdx.x ? (A.nblk - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+	if (tid == 0) {
+		abort_flag = 0;
 #pragma unroll
-	for (int i = 0; i < S - 1; ++i)
-		stage_issue<V, CODED>(A, blockIdx.x + i * gridDim.x, block_meta(A, i, nb), stages[i], i < nb);
-	// bounds are loaded one iteration before their copies are issued, so the
+		for (int s = 0; s < S; ++s)
+			mbar_init(&bars[s], 1);
+		mbar_init_fence();
+	}
+	if constexpr (PAT)
+		for (int i = tid; i < A.npat * kPatW; i += blockDim.x)
+			ptab[i] = __ldg(A.ptab + i);
+	__syncthreads();
+	// bounds are loaded one block before their copies are issued, so the
 	// issue never waits on a global load
-	int4 mnext = block_meta(A, S - 1, nb);
-	for (int i = 0; i < nb; ++i) {
+	int4 mnext = make_int4(0, 0, 0, 0);
+	if (tid == 0) {
+#pragma unroll
+		for (int i = 0; i < S - 1; ++i)
+			if (i < nb)
+				stage_issue<V, PAT>(A, block_meta(A, i, nb), stages[i], &bars[i]);
+		mnext = block_meta(A, S - 1, nb);
+	}
+	int i = 0;
+	for (; i < nb; ++i) {
 		const int ni = i + S - 1;
-		stage_issue<V, CODED>(A, blockIdx.x + ni * gridDim.x, mnext, stages[ni % S], ni < nb);
-		mnext = block_meta(A, ni + 1, nb);
-		cp_async_wait<S - 1>();
+		if (tid == 0 && ni < nb) {
+			stage_issue<V, PAT>(A, mnext, stages[ni % S], &bars[ni % S]);
+			mnext = block_meta(A, ni + 1, nb);
+		}
+		if (!mbar_wait(&bars[i % S], (unsigned)((i / S) & 1)))
+			abort_flag = 1;
 		__syncthreads();
+		if (abort_flag)
+			break;
 		const St &st = stages[i % S];
 		const int r0 = st.r0, r1 = st.r1, k0 = st.k0, k1 = st.k1;
 		if (k1 - k0 > kBlkNnz) {
@@ -255,37 +308,51 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 		else {
 			const int r = r0 + tid;
 			if (r < r1) {
-				const int p0 = r0 & ~3, a0 = k0 & ~(VW - 1), c0 = k0 & ~3;
-				const int ab = (k0 >> 1) & ~15;
-				const int kb = st.rp[r - p0], ke = st.rp[r + 1 - p0];
+				const int p0 = r0 & ~3, a0 = k0 & ~(VW - 1);
+				const int kb = st.rp[r - p0];
 				V s = V(0);
-				// batches of 8: all gathers of a batch are issued before the
-				// first product, so a 7-point row costs one L2 round trip
-				for (int kc = kb; kc < ke; kc += 8) {
-					V a[8], xv[8];
+				if constexpr (PAT) {
+					// the row's offsets: kPatW entries of its pattern
+					const int q0 = r0 & ~15;
+					const int *po = ptab + (int)st.pid[r - q0] * kPatW;
+					const int len = st.rp[r + 1 - p0] - kb;
+					V a[kPatW], xv[kPatW];
 #pragma unroll
-					for (int j = 0; j < 8; ++j) {
-						if (kc + j < ke) {
-							const int k = kc + j;
-							a[j] = st.val[k - a0];
-							int c;
-							if constexpr (CODED) {
-								const unsigned byte = st.code[(k >> 1) - ab];
-								c = r + st.tab[(k & 1) ? (byte >> 4) : (byte & 15u)];
-							}
-							else
-								c = st.col[k - c0];
-							xv[j] = xg<V, SCALE>(x, dscale, c);
+					for (int j = 0; j < kPatW; ++j)
+						if (j < len) {
+							a[j] = st.val[kb + j - a0];
+							xv[j] = xg<V, SCALE>(x, dscale, r + po[j]);
 						}
-					}
 #pragma unroll
-					for (int j = 0; j < 8; ++j) {
-						if (kc + j < ke) {
+					for (int j = 0; j < kPatW; ++j)
+						if (j < len) {
 							if constexpr (EXACT)
 								s = add_rn(s, mul_rn(a[j], xv[j]));
 							else
 								s = fma(a[j], xv[j], s);
 						}
+				}
+				else {
+					const int c0 = k0 & ~3;
+					const int ke = st.rp[r + 1 - p0];
+					// batches of 8: all gathers of a batch are issued before
+					// the first product, so a 7-point row costs one L2 round trip
+					for (int kc = kb; kc < ke; kc += 8) {
+						V a[8], xv[8];
+#pragma unroll
+						for (int j = 0; j < 8; ++j)
+							if (kc + j < ke) {
+								a[j] = st.val[kc + j - a0];
+								xv[j] = xg<V, SCALE>(x, dscale, st.col[kc + j - c0]);
+							}
+#pragma unroll
+						for (int j = 0; j < 8; ++j)
+							if (kc + j < ke) {
+								if constexpr (EXACT)
+									s = add_rn(s, mul_rn(a[j], xv[j]));
+								else
+									s = fma(a[j], xv[j], s);
+							}
 					}
 				}
 				epi.row(r, s, acc);
@@ -293,7 +360,16 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 		}
 		__syncthreads();
 	}
-	cp_async_wait<0>();
+	if (i < nb) {
+		// a wait ran out: report it, and let the copies this CTA issued land
+		// before it exits (bounded as well)
+		if (tid == 0) {
+			atomicOr(A.err, 1u);
+			for (int j = i; j < nb && j < i + S; ++j)
+				mbar_wait(&bars[j % S], (unsigned)((j / S) & 1));
+		}
+		__syncthreads();
+	}
 	if constexpr (NV > 0) {
 		acc.to_part(epi.part, red);
 		if (last_block(epi.counter)) {
@@ -341,12 +417,12 @@ int spmv_grid(Ctx *ctx, int nblk, int per_sm);
 // `static`: every translation unit has its own copy of the kernel (no
 // relocatable device code), so the attribute and the occupancy are set up
 // per unit, in a per-unit cache
-template<class V, bool EXACT, bool SCALE, class Epi, bool CODED>
+template<class V, bool EXACT, bool SCALE, class Epi, bool PAT>
 static inline int launch_spmv_as(Ctx *ctx, const CsrDev<V> &d, const V *x, const V *dscale,
                                  const Epi &epi) {
 	static int per_sm = 0;  // resident CTAs per SM of this instantiation
-	constexpr size_t smem = spmv_smem_bytes<V, CODED>();
-	auto kern = spmv_rb_kernel<V, EXACT, SCALE, Epi, CODED>;
+	constexpr size_t smem = spmv_smem_bytes<V, PAT>();
+	auto kern = spmv_rb_kernel<V, EXACT, SCALE, Epi, PAT>;
 	if (per_sm == 0) {
 		if (smem > 48 * 1024 &&
 		    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -363,12 +439,13 @@ static inline int launch_spmv_as(Ctx *ctx, const CsrDev<V> &d, const V *x, const
 	return check_launch(ctx, "spmv");
 }
 
-// the offset-coded kernel when the matrix carries codes, else the plain one
+// the row-pattern kernel when the matrix carries patterns, else the one
+// reading column ids
 template<class V, bool EXACT, bool SCALE, class Epi>
 static inline int launch_spmv(Ctx *ctx, const Csr *A, const V *vals, const V *x,
-                       const V *dscale, const Epi &epi) {
-	CsrDev<V> d{A->rowptr, A->col, vals, A->blkinfo, A->nblk, A->code, A->tab};
-	if (A->code && A->use_codes)
+                              const V *dscale, const Epi &epi) {
+	CsrDev<V> d{A->rowptr, A->col, vals, A->blkinfo, A->nblk, A->pid, A->ptab, A->npat, ctx->dev_err};
+	if (A->pid && A->use_codes)
 		return launch_spmv_as<V, EXACT, SCALE, Epi, true>(ctx, d, x, dscale, epi);
 	return launch_spmv_as<V, EXACT, SCALE, Epi, false>(ctx, d, x, dscale, epi);
 }

@@ -152,12 +152,13 @@ FS_API int fs_csr_update_values(fs_csr A, const double *val);
 FS_API int fs_csr_update_values_device(fs_csr A, const double *dval);
 FS_API int fs_csr_values_device_ptr(fs_csr A, double **dval);
 /* Index coding (no counterpart in the reference; a storage choice of this
- * library).  When every block of up to 256 rows uses at most 16 distinct
- * column offsets c - r (stencil patterns), fs_csr_create also stores a 4-bit
- * offset code per nonzero and the SpMV reads those instead of the 32-bit
- * column ids; the results are identical.  enable: 1 use the codes when
- * present (the default), 0 read the column ids, -1 leave unchanged;
- * *active (may be NULL) = 1 when the coded SpMV is in use. */
+ * library).  When every row has at most 8 nonzeros and the matrix has at
+ * most 256 distinct sequences of column offsets c - r (stencil operators),
+ * fs_csr_create also stores one byte per row naming its sequence, and the
+ * SpMV reads those instead of the 32-bit column ids; the results are
+ * identical.  enable: 1 use the row patterns when present (the default), 0
+ * read the column ids, -1 leave unchanged; *active (may be NULL) = 1 when
+ * the pattern SpMV is in use. */
 FS_API int fs_csr_index_coding(fs_csr A, int enable, int *active);
 /* number of SpMV row blocks (at most 256 rows and 1792 nonzeros each, a
  * longer row alone); no counterpart in the reference */
