@@ -112,19 +112,31 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def spmv_bytes(nrows, nnz, val_bytes, coded=False, nblk=0):
-    """Algorithmic bytes of one CSR SpMV: values + int32 columns (or, with
-    row patterns, one pattern-id byte per row; the <= 8 KB pattern table is
-    read once per CTA out of L2 and not counted), int32 row offsets, x read
-    once, y written once."""
-    idx = nrows if coded else 4 * nnz
-    return nnz * val_bytes + idx + 4 * (nrows + 1) + 2 * nrows * val_bytes
+CODING_NAMES = {0: "colids", 1: "patterns"}
 
 
-def pcg_iter_bytes(nrows, nnz, val_bytes):
-    """Algorithmic bytes of one fused Jacobi-PCG iteration: SpMV + update
-    (read x, p, r, w, D^-1; write x, r) + direction (read p, r, D^-1; write p)."""
-    return spmv_bytes(nrows, nnz, val_bytes) + 11 * nrows * val_bytes
+def spmv_bytes(nrows, nnz, val_bytes, coding=0, nblk=0):
+    """Algorithmic bytes of one CSR SpMV: values, the index data of the
+    format, x read once, y written once.  Column ids (coding 0): int32 column
+    per nonzero + int32 row offsets.  Row patterns (1): one pattern-id byte
+    per row + 16 bytes of warp offsets per 256-row block (no row offsets).
+    The <= 8 KB pattern table is read once per CTA out of L2 and not
+    counted."""
+    if coding == 0:
+        idx = 4 * nnz + 4 * (nrows + 1)
+    else:
+        idx = nrows + 16 * nblk
+    return nnz * val_bytes + idx + 2 * nrows * val_bytes
+
+
+def pcg_iter_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, fused=False):
+    """Algorithmic bytes of one Jacobi-PCG iteration.  Three kernels: SpMV +
+    update (read x, p, r, w, D^-1; write x, r) + direction (read p, r, D^-1;
+    write p) = B_spmv + 11 N s_v.  Two kernels (row patterns, fused): SpMV
+    with the direction and solution updates (the SpMV's bytes + read z and x,
+    write p, x) + residual update (read r, w, D^-1; write r, z) = B_spmv +
+    9 N s_v."""
+    return spmv_bytes(nrows, nnz, val_bytes, coding, nblk) + (9 if fused else 11) * nrows * val_bytes
 
 
 def _traffic_from_profiles(kernel_key):
@@ -194,19 +206,20 @@ def run_spmv_only(args):
     ctx = fs.Context(0)
     dA = fs.CSR(ctx, A)
     peak, peak_kind = _peaks()
-    coded = dA.index_coding()
+    best = dA.index_coding()
     out = {"mode": "spmv", "workload": args.workload, "rows": n, "nnz": nnz,
-           "index_coding": coded}
-    for use in ([True, False] if coded else [False]):
-        dA.index_coding(use)
+           "index_coding": CODING_NAMES[best]}
+    for coding in ([1, 0] if best == 1 else [0]):
+        if dA.index_coding(coding) != coding:
+            continue
         for dt, vb in (("f64", 8), ("f32", 4)):
             ms = spmv_events_ms(fs, ctx, dA, n, dt, reps=max(1, args.steps))
-            nbytes = spmv_bytes(n, nnz, vb, coded=use, nblk=dA.nblk())
+            nbytes = spmv_bytes(n, nnz, vb, coding, dA.nblk())
             gbs = nbytes / (ms * 1e-3) / 1e9
-            out[dt + ("_coded" if use else "_colids")] = {
+            out[dt + "_" + CODING_NAMES[coding]] = {
                 "ms": ms, "gbs": gbs, "frac": gbs / peak, "peak": peak,
                 "peak_source": f"hbm_gbs of {peak_kind}", "algorithmic_bytes": nbytes}
-    dA.index_coding(True)
+    dA.index_coding(best)
     return out
 
 
@@ -452,11 +465,15 @@ def run_ours(args, ws, rank, local):
     spmv64_ms = spmv_events_ms(fs, ctx, dA, n, "f64")
     spmv32_ms = spmv_events_ms(fs, ctx, dA, n, "f32")
     peak, peak_kind = _peaks()
-    coded = dA.index_coding()
-    b64 = spmv_bytes(n, nnz, 8, coded=coded, nblk=dA.nblk())
-    b32 = spmv_bytes(n, nnz, 4, coded=coded, nblk=dA.nblk())
+    coding = dA.index_coding()
+    cname = CODING_NAMES[coding]
+    b64 = spmv_bytes(n, nnz, 8, coding, dA.nblk())
+    b32 = spmv_bytes(n, nnz, 4, coding, dA.nblk())
     gbs64 = b64 / (spmv64_ms * 1e-3) / 1e9
     gbs32 = b32 / (spmv32_ms * 1e-3) / 1e9
+    # whole mixed iteration: two kernels when the SpMV stages windows
+    it_bytes = pcg_iter_bytes(n, nnz, 4, coding, dA.nblk(), fused=coding == 1)
+    it_s = ms_mx * 1e-3 / max(1, info_mx.iters)
 
     # e2e: through the public API with host buffers
     import torch
@@ -513,15 +530,19 @@ def run_ours(args, ws, rank, local):
         "speedup_mixed_vs_fp64": ms_64 / ms_mx,
         "spmv_hbm_gbs": {"f64": gbs64, "f32": gbs32, "f64_ms": spmv64_ms, "f32_ms": spmv32_ms},
         "roofline": {"bound": "hbm",
-                     "kernel": "spmv_rb_kernel<float> (FP32 CSR SpMV, "
-                               + ("row-pattern ids)" if coded else "int32 column ids)"),
+                     "kernel": {1: "spmv_pat_kernel<float> (FP32 CSR SpMV, row patterns, warp-specialised)",
+                                0: "spmv_rb_kernel<float> (FP32 CSR SpMV, int32 column ids)"}[coding],
                      "achieved": gbs32, "peak": peak, "unit": "GB/s", "frac": gbs32 / peak,
                      "peak_source": f"hbm_gbs of {peak_kind}",
                      "algorithmic_bytes_per_launch": b32,
-                     "traffic": _traffic_from_profiles("spmv_f32" + ("_coded" if coded else ""))},
+                     "traffic": _traffic_from_profiles(f"spmv_f32_{cname}")},
         "roofline_fp64_spmv": {"achieved": gbs64, "peak": peak, "frac": gbs64 / peak,
                                "algorithmic_bytes_per_launch": b64,
-                               "traffic": _traffic_from_profiles("spmv_f64" + ("_coded" if coded else ""))},
+                               "traffic": _traffic_from_profiles(f"spmv_f64_{cname}")},
+        "roofline_mixed_iteration": {"bytes_per_iteration": it_bytes, "s_per_iteration": it_s,
+                                     "achieved": it_bytes / it_s / 1e9, "peak": peak,
+                                     "frac": it_bytes / it_s / 1e9 / peak,
+                                     "kernels_per_iteration": 2 if coding == 1 else 3},
         "e2e": {"value": e2e_ms * 1e-3, "unit": "s", "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 8 * n},
         "gpu_launches": launches_mx,

@@ -322,13 +322,25 @@ class CSR:
         check(lib().fs_csr_row_blocks(self.h, C.byref(n)), self.ctx.h)
         return n.value
 
-    def index_coding(self, enable=None) -> bool:
-        """Whether the SpMV reads 4-bit column-offset codes (stencil
-        patterns) instead of column ids; `enable` switches it (True/False)."""
+    CODINGS = {"colids": 0, "patterns": 1}
+
+    def index_coding(self, enable=None) -> int:
+        """The index format the SpMV uses: 0 = column ids, 1 = row patterns
+        (stencil operators: one pattern id per row, no column ids or row
+        offsets read).  `enable` switches it: True = row patterns when the
+        matrix has them, False = column ids, or a mode number / name; a
+        matrix without patterns always uses column ids."""
+        if enable is None:
+            req = -1
+        elif isinstance(enable, bool):
+            req = 1 if enable else 0
+        elif isinstance(enable, str):
+            req = self.CODINGS[enable]
+        else:
+            req = int(enable)
         a = C.c_int()
-        check(lib().fs_csr_index_coding(self.h, -1 if enable is None else int(bool(enable)),
-                                        C.byref(a)), self.ctx.h)
-        return bool(a.value)
+        check(lib().fs_csr_index_coding(self.h, req, C.byref(a)), self.ctx.h)
+        return a.value
 
     def values(self) -> np.ndarray:
         """The current values (row order) copied to the host."""

@@ -63,6 +63,10 @@ constexpr int kBlkNnz = 1792;
 constexpr int kPatW = 8;
 constexpr int kMaxPat = 256;
 
+// index formats of the SpMV (fs_csr_index_coding)
+constexpr int kCodingColIds = 0;
+constexpr int kCodingPatterns = 1;
+
 struct Csr {
 	int magic = kMagicCsr;
 	Ctx *ctx = nullptr;
@@ -81,7 +85,9 @@ struct Csr {
 	unsigned char *pid = nullptr;
 	int *ptab = nullptr;
 	int npat = 0;
-	bool use_codes = true;
+	unsigned char *plen = nullptr;  // nonzeros per pattern
+	short *pwb = nullptr;           // per row block, per 32-row warp: first nonzero - k0
+	int coding = kCodingPatterns;   // requested format; column ids when absent
 	double *dinv = nullptr;    // 1 / a_ii, built on first use
 	float *dinv32 = nullptr;
 	bool dinv_valid = false;
@@ -97,6 +103,12 @@ struct Csr {
 	bool t_vals_valid = false;
 	std::vector<int> h_rowptr; // host copy of offsets (parcsr splitting)
 };
+
+// index format an SpMV on A uses (the requested one, or the next one the
+// matrix supports)
+inline int active_coding(const Csr *A) {
+	return A->pid && A->coding == kCodingPatterns ? kCodingPatterns : kCodingColIds;
+}
 
 // ------------------------------------------------------------ errors --
 

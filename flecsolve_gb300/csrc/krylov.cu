@@ -82,10 +82,14 @@ __global__ void k_copy(int64_t n, const V *__restrict__ s, V *__restrict__ d) {
 
 // z = P r (PK 0: identity, 1: diagonal); p = z; rho = z'r; res0 = ||r||
 // (cg.hh:75-90).  Early exit when res0 < tol (cg.hh:77-82).
+// With z2 (the fused iteration) z is also kept in z2, and the pending solution
+// step and the direction coefficient start at 0, so the first fused
+// direction update p = z + 0 p reproduces p = z.
 template<class V, int PK>
 __global__ void __launch_bounds__(kThreads)
 k_cg_start(int64_t n, const V *__restrict__ r, const V *__restrict__ dinv,
-           V *__restrict__ p, KState *st, double *part, unsigned *counter) {
+           V *__restrict__ p, KState *st, double *part, unsigned *counter,
+           V *__restrict__ z2 = nullptr) {
 	__shared__ double sh[128];
 	Acc<V, 2> acc;
 	acc.init();
@@ -93,6 +97,8 @@ k_cg_start(int64_t n, const V *__restrict__ r, const V *__restrict__ dinv,
 		V ri = r[i];
 		V zi = PK ? dinv[i] * ri : ri;
 		p[i] = zi;
+		if (z2)
+			z2[i] = zi;
 		acc.add_prod(0, ri, ri);
 		acc.add_prod(1, zi, ri);
 	}
@@ -108,6 +114,9 @@ k_cg_start(int64_t n, const V *__restrict__ r, const V *__restrict__ dinv,
 			st->rho_old = s[1];
 			st->iter = 0;
 			st->flags = 0;
+			st->beta = 0.0;
+			st->alpha_x = 0.0;
+			st->pbuf = 0;
 			if (res < st->tol) {
 				st->done = 1;
 				st->status = FS_CONVERGED_RTOL;
@@ -314,18 +323,149 @@ __global__ void k_rel_fold(int64_t n, double *__restrict__ x, float *__restrict_
 	}
 }
 
+// ----------------------------------------- fused reliable-update CG --
+//
+// Two kernels per iteration instead of three.  The direction update
+// p = z + beta p (cg.hh:124-130) and the solution update x += alpha p of the
+// previous iteration (cg.hh:108) move into the SpMV w = A p (cg.hh:94): the
+// row-pattern SpMV forms the new direction at every column it gathers from
+// the previous direction and z, applies the pending x update and stores p
+// for its own rows.  The second kernel updates
+// r -= alpha w, forms z = D^-1 r and the two dot products (cg.hh:109-123).
+// Blocks read the old direction while others write the new one, so the
+// direction alternates between two buffers (KState::pbuf).  Every value is
+// formed by the same operations as in the three-kernel iteration; only the
+// per-CTA grouping of the p'Ap partial sums follows the SpMV grid.
+
+// gather policy: the new direction at column c, p = z + beta p_old (k_cg_dir's
+// operation), from the previous direction and z; for the block's own rows also
+// the pending solution step xs += alpha_x p_old and the store of p
+template<class V>
+struct GatherCgDir {
+	static constexpr bool kOwn = true;
+	V *pa, *pb;             // the two direction buffers
+	const V *z;
+	V *xs;
+	const KState *st;
+	const V *p;             // set by init(): current direction
+	V *pout;                // the other buffer
+	V beta, alpha_x;
+	__device__ void init() {
+		const int cur = st->pbuf;
+		p = cur ? pb : pa;
+		pout = cur ? pa : pb;
+		beta = (V)st->beta;
+		alpha_x = (V)st->alpha_x;
+	}
+	__device__ V at(int c) const { return fma(beta, __ldg(p + c), __ldg(z + c)); }
+	__device__ V own(int r) const {
+		const V po = __ldg(p + r);
+		const V pn = fma(beta, po, __ldg(z + r));
+		xs[r] = fma(alpha_x, po, xs[r]);
+		pout[r] = pn;
+		return pn;
+	}
+};
+
+// w = A p, p'Ap -> alpha (as EpiCgAp); the direction buffers swap
+struct EpiCgFused {
+	static constexpr int NV = 1;
+	float *w;
+	KState *st;
+	double *part;
+	unsigned *counter;
+	__device__ bool skip() const { return stopped(st); }
+	template<class A>
+	__device__ void row_own(int r, float s, float p, A &acc) const {
+		w[r] = s;
+		acc.add_prod(0, s, p);
+	}
+	template<class A>
+	__device__ void row(int, float, A &) const {}
+	__device__ void finish(const double *s) const {
+		double pap = s[0];
+		st->pAp = pap;
+		if (!(pap > 0.0))
+			st->flags |= KF_NEG_CURVATURE;
+		st->alpha = st->rho / pap;
+		st->pbuf ^= 1;
+	}
+};
+
+// r -= alpha w; z = P r; ||r||, r'z; replacement test and beta (the update
+// of k_rc_update without the solution, which the next SpMV applies)
+template<int PK>
+__global__ void __launch_bounds__(kThreads)
+k_rc_resid(int64_t n, float *__restrict__ r, float *__restrict__ z, const float *__restrict__ w,
+           const float *__restrict__ dinv, KState *st, double *part, unsigned *counter,
+           double *hist, double delta) {
+	__shared__ double sh[128];
+	if (stopped(st))
+		return;
+	const float alpha = (float)st->alpha;
+	Acc<float, 2> acc;
+	acc.init();
+	FOR_EACH(i, n) {
+		float ri = fmaf(-alpha, w[i], r[i]);
+		r[i] = ri;
+		float zi = PK ? dinv[i] * ri : ri;
+		z[i] = zi;
+		acc.add_prod(0, ri, ri);
+		acc.add_prod(1, ri, zi);
+	}
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double s[2];
+		sum_partials<2>(part, gridDim.x, s, sh);
+		if (threadIdx.x == 0) {
+			double res = sqrt(s[0]);
+			int it = st->iter + 1;
+			st->iter = it;
+			st->res = res;
+			if (it <= st->hist_cap)
+				hist[it - 1] = res;
+			if (!isfinite(res))
+				st->flags |= KF_NONFINITE;
+			if (res < delta * st->aux[1] || res < st->tol || it >= st->maxiter ||
+			    (st->flags & KF_NONFINITE))
+				st->flags |= KF_RELIABLE;
+			st->rho_old = st->rho;
+			st->rho = s[1];
+			st->beta = s[1] / st->rho_old;
+			st->alpha_x = st->alpha;
+			*counter = 0;
+		}
+	}
+}
+
+// x64 += (xs + alpha_x p); xs = 0 -- the fold with the pending solution step
+// of the fused iteration (p = the current direction buffer)
+__global__ void k_rel_fold_pending(int64_t n, double *__restrict__ x, float *__restrict__ xs,
+                                   const float *__restrict__ pa, const float *__restrict__ pb,
+                                   const KState *st) {
+	const float *p = st->pbuf ? pb : pa;
+	const float a = (float)st->alpha_x;
+	FOR_EACH(i, n) {
+		x[i] += (double)fmaf(a, p[i], xs[i]);
+		xs[i] = 0.f;
+	}
+}
+
 // after the FP64 residual replaced r32: rho = r'Dr, beta = rho / rho_old,
 // new reference level for the next replacement, stopping test
 template<int PK>
 __global__ void __launch_bounds__(kThreads)
 k_rel_finish(int64_t n, const float *__restrict__ r, const float *__restrict__ dinv, KState *st,
-             double *part, unsigned *counter) {
+             double *part, unsigned *counter, float *__restrict__ z = nullptr) {
 	__shared__ double sh[128];
 	Acc<float, 1> acc;
 	acc.init();
 	FOR_EACH(i, n) {
 		float ri = r[i];
-		acc.add_prod(0, ri, PK ? dinv[i] * ri : ri);
+		float zi = PK ? dinv[i] * ri : ri;
+		if (z)
+			z[i] = zi;
+		acc.add_prod(0, ri, zi);
 	}
 	acc.to_part(part, sh);
 	if (last_block(counter)) {
@@ -336,6 +476,7 @@ k_rel_finish(int64_t n, const float *__restrict__ r, const float *__restrict__ d
 			st->beta = s[0] / st->rho_old;
 			st->aux[1] = st->res;  // true residual after the replacement
 			st->restarts += 1;     // number of replacements
+			st->alpha_x = 0.0;     // the fold applied the pending step
 			st->flags &= ~KF_RELIABLE;
 			if (st->res < st->tol) {
 				st->done = 1;
@@ -752,7 +893,7 @@ int solver_alloc(Solver *s) {
 	case FS_CG: nw64 = 3; break;
 	case FS_BICGSTAB: nw64 = 6; break;
 	case FS_GMRES: nw64 = 3; break;
-	case FS_CG_MIXED: nw64 = 1; nw32 = 5; break;
+	case FS_CG_MIXED: nw64 = 1; nw32 = 6; break;
 	case FS_BICGSTAB_MIXED: nw64 = 1; nw32 = 7; break;
 	case FS_GMRES_MIXED: nw64 = 3; nw32 = 3; break;
 	}
@@ -1167,6 +1308,31 @@ static int rc_body(Solver *s, void *a) {
 	return FS_OK;
 }
 
+// the fused two-kernel iteration runs on the row-pattern SpMV
+static bool cg_fusable(const Solver *s) {
+	return active_coding(s->A) == kCodingPatterns && s->w32[4] && s->w32[5];
+}
+
+template<int PK>
+static int rc_body_fused(Solver *s, void *a) {
+	RcArgs *g = (RcArgs *)a;
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	float *r = s->w32[0], *pa = s->w32[1], *w = s->w32[2], *xs = s->w32[3], *z = s->w32[4],
+	      *pb = s->w32[5];
+	const float *dinv = s->dinv32();
+	const int G = red_grid(ctx, n);
+	GatherCgDir<float> gd{pa, pb, z, xs, s->st, nullptr, nullptr, 0.f, 0.f};
+	for (int k = 0; k < g->k; ++k) {
+		FS_TRY((launch_spmv_pat<float, false>(ctx, s->A, s->A->val32, gd,
+		                                      EpiCgFused{w, s->st, s->part, s->counter})));
+		k_rc_resid<PK><<<G, kThreads, 0, ctx->stream>>>(n, r, z, w, dinv, s->st, s->part, s->counter,
+		                                               s->hist, g->delta);
+		FS_TRY(check_launch(ctx, "reliable cg residual"));
+	}
+	return FS_OK;
+}
+
 // FP32 CG with FP64 reliable updates (residual replacement)
 static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	Ctx *ctx = s->ctx;
@@ -1192,11 +1358,15 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 			ctx, s->A, s->A->val, (const double *)x->d, nullptr,
 			EpiRelResidual{(const double *)b->d, r32, s->st, s->part, s->counter});
 	};
+	const bool fused = cg_fusable(s);
+	float *z32 = fused ? s->w32[4] : nullptr, *pb32 = s->w32[5];
 	FS_TRY(true_residual());
 	if (PK)
-		k_cg_start<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, p32, s->st, s->part, s->counter);
+		k_cg_start<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, p32, s->st, s->part,
+		                                                     s->counter, z32);
 	else
-		k_cg_start<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, p32, s->st, s->part, s->counter);
+		k_cg_start<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, p32, s->st, s->part,
+		                                                     s->counter, z32);
 	FS_TRY(check_launch(ctx, "cg start f32"));
 	FS_TRY(read_state(s));
 	const double res0 = s->hst->res0;
@@ -1212,24 +1382,36 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	int64_t seen = 0;
 	const int k = k_default(s) > 1 ? k_default(s) : 32;
 	RcArgs args{b, x, k, delta};
-	GraphKey key{b->d, x->d, 2000 + k * 2 + PK};
+	GraphKey key{b->d, x->d, (fused ? 3000 : 2000) + k * 2 + PK};
+	auto body = fused ? (PK ? rc_body_fused<1> : rc_body_fused<0>) : (PK ? rc_body<1> : rc_body<0>);
+	auto fold = [&]() -> int {
+		if (fused)
+			k_rel_fold_pending<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs, p32, pb32, s->st);
+		else
+			k_rel_fold<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs);
+		return check_launch(ctx, "reliable fold");
+	};
 	while (!s->hst->done) {
-		FS_TRY(graph_run(s, key, PK ? rc_body<1> : rc_body<0>, &args));
+		FS_TRY(graph_run(s, key, body, &args));
 		FS_TRY(read_state(s));
 		if (s->hst->flags & KF_RELIABLE) {
-			k_rel_fold<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs);
-			FS_TRY(check_launch(ctx, "reliable fold"));
+			FS_TRY(fold());
 			FS_TRY(true_residual());
 			if (PK)
-				k_rel_finish<1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, s->st, s->part, s->counter);
+				k_rel_finish<1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, s->st, s->part, s->counter,
+				                                                z32);
 			else
-				k_rel_finish<0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, s->st, s->part, s->counter);
+				k_rel_finish<0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, s->st, s->part,
+				                                                s->counter, z32);
 			FS_TRY(check_launch(ctx, "reliable finish"));
-			if (PK)
-				k_cg_dir<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, s->st);
-			else
-				k_cg_dir<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, nullptr, s->st);
-			FS_TRY(check_launch(ctx, "cg direction f32"));
+			if (!fused) {
+				// the fused iteration forms the direction in its next SpMV
+				if (PK)
+					k_cg_dir<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, s->st);
+				else
+					k_cg_dir<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, nullptr, s->st);
+				FS_TRY(check_launch(ctx, "cg direction f32"));
+			}
 			FS_TRY(read_state(s));
 		}
 		if (s->diag) {
@@ -1246,10 +1428,8 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 				break;
 		}
 	}
-	if (user_stop) {
-		k_rel_fold<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs);
-		FS_TRY(check_launch(ctx, "reliable fold"));
-	}
+	if (user_stop)
+		FS_TRY(fold());
 	KState &h = *s->hst;
 	s->hhist_count = std::min<int64_t>(h.iter, s->hist_cap);
 	s->mixed_outer = h.restarts;

@@ -49,10 +49,12 @@ static std::vector<int> row_blocks(const std::vector<int> &rp) {
 // used then.  Consecutive rows usually share a sequence, which is checked
 // first.
 static bool row_patterns(const std::vector<int> &rp, const std::vector<int> &ci,
-                         std::vector<unsigned char> &pid, std::vector<int> &ptab, int &npat) {
+                         std::vector<unsigned char> &pid, std::vector<int> &ptab,
+                         std::vector<int> &plen, int &npat) {
 	const int64_t n = (int64_t)rp.size() - 1;
 	pid.assign((size_t)n + 32, 0);
 	ptab.clear();
+	plen.clear();
 	std::map<std::array<int, kPatW + 1>, int> ids;
 	std::array<int, kPatW + 1> key{}, last{};
 	int last_id = -1;
@@ -75,6 +77,7 @@ static bool row_patterns(const std::vector<int> &rp, const std::vector<int> &ci,
 				id = (int)ids.size();
 				ids.emplace(key, id);
 				ptab.insert(ptab.end(), key.begin(), key.begin() + kPatW);
+				plen.push_back(len);
 			}
 			else
 				id = it->second;
@@ -85,6 +88,18 @@ static bool row_patterns(const std::vector<int> &rp, const std::vector<int> &ci,
 	}
 	npat = (int)ids.size();
 	return true;
+}
+
+// Per row block and 32-row warp: where the nonzeros of the warp's first row
+// start, relative to the block's first nonzero (< kBlkNnz, fits a short).
+static std::vector<short> warp_bases(const std::vector<int> &rp, const std::vector<int> &blk) {
+	const int nblk = (int)blk.size() - 1;
+	std::vector<short> wb((size_t)nblk * (kBlkRows / 32), 0);
+	for (int b = 0; b < nblk; ++b)
+		for (int w = 0; w < kBlkRows / 32; ++w)
+			wb[(size_t)b * (kBlkRows / 32) + w] =
+				(short)(rp[std::min(blk[b] + 32 * w, blk[b + 1])] - rp[blk[b]]);
+	return wb;
 }
 
 static std::vector<int4> block_info(const std::vector<int> &blk, const std::vector<int> &rp) {
@@ -360,9 +375,9 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 	    fence_setup_copies() != cudaSuccess)
 		return fail(FS_ERR_CUDA);
 	std::vector<unsigned char> pid;
-	std::vector<int> ptab;
+	std::vector<int> ptab, plen;
 	int npat = 0;
-	if (nnz > 0 && nrows > 0 && row_patterns(rp, ci, pid, ptab, npat)) {
+	if (nnz > 0 && nrows > 0 && row_patterns(rp, ci, pid, ptab, plen, npat)) {
 		if (cudaMalloc(&A->pid, pid.size()) != cudaSuccess ||
 		    cudaMalloc(&A->ptab, ptab.size() * sizeof(int)) != cudaSuccess ||
 		    cudaMemcpy(A->pid, pid.data(), pid.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -374,6 +389,21 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 			return fail(FS_ERR_OUT_OF_MEMORY);
 		}
 		A->npat = npat;
+		std::vector<short> wb = warp_bases(rp, blk);
+		std::vector<unsigned char> pl(plen.begin(), plen.end());
+		pl.resize(std::max<size_t>(pl.size(), 16), 0);
+		if (cudaMalloc(&A->pwb, wb.size() * sizeof(short)) != cudaSuccess ||
+		    cudaMalloc(&A->plen, pl.size()) != cudaSuccess ||
+		    cudaMemcpy(A->pwb, wb.data(), wb.size() * sizeof(short), cudaMemcpyHostToDevice) !=
+		        cudaSuccess ||
+		    cudaMemcpy(A->plen, pl.data(), pl.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+		    fence_setup_copies() != cudaSuccess) {
+			cudaFree(A->pid);
+			cudaFree(A->ptab);
+			cudaFree(A->pwb);
+			cudaFree(A->plen);
+			return fail(FS_ERR_OUT_OF_MEMORY);
+		}
 	}
 	*out = reinterpret_cast<fs_csr>(A);
 	return FS_OK;
@@ -383,10 +413,12 @@ FS_API int fs_csr_index_coding(fs_csr h, int enable, int *active) {
 	Csr *A = reinterpret_cast<Csr *>(h);
 	if (!ok_csr(A))
 		return FS_ERR_BAD_HANDLE;
+	if (enable > kCodingPatterns)
+		return set_err(A->ctx, FS_ERR_INVALID_ARG, "fs_csr_index_coding: enable must be -1, 0 or 1");
 	if (enable >= 0)
-		A->use_codes = enable != 0;
+		A->coding = enable;
 	if (active)
-		*active = A->pid && A->use_codes ? 1 : 0;
+		*active = active_coding(A);
 	return FS_OK;
 }
 
@@ -405,7 +437,7 @@ FS_API int fs_csr_destroy(fs_csr h) {
 	cudaStreamSynchronize(A->ctx->stream);
 	for (void *p : {(void *)A->rowptr, (void *)A->col, (void *)A->val, (void *)A->val32,
 	                (void *)A->blk, (void *)A->blkinfo, (void *)A->dinv, (void *)A->dinv32,
-	                (void *)A->pid, (void *)A->ptab,
+	                (void *)A->pid, (void *)A->ptab, (void *)A->pwb, (void *)A->plen,
 	                (void *)A->t_colptr, (void *)A->t_row, (void *)A->t_perm, (void *)A->t_val,
 	                (void *)A->t_blk, (void *)A->t_blkinfo})
 		if (p)

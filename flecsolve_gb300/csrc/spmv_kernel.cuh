@@ -18,15 +18,9 @@
 // records an error in the context's device error word, waits (again bounded)
 // for the copies it issued, and finishes without summing further blocks.
 //
-// Index formats:
-//  * column ids: 32-bit column id per nonzero;
-//  * row patterns: when every row has at most kPatW nonzeros and the matrix
-//    has at most kMaxPat distinct sequences of column offsets c - r (a
-//    stencil operator: 27 for a 7-point 3-D one), each row stores the 8-bit id
-//    of its sequence and the kernel keeps the sequences in shared memory:
-//    index traffic one byte per row instead of four per nonzero.  The columns,
-//    the products and their order are the same, so the result is the same bit
-//    for bit.
+// This kernel reads 32-bit column ids.  Matrices whose rows follow a few
+// column-offset patterns (stencil operators) use the row-pattern kernel of
+// spmv_pat.cuh instead; both give the same bits.
 //
 // EXACT mode rounds every product a_k * x[c_k] and adds the products left to
 // right per row, which is the reference's operation order bit for bit.
@@ -45,9 +39,6 @@ struct CsrDev {
 	const V *__restrict__ val;
 	const int4 *__restrict__ info;  // per row block {r0, r1, k0, k1}
 	int nblk;
-	const unsigned char *__restrict__ pid;  // row patterns: pattern id per row
-	const int *__restrict__ ptab;           // row patterns: kPatW offsets per pattern
-	int npat;
 	unsigned *err;                          // device error word of the context
 };
 
@@ -103,25 +94,23 @@ template<class V, int NV>
 using Acc = std::conditional_t<std::is_same_v<V, double>, AccD<NV>, AccF<NV>>;
 
 // One pipeline stage: the 16-byte aligned covers of a row block's values,
-// indices (column ids, or pattern ids) and row offsets, plus the block's
-// bounds.  Every array starts on a 16-byte boundary.
-template<class V, bool PAT>
+// column ids and row offsets, plus the block's bounds.  Every array starts on
+// a 16-byte boundary.
+template<class V>
 struct alignas(16) Stage {
 	V val[kBlkNnz + 16 / sizeof(V)];
-	int col[PAT ? 4 : kBlkNnz + 4];
-	unsigned char pid[PAT ? kBlkRows + 32 : 16];
+	int col[kBlkNnz + 4];
 	int rp[kBlkRows + 1 + 7];
 	int r0, r1, k0, k1;
 };
 
-// pipeline depth: <= 48 KB of stages per CTA with column ids; pattern stages
-// are about half as large
-template<class V, bool PAT>
-constexpr int kStages = PAT ? (sizeof(V) == 8 ? 3 : 4) : (sizeof(V) == 8 ? 2 : 3);
+// pipeline depth: <= 48 KB of stages per CTA
+template<class V>
+constexpr int kStages = sizeof(V) == 8 ? 2 : 3;
 
-template<class V, bool PAT>
+template<class V>
 constexpr size_t spmv_smem_bytes() {
-	return sizeof(Stage<V, PAT>) * kStages<V, PAT> + (PAT ? sizeof(int) * kMaxPat * kPatW : 0);
+	return sizeof(Stage<V>) * kStages<V>;
 }
 
 // ------------------------------------------------- mbarrier / bulk copy --
@@ -187,8 +176,8 @@ __device__ __forceinline__ V xg(const V *__restrict__ x, const V *__restrict__ d
 // stage `st`; thread 0 only.  Each cover starts at an aligned index <= the
 // first element and ends within 16 bytes past the last, inside the padded
 // allocations.  A long row copies nothing (it is summed from global memory).
-template<class V, bool PAT>
-__device__ __forceinline__ void stage_issue(const CsrDev<V> &A, int4 m, Stage<V, PAT> &st,
+template<class V>
+__device__ __forceinline__ void stage_issue(const CsrDev<V> &A, int4 m, Stage<V> &st,
                                             unsigned long long *bar) {
 	constexpr int VW = 16 / sizeof(V);
 	const int r0 = m.x, r1 = m.y, k0 = m.z, k1 = m.w;
@@ -196,23 +185,18 @@ __device__ __forceinline__ void stage_issue(const CsrDev<V> &A, int4 m, Stage<V,
 	st.r1 = r1;
 	st.k0 = k0;
 	st.k1 = k1;
-	unsigned bv = 0, bc = 0, bp = 0, br = 0;
-	const int a0 = k0 & ~(VW - 1), c0 = k0 & ~3, q0 = r0 & ~15, p0 = r0 & ~3;
+	unsigned bv = 0, bc = 0, br = 0;
+	const int a0 = k0 & ~(VW - 1), c0 = k0 & ~3, p0 = r0 & ~3;
 	if (k1 - k0 <= kBlkNnz) {
 		bv = k1 > k0 ? (unsigned)(((k1 - a0 + VW - 1) / VW) * 16) : 0u;
-		if constexpr (PAT)
-			bp = (unsigned)(((r1 - q0 + 15) / 16) * 16);
-		else
-			bc = k1 > k0 ? (unsigned)(((k1 - c0 + 3) / 4) * 16) : 0u;
+		bc = k1 > k0 ? (unsigned)(((k1 - c0 + 3) / 4) * 16) : 0u;
 		br = (unsigned)(((r1 + 1 - p0 + 3) / 4) * 16);
 	}
-	mbar_arrive_expect_tx(bar, bv + bc + bp + br);
+	mbar_arrive_expect_tx(bar, bv + bc + br);
 	if (bv)
 		bulk_g2s(st.val, A.val + a0, bv, bar);
 	if (bc)
 		bulk_g2s(st.col, A.col + c0, bc, bar);
-	if (bp)
-		bulk_g2s(st.pid, A.pid + q0, bp, bar);
 	if (br)
 		bulk_g2s(st.rp, A.rowptr + p0, br, bar);
 }
@@ -233,16 +217,15 @@ __device__ __forceinline__ int4 block_meta(const CsrDev<V> &A, int i, int nb) {
 // Persistent CTAs walk the row blocks b = blockIdx.x + i * gridDim.x through a
 // kStages-deep ring: the copies of block i + kStages - 1 are in flight while
 // block i is summed out of shared memory.
-template<class V, bool EXACT, bool SCALE, class Epi, bool PAT = false>
+template<class V, bool EXACT, bool SCALE, class Epi>
 __global__ void __launch_bounds__(kBlkRows)
 spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscale, Epi epi) {
 	constexpr int NV = Epi::NV;
-	constexpr int S = kStages<V, PAT>;
+	constexpr int S = kStages<V>;
 	constexpr int VW = 16 / sizeof(V);
-	using St = Stage<V, PAT>;
+	using St = Stage<V>;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	St *stages = reinterpret_cast<St *>(smem_raw);
-	int *ptab = reinterpret_cast<int *>(smem_raw + sizeof(St) * S);
 	__shared__ double red[128];
 	__shared__ unsigned long long bars[S];
 	__shared__ int abort_flag;
@@ -259,9 +242,6 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 			mbar_init(&bars[s], 1);
 		mbar_init_fence();
 	}
-	if constexpr (PAT)
-		for (int i = tid; i < A.npat * kPatW; i += blockDim.x)
-			ptab[i] = __ldg(A.ptab + i);
 	__syncthreads();
 	// bounds are loaded one block before their copies are issued, so the
 	// issue never waits on a global load
@@ -270,14 +250,14 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 #pragma unroll
 		for (int i = 0; i < S - 1; ++i)
 			if (i < nb)
-				stage_issue<V, PAT>(A, block_meta(A, i, nb), stages[i], &bars[i]);
+				stage_issue<V>(A, block_meta(A, i, nb), stages[i], &bars[i]);
 		mnext = block_meta(A, S - 1, nb);
 	}
 	int i = 0;
 	for (; i < nb; ++i) {
 		const int ni = i + S - 1;
 		if (tid == 0 && ni < nb) {
-			stage_issue<V, PAT>(A, mnext, stages[ni % S], &bars[ni % S]);
+			stage_issue<V>(A, mnext, stages[ni % S], &bars[ni % S]);
 			mnext = block_meta(A, ni + 1, nb);
 		}
 		if (!mbar_wait(&bars[i % S], (unsigned)((i / S) & 1)))
@@ -311,49 +291,26 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 				const int p0 = r0 & ~3, a0 = k0 & ~(VW - 1);
 				const int kb = st.rp[r - p0];
 				V s = V(0);
-				if constexpr (PAT) {
-					// the row's offsets: kPatW entries of its pattern
-					const int q0 = r0 & ~15;
-					const int *po = ptab + (int)st.pid[r - q0] * kPatW;
-					const int len = st.rp[r + 1 - p0] - kb;
-					V a[kPatW], xv[kPatW];
+				const int c0 = k0 & ~3;
+				const int ke = st.rp[r + 1 - p0];
+				// batches of 8: all gathers of a batch are issued before the
+				// first product, so a 7-point row costs one L2 round trip
+				for (int kc = kb; kc < ke; kc += 8) {
+					V a[8], xv[8];
 #pragma unroll
-					for (int j = 0; j < kPatW; ++j)
-						if (j < len) {
-							a[j] = st.val[kb + j - a0];
-							xv[j] = xg<V, SCALE>(x, dscale, r + po[j]);
+					for (int j = 0; j < 8; ++j)
+						if (kc + j < ke) {
+							a[j] = st.val[kc + j - a0];
+							xv[j] = xg<V, SCALE>(x, dscale, st.col[kc + j - c0]);
 						}
 #pragma unroll
-					for (int j = 0; j < kPatW; ++j)
-						if (j < len) {
+					for (int j = 0; j < 8; ++j)
+						if (kc + j < ke) {
 							if constexpr (EXACT)
 								s = add_rn(s, mul_rn(a[j], xv[j]));
 							else
 								s = fma(a[j], xv[j], s);
 						}
-				}
-				else {
-					const int c0 = k0 & ~3;
-					const int ke = st.rp[r + 1 - p0];
-					// batches of 8: all gathers of a batch are issued before
-					// the first product, so a 7-point row costs one L2 round trip
-					for (int kc = kb; kc < ke; kc += 8) {
-						V a[8], xv[8];
-#pragma unroll
-						for (int j = 0; j < 8; ++j)
-							if (kc + j < ke) {
-								a[j] = st.val[kc + j - a0];
-								xv[j] = xg<V, SCALE>(x, dscale, st.col[kc + j - c0]);
-							}
-#pragma unroll
-						for (int j = 0; j < 8; ++j)
-							if (kc + j < ke) {
-								if constexpr (EXACT)
-									s = add_rn(s, mul_rn(a[j], xv[j]));
-								else
-									s = fma(a[j], xv[j], s);
-							}
-					}
 				}
 				epi.row(r, s, acc);
 			}
@@ -417,12 +374,12 @@ int spmv_grid(Ctx *ctx, int nblk, int per_sm);
 // `static`: every translation unit has its own copy of the kernel (no
 // relocatable device code), so the attribute and the occupancy are set up
 // per unit, in a per-unit cache
-template<class V, bool EXACT, bool SCALE, class Epi, bool PAT>
+template<class V, bool EXACT, bool SCALE, class Epi>
 static inline int launch_spmv_as(Ctx *ctx, const CsrDev<V> &d, const V *x, const V *dscale,
                                  const Epi &epi) {
 	static int per_sm = 0;  // resident CTAs per SM of this instantiation
-	constexpr size_t smem = spmv_smem_bytes<V, PAT>();
-	auto kern = spmv_rb_kernel<V, EXACT, SCALE, Epi, PAT>;
+	constexpr size_t smem = spmv_smem_bytes<V>();
+	auto kern = spmv_rb_kernel<V, EXACT, SCALE, Epi>;
 	if (per_sm == 0) {
 		if (smem > 48 * 1024 &&
 		    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -439,15 +396,26 @@ static inline int launch_spmv_as(Ctx *ctx, const CsrDev<V> &d, const V *x, const
 	return check_launch(ctx, "spmv");
 }
 
-// the row-pattern kernel when the matrix carries patterns, else the one
-// reading column ids
+}  // namespace fsg
+
+#include "spmv_pat.cuh"
+
+namespace fsg {
+
+// The index format in use: the warp-specialised row-pattern kernel when the
+// matrix carries patterns, else column ids.
 template<class V, bool EXACT, bool SCALE, class Epi>
 static inline int launch_spmv(Ctx *ctx, const Csr *A, const V *vals, const V *x,
                               const V *dscale, const Epi &epi) {
-	CsrDev<V> d{A->rowptr, A->col, vals, A->blkinfo, A->nblk, A->pid, A->ptab, A->npat, ctx->dev_err};
-	if (A->pid && A->use_codes)
-		return launch_spmv_as<V, EXACT, SCALE, Epi, true>(ctx, d, x, dscale, epi);
-	return launch_spmv_as<V, EXACT, SCALE, Epi, false>(ctx, d, x, dscale, epi);
+	const int coding = active_coding(A);
+	if (coding == kCodingPatterns) {
+		if constexpr (SCALE)
+			return launch_spmv_pat<V, EXACT>(ctx, A, vals, GatherScale<V>{x, dscale}, epi);
+		else
+			return launch_spmv_pat<V, EXACT>(ctx, A, vals, GatherX<V>{x}, epi);
+	}
+	CsrDev<V> d{A->rowptr, A->col, vals, A->blkinfo, A->nblk, ctx->dev_err};
+	return launch_spmv_as<V, EXACT, SCALE, Epi>(ctx, d, x, dscale, epi);
 }
 
 }  // namespace fsg

@@ -1,6 +1,7 @@
 """CSR operator on the GPU against the oracle's reference row loop
 (flecsolve/matrices/seq.hh:177-193): bit-exact in EXACT mode, within a few
-ulps of the row sum in FMA mode; ragged, empty and long rows; FP32 values;
+ulps of the row sum in FMA mode; the index formats (column ids, row
+patterns) identical bit for bit; ragged, empty and long rows; FP32 values;
 residual; parcsr split; transpose."""
 import numpy as np
 import pytest
@@ -31,37 +32,80 @@ def test_spmv_exact_mode_is_bit_exact(ctx, wl):
     assert (np.abs(y - O.spmv(A, x)) <= _bound(A, x)).all()
 
 
-@pytest.mark.parametrize("wl", ["poisson2d-128", "diffusion3d-24", "convdiff3d-20"])
-def test_offset_coded_spmv_matches_column_ids(ctx, wl):
-    """Stencil patterns get 4-bit column-offset codes; the coded SpMV gives
-    the same bits as the one reading column ids, in every mode and type."""
-    A, _ = P.workload(wl)
+def _pattern_rect(n2, rows, cols):
+    """Rows [0, rows) of the 2-D Poisson operator on an n2 x n2 grid, with the
+    entries of columns >= cols dropped: a rectangular stencil matrix."""
+    A = P.poisson2d(n2)
+    S = A.to_scipy()[:rows, :cols].tocsr()
+    S.sort_indices()
+    return P.CSR(rows, cols, S.indptr.astype(np.int64), S.indices.astype(np.int32),
+                 S.data.astype(np.float64), "poisson-rect")
+
+
+PATTERN_CASES = ["poisson2d-128", "poisson2d-127", "diffusion3d-24", "diffusion3d-23",
+                 "convdiff3d-20", "rect-wide", "rect-tall"]
+
+
+def _pattern_matrix(name):
+    if name == "rect-wide":
+        return _pattern_rect(61, 3001, 61 * 61)   # ncols > nrows, odd sizes
+    if name == "rect-tall":
+        return _pattern_rect(61, 61 * 61, 3003)   # ncols < nrows
+    return P.workload(name)[0]
+
+
+@pytest.mark.parametrize("wl", PATTERN_CASES)
+def test_row_pattern_spmv_matches_column_ids(ctx, wl):
+    """Stencil matrices carry row patterns; the row-pattern SpMV (coding 1,
+    warp-specialised, row offsets from pattern lengths) gives the same bits
+    as the one reading column ids (coding 0), in every mode and type, on odd
+    sizes and rectangular matrices."""
+    A = _pattern_matrix(wl)
     x = P.uniform(43, A.ncols)
     dA = fs.CSR(ctx, A)
-    assert dA.index_coding()
+    assert dA.index_coding() == 1, "stencil matrices use row patterns by default"
     out = {}
-    for coded in (True, False):
-        assert dA.index_coding(coded) == coded
+    for coding in (1, 0):
+        assert dA.index_coding(coding) == coding
         for dt in ("f64", "f32"):
             vx, vy = fs.Vector(ctx, x.astype(np.float32) if dt == "f32" else x, dt), fs.Vector(ctx, A.nrows, dt)
             for exact in (True, False):
                 dA.apply(vx, vy, exact=exact)
-                out[coded, dt, exact] = vy.numpy()
+                out[coding, dt, exact] = vy.numpy()
+        if A.nrows == A.ncols:
+            b = fs.Vector(ctx, P.uniform(44, A.nrows))
             r = fs.Vector(ctx, A.nrows)
-        b = fs.Vector(ctx, P.uniform(44, A.nrows))
-        r = fs.Vector(ctx, A.nrows)
-        dA.residual(b, fs.Vector(ctx, x), r)
-        out[coded, "res"] = r.numpy()
-    for key in [k for k in out if k[0]]:
-        assert np.array_equal(out[key], out[(False,) + key[1:]]), key
-    assert np.array_equal(out[True, "f64", True], O.spmv(A, x))
+            dA.residual(b, fs.Vector(ctx, x), r)
+            out[coding, "res"] = r.numpy()
+    for key in [k for k in out if k[0] != 0]:
+        assert np.array_equal(out[key], out[(0,) + key[1:]]), key
+    assert np.array_equal(out[1, "f64", True], O.spmv(A, x))
 
 
-def test_offset_coding_falls_back_on_irregular_patterns(ctx):
+def test_spmv_on_unaligned_wrapped_vectors(ctx):
+    """A wrapped device vector that starts on an 8-byte boundary only (a
+    torch view at an odd offset) is gathered element by element: same bits."""
+    torch = pytest.importorskip("torch")
+    A, _ = P.workload("diffusion3d-23")
+    x = P.uniform(45, A.ncols)
+    dA = fs.CSR(ctx, A)
+    base = torch.zeros(A.ncols + 1, dtype=torch.float64, device="cuda")
+    base[1:] = torch.from_numpy(x).cuda()
+    torch.cuda.synchronize()
+    xv = fs.Vector.wrap(ctx, A.ncols, base.data_ptr() + 8)   # 8-byte aligned only
+    y1, y2 = fs.Vector(ctx, A.nrows), fs.Vector(ctx, A.nrows)
+    dA.apply(xv, y1, exact=True)
+    dA.apply(fs.Vector(ctx, x), y2, exact=True)
+    assert np.array_equal(y1.numpy(), y2.numpy())
+    assert np.array_equal(y1.numpy(), O.spmv(A, x))
+
+
+def test_row_patterns_fall_back_on_irregular_patterns(ctx):
     A = _ragged(3000, 7000, 5)
     dA = fs.CSR(ctx, A)
-    assert not dA.index_coding()
-    assert not dA.index_coding(True)
+    assert dA.index_coding() == 0
+    assert dA.index_coding(True) == 0
+    assert dA.index_coding("patterns") == 0
 
 
 def _ragged(n, m, seed, long_rows=()):
