@@ -112,21 +112,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-CODING_NAMES = {0: "colids", 1: "patterns"}
+CODING_NAMES = {0: "colids", 1: "patterns", 2: "symmetric"}
 
 
-def spmv_bytes(nrows, nnz, val_bytes, coding=0, nblk=0):
-    """Algorithmic bytes of one CSR SpMV: values, the index data of the
-    format, x read once, y written once.  Column ids (coding 0): int32 column
-    per nonzero + int32 row offsets.  Row patterns (1): one pattern-id byte
-    per row + 16 bytes of warp offsets per 256-row block (no row offsets).
-    The <= 8 KB pattern table is read once per CTA out of L2 and not
-    counted."""
+def spmv_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, nsym=3):
+    """Algorithmic bytes of one CSR SpMV: the matrix data of the format, x
+    read once, y written once.  Column ids (coding 0): values + int32 column
+    per nonzero + int32 row offsets.  Row patterns (1): values + one
+    pattern-id byte per row + 16 bytes of warp offsets per 256-row block.
+    Symmetric storage (2): the diagonal and `nsym` upper diagonals (3 for a
+    7-point operator) + one pattern-id byte per row.  Pattern tables (<= 8 KB)
+    are read once per CTA out of L2 and not counted."""
     if coding == 0:
-        idx = 4 * nnz + 4 * (nrows + 1)
+        mat = nnz * val_bytes + 4 * nnz + 4 * (nrows + 1)
+    elif coding == 1:
+        mat = nnz * val_bytes + nrows + 16 * nblk
     else:
-        idx = nrows + 16 * nblk
-    return nnz * val_bytes + idx + 2 * nrows * val_bytes
+        mat = (nsym + 1) * nrows * val_bytes + nrows
+    return mat + 2 * nrows * val_bytes
 
 
 def pcg_iter_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, fused=False):
@@ -209,7 +212,7 @@ def run_spmv_only(args):
     best = dA.index_coding()
     out = {"mode": "spmv", "workload": args.workload, "rows": n, "nnz": nnz,
            "index_coding": CODING_NAMES[best]}
-    for coding in ([1, 0] if best == 1 else [0]):
+    for coding in [c for c in (2, 1, 0) if c <= best]:
         if dA.index_coding(coding) != coding:
             continue
         for dt, vb in (("f64", 8), ("f32", 4)):
@@ -530,7 +533,8 @@ def run_ours(args, ws, rank, local):
         "speedup_mixed_vs_fp64": ms_64 / ms_mx,
         "spmv_hbm_gbs": {"f64": gbs64, "f32": gbs32, "f64_ms": spmv64_ms, "f32_ms": spmv32_ms},
         "roofline": {"bound": "hbm",
-                     "kernel": {1: "spmv_pat_kernel<float> (FP32 CSR SpMV, row patterns, warp-specialised)",
+                     "kernel": {2: "spmv_sym_kernel<float> (FP32 CSR SpMV, symmetric storage: diagonal + upper diagonals)",
+                                1: "spmv_pat_kernel<float> (FP32 CSR SpMV, row patterns, warp-specialised)",
                                 0: "spmv_rb_kernel<float> (FP32 CSR SpMV, int32 column ids)"}[coding],
                      "achieved": gbs32, "peak": peak, "unit": "GB/s", "frac": gbs32 / peak,
                      "peak_source": f"hbm_gbs of {peak_kind}",

@@ -322,18 +322,21 @@ class CSR:
         check(lib().fs_csr_row_blocks(self.h, C.byref(n)), self.ctx.h)
         return n.value
 
-    CODINGS = {"colids": 0, "patterns": 1}
+    CODINGS = {"colids": 0, "patterns": 1, "symmetric": 2}
 
     def index_coding(self, enable=None) -> int:
-        """The index format the SpMV uses: 0 = column ids, 1 = row patterns
-        (stencil operators: one pattern id per row, no column ids or row
-        offsets read).  `enable` switches it: True = row patterns when the
-        matrix has them, False = column ids, or a mode number / name; a
-        matrix without patterns always uses column ids."""
+        """The index format the FP64 SpMV uses: 0 = column ids, 1 = row
+        patterns (stencil operators: one pattern id per row, no column ids or
+        row offsets read), 2 = row patterns with symmetric storage (the
+        diagonal and upper diagonals of a matrix that is symmetric bit for
+        bit).  `enable` switches it: True = the best format the matrix
+        supports, False = column ids, or a mode number / name; a format the
+        matrix (or its current values) does not support falls back to the
+        next one down."""
         if enable is None:
             req = -1
         elif isinstance(enable, bool):
-            req = 1 if enable else 0
+            req = 2 if enable else 0
         elif isinstance(enable, str):
             req = self.CODINGS[enable]
         else:

@@ -174,10 +174,9 @@ FS_API int fs_fv_assemble(fs_csr Ah, int dim, int64_t n, fs_vec facesh, double s
 	k_fv_assemble<<<grid_for(ctx, N, 256, 4), 256, 0, ctx->stream>>>(dim, n, (const double *)c->d,
 	                                                               A->rowptr, A->val, scale, shift);
 	FS_TRY(check_launch(ctx, "fv assemble"));
-	// values changed: float copy, diagonal and CSC values are rebuilt on use
-	A->val32_valid = false;
-	A->dinv_valid = false;
-	A->t_vals_valid = false;
+	// values changed: float copy, diagonal, CSC values and symmetric storage
+	// are rebuilt on use
+	invalidate_values(A);
 	return FS_OK;
 }
 

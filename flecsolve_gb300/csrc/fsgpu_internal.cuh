@@ -66,6 +66,8 @@ constexpr int kMaxPat = 256;
 // index formats of the SpMV (fs_csr_index_coding)
 constexpr int kCodingColIds = 0;
 constexpr int kCodingPatterns = 1;
+constexpr int kCodingSym = 2;   // row patterns + symmetric storage (diagonal, upper diagonals)
+constexpr int kMaxSym = 4;      // positive column offsets of the symmetric storage
 
 struct Csr {
 	int magic = kMagicCsr;
@@ -87,7 +89,24 @@ struct Csr {
 	int npat = 0;
 	unsigned char *plen = nullptr;  // nonzeros per pattern
 	short *pwb = nullptr;           // per row block, per 32-row warp: first nonzero - k0
-	int coding = kCodingPatterns;   // requested format; column ids when absent
+	int coding = kCodingSym;        // requested format; the next one down when absent
+	// symmetric storage (square row-pattern matrices whose patterns pair every
+	// offset -d with +d, at most kMaxSym of them): per pattern entry a slot
+	// code (0 diagonal, k + 1 upper offset k, -(k + 1) lower offset k), per
+	// pattern the entry of each upper offset, the offsets; when the values are
+	// symmetric bit for bit, the diagonal and upper diagonals (FP64, FP32),
+	// (nsym + 1) x sym_ld each, rebuilt in place when the values change
+	signed char *pslot = nullptr;   // npat x kPatW
+	signed char *pinv = nullptr;    // npat x kMaxSym (-1: absent)
+	int *sofs = nullptr;            // nsym
+	int2 *stab = nullptr;           // npat x kPatW: {value offset, column offset} from r
+	int nsym = 0;
+	int64_t sym_ld = 0;
+	double *sym64 = nullptr;
+	float *sym32 = nullptr;
+	unsigned *sym_flag = nullptr;   // device: set by the build when a pair differs
+	bool sym64_valid = false, sym32_valid = false;
+	int sym_state = -1;             // -1 not checked since the values changed, 0 no, 1 yes
 	double *dinv = nullptr;    // 1 / a_ii, built on first use
 	float *dinv32 = nullptr;
 	bool dinv_valid = false;
@@ -106,9 +125,21 @@ struct Csr {
 
 // index format an SpMV on A uses (the requested one, or the next one the
 // matrix supports)
-inline int active_coding(const Csr *A) {
-	return A->pid && A->coding == kCodingPatterns ? kCodingPatterns : kCodingColIds;
+inline int active_coding(const Csr *A, bool f32 = false) {
+	if (!A->pid || A->coding == kCodingColIds)
+		return kCodingColIds;
+	if (A->coding == kCodingSym && (f32 ? A->sym32_valid : A->sym64_valid))
+		return kCodingSym;
+	return kCodingPatterns;
 }
+
+// derived data of A's values (float copy, Jacobi diagonal, CSC values,
+// symmetric storage) is stale: rebuilt on next use
+void invalidate_values(Csr *A);
+// build the symmetric storage of A's current values for FP64 or FP32 SpMVs
+// when the format is requested and the values are symmetric (setup path: may
+// allocate and synchronise; never called during stream capture)
+int ensure_sym(Csr *A, bool f32);
 
 // ------------------------------------------------------------ errors --
 

@@ -943,8 +943,13 @@ int read_state(Solver *s) {
 }
 
 // Capture `body` (k iterations) once per key, then replay it.
-int graph_run(Solver *s, const GraphKey &key, int (*body)(Solver *, void *), void *arg) {
+int graph_run(Solver *s, const GraphKey &key_in, int (*body)(Solver *, void *), void *arg) {
 	Ctx *ctx = s->ctx;
+	// a graph embeds the SpMV kernels chosen at capture: the formats in use
+	// are part of the key, so a format that changes with the values (the
+	// symmetric storage) or by request gets its own capture
+	GraphKey key = key_in;
+	key.fmt = active_coding(s->A, false) * 4 + active_coding(s->A, true);
 	const auto gkey = std::make_pair((const Csr *)s->A, key);
 	auto it = s->graphs.find(gkey);
 	if (it == s->graphs.end()) {
@@ -1310,7 +1315,7 @@ static int rc_body(Solver *s, void *a) {
 
 // the fused two-kernel iteration runs on the row-pattern SpMV
 static bool cg_fusable(const Solver *s) {
-	return active_coding(s->A) == kCodingPatterns && s->w32[4] && s->w32[5];
+	return active_coding(s->A, true) == kCodingPatterns && s->w32[4] && s->w32[5];
 }
 
 template<int PK>
@@ -1323,9 +1328,14 @@ static int rc_body_fused(Solver *s, void *a) {
 	const float *dinv = s->dinv32();
 	const int G = red_grid(ctx, n);
 	GatherCgDir<float> gd{pa, pb, z, xs, s->st, nullptr, nullptr, 0.f, 0.f};
+	const bool sym = active_coding(s->A, true) == kCodingSym;
 	for (int k = 0; k < g->k; ++k) {
-		FS_TRY((launch_spmv_pat<float, false>(ctx, s->A, s->A->val32, gd,
-		                                      EpiCgFused{w, s->st, s->part, s->counter})));
+		if (sym)
+			FS_TRY((launch_spmv_sym<float, false>(ctx, s->A, gd,
+			                                      EpiCgFused{w, s->st, s->part, s->counter})));
+		else
+			FS_TRY((launch_spmv_pat<float, false>(ctx, s->A, s->A->val32, gd,
+			                                      EpiCgFused{w, s->st, s->part, s->counter})));
 		k_rc_resid<PK><<<G, kThreads, 0, ctx->stream>>>(n, r, z, w, dinv, s->st, s->part, s->counter,
 		                                               s->hist, g->delta);
 		FS_TRY(check_launch(ctx, "reliable cg residual"));
@@ -1935,8 +1945,13 @@ FS_API int fs_krylov_apply(fs_solver h, fs_vec bh, fs_vec xh, fs_solve_info *inf
 	// place, so captured graphs stay valid
 	if (s->P.kind == FS_PRECOND_JACOBI)
 		FS_TRY(ensure_dinv(s->A));
-	if (s->method == FS_CG_MIXED || s->method == FS_BICGSTAB_MIXED || s->method == FS_GMRES_MIXED)
+	const bool mixed =
+		s->method == FS_CG_MIXED || s->method == FS_BICGSTAB_MIXED || s->method == FS_GMRES_MIXED;
+	if (mixed)
 		FS_TRY(ensure_val32(s->A));
+	FS_TRY(ensure_sym(s->A, false));
+	if (mixed)
+		FS_TRY(ensure_sym(s->A, true));
 	switch (s->method) {
 	case FS_CG: return cg_apply64(s, b, x, info);
 	case FS_BICGSTAB: return bicgstab_apply64(s, b, x, info);

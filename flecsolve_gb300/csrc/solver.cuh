@@ -69,8 +69,9 @@ struct Precond {
 struct GraphKey {
 	const void *b, *x;
 	int k;
+	int fmt = 0;  // SpMV formats in use at capture (set by graph_run)
 	bool operator<(const GraphKey &o) const {
-		return std::tie(b, x, k) < std::tie(o.b, o.x, o.k);
+		return std::tie(b, x, k, fmt) < std::tie(o.b, o.x, o.k, o.fmt);
 	}
 };
 

@@ -102,6 +102,40 @@ static std::vector<short> warp_bases(const std::vector<int> &rp, const std::vect
 	return wb;
 }
 
+// Slot codes of the symmetric storage: the positive offsets of all patterns
+// (at most kMaxSym), each pattern entry coded as diagonal / upper offset k /
+// lower offset k, and per pattern the entry holding each upper offset.  False
+// when a negative offset has no positive partner or there are too many.
+static bool sym_slots(const std::vector<int> &ptab, const std::vector<int> &plen, int npat,
+                      std::vector<int> &sofs, std::vector<signed char> &pslot,
+                      std::vector<signed char> &pinv) {
+	sofs.clear();
+	for (int p = 0; p < npat; ++p)
+		for (int j = 0; j < plen[p]; ++j) {
+			const int d = ptab[(size_t)p * kPatW + j];
+			if (d > 0 && std::find(sofs.begin(), sofs.end(), d) == sofs.end())
+				sofs.push_back(d);
+		}
+	if ((int)sofs.size() > kMaxSym)
+		return false;
+	std::sort(sofs.begin(), sofs.end());
+	pslot.assign((size_t)npat * kPatW, 0);
+	pinv.assign((size_t)npat * kMaxSym, -1);
+	for (int p = 0; p < npat; ++p)
+		for (int j = 0; j < plen[p]; ++j) {
+			const int d = ptab[(size_t)p * kPatW + j];
+			if (d == 0)
+				continue;
+			const int k = (int)(std::find(sofs.begin(), sofs.end(), d < 0 ? -d : d) - sofs.begin());
+			if (k == (int)sofs.size())
+				return false;
+			pslot[(size_t)p * kPatW + j] = (signed char)(d > 0 ? k + 1 : -(k + 1));
+			if (d > 0)
+				pinv[(size_t)p * kMaxSym + k] = (signed char)j;
+		}
+	return true;
+}
+
 static std::vector<int4> block_info(const std::vector<int> &blk, const std::vector<int> &rp) {
 	std::vector<int4> info(blk.size() > 0 ? blk.size() - 1 : 0);
 	for (size_t b = 0; b + 1 < blk.size(); ++b)
@@ -167,10 +201,83 @@ int ensure_dinv(Csr *A) {
 	return FS_OK;
 }
 
-static void invalidate_values(Csr *A) {
+void invalidate_values(Csr *A) {
 	A->val32_valid = false;
 	A->dinv_valid = false;
 	A->t_vals_valid = false;
+	A->sym64_valid = false;
+	A->sym32_valid = false;
+	A->sym_state = -1;
+}
+
+// The diagonal and upper diagonals from the CSR values, and the check that
+// every lower entry a(r, r - d) equals its partner a(r - d, r) bit for bit
+// (else *bad is set and the storage is not used).
+template<class V>
+__global__ void k_sym_build(int n, const int *__restrict__ rp, const double *__restrict__ val,
+                            const unsigned char *__restrict__ pid,
+                            const unsigned char *__restrict__ plen,
+                            const signed char *__restrict__ pslot,
+                            const signed char *__restrict__ pinv, const int *__restrict__ sofs,
+                            int64_t ld, V *__restrict__ diag, V *__restrict__ up, int check,
+                            unsigned *bad) {
+	for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+		const int p = pid[r], len = plen[p], k0 = rp[r];
+		for (int j = 0; j < len; ++j) {
+			const int code = pslot[p * kPatW + j];
+			const double v = val[k0 + j];
+			if (code == 0)
+				diag[r] = (V)v;
+			else if (code > 0)
+				up[(int64_t)(code - 1) * ld + r] = (V)v;
+			else if (check) {
+				const int k = -code - 1, c = r - sofs[k];
+				const int jj = c >= 0 ? pinv[pid[c] * kMaxSym + k] : -1;
+				if (jj < 0 || __double_as_longlong(val[rp[c] + jj]) != __double_as_longlong(v))
+					atomicOr(bad, 1u);
+			}
+		}
+	}
+}
+
+int ensure_sym(Csr *A, bool f32) {
+	if (!A->pslot || A->coding != kCodingSym || A->sym_state == 0)
+		return FS_OK;
+	bool &valid = f32 ? A->sym32_valid : A->sym64_valid;
+	if (valid)
+		return FS_OK;
+	Ctx *ctx = A->ctx;
+	const size_t elems = (size_t)(A->nsym + 1) * (size_t)A->sym_ld;
+	void **buf = f32 ? (void **)&A->sym32 : (void **)&A->sym64;
+	if (!*buf) {
+		const size_t bytes = elems * (f32 ? sizeof(float) : sizeof(double));
+		FS_CUDA_TRY(ctx, cudaMalloc(buf, bytes));
+		FS_CUDA_TRY(ctx, cudaMemsetAsync(*buf, 0, bytes, ctx->stream));
+	}
+	if (!A->sym_flag)
+		FS_CUDA_TRY(ctx, cudaMalloc(&A->sym_flag, sizeof(unsigned)));
+	const int check = A->sym_state < 0;
+	if (check)
+		FS_CUDA_TRY(ctx, cudaMemsetAsync(A->sym_flag, 0, sizeof(unsigned), ctx->stream));
+	const int n = (int)A->nrows;
+	if (f32)
+		k_sym_build<float><<<grid_for(ctx, n, 256, 4), 256, 0, ctx->stream>>>(
+			n, A->rowptr, A->val, A->pid, A->plen, A->pslot, A->pinv, A->sofs, A->sym_ld, A->sym32,
+			A->sym32 + A->sym_ld, check, A->sym_flag);
+	else
+		k_sym_build<double><<<grid_for(ctx, n, 256, 4), 256, 0, ctx->stream>>>(
+			n, A->rowptr, A->val, A->pid, A->plen, A->pslot, A->pinv, A->sofs, A->sym_ld, A->sym64,
+			A->sym64 + A->sym_ld, check, A->sym_flag);
+	FS_TRY(check_launch(ctx, "symmetric storage"));
+	if (check) {
+		unsigned bad = 0;
+		FS_CUDA_TRY(ctx, cudaMemcpyAsync(&bad, A->sym_flag, sizeof(unsigned), cudaMemcpyDeviceToHost,
+		                                 ctx->stream));
+		FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+		A->sym_state = bad ? 0 : 1;
+	}
+	valid = A->sym_state == 1;
+	return FS_OK;
 }
 
 // ------------------------------------------------------ parcsr split --
@@ -404,6 +511,45 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 			cudaFree(A->plen);
 			return fail(FS_ERR_OUT_OF_MEMORY);
 		}
+		std::vector<int> sofs;
+		std::vector<signed char> pslot, pinv;
+		const int64_t sym_ld = (nrows + 31) / 32 * 32 + 32;
+		if (nrows == ncols && sym_slots(ptab, plen, npat, sofs, pslot, pinv) &&
+		    (int64_t)(sofs.size() + 1) * sym_ld < ((int64_t)1 << 31)) {
+			// per pattern entry: value at S[r + vo], column r + xo (S holds the
+			// diagonal, then upper diagonal k at (k + 1) * ld)
+			std::vector<int2> stab((size_t)npat * kPatW, make_int2(0, 0));
+			for (int p = 0; p < npat; ++p)
+				for (int j = 0; j < plen[p]; ++j) {
+					const int code = pslot[(size_t)p * kPatW + j];
+					const int d = ptab[(size_t)p * kPatW + j];
+					int vo = 0;
+					if (code > 0)
+						vo = (int)(code * sym_ld);
+					else if (code < 0)
+						vo = (int)(-code * sym_ld) + d;  // d < 0: u at r + d
+					stab[(size_t)p * kPatW + j] = make_int2(vo, d);
+				}
+			if (cudaMalloc(&A->stab, stab.size() * sizeof(int2)) != cudaSuccess ||
+			    cudaMemcpy(A->stab, stab.data(), stab.size() * sizeof(int2), cudaMemcpyHostToDevice) !=
+			        cudaSuccess ||
+			    cudaMalloc(&A->pslot, pslot.size()) != cudaSuccess ||
+			    cudaMalloc(&A->pinv, pinv.size()) != cudaSuccess ||
+			    cudaMalloc(&A->sofs, std::max<size_t>(1, sofs.size()) * sizeof(int)) != cudaSuccess ||
+			    cudaMemcpy(A->pslot, pslot.data(), pslot.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+			    cudaMemcpy(A->pinv, pinv.data(), pinv.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+			    (!sofs.empty() && cudaMemcpy(A->sofs, sofs.data(), sofs.size() * sizeof(int),
+			                                 cudaMemcpyHostToDevice) != cudaSuccess) ||
+			    fence_setup_copies() != cudaSuccess) {
+				for (void *q : {(void *)A->pid, (void *)A->ptab, (void *)A->pwb, (void *)A->plen, (void *)A->pslot, (void *)A->pinv,
+	                (void *)A->sofs, (void *)A->stab, (void *)A->sym64, (void *)A->sym32, (void *)A->sym_flag,
+				                (void *)A->pslot, (void *)A->pinv, (void *)A->sofs})
+					cudaFree(q);
+				return fail(FS_ERR_OUT_OF_MEMORY);
+			}
+			A->nsym = (int)sofs.size();
+			A->sym_ld = sym_ld;
+		}
 	}
 	*out = reinterpret_cast<fs_csr>(A);
 	return FS_OK;
@@ -413,12 +559,14 @@ FS_API int fs_csr_index_coding(fs_csr h, int enable, int *active) {
 	Csr *A = reinterpret_cast<Csr *>(h);
 	if (!ok_csr(A))
 		return FS_ERR_BAD_HANDLE;
-	if (enable > kCodingPatterns)
-		return set_err(A->ctx, FS_ERR_INVALID_ARG, "fs_csr_index_coding: enable must be -1, 0 or 1");
+	if (enable > kCodingSym)
+		return set_err(A->ctx, FS_ERR_INVALID_ARG, "fs_csr_index_coding: enable must be -1, 0, 1 or 2");
 	if (enable >= 0)
 		A->coding = enable;
-	if (active)
+	if (active) {
+		FS_TRY(ensure_sym(A, false));
 		*active = active_coding(A);
+	}
 	return FS_OK;
 }
 
@@ -437,7 +585,8 @@ FS_API int fs_csr_destroy(fs_csr h) {
 	cudaStreamSynchronize(A->ctx->stream);
 	for (void *p : {(void *)A->rowptr, (void *)A->col, (void *)A->val, (void *)A->val32,
 	                (void *)A->blk, (void *)A->blkinfo, (void *)A->dinv, (void *)A->dinv32,
-	                (void *)A->pid, (void *)A->ptab, (void *)A->pwb, (void *)A->plen,
+	                (void *)A->pid, (void *)A->ptab, (void *)A->pwb, (void *)A->plen, (void *)A->pslot, (void *)A->pinv,
+	                (void *)A->sofs, (void *)A->stab, (void *)A->sym64, (void *)A->sym32, (void *)A->sym_flag,
 	                (void *)A->t_colptr, (void *)A->t_row, (void *)A->t_perm, (void *)A->t_val,
 	                (void *)A->t_blk, (void *)A->t_blkinfo})
 		if (p)
@@ -508,6 +657,7 @@ FS_API int fs_csr_spmv(fs_csr h, fs_vec xh, fs_vec yh, int mode) {
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_spmv: bad mode");
 	if (A->nrows == 0)
 		return FS_OK;
+	FS_TRY(ensure_sym(A, x->dtype == FS_F32));
 	if (x->dtype == FS_F64) {
 		EpiStore<double> e{(double *)y->d};
 		if (mode == FS_SPMV_EXACT)
@@ -535,6 +685,7 @@ FS_API int fs_csr_residual(fs_csr h, fs_vec bh, fs_vec xh, fs_vec rh) {
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_residual: x and r must differ");
 	if (A->nrows == 0)
 		return FS_OK;
+	FS_TRY(ensure_sym(A, x->dtype == FS_F32));
 	if (x->dtype == FS_F64)
 		return launch_spmv<double, false, false>(
 			ctx, A, A->val, (const double *)x->d, nullptr,

@@ -399,16 +399,26 @@ static inline int launch_spmv_as(Ctx *ctx, const CsrDev<V> &d, const V *x, const
 }  // namespace fsg
 
 #include "spmv_pat.cuh"
+#include "spmv_sym.cuh"
 
 namespace fsg {
 
-// The index format in use: the warp-specialised row-pattern kernel when the
-// matrix carries patterns, else column ids.
+// The index format in use: the symmetric storage when it is built for the
+// current values (and `vals` are A's own values), else the warp-specialised
+// row-pattern kernel when the matrix carries patterns, else column ids.
 template<class V, bool EXACT, bool SCALE, class Epi>
 static inline int launch_spmv(Ctx *ctx, const Csr *A, const V *vals, const V *x,
                               const V *dscale, const Epi &epi) {
-	const int coding = active_coding(A);
-	if (coding == kCodingPatterns) {
+	constexpr bool F32 = std::is_same_v<V, float>;
+	const int coding = active_coding(A, F32);
+	const bool own_vals = vals == (F32 ? (const V *)A->val32 : (const V *)A->val);
+	if (coding == kCodingSym && own_vals) {
+		if constexpr (SCALE)
+			return launch_spmv_sym<V, EXACT>(ctx, A, GatherScale<V>{x, dscale}, epi);
+		else
+			return launch_spmv_sym<V, EXACT>(ctx, A, GatherX<V>{x}, epi);
+	}
+	if (coding != kCodingColIds) {
 		if constexpr (SCALE)
 			return launch_spmv_pat<V, EXACT>(ctx, A, vals, GatherScale<V>{x, dscale}, epi);
 		else

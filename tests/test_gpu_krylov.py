@@ -197,17 +197,18 @@ def test_mixed_cg_refinement(ctx, wl):
 @pytest.mark.parametrize("wl", ["diffusion3d-40", "poisson2d-127", "diffusion3d-23"])
 def test_mixed_cg_fused_iteration(ctx, wl):
     """On a stencil matrix the mixed CG runs two kernels per iteration (the
-    direction and solution updates fused into the row-pattern SpMV); with
-    column ids it runs the three-kernel iteration.  Both follow the same
-    recurrences: same stopping test, iteration counts within one of each
-    other and of the FP64 reference count, and the same accuracy bar."""
+    direction and solution updates fused into the symmetric-storage or
+    row-pattern SpMV); with column ids it runs the three-kernel iteration.
+    All follow the same recurrences: same stopping test, iteration counts
+    within one of each other and of the FP64 reference count, and the same
+    accuracy bar."""
     A, b = P.workload(wl)
     ref64 = O.solve("cg", A, b, maxiter=20000, rtol=1e-8)
     xs = O.solve("cg", A, b, maxiter=20000, rtol=1e-14).x
     dA = fs.CSR(ctx, A)
     vb = fs.Vector(ctx, b)
     res = {}
-    for coding in ("patterns", "colids"):
+    for coding in ("symmetric", "patterns", "colids"):
         dA.index_coding(coding)
         for rtol in (1e-8, 1e-11):
             vx = fs.Vector(ctx, A.nrows)
@@ -215,7 +216,7 @@ def test_mixed_cg_fused_iteration(ctx, wl):
                                      fs.mixed_cg.make_work(vb))(fs.op.ref(dA), fs.op.jacobi)
             info = slv(vb, vx)
             res[coding, rtol] = (info, vx.numpy(), slv.mixed_stats())
-    for coding in ("patterns", "colids"):
+    for coding in ("symmetric", "patterns", "colids"):
         info, x, (outer, inner) = res[coding, 1e-8]
         assert info.status == "converged_rtol"
         assert _true_relres(A, b, x) <= 1e-8
@@ -224,9 +225,10 @@ def test_mixed_cg_fused_iteration(ctx, wl):
         assert info2.status == "converged_rtol"
         assert _rel(x2, xs) <= X_RTOL_MIXED
     assert abs(res["patterns", 1e-8][0].iters - res["colids", 1e-8][0].iters) <= 1
+    assert abs(res["symmetric", 1e-8][0].iters - res["colids", 1e-8][0].iters) <= 1
     # with a diagnostic the loop reads back every iteration and a user stop
     # folds the pending solution step into x
-    dA.index_coding("patterns")
+    dA.index_coding("symmetric")
     seen = []
 
     def stop_at_5(x, r):

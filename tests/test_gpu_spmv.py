@@ -1,8 +1,8 @@
 """CSR operator on the GPU against the oracle's reference row loop
 (flecsolve/matrices/seq.hh:177-193): bit-exact in EXACT mode, within a few
 ulps of the row sum in FMA mode; the index formats (column ids, row
-patterns) identical bit for bit; ragged, empty and long rows; FP32 values;
-residual; parcsr split; transpose."""
+patterns, symmetric storage) identical bit for bit; ragged, empty and long
+rows; FP32 values; residual; parcsr split; transpose."""
 import numpy as np
 import pytest
 
@@ -56,17 +56,22 @@ def _pattern_matrix(name):
 
 @pytest.mark.parametrize("wl", PATTERN_CASES)
 def test_row_pattern_spmv_matches_column_ids(ctx, wl):
-    """Stencil matrices carry row patterns; the row-pattern SpMV (coding 1,
-    warp-specialised, row offsets from pattern lengths) gives the same bits
-    as the one reading column ids (coding 0), in every mode and type, on odd
-    sizes and rectangular matrices."""
+    """Stencil matrices carry row patterns.  The symmetric storage (coding 2:
+    diagonal and upper diagonals, lower entries read from their partners) and
+    the row-pattern SpMV (coding 1, warp-specialised, row offsets from pattern
+    lengths) give the same bits as the one reading column ids (coding 0), in
+    every mode and type, on odd sizes and rectangular matrices.  A matrix that
+    is not symmetric bit for bit falls back to coding 1."""
     A = _pattern_matrix(wl)
     x = P.uniform(43, A.ncols)
     dA = fs.CSR(ctx, A)
-    assert dA.index_coding() == 1, "stencil matrices use row patterns by default"
+    S = A.to_scipy()
+    symmetric = A.nrows == A.ncols and (S != S.T).nnz == 0
+    best = 2 if symmetric else 1
+    assert dA.index_coding() == best
     out = {}
-    for coding in (1, 0):
-        assert dA.index_coding(coding) == coding
+    for coding in (2, 1, 0):
+        assert dA.index_coding(coding) == min(coding, best)
         for dt in ("f64", "f32"):
             vx, vy = fs.Vector(ctx, x.astype(np.float32) if dt == "f32" else x, dt), fs.Vector(ctx, A.nrows, dt)
             for exact in (True, False):
@@ -79,7 +84,34 @@ def test_row_pattern_spmv_matches_column_ids(ctx, wl):
             out[coding, "res"] = r.numpy()
     for key in [k for k in out if k[0] != 0]:
         assert np.array_equal(out[key], out[(0,) + key[1:]]), key
-    assert np.array_equal(out[1, "f64", True], O.spmv(A, x))
+    assert np.array_equal(out[2, "f64", True], O.spmv(A, x))
+
+
+def test_symmetric_storage_follows_value_changes(ctx):
+    """The symmetric storage is derived from the current values: a value
+    change that breaks the symmetry switches the operator (and a bound
+    solver's captured iterations) to the row-pattern kernel; restoring it
+    switches back.  Results follow the values every time."""
+    A, b = P.workload("diffusion3d-24")
+    x = P.uniform(46, A.ncols)
+    dA = fs.CSR(ctx, A)
+    assert dA.index_coding() == 2
+    vx, vy = fs.Vector(ctx, x), fs.Vector(ctx, A.nrows)
+    vb = fs.Vector(ctx, b)
+    slv = fs.bicgstab.solver(fs.bicgstab.settings(maxiter=2000, rtol=1e-8))(dA, fs.op.jacobi)
+    for step in range(3):
+        M = P.CSR(A.nrows, A.ncols, A.rowptr, A.col, A.val.copy())
+        if step == 1:
+            M.val[A.rowptr[100] + 1] *= 1.5     # one lower entry no longer matches its partner
+        dA.update_values(M.val)
+        assert dA.index_coding() == (1 if step == 1 else 2)
+        dA.apply(vx, vy, exact=True)
+        assert np.array_equal(vy.numpy(), O.spmv(M, x))
+        vsol = fs.Vector(ctx, A.nrows)
+        info = slv(vb, vsol)
+        assert info.status == "converged_rtol"
+        r = b - M.to_scipy() @ vsol.numpy()
+        assert np.linalg.norm(r) <= 1.5e-8 * np.linalg.norm(b)
 
 
 def test_spmv_on_unaligned_wrapped_vectors(ctx):
@@ -105,7 +137,7 @@ def test_row_patterns_fall_back_on_irregular_patterns(ctx):
     dA = fs.CSR(ctx, A)
     assert dA.index_coding() == 0
     assert dA.index_coding(True) == 0
-    assert dA.index_coding("patterns") == 0
+    assert dA.index_coding("symmetric") == 0
 
 
 def _ragged(n, m, seed, long_rows=()):
