@@ -132,14 +132,19 @@ def spmv_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, nsym=3):
     return mat + 2 * nrows * val_bytes
 
 
-def pcg_iter_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, fused=False):
-    """Algorithmic bytes of one Jacobi-PCG iteration.  Three kernels: SpMV +
-    update (read x, p, r, w, D^-1; write x, r) + direction (read p, r, D^-1;
-    write p) = B_spmv + 11 N s_v.  Two kernels (row patterns, fused): SpMV
-    with the direction and solution updates (the SpMV's bytes + read z and x,
-    write p, x) + residual update (read r, w, D^-1; write r, z) = B_spmv +
-    9 N s_v."""
-    return spmv_bytes(nrows, nnz, val_bytes, coding, nblk) + (9 if fused else 11) * nrows * val_bytes
+def pcg_iter_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, kind="fp64"):
+    """Algorithmic bytes of one Jacobi-PCG iteration beyond the SpMV's own
+    (B_spmv: matrix data, p read once, w written once).
+    * "fp64": update (read x, p, r, w, D^-1; write x, r) + direction (read p,
+      r, D^-1; write p) = 11 N s_v.
+    * "reliable" (mixed, three kernels): residual update (read r, w, D^-1;
+      write r) + direction with the solution step (read p, r, D^-1, x; write
+      p, x) = 10 N s_v.
+    * "fused" (mixed, two kernels, row-pattern SpMV): the SpMV also reads z
+      and x and writes p and x; residual update (read r, w, D^-1; write r, z)
+      = 9 N s_v."""
+    extra = {"fp64": 11, "reliable": 10, "fused": 9}[kind]
+    return spmv_bytes(nrows, nnz, val_bytes, coding, nblk) + extra * nrows * val_bytes
 
 
 def _traffic_from_profiles(kernel_key):
@@ -475,7 +480,7 @@ def run_ours(args, ws, rank, local):
     gbs64 = b64 / (spmv64_ms * 1e-3) / 1e9
     gbs32 = b32 / (spmv32_ms * 1e-3) / 1e9
     # whole mixed iteration: two kernels when the SpMV stages windows
-    it_bytes = pcg_iter_bytes(n, nnz, 4, coding, dA.nblk(), fused=coding == 1)
+    it_bytes = pcg_iter_bytes(n, nnz, 4, coding, dA.nblk(), "fused" if coding == 1 else "reliable")
     it_s = ms_mx * 1e-3 / max(1, info_mx.iters)
 
     # e2e: through the public API with host buffers

@@ -165,6 +165,43 @@ int set_err(Ctx *ctx, int status, const char *fmt, ...);
 
 int check_launch(Ctx *ctx, const char *what);
 
+// Programmatic dependent launch: a kernel launched with launch_pdl may be
+// scheduled while the previous kernel on the stream is still finishing (its
+// launch and ramp-up overlap that kernel's tail).  Such a kernel calls
+// pdl_wait() first, which returns once the previous kernel has completed and
+// its writes are visible, and pdl_trigger() to let the next kernel be
+// scheduled early in turn.  In a kernel launched normally both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+	asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+template<class... KArgs, class... Args>
+inline cudaError_t launch_pdl(cudaStream_t stream, void (*kern)(KArgs...), int grid, int block,
+                              size_t smem, Args... args) {
+	cudaLaunchConfig_t cfg{};
+	cfg.gridDim = dim3((unsigned)grid);
+	cfg.blockDim = dim3((unsigned)block);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = stream;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, kern, (KArgs)args...);
+}
+
+// check_launch for a launch that returned its status
+inline int check_launch_rc(Ctx *ctx, cudaError_t e, const char *what) {
+	if (e != cudaSuccess) {
+		ctx->launches++;
+		cudaGetLastError();
+		return set_err(ctx, FS_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+	}
+	return check_launch(ctx, what);
+}
+
 inline bool ok_ctx(const Ctx *c) { return c && c->magic == kMagicCtx; }
 
 // Setup copies and memsets go through the legacy default stream; a pageable

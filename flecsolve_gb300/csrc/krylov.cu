@@ -163,6 +163,8 @@ k_cg_update(int64_t n, V *__restrict__ x, const V *__restrict__ p, V *__restrict
             const V *__restrict__ w, const V *__restrict__ dinv, KState *st,
             double *part, unsigned *counter, double *hist) {
 	__shared__ double sh[128];
+	pdl_wait();
+	pdl_trigger();
 	if (stopped(st))
 		return;
 	const V alpha = (V)st->alpha;
@@ -213,6 +215,8 @@ template<class V, int PK>
 __global__ void __launch_bounds__(kThreads)
 k_cg_dir(int64_t n, V *__restrict__ p, const V *__restrict__ r,
          const V *__restrict__ dinv, const KState *st) {
+	pdl_wait();
+	pdl_trigger();
 	if (stopped(st))
 		return;
 	const V beta = (V)st->beta;
@@ -270,50 +274,10 @@ __global__ void k_inner_init(KState *in, const KState *out, double inner_rtol, i
 // correction xs, and whenever the recurrence residual has dropped by `delta`
 // since the last replacement (or below the tolerance) the host folds xs into
 // the FP64 solution and replaces r by the FP64 true residual b - A x.  The
-// search direction is kept, so no Krylov information is lost.
-template<int PK>
-__global__ void __launch_bounds__(kThreads)
-k_rc_update(int64_t n, float *__restrict__ x, const float *__restrict__ p, float *__restrict__ r,
-            const float *__restrict__ w, const float *__restrict__ dinv, KState *st,
-            double *part, unsigned *counter, double *hist, double delta) {
-	__shared__ double sh[128];
-	if (stopped(st))
-		return;
-	const float alpha = (float)st->alpha;
-	Acc<float, 2> acc;
-	acc.init();
-	FOR_EACH(i, n) {
-		float xi = fmaf(alpha, p[i], x[i]);
-		float ri = fmaf(-alpha, w[i], r[i]);
-		x[i] = xi;
-		r[i] = ri;
-		float zi = PK ? dinv[i] * ri : ri;
-		acc.add_prod(0, ri, ri);
-		acc.add_prod(1, ri, zi);
-	}
-	acc.to_part(part, sh);
-	if (last_block(counter)) {
-		double s[2];
-		sum_partials<2>(part, gridDim.x, s, sh);
-		if (threadIdx.x == 0) {
-			double res = sqrt(s[0]);
-			int it = st->iter + 1;
-			st->iter = it;
-			st->res = res;
-			if (it <= st->hist_cap)
-				hist[it - 1] = res;
-			if (!isfinite(res))
-				st->flags |= KF_NONFINITE;
-			if (res < delta * st->aux[1] || res < st->tol || it >= st->maxiter ||
-			    (st->flags & KF_NONFINITE))
-				st->flags |= KF_RELIABLE;
-			st->rho_old = st->rho;
-			st->rho = s[1];
-			st->beta = s[1] / st->rho_old;
-			*counter = 0;
-		}
-	}
-}
+// search direction is kept, so no Krylov information is lost.  One iteration
+// is three kernels: the SpMV with p'Ap, k_rc_resid (r -= alpha w, the dot
+// products, the replacement test) and k_cg_dir_x (the solution step
+// xs += alpha p and the direction update).
 
 // x64 += xs; xs = 0
 __global__ void k_rel_fold(int64_t n, double *__restrict__ x, float *__restrict__ xs) {
@@ -358,6 +322,7 @@ struct GatherCgDir {
 		alpha_x = (V)st->alpha_x;
 	}
 	__device__ V at(int c) const { return fma(beta, __ldg(p + c), __ldg(z + c)); }
+	__device__ V at_stream(int c) const { return fma(beta, ld_stream(p + c), ld_stream(z + c)); }
 	__device__ V own(int r) const {
 		const V po = __ldg(p + r);
 		const V pn = fma(beta, po, __ldg(z + r));
@@ -392,14 +357,19 @@ struct EpiCgFused {
 	}
 };
 
-// r -= alpha w; z = P r; ||r||, r'z; replacement test and beta (the update
-// of k_rc_update without the solution, which the next SpMV applies)
-template<int PK>
+// r -= alpha w; z = P r (stored when STOREZ); ||r||, r'z; replacement test
+// (the recurrence residual dropped by delta since the last replacement, or
+// below the tolerance, or maxiter) and beta.  The solution step xs += alpha p
+// of this iteration is left pending (alpha_x) for the kernel that next reads
+// p: the fused SpMV, or k_cg_dir_x.
+template<int PK, bool STOREZ = true>
 __global__ void __launch_bounds__(kThreads)
 k_rc_resid(int64_t n, float *__restrict__ r, float *__restrict__ z, const float *__restrict__ w,
            const float *__restrict__ dinv, KState *st, double *part, unsigned *counter,
            double *hist, double delta) {
 	__shared__ double sh[128];
+	pdl_wait();
+	pdl_trigger();
 	if (stopped(st))
 		return;
 	const float alpha = (float)st->alpha;
@@ -409,7 +379,8 @@ k_rc_resid(int64_t n, float *__restrict__ r, float *__restrict__ z, const float 
 		float ri = fmaf(-alpha, w[i], r[i]);
 		r[i] = ri;
 		float zi = PK ? dinv[i] * ri : ri;
-		z[i] = zi;
+		if (STOREZ)
+			z[i] = zi;
 		acc.add_prod(0, ri, ri);
 		acc.add_prod(1, ri, zi);
 	}
@@ -435,6 +406,27 @@ k_rc_resid(int64_t n, float *__restrict__ r, float *__restrict__ z, const float 
 			st->alpha_x = st->alpha;
 			*counter = 0;
 		}
+	}
+}
+
+// xs += alpha_x p (the pending solution step, cg.hh:108 in FP32); p = beta p
+// + z, z = P r (cg.hh:124-130).  A replacement folds the pending step into x
+// and clears alpha_x, so it is applied once.
+template<int PK>
+__global__ void __launch_bounds__(kThreads)
+k_cg_dir_x(int64_t n, float *__restrict__ p, const float *__restrict__ r,
+           const float *__restrict__ dinv, float *__restrict__ xs, const KState *st) {
+	pdl_wait();
+	pdl_trigger();
+	if (stopped(st))
+		return;
+	const float beta = (float)st->beta;
+	const float ax = (float)st->alpha_x;
+	FOR_EACH(i, n) {
+		const float po = p[i];
+		xs[i] = fmaf(ax, po, xs[i]);
+		const float zi = PK ? dinv[i] * r[i] : r[i];
+		p[i] = fmaf(beta, po, zi);
 	}
 }
 
@@ -1059,11 +1051,13 @@ static int cg_body64(Solver *s, void *a) {
 		FS_TRY(launch_spmv<double, false, false>(
 			ctx, s->A, s->A->val, p, nullptr,
 			EpiCgAp<double>{w, p, s->st, s->part, s->counter}));
-		k_cg_update<double, PK><<<G, kThreads, 0, ctx->stream>>>(n, x, p, r, w, dinv, s->st, s->part,
-		                                                        s->counter, s->hist);
-		FS_TRY(check_launch(ctx, "cg update"));
-		k_cg_dir<double, PK><<<G, kThreads, 0, ctx->stream>>>(n, p, r, dinv, s->st);
-		FS_TRY(check_launch(ctx, "cg direction"));
+		FS_TRY(check_launch_rc(ctx,
+		                       launch_pdl(ctx->stream, k_cg_update<double, PK>, G, kThreads, 0, n, x, p,
+		                                  r, w, dinv, s->st, s->part, s->counter, s->hist),
+		                       "cg update"));
+		FS_TRY(check_launch_rc(ctx, launch_pdl(ctx->stream, k_cg_dir<double, PK>, G, kThreads, 0, n, p, r,
+		                                       dinv, (const KState *)s->st),
+		                       "cg direction"));
 	}
 	return FS_OK;
 }
@@ -1080,11 +1074,13 @@ static int cg_body32(Solver *s, void *a) {
 		FS_TRY(launch_spmv<float, false, false>(
 			ctx, s->A, s->A->val32, p, nullptr,
 			EpiCgAp<float>{w, p, s->st_in, s->part, s->counter}));
-		k_cg_update<float, PK><<<G, kThreads, 0, ctx->stream>>>(n, x, p, r, w, dinv, s->st_in,
-		                                                       s->part, s->counter, s->hist);
-		FS_TRY(check_launch(ctx, "cg update f32"));
-		k_cg_dir<float, PK><<<G, kThreads, 0, ctx->stream>>>(n, p, r, dinv, s->st_in);
-		FS_TRY(check_launch(ctx, "cg direction f32"));
+		FS_TRY(check_launch_rc(ctx,
+		                       launch_pdl(ctx->stream, k_cg_update<float, PK>, G, kThreads, 0, n, x, p, r,
+		                                  w, dinv, s->st_in, s->part, s->counter, s->hist),
+		                       "cg update f32"));
+		FS_TRY(check_launch_rc(ctx, launch_pdl(ctx->stream, k_cg_dir<float, PK>, G, kThreads, 0, n, p, r,
+		                                       dinv, (const KState *)s->st_in),
+		                       "cg direction f32"));
 	}
 	return FS_OK;
 }
@@ -1304,11 +1300,14 @@ static int rc_body(Solver *s, void *a) {
 		FS_TRY(launch_spmv<float, false, false>(
 			ctx, s->A, s->A->val32, p, nullptr,
 			EpiCgAp<float>{w, p, s->st, s->part, s->counter}));
-		k_rc_update<PK><<<G, kThreads, 0, ctx->stream>>>(n, xs, p, r, w, dinv, s->st, s->part,
-		                                                s->counter, s->hist, g->delta);
-		FS_TRY(check_launch(ctx, "reliable cg update"));
-		k_cg_dir<float, PK><<<G, kThreads, 0, ctx->stream>>>(n, p, r, dinv, s->st);
-		FS_TRY(check_launch(ctx, "cg direction f32"));
+		FS_TRY(check_launch_rc(ctx,
+		                       launch_pdl(ctx->stream, k_rc_resid<PK, false>, G, kThreads, 0, n, r,
+		                                  (float *)nullptr, w, dinv, s->st, s->part, s->counter,
+		                                  s->hist, g->delta),
+		                       "reliable cg update"));
+		FS_TRY(check_launch_rc(ctx, launch_pdl(ctx->stream, k_cg_dir_x<PK>, G, kThreads, 0, n, p, r,
+		                                       dinv, xs, (const KState *)s->st),
+		                       "cg direction f32"));
 	}
 	return FS_OK;
 }
@@ -1336,9 +1335,10 @@ static int rc_body_fused(Solver *s, void *a) {
 		else
 			FS_TRY((launch_spmv_pat<float, false>(ctx, s->A, s->A->val32, gd,
 			                                      EpiCgFused{w, s->st, s->part, s->counter})));
-		k_rc_resid<PK><<<G, kThreads, 0, ctx->stream>>>(n, r, z, w, dinv, s->st, s->part, s->counter,
-		                                               s->hist, g->delta);
-		FS_TRY(check_launch(ctx, "reliable cg residual"));
+		FS_TRY(check_launch_rc(ctx,
+		                       launch_pdl(ctx->stream, k_rc_resid<PK>, G, kThreads, 0, n, r, z, w, dinv,
+		                                  s->st, s->part, s->counter, s->hist, g->delta),
+		                       "reliable cg residual"));
 	}
 	return FS_OK;
 }
@@ -1395,10 +1395,10 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	GraphKey key{b->d, x->d, (fused ? 3000 : 2000) + k * 2 + PK};
 	auto body = fused ? (PK ? rc_body_fused<1> : rc_body_fused<0>) : (PK ? rc_body<1> : rc_body<0>);
 	auto fold = [&]() -> int {
-		if (fused)
-			k_rel_fold_pending<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs, p32, pb32, s->st);
-		else
-			k_rel_fold<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs);
+		// the last iteration's solution step is still pending in both
+		// iterations (p = the current direction)
+		k_rel_fold_pending<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs, p32,
+		                                                    fused ? pb32 : p32, s->st);
 		return check_launch(ctx, "reliable fold");
 	};
 	while (!s->hst->done) {
@@ -1415,11 +1415,12 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 				                                                s->counter, z32);
 			FS_TRY(check_launch(ctx, "reliable finish"));
 			if (!fused) {
-				// the fused iteration forms the direction in its next SpMV
+				// the fused iteration forms the direction in its next SpMV;
+				// alpha_x is 0 here, so xs (cleared by the fold) stays 0
 				if (PK)
-					k_cg_dir<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, s->st);
+					k_cg_dir_x<1><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, xs, s->st);
 				else
-					k_cg_dir<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, nullptr, s->st);
+					k_cg_dir_x<0><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, nullptr, xs, s->st);
 				FS_TRY(check_launch(ctx, "cg direction f32"));
 			}
 			FS_TRY(read_state(s));

@@ -157,6 +157,24 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
 		: "memory");
 }
 
+// read-only loads that ask L2 to fetch the whole 256-byte group around the
+// address (streams whose neighbouring bytes are read by other warps soon)
+__device__ __forceinline__ float ld_stream(const float *p) {
+	float v;
+	asm("ld.global.nc.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+	return v;
+}
+__device__ __forceinline__ double ld_stream(const double *p) {
+	double v;
+	asm("ld.global.nc.L2::256B.f64 %0, [%1];" : "=d"(v) : "l"(p));
+	return v;
+}
+__device__ __forceinline__ unsigned char ld_stream(const unsigned char *p) {
+	unsigned short v;
+	asm("ld.global.nc.L2::256B.u8 %0, [%1];" : "=h"(v) : "l"(p));
+	return (unsigned char)v;
+}
+
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
@@ -229,6 +247,8 @@ spmv_rb_kernel(CsrDev<V> A, const V *__restrict__ x, const V *__restrict__ dscal
 	__shared__ double red[128];
 	__shared__ unsigned long long bars[S];
 	__shared__ int abort_flag;
+	pdl_wait();
+	pdl_trigger();
 	if (epi.skip())
 		return;
 	Acc<V, NV> acc;
@@ -392,8 +412,8 @@ static inline int launch_spmv_as(Ctx *ctx, const CsrDev<V> &d, const V *x, const
 		per_sm = nb;
 	}
 	int g = spmv_grid(ctx, d.nblk, per_sm);
-	kern<<<g, kBlkRows, smem, ctx->stream>>>(d, x, dscale, epi);
-	return check_launch(ctx, "spmv");
+	return check_launch_rc(ctx, launch_pdl(ctx->stream, kern, g, kBlkRows, smem, d, x, dscale, epi),
+	                       "spmv");
 }
 
 }  // namespace fsg

@@ -74,6 +74,8 @@ struct GatherX {
 	const V *x;
 	__device__ void init() {}
 	__device__ V at(int c) const { return __ldg(x + c); }
+	// the same value, read with a 256-byte L2 fetch (contiguous sweeps)
+	__device__ V at_stream(int c) const { return ld_stream(x + c); }
 	__device__ V own(int) const { return V(0); }
 };
 
@@ -85,6 +87,7 @@ struct GatherScale {
 	const V *x, *d;
 	__device__ void init() {}
 	__device__ V at(int c) const { return mul_rn(__ldg(d + c), __ldg(x + c)); }
+	__device__ V at_stream(int c) const { return mul_rn(ld_stream(d + c), ld_stream(x + c)); }
 	__device__ V own(int) const { return V(0); }
 };
 
@@ -120,6 +123,8 @@ spmv_pat_kernel(CsrPat<V> A, G g_in, Epi epi) {
 	__shared__ double red[128];
 	__shared__ unsigned long long full[S], empty[S];
 	__shared__ int abort_flag;
+	pdl_wait();
+	pdl_trigger();
 	if (epi.skip())
 		return;
 	G g = g_in;
@@ -263,8 +268,8 @@ static inline int launch_spmv_pat(Ctx *ctx, const Csr *A, const V *vals, const G
 	}
 	CsrPat<V> d{vals, A->blkinfo, A->pwb, A->pid, A->ptab, A->plen, A->nblk, A->npat, ctx->dev_err};
 	const int grid = spmv_grid(ctx, A->nblk, per_sm);
-	kern<<<grid, kPatThreads, smem, ctx->stream>>>(d, g, epi);
-	return check_launch(ctx, "spmv (row patterns)");
+	return check_launch_rc(ctx, launch_pdl(ctx->stream, kern, grid, kPatThreads, smem, d, g, epi),
+	                       "spmv (row patterns)");
 }
 
 }  // namespace fsg

@@ -48,6 +48,8 @@ spmv_sym_kernel(CsrSym<V> A, G g_in, Epi epi) {
 	extern __shared__ __align__(16) int2 tab[];  // npat x kPatW
 	__shared__ unsigned char plen[kMaxPat];
 	__shared__ double red[128];
+	pdl_wait();
+	pdl_trigger();
 	if (epi.skip())
 		return;
 	G g = g_in;
@@ -68,7 +70,7 @@ spmv_sym_kernel(CsrSym<V> A, G g_in, Epi epi) {
 	const int stride = (int)gridDim.x * kSymRows;
 	auto pid_at = [&](int t) -> int {
 		const int r = t * kSymThreads + threadIdx.x;
-		return t < ntile && r < A.n ? (int)__ldg(A.pid + r) : -1;
+		return t < ntile && r < A.n ? (int)ld_stream(A.pid + r) : -1;
 	};
 	int pnext[kSymRows];
 #pragma unroll
@@ -96,8 +98,8 @@ spmv_sym_kernel(CsrSym<V> A, G g_in, Epi epi) {
 #pragma unroll
 				for (int j = 0; j < kPatW; ++j)
 					if (j < len[u]) {
-						a[u][j] = __ldg(A.S + (r + vo[j]));
-						xv[u][j] = g.at(r + xo[j]);
+						a[u][j] = ld_stream(A.S + (r + vo[j]));
+						xv[u][j] = g.at_stream(r + xo[j]);
 					}
 			}
 		}
@@ -156,8 +158,8 @@ static inline int launch_spmv_sym(Ctx *ctx, const Csr *A, const G &g, const Epi 
 	CsrSym<V> d{sym_vals<V>(A), A->pid, A->stab, A->plen, (int)A->nrows, A->npat};
 	const int nstep = (int)((A->nrows + kSymThreads * kSymRows<V> - 1) / (kSymThreads * kSymRows<V>));
 	const int grid = std::max(1, std::min(nstep, ctx->sms * std::min(per_sm, 8)));
-	kern<<<grid, kSymThreads, smem, ctx->stream>>>(d, g, epi);
-	return check_launch(ctx, "spmv (symmetric row patterns)");
+	return check_launch_rc(ctx, launch_pdl(ctx->stream, kern, grid, kSymThreads, smem, d, g, epi),
+	                       "spmv (symmetric row patterns)");
 }
 
 }  // namespace fsg
