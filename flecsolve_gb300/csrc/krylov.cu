@@ -357,12 +357,13 @@ struct EpiCgFused {
 	}
 };
 
-// r -= alpha w; z = P r (stored when STOREZ); ||r||, r'z; replacement test
+// r -= alpha w; z = P r (stored); ||r||, r'z; replacement test
 // (the recurrence residual dropped by delta since the last replacement, or
 // below the tolerance, or maxiter) and beta.  The solution step xs += alpha p
 // of this iteration is left pending (alpha_x) for the kernel that next reads
-// p: the fused SpMV, or k_cg_dir_x.
-template<int PK, bool STOREZ = true>
+// p: the fused SpMV (k_rc_resid4 is the same update for the three-kernel
+// iteration, where k_cg_dir_x applies the step).
+template<int PK>
 __global__ void __launch_bounds__(kThreads)
 k_rc_resid(int64_t n, float *__restrict__ r, float *__restrict__ z, const float *__restrict__ w,
            const float *__restrict__ dinv, KState *st, double *part, unsigned *counter,
@@ -379,8 +380,7 @@ k_rc_resid(int64_t n, float *__restrict__ r, float *__restrict__ z, const float 
 		float ri = fmaf(-alpha, w[i], r[i]);
 		r[i] = ri;
 		float zi = PK ? dinv[i] * ri : ri;
-		if (STOREZ)
-			z[i] = zi;
+		z[i] = zi;
 		acc.add_prod(0, ri, ri);
 		acc.add_prod(1, ri, zi);
 	}
@@ -411,7 +411,9 @@ k_rc_resid(int64_t n, float *__restrict__ r, float *__restrict__ z, const float 
 
 // xs += alpha_x p (the pending solution step, cg.hh:108 in FP32); p = beta p
 // + z, z = P r (cg.hh:124-130).  A replacement folds the pending step into x
-// and clears alpha_x, so it is applied once.
+// and clears alpha_x, so it is applied once.  Four elements per thread and
+// pass (16-byte accesses; the solver's vectors and D^-1 are 16-byte aligned),
+// the last n mod 4 elements one by one.
 template<int PK>
 __global__ void __launch_bounds__(kThreads)
 k_cg_dir_x(int64_t n, float *__restrict__ p, const float *__restrict__ r,
@@ -422,11 +424,90 @@ k_cg_dir_x(int64_t n, float *__restrict__ p, const float *__restrict__ r,
 		return;
 	const float beta = (float)st->beta;
 	const float ax = (float)st->alpha_x;
-	FOR_EACH(i, n) {
-		const float po = p[i];
-		xs[i] = fmaf(ax, po, xs[i]);
-		const float zi = PK ? dinv[i] * r[i] : r[i];
-		p[i] = fmaf(beta, po, zi);
+	auto one = [&](float &pi, float ri, float di, float &xi) {
+		xi = fmaf(ax, pi, xi);
+		pi = fmaf(beta, pi, PK ? di * ri : ri);
+	};
+	const int64_t n4 = n >> 2;
+	float4 *p4 = reinterpret_cast<float4 *>(p), *x4 = reinterpret_cast<float4 *>(xs);
+	const float4 *r4 = reinterpret_cast<const float4 *>(r);
+	const float4 *d4 = reinterpret_cast<const float4 *>(dinv);
+	FOR_EACH(i, n4) {
+		float4 pv = p4[i], xv = x4[i];
+		const float4 rv = r4[i];
+		const float4 dv = PK ? __ldg(d4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+		one(pv.x, rv.x, dv.x, xv.x);
+		one(pv.y, rv.y, dv.y, xv.y);
+		one(pv.z, rv.z, dv.z, xv.z);
+		one(pv.w, rv.w, dv.w, xv.w);
+		p4[i] = pv;
+		x4[i] = xv;
+	}
+	for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+	     i += (int64_t)gridDim.x * blockDim.x)
+		one(p[i], r[i], PK ? dinv[i] : 0.f, xs[i]);
+}
+
+// r -= alpha w; z = P r; ||r||, r'z; replacement test and beta, as
+// k_rc_resid (without storing z), four elements per thread and pass
+template<int PK>
+__global__ void __launch_bounds__(kThreads)
+k_rc_resid4(int64_t n, float *__restrict__ r, const float *__restrict__ w,
+            const float *__restrict__ dinv, KState *st, double *part, unsigned *counter,
+            double *hist, double delta) {
+	__shared__ double sh[128];
+	pdl_wait();
+	pdl_trigger();
+	if (stopped(st))
+		return;
+	const float alpha = (float)st->alpha;
+	Acc<float, 2> acc;
+	acc.init();
+	auto one = [&](float &ri, float wi, float di) {
+		ri = fmaf(-alpha, wi, ri);
+		const float zi = PK ? di * ri : ri;
+		acc.add_prod(0, ri, ri);
+		acc.add_prod(1, ri, zi);
+	};
+	const int64_t n4 = n >> 2;
+	float4 *r4 = reinterpret_cast<float4 *>(r);
+	const float4 *w4 = reinterpret_cast<const float4 *>(w);
+	const float4 *d4 = reinterpret_cast<const float4 *>(dinv);
+	FOR_EACH(i, n4) {
+		float4 rv = r4[i];
+		const float4 wv = w4[i];
+		const float4 dv = PK ? __ldg(d4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+		one(rv.x, wv.x, dv.x);
+		one(rv.y, wv.y, dv.y);
+		one(rv.z, wv.z, dv.z);
+		one(rv.w, wv.w, dv.w);
+		r4[i] = rv;
+	}
+	for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+	     i += (int64_t)gridDim.x * blockDim.x)
+		one(r[i], w[i], PK ? dinv[i] : 0.f);
+	acc.to_part(part, sh);
+	if (last_block(counter)) {
+		double s[2];
+		sum_partials<2>(part, gridDim.x, s, sh);
+		if (threadIdx.x == 0) {
+			double res = sqrt(s[0]);
+			int it = st->iter + 1;
+			st->iter = it;
+			st->res = res;
+			if (it <= st->hist_cap)
+				hist[it - 1] = res;
+			if (!isfinite(res))
+				st->flags |= KF_NONFINITE;
+			if (res < delta * st->aux[1] || res < st->tol || it >= st->maxiter ||
+			    (st->flags & KF_NONFINITE))
+				st->flags |= KF_RELIABLE;
+			st->rho_old = st->rho;
+			st->rho = s[1];
+			st->beta = s[1] / st->rho_old;
+			st->alpha_x = st->alpha;
+			*counter = 0;
+		}
 	}
 }
 
@@ -1295,17 +1376,17 @@ static int rc_body(Solver *s, void *a) {
 	const int64_t n = s->n;
 	float *r = s->w32[0], *p = s->w32[1], *w = s->w32[2], *xs = s->w32[3];
 	const float *dinv = s->dinv32();
-	const int G = red_grid(ctx, n);
+	// four elements per thread and pass: a quarter of the grid
+	const int G4 = grid_for(ctx, (n + 3) / 4, kThreads, 8);
 	for (int k = 0; k < g->k; ++k) {
 		FS_TRY(launch_spmv<float, false, false>(
 			ctx, s->A, s->A->val32, p, nullptr,
 			EpiCgAp<float>{w, p, s->st, s->part, s->counter}));
 		FS_TRY(check_launch_rc(ctx,
-		                       launch_pdl(ctx->stream, k_rc_resid<PK, false>, G, kThreads, 0, n, r,
-		                                  (float *)nullptr, w, dinv, s->st, s->part, s->counter,
-		                                  s->hist, g->delta),
+		                       launch_pdl(ctx->stream, k_rc_resid4<PK>, G4, kThreads, 0, n, r, w, dinv,
+		                                  s->st, s->part, s->counter, s->hist, g->delta),
 		                       "reliable cg update"));
-		FS_TRY(check_launch_rc(ctx, launch_pdl(ctx->stream, k_cg_dir_x<PK>, G, kThreads, 0, n, p, r,
+		FS_TRY(check_launch_rc(ctx, launch_pdl(ctx->stream, k_cg_dir_x<PK>, G4, kThreads, 0, n, p, r,
 		                                       dinv, xs, (const KState *)s->st),
 		                       "cg direction f32"));
 	}
@@ -1417,10 +1498,11 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 			if (!fused) {
 				// the fused iteration forms the direction in its next SpMV;
 				// alpha_x is 0 here, so xs (cleared by the fold) stays 0
+				const int G4 = grid_for(ctx, (n + 3) / 4, kThreads, 8);
 				if (PK)
-					k_cg_dir_x<1><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, xs, s->st);
+					k_cg_dir_x<1><<<G4, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, xs, s->st);
 				else
-					k_cg_dir_x<0><<<G, kThreads, 0, ctx->stream>>>(n, p32, r32, nullptr, xs, s->st);
+					k_cg_dir_x<0><<<G4, kThreads, 0, ctx->stream>>>(n, p32, r32, nullptr, xs, s->st);
 				FS_TRY(check_launch(ctx, "cg direction f32"));
 			}
 			FS_TRY(read_state(s));
