@@ -137,13 +137,10 @@ def pcg_iter_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, kind="fp64"):
     (B_spmv: matrix data, p read once, w written once).
     * "fp64": update (read x, p, r, w, D^-1; write x, r) + direction (read p,
       r, D^-1; write p) = 11 N s_v.
-    * "reliable" (mixed, three kernels): residual update (read r, w, D^-1;
-      write r) + direction with the solution step (read p, r, D^-1, x; write
-      p, x) = 10 N s_v.
-    * "fused" (mixed, two kernels, row-pattern SpMV): the SpMV also reads z
-      and x and writes p and x; residual update (read r, w, D^-1; write r, z)
-      = 9 N s_v."""
-    extra = {"fp64": 11, "reliable": 10, "fused": 9}[kind]
+    * "reliable" (mixed): residual update (read r, w, D^-1; write r) +
+      direction with the solution step (read p, r, D^-1, x; write p, x) =
+      10 N s_v."""
+    extra = {"fp64": 11, "reliable": 10}[kind]
     return spmv_bytes(nrows, nnz, val_bytes, coding, nblk) + extra * nrows * val_bytes
 
 
@@ -480,7 +477,7 @@ def run_ours(args, ws, rank, local):
     gbs64 = b64 / (spmv64_ms * 1e-3) / 1e9
     gbs32 = b32 / (spmv32_ms * 1e-3) / 1e9
     # whole mixed iteration: two kernels when the SpMV stages windows
-    it_bytes = pcg_iter_bytes(n, nnz, 4, coding, dA.nblk(), "fused" if coding == 1 else "reliable")
+    it_bytes = pcg_iter_bytes(n, nnz, 4, coding, dA.nblk(), "reliable")
     it_s = ms_mx * 1e-3 / max(1, info_mx.iters)
 
     # e2e: through the public API with host buffers
@@ -551,7 +548,7 @@ def run_ours(args, ws, rank, local):
         "roofline_mixed_iteration": {"bytes_per_iteration": it_bytes, "s_per_iteration": it_s,
                                      "achieved": it_bytes / it_s / 1e9, "peak": peak,
                                      "frac": it_bytes / it_s / 1e9 / peak,
-                                     "kernels_per_iteration": 2 if coding == 1 else 3},
+                                     "kernels_per_iteration": 3},
         "e2e": {"value": e2e_ms * 1e-3, "unit": "s", "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 8 * n},
         "gpu_launches": launches_mx,

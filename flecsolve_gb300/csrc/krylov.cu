@@ -82,14 +82,11 @@ __global__ void k_copy(int64_t n, const V *__restrict__ s, V *__restrict__ d) {
 
 // z = P r (PK 0: identity, 1: diagonal); p = z; rho = z'r; res0 = ||r||
 // (cg.hh:75-90).  Early exit when res0 < tol (cg.hh:77-82).
-// With z2 (the fused iteration) z is also kept in z2, and the pending solution
-// step and the direction coefficient start at 0, so the first fused
-// direction update p = z + 0 p reproduces p = z.
+// The pending solution step of the reliable-update iteration starts at 0.
 template<class V, int PK>
 __global__ void __launch_bounds__(kThreads)
 k_cg_start(int64_t n, const V *__restrict__ r, const V *__restrict__ dinv,
-           V *__restrict__ p, KState *st, double *part, unsigned *counter,
-           V *__restrict__ z2 = nullptr) {
+           V *__restrict__ p, KState *st, double *part, unsigned *counter) {
 	__shared__ double sh[128];
 	Acc<V, 2> acc;
 	acc.init();
@@ -97,8 +94,6 @@ k_cg_start(int64_t n, const V *__restrict__ r, const V *__restrict__ dinv,
 		V ri = r[i];
 		V zi = PK ? dinv[i] * ri : ri;
 		p[i] = zi;
-		if (z2)
-			z2[i] = zi;
 		acc.add_prod(0, ri, ri);
 		acc.add_prod(1, zi, ri);
 	}
@@ -114,9 +109,7 @@ k_cg_start(int64_t n, const V *__restrict__ r, const V *__restrict__ dinv,
 			st->rho_old = s[1];
 			st->iter = 0;
 			st->flags = 0;
-			st->beta = 0.0;
 			st->alpha_x = 0.0;
-			st->pbuf = 0;
 			if (res < st->tol) {
 				st->done = 1;
 				st->status = FS_CONVERGED_RTOL;
@@ -275,7 +268,7 @@ __global__ void k_inner_init(KState *in, const KState *out, double inner_rtol, i
 // since the last replacement (or below the tolerance) the host folds xs into
 // the FP64 solution and replaces r by the FP64 true residual b - A x.  The
 // search direction is kept, so no Krylov information is lost.  One iteration
-// is three kernels: the SpMV with p'Ap, k_rc_resid (r -= alpha w, the dot
+// is three kernels: the SpMV with p'Ap, k_rc_resid4 (r -= alpha w, the dot
 // products, the replacement test) and k_cg_dir_x (the solution step
 // xs += alpha p and the direction update).
 
@@ -287,127 +280,7 @@ __global__ void k_rel_fold(int64_t n, double *__restrict__ x, float *__restrict_
 	}
 }
 
-// ----------------------------------------- fused reliable-update CG --
-//
-// Two kernels per iteration instead of three.  The direction update
-// p = z + beta p (cg.hh:124-130) and the solution update x += alpha p of the
-// previous iteration (cg.hh:108) move into the SpMV w = A p (cg.hh:94): the
-// row-pattern SpMV forms the new direction at every column it gathers from
-// the previous direction and z, applies the pending x update and stores p
-// for its own rows.  The second kernel updates
-// r -= alpha w, forms z = D^-1 r and the two dot products (cg.hh:109-123).
-// Blocks read the old direction while others write the new one, so the
-// direction alternates between two buffers (KState::pbuf).  Every value is
-// formed by the same operations as in the three-kernel iteration; only the
-// per-CTA grouping of the p'Ap partial sums follows the SpMV grid.
-
-// gather policy: the new direction at column c, p = z + beta p_old (k_cg_dir's
-// operation), from the previous direction and z; for the block's own rows also
-// the pending solution step xs += alpha_x p_old and the store of p
-template<class V>
-struct GatherCgDir {
-	static constexpr bool kOwn = true;
-	V *pa, *pb;             // the two direction buffers
-	const V *z;
-	V *xs;
-	const KState *st;
-	const V *p;             // set by init(): current direction
-	V *pout;                // the other buffer
-	V beta, alpha_x;
-	__device__ void init() {
-		const int cur = st->pbuf;
-		p = cur ? pb : pa;
-		pout = cur ? pa : pb;
-		beta = (V)st->beta;
-		alpha_x = (V)st->alpha_x;
-	}
-	__device__ V at(int c) const { return fma(beta, __ldg(p + c), __ldg(z + c)); }
-	__device__ V at_stream(int c) const { return fma(beta, ld_stream(p + c), ld_stream(z + c)); }
-	__device__ V own(int r) const {
-		const V po = __ldg(p + r);
-		const V pn = fma(beta, po, __ldg(z + r));
-		xs[r] = fma(alpha_x, po, xs[r]);
-		pout[r] = pn;
-		return pn;
-	}
-};
-
-// w = A p, p'Ap -> alpha (as EpiCgAp); the direction buffers swap
-struct EpiCgFused {
-	static constexpr int NV = 1;
-	float *w;
-	KState *st;
-	double *part;
-	unsigned *counter;
-	__device__ bool skip() const { return stopped(st); }
-	template<class A>
-	__device__ void row_own(int r, float s, float p, A &acc) const {
-		w[r] = s;
-		acc.add_prod(0, s, p);
-	}
-	template<class A>
-	__device__ void row(int, float, A &) const {}
-	__device__ void finish(const double *s) const {
-		double pap = s[0];
-		st->pAp = pap;
-		if (!(pap > 0.0))
-			st->flags |= KF_NEG_CURVATURE;
-		st->alpha = st->rho / pap;
-		st->pbuf ^= 1;
-	}
-};
-
-// r -= alpha w; z = P r (stored); ||r||, r'z; replacement test
-// (the recurrence residual dropped by delta since the last replacement, or
-// below the tolerance, or maxiter) and beta.  The solution step xs += alpha p
-// of this iteration is left pending (alpha_x) for the kernel that next reads
-// p: the fused SpMV (k_rc_resid4 is the same update for the three-kernel
-// iteration, where k_cg_dir_x applies the step).
-template<int PK>
-__global__ void __launch_bounds__(kThreads)
-k_rc_resid(int64_t n, float *__restrict__ r, float *__restrict__ z, const float *__restrict__ w,
-           const float *__restrict__ dinv, KState *st, double *part, unsigned *counter,
-           double *hist, double delta) {
-	__shared__ double sh[128];
-	pdl_wait();
-	pdl_trigger();
-	if (stopped(st))
-		return;
-	const float alpha = (float)st->alpha;
-	Acc<float, 2> acc;
-	acc.init();
-	FOR_EACH(i, n) {
-		float ri = fmaf(-alpha, w[i], r[i]);
-		r[i] = ri;
-		float zi = PK ? dinv[i] * ri : ri;
-		z[i] = zi;
-		acc.add_prod(0, ri, ri);
-		acc.add_prod(1, ri, zi);
-	}
-	acc.to_part(part, sh);
-	if (last_block(counter)) {
-		double s[2];
-		sum_partials<2>(part, gridDim.x, s, sh);
-		if (threadIdx.x == 0) {
-			double res = sqrt(s[0]);
-			int it = st->iter + 1;
-			st->iter = it;
-			st->res = res;
-			if (it <= st->hist_cap)
-				hist[it - 1] = res;
-			if (!isfinite(res))
-				st->flags |= KF_NONFINITE;
-			if (res < delta * st->aux[1] || res < st->tol || it >= st->maxiter ||
-			    (st->flags & KF_NONFINITE))
-				st->flags |= KF_RELIABLE;
-			st->rho_old = st->rho;
-			st->rho = s[1];
-			st->beta = s[1] / st->rho_old;
-			st->alpha_x = st->alpha;
-			*counter = 0;
-		}
-	}
-}
+// ------------------------------------------- reliable-update CG loop --
 
 // xs += alpha_x p (the pending solution step, cg.hh:108 in FP32); p = beta p
 // + z, z = P r (cg.hh:124-130).  A replacement folds the pending step into x
@@ -448,8 +321,11 @@ k_cg_dir_x(int64_t n, float *__restrict__ p, const float *__restrict__ r,
 		one(p[i], r[i], PK ? dinv[i] : 0.f, xs[i]);
 }
 
-// r -= alpha w; z = P r; ||r||, r'z; replacement test and beta, as
-// k_rc_resid (without storing z), four elements per thread and pass
+// r -= alpha w; z = P r; ||r||, r'z (cg.hh:109-123 in FP32, compensated
+// sums); replacement test (the recurrence residual dropped by delta since the
+// last replacement, or below the tolerance, or maxiter) and beta.  The
+// solution step xs += alpha p of this iteration is left pending (alpha_x)
+// for k_cg_dir_x, which reads p next.  Four elements per thread and pass.
 template<int PK>
 __global__ void __launch_bounds__(kThreads)
 k_rc_resid4(int64_t n, float *__restrict__ r, const float *__restrict__ w,
@@ -512,11 +388,9 @@ k_rc_resid4(int64_t n, float *__restrict__ r, const float *__restrict__ w,
 }
 
 // x64 += (xs + alpha_x p); xs = 0 -- the fold with the pending solution step
-// of the fused iteration (p = the current direction buffer)
+// of the last iteration
 __global__ void k_rel_fold_pending(int64_t n, double *__restrict__ x, float *__restrict__ xs,
-                                   const float *__restrict__ pa, const float *__restrict__ pb,
-                                   const KState *st) {
-	const float *p = st->pbuf ? pb : pa;
+                                   const float *__restrict__ p, const KState *st) {
 	const float a = (float)st->alpha_x;
 	FOR_EACH(i, n) {
 		x[i] += (double)fmaf(a, p[i], xs[i]);
@@ -529,16 +403,13 @@ __global__ void k_rel_fold_pending(int64_t n, double *__restrict__ x, float *__r
 template<int PK>
 __global__ void __launch_bounds__(kThreads)
 k_rel_finish(int64_t n, const float *__restrict__ r, const float *__restrict__ dinv, KState *st,
-             double *part, unsigned *counter, float *__restrict__ z = nullptr) {
+             double *part, unsigned *counter) {
 	__shared__ double sh[128];
 	Acc<float, 1> acc;
 	acc.init();
 	FOR_EACH(i, n) {
 		float ri = r[i];
-		float zi = PK ? dinv[i] * ri : ri;
-		if (z)
-			z[i] = zi;
-		acc.add_prod(0, ri, zi);
+		acc.add_prod(0, ri, PK ? dinv[i] * ri : ri);
 	}
 	acc.to_part(part, sh);
 	if (last_block(counter)) {
@@ -966,7 +837,7 @@ int solver_alloc(Solver *s) {
 	case FS_CG: nw64 = 3; break;
 	case FS_BICGSTAB: nw64 = 6; break;
 	case FS_GMRES: nw64 = 3; break;
-	case FS_CG_MIXED: nw64 = 1; nw32 = 6; break;
+	case FS_CG_MIXED: nw64 = 1; nw32 = 5; break;
 	case FS_BICGSTAB_MIXED: nw64 = 1; nw32 = 7; break;
 	case FS_GMRES_MIXED: nw64 = 3; nw32 = 3; break;
 	}
@@ -1393,37 +1264,6 @@ static int rc_body(Solver *s, void *a) {
 	return FS_OK;
 }
 
-// the fused two-kernel iteration runs on the row-pattern SpMV
-static bool cg_fusable(const Solver *s) {
-	return active_coding(s->A, true) == kCodingPatterns && s->w32[4] && s->w32[5];
-}
-
-template<int PK>
-static int rc_body_fused(Solver *s, void *a) {
-	RcArgs *g = (RcArgs *)a;
-	Ctx *ctx = s->ctx;
-	const int64_t n = s->n;
-	float *r = s->w32[0], *pa = s->w32[1], *w = s->w32[2], *xs = s->w32[3], *z = s->w32[4],
-	      *pb = s->w32[5];
-	const float *dinv = s->dinv32();
-	const int G = red_grid(ctx, n);
-	GatherCgDir<float> gd{pa, pb, z, xs, s->st, nullptr, nullptr, 0.f, 0.f};
-	const bool sym = active_coding(s->A, true) == kCodingSym;
-	for (int k = 0; k < g->k; ++k) {
-		if (sym)
-			FS_TRY((launch_spmv_sym<float, false>(ctx, s->A, gd,
-			                                      EpiCgFused{w, s->st, s->part, s->counter})));
-		else
-			FS_TRY((launch_spmv_pat<float, false>(ctx, s->A, s->A->val32, gd,
-			                                      EpiCgFused{w, s->st, s->part, s->counter})));
-		FS_TRY(check_launch_rc(ctx,
-		                       launch_pdl(ctx->stream, k_rc_resid<PK>, G, kThreads, 0, n, r, z, w, dinv,
-		                                  s->st, s->part, s->counter, s->hist, g->delta),
-		                       "reliable cg residual"));
-	}
-	return FS_OK;
-}
-
 // FP32 CG with FP64 reliable updates (residual replacement)
 static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	Ctx *ctx = s->ctx;
@@ -1449,15 +1289,13 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 			ctx, s->A, s->A->val, (const double *)x->d, nullptr,
 			EpiRelResidual{(const double *)b->d, r32, s->st, s->part, s->counter});
 	};
-	const bool fused = cg_fusable(s);
-	float *z32 = fused ? s->w32[4] : nullptr, *pb32 = s->w32[5];
 	FS_TRY(true_residual());
 	if (PK)
 		k_cg_start<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, p32, s->st, s->part,
-		                                                     s->counter, z32);
+		                                                     s->counter);
 	else
 		k_cg_start<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, p32, s->st, s->part,
-		                                                     s->counter, z32);
+		                                                     s->counter);
 	FS_TRY(check_launch(ctx, "cg start f32"));
 	FS_TRY(read_state(s));
 	const double res0 = s->hst->res0;
@@ -1473,13 +1311,11 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	int64_t seen = 0;
 	const int k = k_default(s) > 1 ? k_default(s) : 32;
 	RcArgs args{b, x, k, delta};
-	GraphKey key{b->d, x->d, (fused ? 3000 : 2000) + k * 2 + PK};
-	auto body = fused ? (PK ? rc_body_fused<1> : rc_body_fused<0>) : (PK ? rc_body<1> : rc_body<0>);
+	GraphKey key{b->d, x->d, 2000 + k * 2 + PK};
+	auto body = PK ? rc_body<1> : rc_body<0>;
 	auto fold = [&]() -> int {
-		// the last iteration's solution step is still pending in both
-		// iterations (p = the current direction)
-		k_rel_fold_pending<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs, p32,
-		                                                    fused ? pb32 : p32, s->st);
+		// the last iteration's solution step is still pending
+		k_rel_fold_pending<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs, p32, s->st);
 		return check_launch(ctx, "reliable fold");
 	};
 	while (!s->hst->done) {
@@ -1489,22 +1325,19 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 			FS_TRY(fold());
 			FS_TRY(true_residual());
 			if (PK)
-				k_rel_finish<1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, s->st, s->part, s->counter,
-				                                                z32);
+				k_rel_finish<1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, s->st, s->part, s->counter);
 			else
 				k_rel_finish<0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, s->st, s->part,
-				                                                s->counter, z32);
+				                                                s->counter);
 			FS_TRY(check_launch(ctx, "reliable finish"));
-			if (!fused) {
-				// the fused iteration forms the direction in its next SpMV;
-				// alpha_x is 0 here, so xs (cleared by the fold) stays 0
-				const int G4 = grid_for(ctx, (n + 3) / 4, kThreads, 8);
-				if (PK)
-					k_cg_dir_x<1><<<G4, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, xs, s->st);
-				else
-					k_cg_dir_x<0><<<G4, kThreads, 0, ctx->stream>>>(n, p32, r32, nullptr, xs, s->st);
-				FS_TRY(check_launch(ctx, "cg direction f32"));
-			}
+			// the direction from the replaced residual; alpha_x is 0 here, so
+			// xs (cleared by the fold) stays 0
+			const int G4 = grid_for(ctx, (n + 3) / 4, kThreads, 8);
+			if (PK)
+				k_cg_dir_x<1><<<G4, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, xs, s->st);
+			else
+				k_cg_dir_x<0><<<G4, kThreads, 0, ctx->stream>>>(n, p32, r32, nullptr, xs, s->st);
+			FS_TRY(check_launch(ctx, "cg direction f32"));
 			FS_TRY(read_state(s));
 		}
 		if (s->diag) {

@@ -32,7 +32,7 @@ struct KState {
 	double rho, rho_old, alpha, beta, omega, pAp;
 	double r_tilde_norm, s_norm, t_sq, t_s;
 	double aux[4];
-	double alpha_x;                   // fused CG: step of the pending x += alpha p
+	double alpha_x;                   // reliable CG: step of the pending xs += alpha p
 	int iter;                         // iterations completed (loop counter)
 	int done;                         // nonzero: stop
 	int status;                       // fs_stop_reason
@@ -42,7 +42,7 @@ struct KState {
 	int restarts;
 	int hist_cap;
 	int nhist;                        // history entries written
-	int pbuf;                         // fused CG: which buffer holds the direction
+	int pad_;
 };
 
 // GMRES least-squares state (gmres.cu): Hessenberg (column-major, ld = m+1),

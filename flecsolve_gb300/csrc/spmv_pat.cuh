@@ -20,10 +20,8 @@
 // error word and the CTA winds down; the producer waits (bounded) for its
 // copies in flight before the CTA exits.
 //
-// The x value of column c comes from a gather policy: x[c] (y = A x),
-// d[c] x[c] (y = A D x), or a value formed from several vectors (the fused CG
-// direction update, krylov.cu).  A policy with per-row work for the block's
-// own rows provides own(r); its result goes to the epilogue's row_own.
+// The x value of column c comes from a gather policy: x[c] (y = A x) or
+// d[c] x[c] (y = A D x).
 //
 // Every row sums the same products in the same order as spmv_rb_kernel (FMA,
 // or EXACT: rounded products summed left to right), so y is identical bit for
@@ -70,25 +68,21 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
 // y = A x
 template<class V>
 struct GatherX {
-	static constexpr bool kOwn = false;
 	const V *x;
 	__device__ void init() {}
 	__device__ V at(int c) const { return __ldg(x + c); }
 	// the same value, read with a 256-byte L2 fetch (contiguous sweeps)
 	__device__ V at_stream(int c) const { return ld_stream(x + c); }
-	__device__ V own(int) const { return V(0); }
 };
 
 // y = A D x (right Jacobi preconditioning without materialising D x); the
 // product is rounded once, as in the column-id kernel
 template<class V>
 struct GatherScale {
-	static constexpr bool kOwn = false;
 	const V *x, *d;
 	__device__ void init() {}
 	__device__ V at(int c) const { return mul_rn(__ldg(d + c), __ldg(x + c)); }
 	__device__ V at_stream(int c) const { return mul_rn(ld_stream(d + c), ld_stream(x + c)); }
-	__device__ V own(int) const { return V(0); }
 };
 
 // Issue the copies of row block `b` (bounds m) into stage `st`; the
@@ -223,10 +217,7 @@ spmv_pat_kernel(CsrPat<V> A, G g_in, Epi epi) {
 						else
 							sum = fma(a[j], xv[j], sum);
 					}
-				if constexpr (G::kOwn)
-					epi.row_own(r, sum, g.own(r), acc);
-				else
-					epi.row(r, sum, acc);
+				epi.row(r, sum, acc);
 			}
 			__syncwarp();
 			if (lane == 0)

@@ -19,8 +19,9 @@
 // from r in the storage (the diagonal, an upper diagonal at r, or an upper
 // diagonal at r - d) and of its column from r, so a row costs two adds, two
 // loads and one multiply-add per nonzero and sums the same products in the
-// same order as the CSR kernels: the results are identical bit for bit.  x comes from the same gather policies as the row-pattern
-// kernel (spmv_pat.cuh).
+// same order as the CSR kernels: the results are identical bit for bit.  x
+// comes from the same gather policies as the row-pattern kernel
+// (spmv_pat.cuh).
 #pragma once
 
 namespace fsg {
@@ -117,10 +118,7 @@ spmv_sym_kernel(CsrSym<V> A, G g_in, Epi epi) {
 					else
 						sum = fma(a[u][j], xv[u][j], sum);
 				}
-			if constexpr (G::kOwn)
-				epi.row_own(r, sum, g.own(r), acc);
-			else
-				epi.row(r, sum, acc);
+			epi.row(r, sum, acc);
 		}
 	}
 	if constexpr (NV > 0) {

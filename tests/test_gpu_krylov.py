@@ -195,13 +195,12 @@ def test_mixed_cg_refinement(ctx, wl):
 
 
 @pytest.mark.parametrize("wl", ["diffusion3d-40", "poisson2d-127", "diffusion3d-23"])
-def test_mixed_cg_fused_iteration(ctx, wl):
-    """On a stencil matrix the mixed CG runs two kernels per iteration (the
-    direction and solution updates fused into the symmetric-storage or
-    row-pattern SpMV); with column ids it runs the three-kernel iteration.
-    All follow the same recurrences: same stopping test, iteration counts
-    within one of each other and of the FP64 reference count, and the same
-    accuracy bar."""
+def test_mixed_cg_index_formats(ctx, wl):
+    """The mixed CG on a stencil matrix with each SpMV format (symmetric
+    storage, row patterns, column ids): the same recurrences, the same
+    stopping test, iteration counts within one of each other and of the FP64
+    reference count, the same accuracy bar; a user stop folds the pending
+    solution step into x."""
     A, b = P.workload(wl)
     ref64 = O.solve("cg", A, b, maxiter=20000, rtol=1e-8)
     xs = O.solve("cg", A, b, maxiter=20000, rtol=1e-14).x
