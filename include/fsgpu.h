@@ -152,13 +152,19 @@ FS_API int fs_csr_update_values(fs_csr A, const double *val);
 FS_API int fs_csr_update_values_device(fs_csr A, const double *dval);
 FS_API int fs_csr_values_device_ptr(fs_csr A, double **dval);
 /* Index coding (no counterpart in the reference; a storage choice of this
- * library).  When every row has at most 8 nonzeros and the matrix has at
- * most 256 distinct sequences of column offsets c - r (stencil operators),
- * fs_csr_create also stores one byte per row naming its sequence, and the
- * SpMV reads those instead of the 32-bit column ids; the results are
- * identical.  enable: 1 use the row patterns when present (the default), 0
- * read the column ids, -1 leave unchanged; *active (may be NULL) = 1 when
- * the pattern SpMV is in use. */
+ * library).  All formats give identical results.
+ *  0 column ids: 32-bit column id per nonzero.
+ *  1 row patterns: when every row has at most 8 nonzeros and the matrix has at
+ *    most 256 distinct sequences of column offsets c - r (stencil operators),
+ *    one byte per row names its sequence; neither column ids nor row offsets
+ *    are read.
+ *  2 symmetric storage (the default): row patterns of a square matrix whose
+ *    values are symmetric bit for bit are read from the diagonal and the upper
+ *    diagonals only (a(r, r-d) = a(r-d, r)).  Derived from the current values
+ *    and checked whenever they change; an asymmetric matrix uses format 1.
+ * enable: 0, 1 or 2 requests a format (a matrix falls back to the best format
+ * it supports), -1 leaves it unchanged; *active (may be NULL) = the format the
+ * FP64 SpMV uses now. */
 FS_API int fs_csr_index_coding(fs_csr A, int enable, int *active);
 /* number of SpMV row blocks (at most 256 rows and 1792 nonzeros each, a
  * longer row alone); no counterpart in the reference */
