@@ -40,6 +40,7 @@ constexpr int kSymThreads = 256;
 // for double (two would need ~100 registers)
 template<class V>
 constexpr int kSymRows = sizeof(V) == 4 ? 2 : 1;
+constexpr int kSymChunk = 4;  // consecutive steps per chunk
 
 template<class V, bool EXACT, class G, class Epi>
 __global__ void __launch_bounds__(kSymThreads)
@@ -62,13 +63,18 @@ spmv_sym_kernel(CsrSym<V> A, G g_in, Epi epi) {
 	__syncthreads();
 	Acc<V, NV> acc;
 	acc.init();
-	// kSymRows adjacent tiles per step, steps strided over the grid, so all
-	// CTAs work inside one moving window of the vectors (few pages in flight,
-	// neighbouring planes still in L2); a thread sums one row of each tile,
-	// and the pattern ids of its next step are loaded before this step's
-	// values
+	// kSymRows adjacent tiles per step; kSymChunk consecutive steps per chunk
+	// (the x and u values of neighbouring grid lines are then re-read out of
+	// L1); chunks strided over the grid, so all CTAs work inside one moving
+	// window of the vectors (few pages in flight, neighbouring planes in L2).
+	// A thread sums one row of each tile; the pattern ids of its next step
+	// are loaded before this step's values.
 	const int ntile = (A.n + kSymThreads - 1) / kSymThreads;
-	const int stride = (int)gridDim.x * kSymRows;
+	const int nstep = (ntile + kSymRows - 1) / kSymRows;
+	auto step_tile = [&](int k) -> int {  // first tile of this CTA's k-th step
+		const int chunk = (int)blockIdx.x + (k / kSymChunk) * (int)gridDim.x;
+		return (chunk * kSymChunk + k % kSymChunk) * kSymRows;
+	};
 	auto pid_at = [&](int t) -> int {
 		const int r = t * kSymThreads + threadIdx.x;
 		return t < ntile && r < A.n ? (int)ld_stream(A.pid + r) : -1;
@@ -76,13 +82,15 @@ spmv_sym_kernel(CsrSym<V> A, G g_in, Epi epi) {
 	int pnext[kSymRows];
 #pragma unroll
 	for (int u = 0; u < kSymRows; ++u)
-		pnext[u] = pid_at((int)blockIdx.x * kSymRows + u);
-	for (int t = (int)blockIdx.x * kSymRows; t < ntile; t += stride) {
+		pnext[u] = pid_at(step_tile(0) + u);
+	for (int k = 0; step_tile(k) < nstep * kSymRows; ++k) {
+		const int t = step_tile(k);
 		int pc[kSymRows];
+		const int tn = step_tile(k + 1);
 #pragma unroll
 		for (int u = 0; u < kSymRows; ++u) {
 			pc[u] = pnext[u];
-			pnext[u] = pid_at(t + stride + u);
+			pnext[u] = pid_at(tn + u);
 		}
 		V a[kSymRows][kPatW], xv[kSymRows][kPatW];
 		int len[kSymRows];
@@ -155,7 +163,8 @@ static inline int launch_spmv_sym(Ctx *ctx, const Csr *A, const G &g, const Epi 
 	}
 	CsrSym<V> d{sym_vals<V>(A), A->pid, A->stab, A->plen, (int)A->nrows, A->npat};
 	const int nstep = (int)((A->nrows + kSymThreads * kSymRows<V> - 1) / (kSymThreads * kSymRows<V>));
-	const int grid = std::max(1, std::min(nstep, ctx->sms * std::min(per_sm, 8)));
+	const int nchunk = (nstep + kSymChunk - 1) / kSymChunk;
+	const int grid = std::max(1, std::min(nchunk, ctx->sms * std::min(per_sm, 8)));
 	return check_launch_rc(ctx, launch_pdl(ctx->stream, kern, grid, kSymThreads, smem, d, g, epi),
 	                       "spmv (symmetric row patterns)");
 }
