@@ -33,6 +33,7 @@ struct CsrSym {
 	const int2 *__restrict__ tab;             // npat x kPatW {value offset, column offset}
 	const unsigned char *__restrict__ plen;
 	int n, npat;
+	int chunk;  // consecutive steps per chunk (1 .. kSymChunk)
 };
 
 constexpr int kSymThreads = 256;
@@ -40,7 +41,7 @@ constexpr int kSymThreads = 256;
 // for double (two would need ~100 registers)
 template<class V>
 constexpr int kSymRows = sizeof(V) == 4 ? 2 : 1;
-constexpr int kSymChunk = 4;  // consecutive steps per chunk
+constexpr int kSymChunk = 4;  // consecutive steps per chunk on large operators
 
 template<class V, bool EXACT, class G, class Epi>
 __global__ void __launch_bounds__(kSymThreads)
@@ -63,7 +64,7 @@ spmv_sym_kernel(CsrSym<V> A, G g_in, Epi epi) {
 	__syncthreads();
 	Acc<V, NV> acc;
 	acc.init();
-	// kSymRows adjacent tiles per step; kSymChunk consecutive steps per chunk
+	// kSymRows adjacent tiles per step; A.chunk consecutive steps per chunk
 	// (the x and u values of neighbouring grid lines are then re-read out of
 	// L1); chunks strided over the grid, so all CTAs work inside one moving
 	// window of the vectors (few pages in flight, neighbouring planes in L2).
@@ -72,8 +73,8 @@ spmv_sym_kernel(CsrSym<V> A, G g_in, Epi epi) {
 	const int ntile = (A.n + kSymThreads - 1) / kSymThreads;
 	const int nstep = (ntile + kSymRows - 1) / kSymRows;
 	auto step_tile = [&](int k) -> int {  // first tile of this CTA's k-th step
-		const int chunk = (int)blockIdx.x + (k / kSymChunk) * (int)gridDim.x;
-		return (chunk * kSymChunk + k % kSymChunk) * kSymRows;
+		const int chunk = (int)blockIdx.x + (k / A.chunk) * (int)gridDim.x;
+		return (chunk * A.chunk + k % A.chunk) * kSymRows;
 	};
 	auto pid_at = [&](int t) -> int {
 		const int r = t * kSymThreads + threadIdx.x;
@@ -161,10 +162,15 @@ static inline int launch_spmv_sym(Ctx *ctx, const Csr *A, const G &g, const Epi 
 			nb = 1;
 		per_sm = nb;
 	}
-	CsrSym<V> d{sym_vals<V>(A), A->pid, A->stab, A->plen, (int)A->nrows, A->npat};
+	// chunks of consecutive steps only on operators with at least kSymChunk
+	// steps per resident CTA; a smaller operator keeps one step per chunk
+	// (and its CTA grouping of the fused reductions)
 	const int nstep = (int)((A->nrows + kSymThreads * kSymRows<V> - 1) / (kSymThreads * kSymRows<V>));
-	const int nchunk = (nstep + kSymChunk - 1) / kSymChunk;
-	const int grid = std::max(1, std::min(nchunk, ctx->sms * std::min(per_sm, 8)));
+	const int resident = ctx->sms * std::min(per_sm, 8);
+	const int chunk = nstep >= kSymChunk * resident ? kSymChunk : 1;
+	const int nchunk = (nstep + chunk - 1) / chunk;
+	const int grid = std::max(1, std::min(nchunk, resident));
+	CsrSym<V> d{sym_vals<V>(A), A->pid, A->stab, A->plen, (int)A->nrows, A->npat, chunk};
 	return check_launch_rc(ctx, launch_pdl(ctx->stream, kern, grid, kSymThreads, smem, d, g, epi),
 	                       "spmv (symmetric row patterns)");
 }
