@@ -18,9 +18,10 @@ LIB_PATH = _build.BUILD / "libfsgpu.so"
 OK = 0
 STATUS_NAMES = {0: "ok", 1: "bad handle", 2: "size mismatch", 3: "out of memory",
                 4: "CUDA error", 5: "non-finite", 6: "breakdown", 7: "invalid argument",
-                8: "no device", 9: "unsupported"}
+                8: "no device", 9: "unsupported", 10: "file error"}
 ERR_BAD_HANDLE, ERR_SIZE_MISMATCH, ERR_OUT_OF_MEMORY, ERR_CUDA = 1, 2, 3, 4
 ERR_NON_FINITE, ERR_BREAKDOWN, ERR_INVALID_ARG, ERR_NO_DEVICE, ERR_UNSUPPORTED = 5, 6, 7, 8, 9
+ERR_IO = 10
 
 F64, F32 = 0, 1
 CG, BICGSTAB, GMRES, CG_MIXED, BICGSTAB_MIXED, GMRES_MIXED = 0, 1, 2, 3, 4, 5
@@ -119,6 +120,10 @@ _PROTOS = {
     "fs_csr_spmv_transpose": [_vp, _vp, _vp],
     "fs_csr_diag_inv": [_vp, _vp],
     "fs_parcsr_spmv": [_vp, C.c_int, _vp, _vp],
+    "fs_mm_read": [C.c_char_p, C.POINTER(_vp)],
+    "fs_mm_shape": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(C.c_int)],
+    "fs_mm_rows": [_vp, _i64, _i64, _vp, _vp, _vp, C.POINTER(_i64)],
+    "fs_mm_destroy": [_vp],
     "fs_krylov_settings_default": [C.POINTER(KrylovSettings)],
     "fs_krylov_create": [_vp, C.c_int, C.POINTER(KrylovSettings), _vp,
                          C.POINTER(Precond), C.POINTER(_vp)],

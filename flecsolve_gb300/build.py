@@ -31,8 +31,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr",
               "-I", str(INCLUDE), "-I", str(CSRC)]
 
-CU_SOURCES = ["context.cu", "vecops.cu", "spmv.cu", "krylov.cu", "gmres.cu",
-              "batched.cu", "blockcg.cu", "adjoint.cu", "noalloc.cu"]
+CU_SOURCES = ["context.cu", "spmv.cu", "krylov.cu", "gmres.cu", "batched.cu", "blockcg.cu",
+              "adjoint.cu", "noalloc.cu", "matrix_market.cu"]
 
 
 def _nvcc() -> str:

@@ -300,6 +300,7 @@ FS_API const char *fs_status_string(int s) {
 	case FS_ERR_INVALID_ARG: return "invalid argument";
 	case FS_ERR_NO_DEVICE: return "no CUDA device";
 	case FS_ERR_UNSUPPORTED: return "unsupported";
+	case FS_ERR_IO: return "file missing, unreadable or malformed";
 	default: return "unknown status";
 	}
 }

@@ -23,8 +23,10 @@
 // reference's flog_assert sites (FS_ERR_BREAKDOWN) raise too.
 #pragma once
 
+#include <array>
 #include <cmath>
 #include <cstdint>
+#include <iterator>
 #include <functional>
 #include <memory>
 #include <stdexcept>
@@ -395,6 +397,13 @@ public:
 		      ctx_, "fs_csr_create");
 	}
 	device_csr(device_csr &&o) noexcept : ctx_(o.ctx_), h_(o.h_) { o.h_ = nullptr; }
+	// from a host CSR as mat::io::matrix_market produces it
+	template<class H, class = decltype(std::declval<const H &>().rowptr)>
+	device_csr(const context &c, const H &A) : ctx_(c.get()) {
+		check(fs_csr_create(ctx_, (int64_t)A.nrows, (int64_t)A.ncols, (int64_t)A.val.size(),
+		                    A.rowptr.data(), A.col.data(), 8, A.val.data(), &h_),
+		      ctx_, "fs_csr_create");
+	}
 	device_csr(const device_csr &) = delete;
 	~device_csr() {
 		if (h_)
@@ -431,6 +440,85 @@ private:
 };
 
 using csr = op::core<device_csr>;
+
+// Host CSR as the reference's MatrixMarket reader produces it: int64 row
+// offsets and global column ids, double values.
+struct host_csr {
+	std::size_t nrows = 0, ncols = 0;
+	std::vector<int64_t> rowptr, col;
+	std::vector<double> val;
+	std::size_t rows() const { return nrows; }
+	std::size_t cols() const { return ncols; }
+};
+
+namespace io {
+
+// mat::io::matrix_market (flecsolve/matrices/io/matrix_market.hh:31-183) over
+// fs_mm_*: read(file).tocsr() for the whole matrix and definition(file)
+// .matrix(range) for a row range, with the reference reader's rules (float
+// rounding of values, "symmetric" mirroring, file order within rows).
+template<class scalar = double, class size = std::size_t>
+struct matrix_market {
+	class file {
+	public:
+		explicit file(const char *fname) {
+			const int st = fs_mm_read(fname, &h_);
+			if (st != FS_OK)
+				throw fs_error(st, std::string("matrix_market: cannot read ") + fname);
+		}
+		file(file &&o) noexcept : h_(o.h_) { o.h_ = nullptr; }
+		file(const file &) = delete;
+		~file() {
+			if (h_)
+				fs_mm_destroy(h_);
+		}
+		std::size_t num_rows() const { return shape()[0]; }
+		std::size_t num_cols() const { return shape()[1]; }
+		host_csr rows(std::size_t begin, std::size_t end) const {
+			host_csr A;
+			A.nrows = end - begin;
+			A.ncols = num_cols();
+			int64_t nz = 0;
+			check(fs_mm_rows(h_, (int64_t)begin, (int64_t)end, nullptr, nullptr, nullptr, &nz), nullptr,
+			      "fs_mm_rows");
+			A.rowptr.resize(A.nrows + 1);
+			A.col.resize((std::size_t)nz);
+			A.val.resize((std::size_t)nz);
+			check(fs_mm_rows(h_, (int64_t)begin, (int64_t)end, A.rowptr.data(), A.col.data(), A.val.data(),
+			                 nullptr),
+			      nullptr, "fs_mm_rows");
+			return A;
+		}
+		// coo::tocsr (matrices/seq.hh:324-352) of the whole file
+		host_csr tocsr() const { return rows(0, num_rows()); }
+
+	private:
+		std::array<int64_t, 2> shape() const {
+			int64_t r = 0, c = 0;
+			check(fs_mm_shape(h_, &r, &c, nullptr, nullptr), nullptr, "fs_mm_shape");
+			return {r, c};
+		}
+		fs_mm h_ = nullptr;
+	};
+
+	// matrix_market::read (matrix_market.hh:64-70)
+	static file read(const char *fname) { return file(fname); }
+
+	// matrix_market::definition (matrix_market.hh:103-165)
+	struct definition {
+		explicit definition(const char *fname) : f(fname) {}
+		std::size_t num_rows() const { return f.num_rows(); }
+		std::size_t num_cols() const { return f.num_cols(); }
+		// rows rng (contiguous), offsets relative to the first, global columns
+		template<class Range>
+		host_csr matrix(const Range &rng) const {
+			return f.rows((std::size_t)*std::begin(rng), (std::size_t)*std::begin(rng) + rng.size());
+		}
+		file f;
+	};
+};
+
+}  // namespace io
 
 }  // namespace mat
 

@@ -47,7 +47,8 @@ enum fs_status {
 	FS_ERR_BREAKDOWN = 6,      /* a solver hit a reference flog_assert      */
 	FS_ERR_INVALID_ARG = 7,    /* argument out of range                     */
 	FS_ERR_NO_DEVICE = 8,      /* no usable CUDA device                     */
-	FS_ERR_UNSUPPORTED = 9     /* valid request this build does not handle  */
+	FS_ERR_UNSUPPORTED = 9,    /* valid request this build does not handle  */
+	FS_ERR_IO = 10             /* file missing, unreadable or malformed     */
 };
 
 /* value types of vectors and matrix values */
@@ -68,6 +69,7 @@ typedef struct fs_ctx_s *fs_ctx;
 typedef struct fs_vec_s *fs_vec;
 typedef struct fs_csr_s *fs_csr;
 typedef struct fs_solver_s *fs_solver;
+typedef struct fs_mm_s *fs_mm;
 
 /* ----------------------------------------------------------- context --- */
 /* Replaces the FleCSI runtime/scheduler context the reference's vector ops
@@ -169,6 +171,35 @@ FS_API int fs_csr_index_coding(fs_csr A, int enable, int *active);
 /* number of SpMV row blocks (at most 256 rows and 1792 nonzeros each, a
  * longer row alone); no counterpart in the reference */
 FS_API int fs_csr_row_blocks(fs_csr A, int64_t *nblk);
+
+/* ---------------------------------------------- MatrixMarket input ----
+ * Host only: no context or device needed.  Reads a MatrixMarket coordinate
+ * file into CSR exactly as mat::io::matrix_market<double>::read(file)
+ * .tocsr() does (flecsolve/matrices/io/matrix_market.hh:31-123,
+ * coo::tocsr matrices/seq.hh:324-352):
+ *  - a "symmetric" anywhere in the header lines (also "skew-symmetric")
+ *    mirrors every off-diagonal entry with the same value, right after it;
+ *  - sizes are the atoi of the first three ' '-separated fields of the first
+ *    line not starting with '%';
+ *  - entries are ' '-separated "row col value" (1-based) read with
+ *    std::stoi / std::stof: values are rounded to float, then widened; a
+ *    missing value repeats the column field (the reference reads all three
+ *    fields into one string);
+ *  - rows keep the file order of their entries, duplicates included.
+ * A file the reference's reader throws on (an empty or non-numeric field, a
+ * value outside the float range, too few entry lines) returns FS_ERR_IO, as
+ * does a row or column id outside the matrix. */
+FS_API int fs_mm_read(const char *path, fs_mm *out);
+/* rows, columns, stored entries (after mirroring), symmetric flag */
+FS_API int fs_mm_shape(fs_mm m, int64_t *nrows, int64_t *ncols, int64_t *nnz, int *symmetric);
+/* Rows [row_begin, row_end) in CSR, as matrix_market::definition::matrix(range)
+ * cuts them (matrix_market.hh:126-156): rowptr (row_end - row_begin + 1
+ * entries) relative to the range's first entry, global column ids, values.
+ * Any array may be NULL; *nnz_out (may be NULL) = entries in the range.
+ * [0, nrows) is the whole matrix, ready for fs_csr_create (index_bytes 8). */
+FS_API int fs_mm_rows(fs_mm m, int64_t row_begin, int64_t row_end, int64_t *rowptr,
+                      int64_t *col, double *val, int64_t *nnz_out);
+FS_API int fs_mm_destroy(fs_mm m);
 
 /* SpMV modes */
 enum fs_spmv_mode {

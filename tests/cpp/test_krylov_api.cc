@@ -5,6 +5,7 @@
 // check; the exit status is the number of failures.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "flecsolve_gb300/flecsolve.hh"
@@ -208,6 +209,36 @@ int main() {
 			threw = e.status == FS_ERR_BREAKDOWN;
 		}
 		expect(threw, "gmres validate(): restart = false with maxiter > max_krylov_dim rejected");
+	}
+	{
+		// mat::io::matrix_market as the reference's tests load an operator
+		// (solvers/test/cg.cc reads SuiteSparse files the same way)
+		const char *fname = std::getenv("FS_MM_FIXTURE");
+		if (fname) {
+			auto A = mat::io::matrix_market<>::read(fname).tocsr();
+			mat::io::matrix_market<>::definition def(fname);
+			std::vector<std::size_t> rng(70);
+			for (std::size_t i = 0; i < rng.size(); ++i)
+				rng[i] = 50 + i;
+			auto part = def.matrix(rng);
+			expect(A.rows() == 216 && def.num_cols() == 216 && part.rows() == 70 &&
+			           part.rowptr.back() == A.rowptr[120] - A.rowptr[50],
+			       "matrix_market: read(...).tocsr() and definition::matrix(range)");
+			mat::csr dA(ctx, A);
+			vec::device_vec b(ctx, 216), x(ctx, 216);
+			b.set_scalar(1.0);
+			auto info = cg::solver(cg::settings{500, 1e-10f, 0.f, true}, cg::make_work(b))(op::ref(dA),
+			                                                                             jacobi)(b, x);
+			expect(info.success(), "cg on a MatrixMarket operator converged");
+			bool threw = false;
+			try {
+				mat::io::matrix_market<>::read("/nonexistent.mtx");
+			}
+			catch (const fs_error &e) {
+				threw = e.status == FS_ERR_IO;
+			}
+			expect(threw, "matrix_market: a missing file raises FS_ERR_IO");
+		}
 	}
 	std::printf("%d failure(s)\n", failures);
 	return failures;
