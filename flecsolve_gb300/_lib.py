@@ -56,11 +56,19 @@ class KrylovSettings(C.Structure):
                 ("inner_rtol", C.c_double), ("max_outer", C.c_int)]
 
 
+class NkaSettings(C.Structure):
+    _fields_ = [("base", SolverSettings), ("max_dim", C.c_int), ("angle_tol", C.c_double),
+                ("max_fun_evals", C.c_int), ("freeze_pc", C.c_int), ("use_qr", C.c_int),
+                ("use_damping", C.c_int), ("adaptive_damping", C.c_int),
+                ("damping_factor", C.c_double)]
+
+
 class Precond(C.Structure):
     _fields_ = [("kind", C.c_int), ("diag", C.c_void_p), ("op", C.c_void_p)]
 
 
 DIAG_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_double)
+RESIDUAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p)
 
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -120,6 +128,12 @@ _PROTOS = {
     "fs_csr_spmv_transpose": [_vp, _vp, _vp],
     "fs_csr_diag_inv": [_vp, _vp],
     "fs_parcsr_spmv": [_vp, C.c_int, _vp, _vp],
+    "fs_nka_settings_default": [C.POINTER(NkaSettings)],
+    "fs_nka_create": [_vp, C.POINTER(NkaSettings), _vp, RESIDUAL_FN, _vp, _vp, C.POINTER(_vp)],
+    "fs_nka_set_diagnostic": [_vp, DIAG_FN, _vp],
+    "fs_nka_apply": [_vp, _vp, _vp, C.POINTER(SolveInfo)],
+    "fs_nka_reset": [_vp],
+    "fs_nka_destroy": [_vp],
     "fs_mm_read": [C.c_char_p, C.POINTER(_vp)],
     "fs_mm_shape": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(C.c_int)],
     "fs_mm_rows": [_vp, _i64, _i64, _vp, _vp, _vp, C.POINTER(_i64)],

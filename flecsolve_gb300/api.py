@@ -704,3 +704,119 @@ gmres = _namespace(_lib.GMRES, 104, max_krylov_dim=-1, pre_side="right", restart
 mixed_cg = _namespace(_lib.CG_MIXED, 4)     # FP32 inner PCG in FP64 refinement
 mixed_bicgstab = _namespace(_lib.BICGSTAB_MIXED, 8)
 mixed_gmres = _namespace(_lib.GMRES_MIXED, 104, max_krylov_dim=-1, pre_side="right", restart=False)
+
+
+# ---------------------------------------------------------------- NKA --
+
+class NkaSolver:
+    """``op::core<op::nka<...>>`` (flecsolve/solvers/nka.hh:31-605):
+    apply(f, u) -> SolveInfo.  ``F`` is the CSR operator (or ``None`` with
+    ``residual(f, u, r)`` computing r = f - F(u) on device vectors for a
+    nonlinear operator); ``P`` a bound Krylov solver used as the
+    preconditioner (solvers/test/nka.cc:72-80 uses a CG solver), or ``None``.
+    The acceleration subspace persists across applies, as the reference's
+    does; :meth:`reset` empties it."""
+
+    def __init__(self, settings, F=None, P=None, diag=None, residual=None, ctx=None):
+        self.ctx = ctx or (F.ctx if F is not None else P.ctx)
+        self._keep = [F, P]
+        self._res_cb = None
+        if residual is not None:
+            ctxr = self.ctx
+
+            def _rcb(user, fh, uh, rh):
+                vs = []
+                for hnd in (fh, uh, rh):
+                    v = Vector.__new__(Vector)
+                    v.ctx = ctxr
+                    v.h = C.c_void_p(hnd)
+                    vs.append(v)
+                try:
+                    residual(*vs)
+                    return 0
+                except Exception:
+                    return _lib.ERR_INVALID_ARG
+                finally:
+                    for v in vs:
+                        v.h = None  # borrowed handles
+
+            self._res_cb = _lib.RESIDUAL_FN(_rcb)
+        h = C.c_void_p()
+        check(lib().fs_nka_create(self.ctx.h, C.byref(settings), F.h if F is not None else None,
+                                  self._res_cb or _lib.RESIDUAL_FN(), None,
+                                  P.h if P is not None else None, C.byref(h)),
+              self.ctx.h, "fs_nka_create")
+        self.h = h
+        self._diag_cb = None
+        if diag is not None:
+            ctx = self.ctx
+
+            def _cb(user, xh, res):
+                v = Vector.__new__(Vector)
+                v.ctx = ctx
+                v.h = C.c_void_p(xh)
+                try:
+                    return 1 if diag(v, res) else 0
+                finally:
+                    v.h = None
+
+            self._diag_cb = _lib.DIAG_FN(_cb)
+            check(lib().fs_nka_set_diagnostic(self.h, self._diag_cb, None), self.ctx.h)
+
+    def apply(self, f: Vector, u: Vector) -> SolveInfo:
+        info = _lib.SolveInfo()
+        st = lib().fs_nka_apply(self.h, f.h, u.h, C.byref(info))
+        out = _info(info)
+        if st != _lib.OK:
+            err = _lib.FsError(st, (lib().fs_last_error(self.ctx.h) or b"").decode())
+            err.info = out
+            raise err
+        return out
+
+    __call__ = apply
+
+    def reset(self):
+        check(lib().fs_nka_reset(self.h), self.ctx.h)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().fs_nka_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+def _nka_settings(maxiter=100, rtol=0.0, atol=0.0, use_zero_guess=False, max_dim=0,
+                  angle_tol=0.9, max_fun_evals=0, freeze_pc=True, use_qr=False,
+                  use_damping=False, adaptive_damping=False, damping_factor=1.0):
+    """nka::settings with the reference's option defaults (nka.hh:536-552)."""
+    s = _lib.NkaSettings()
+    check(lib().fs_nka_settings_default(C.byref(s)))
+    s.base = _lib.SolverSettings(int(maxiter), float(rtol), float(atol), int(bool(use_zero_guess)))
+    s.max_dim, s.angle_tol, s.max_fun_evals = int(max_dim), float(angle_tol), int(max_fun_evals)
+    s.freeze_pc, s.use_qr = int(bool(freeze_pc)), int(bool(use_qr))
+    s.use_damping, s.adaptive_damping = int(bool(use_damping)), int(bool(adaptive_damping))
+    s.damping_factor = float(damping_factor)
+    return s
+
+
+class _NkaFactory:
+    def __init__(self, settings, work):
+        self.settings = settings
+        self.work = work
+
+    def __call__(self, F, P=None, diag=None, residual=None, ctx=None) -> NkaSolver:
+        return NkaSolver(self.settings, F, P, diag, residual, ctx)
+
+    bind = __call__
+
+
+# nka::settings / make_work / solver (nka.hh:514-597); the work vectors
+# ((dim_bound + 1) * 2 + nwork) are owned by the bound solver
+nka = SimpleNamespace(
+    settings=_nka_settings,
+    make_work=lambda b, dim_bound=10: Work(len(b), 3 + 2 * (dim_bound + 1)),
+    solver=lambda settings, work=None: _NkaFactory(settings, work),
+    nwork=3)
+

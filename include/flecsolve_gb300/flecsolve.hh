@@ -565,6 +565,7 @@ public:
 		return solve_info::from(i);
 	}
 	solve_info operator()(const vec::device_vec &b, vec::device_vec &x) const { return apply(b, x); }
+	fs_solver handle() const { return h_; }
 
 private:
 	fs_ctx ctx_;
@@ -625,6 +626,86 @@ struct krylov_solver {
 
 // the Jacobi (D^-1) preconditioner computed from A on the device
 inline constexpr detail::jacobi_t jacobi{};
+
+// --------------------------------------------------------------- NKA ----
+//
+// nka::settings / make_work / solver (flecsolve/solvers/nka.hh:514-597) over
+// fs_nka_*: solver(settings, work)(A, op::ref(P)) with P a bound Krylov
+// solver used as the preconditioner, as solvers/test/nka.cc:72-80 binds it.
+namespace nka {
+static constexpr std::size_t nwork = 3;  // nka.hh:29
+// nka.hh:514-545 with the defaults of nka::options (nka.hh:536-552)
+struct settings : solver_settings {
+	int max_dim = 0;
+	double angle_tol = 0.9;
+	int max_fun_evals = 0;
+	bool freeze_pc = true;
+	bool use_qr = false;
+	bool use_damping = false;
+	bool adaptive_damping = false;
+	double damping_factor = 1.0;
+};
+template<std::size_t V>
+struct dim_bound_t {
+	static constexpr std::size_t value = V;
+};
+template<std::size_t V>
+inline constexpr dim_bound_t<V> dim_bound{};
+inline detail::work make_work(const vec::device_vec &b) { return {b.local_size()}; }
+template<std::size_t V>
+detail::work make_work(dim_bound_t<V>, const vec::device_vec &b) {
+	return {b.local_size()};
+}
+
+// op::core<op::nka<...>>: apply(f, u) -> solve_info
+class bound {
+public:
+	bound(const settings &s, const mat::csr &F, fs_solver P) : ctx_(F.ctx()) {
+		fs_nka_settings c;
+		fs_nka_settings_default(&c);
+		c.base.maxiter = s.maxiter;
+		c.base.rtol = s.rtol;
+		c.base.atol = s.atol;
+		c.base.use_zero_guess = s.use_zero_guess ? 1 : 0;
+		c.max_dim = s.max_dim;
+		c.angle_tol = s.angle_tol;
+		c.max_fun_evals = s.max_fun_evals;
+		c.freeze_pc = s.freeze_pc;
+		c.use_qr = s.use_qr;
+		c.use_damping = s.use_damping;
+		c.adaptive_damping = s.adaptive_damping;
+		c.damping_factor = s.damping_factor;
+		check(fs_nka_create(ctx_, &c, F.handle(), nullptr, nullptr, P, &h_), ctx_, "fs_nka_create");
+	}
+	bound(bound &&o) noexcept : ctx_(o.ctx_), h_(o.h_) { o.h_ = nullptr; }
+	bound(const bound &) = delete;
+	~bound() {
+		if (h_)
+			fs_nka_destroy(h_);
+	}
+	solve_info apply(const vec::device_vec &f, vec::device_vec &u) const {
+		fs_solve_info i{};
+		check(fs_nka_apply(h_, f.handle(), u.handle(), &i), ctx_, "fs_nka_apply");
+		return solve_info::from(i);
+	}
+	solve_info operator()(const vec::device_vec &f, vec::device_vec &u) const { return apply(f, u); }
+
+private:
+	fs_ctx ctx_;
+	fs_nka h_ = nullptr;
+};
+
+struct solver {
+	settings s;
+	detail::work workspace;
+	solver(settings st, detail::work w) : s(std::move(st)), workspace(w) {}
+	template<class PS>
+	bound operator()(const op::handle<mat::csr> &F, const op::handle<PS> &P) const {
+		return bound(s, F.get(), P.get().handle());
+	}
+	bound operator()(const op::handle<mat::csr> &F) const { return bound(s, F.get(), nullptr); }
+};
+}  // namespace nka
 
 namespace cg {
 static constexpr std::size_t nwork = 4;  // cg.hh:252

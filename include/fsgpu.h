@@ -70,6 +70,7 @@ typedef struct fs_vec_s *fs_vec;
 typedef struct fs_csr_s *fs_csr;
 typedef struct fs_solver_s *fs_solver;
 typedef struct fs_mm_s *fs_mm;
+typedef struct fs_nka_s *fs_nka;
 
 /* ----------------------------------------------------------- context --- */
 /* Replaces the FleCSI runtime/scheduler context the reference's vector ops
@@ -403,6 +404,43 @@ FS_API int fs_block_cg_solve_mixed(fs_ctx ctx, const fs_krylov_settings *s, fs_c
 #define FS_DOT_NOALLOC_MAX_N ((int64_t)67108864)
 FS_API int fs_dot_f64_noalloc(const double *x, const double *y, int64_t n,
                               double *result, void *stream);
+
+/* ------------------------------------------------------------- NKA ----
+ * Nonlinear Krylov accelerator (Carlson and Miller), op::nka of
+ * flecsolve/solvers/nka.hh:31-605, over device vectors.  Settings are
+ * nka::settings (nka.hh:518-545): the common solver settings (maxiter,
+ * rtol, atol, use_zero_guess) plus the acceleration controls. */
+typedef struct {
+	fs_solver_settings base;
+	int max_dim;            /* acceleration subspace dimension (> 0)            */
+	double angle_tol;       /* drop a vector whose factor diagonal <= angle_tol */
+	int max_fun_evals;      /* accepted, unused (as in the reference)           */
+	int freeze_pc;          /* accepted: a linear F's preconditioner is fixed   */
+	int use_qr;             /* not implemented (as in the reference)            */
+	int use_damping;
+	int adaptive_damping;   /* eta = 1 - 0.9^min(k, max_dim); needs use_damping */
+	double damping_factor;
+} fs_nka_settings;
+/* the reference's option defaults (nka.hh:536-552, solver_settings.hh:40-52);
+ * max_dim has none there and is set to 0 (must be set) */
+FS_API int fs_nka_settings_default(fs_nka_settings *s);
+/* r = f - F(u): the residual of a (nonlinear) operator, op::core::residual */
+typedef int (*fs_residual_fn)(void *user, fs_vec f, fs_vec u, fs_vec r);
+/* Bind NKA (nka::solver(settings, work)(F, P), nka.hh:587-597): F is a CSR
+ * operator, or NULL with `fres` for a nonlinear residual; P is a bound
+ * Krylov solver applied as the preconditioner (P.apply(res, correction):
+ * solvers/test/nka.cc:72-80 uses CG), or NULL for none.  The solver owns
+ * (max_dim + 1) * 2 + 3 work vectors.  Invalid settings return
+ * FS_ERR_BREAKDOWN (the reference asserts), use_qr FS_ERR_UNSUPPORTED. */
+FS_API int fs_nka_create(fs_ctx ctx, const fs_nka_settings *s, fs_csr F, fs_residual_fn fres,
+                         void *fres_user, fs_solver P, fs_nka *out);
+FS_API int fs_nka_set_diagnostic(fs_nka k, fs_diag_fn fn, void *user);
+/* op::nka::apply(f, u) (nka.hh:64-137).  The acceleration subspace persists
+ * across applies, as the reference's does; fs_nka_reset empties it.  A solve
+ * that runs out of iterations leaves status FS_STATUS_UNKNOWN and iters 0. */
+FS_API int fs_nka_apply(fs_nka k, fs_vec f, fs_vec u, fs_solve_info *info);
+FS_API int fs_nka_reset(fs_nka k);
+FS_API int fs_nka_destroy(fs_nka k);
 
 #ifdef __cplusplus
 }

@@ -6,3 +6,5 @@
 #include <stdexcept>
 #define flog(lvl) std::cerr << "[" #lvl "] "
 #define flog_assert(c, m) do { if(!(c)) { throw std::runtime_error(m); } } while(0)
+#define flog_warn(m) (std::cerr << "[warn] " << (m) << std::endl)
+#define flog_error(m) (std::cerr << "[error] " << (m) << std::endl)

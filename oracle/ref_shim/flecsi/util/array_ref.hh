@@ -25,4 +25,13 @@ template<class T, std::size_t D> struct mdcolex {
   T& operator()(std::size_t i, std::size_t j) const { return p[i + s[0]*j]; }
 };
 template<class T> struct iota_view { T b, e; iota_view(T b, T e):b(b),e(e){} };
+// 2-D view used by NKA's normal-equation matrix (solvers/nka.hh:468-484):
+// h[i] is row i, h[i][j] an element; only read back through the same view
+template<class T, std::size_t D> struct mdspan;
+template<class T> struct mdspan<T, 2> {
+  using size_type = std::size_t;
+  mdspan(T* p, std::array<size_type, 2> e) : p(p), e(e) {}
+  T* operator[](size_type i) const { return p + i * e[1]; }
+  T* p; std::array<size_type, 2> e;
+};
 }

@@ -211,6 +211,39 @@ int main() {
 		expect(threw, "gmres validate(): restart = false with maxiter > max_krylov_dim rejected");
 	}
 	{
+		// NKA with a CG preconditioner, bound as solvers/test/nka.cc:72-80
+		// binds it (b = 1, x0 = 3, the settings of solvers/test/nka.cfg), on
+		// the 64^2 Poisson operator: the reference takes 34 iterations
+		// (tests/golden/nka_golden.json)
+		host_csr H = diffusion(2, 64, false);
+		mat::csr A(ctx, H.n, H.n, H.rp, H.col, H.val);
+		vec::device_vec b(ctx, H.n), x(ctx, H.n);
+		b.set_scalar(1.);
+		x.set_scalar(3.);
+		cg::settings pre{11, 1e-9f, 1e-9f, true};
+		nka::settings nnl{};
+		nnl.maxiter = 100;
+		nnl.atol = 1e-6f;
+		nnl.max_dim = 5;
+		nnl.angle_tol = 0.2;
+		nnl.use_zero_guess = false;
+		auto P = cg::solver(pre, cg::make_work(b))(op::ref(A));
+		auto slv = nka::solver(nnl, nka::make_work(nka::dim_bound<5>, b))(op::ref(A), op::ref(P));
+		auto info = slv(b, x);
+		expect(info.status == solve_info::stop_reason::converged_atol && std::abs(info.iters - 34) <= 2,
+		       "nka + cg preconditioner on poisson2d-64: 34 +- 2 iterations");
+		nka::settings bad = nnl;
+		bad.max_dim = 0;
+		bool threw = false;
+		try {
+			nka::solver(bad, nka::make_work(b))(op::ref(A), op::ref(P));
+		}
+		catch (const fs_error &e) {
+			threw = e.status == FS_ERR_BREAKDOWN;
+		}
+		expect(threw, "nka settings::validate: max_dim = 0 rejected");
+	}
+	{
 		// mat::io::matrix_market as the reference's tests load an operator
 		// (solvers/test/cg.cc reads SuiteSparse files the same way)
 		const char *fname = std::getenv("FS_MM_FIXTURE");

@@ -21,4 +21,4 @@ def test_cpp_api_program():
     print(r.stdout)
     assert "FAIL" not in r.stdout
     assert r.returncode == 0, r.stdout
-    assert r.stdout.count("PASS") >= 18
+    assert r.stdout.count("PASS") >= 20
