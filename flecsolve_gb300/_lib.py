@@ -24,6 +24,7 @@ ERR_NON_FINITE, ERR_BREAKDOWN, ERR_INVALID_ARG, ERR_NO_DEVICE, ERR_UNSUPPORTED =
 ERR_IO = 10
 
 F64, F32 = 0, 1
+BC_NONE, BC_DIRICHLET, BC_NEUMANN = 0, 1, 2
 CG, BICGSTAB, GMRES, CG_MIXED, BICGSTAB_MIXED, GMRES_MIXED = 0, 1, 2, 3, 4, 5
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_DIAG, PRECOND_CSR = 0, 1, 2, 3
 LEFT, RIGHT = 0, 1
@@ -61,6 +62,16 @@ class NkaSettings(C.Structure):
                 ("max_fun_evals", C.c_int), ("freeze_pc", C.c_int), ("use_qr", C.c_int),
                 ("use_damping", C.c_int), ("adaptive_damping", C.c_int),
                 ("damping_factor", C.c_double)]
+
+
+class FvmMesh(C.Structure):
+    _fields_ = [("n", C.c_int64 * 3), ("box", (C.c_double * 2) * 3)]
+
+
+class FvmOperatorSettings(C.Structure):
+    _fields_ = [("mesh", FvmMesh), ("beta", C.c_double), ("alpha", C.c_double),
+                ("bc_kind", C.c_int * 6), ("bc_value", C.c_double * 6),
+                ("a_value", C.c_double), ("b_value", C.c_double)]
 
 
 class Precond(C.Structure):
@@ -134,6 +145,17 @@ _PROTOS = {
     "fs_nka_apply": [_vp, _vp, _vp, C.POINTER(SolveInfo)],
     "fs_nka_reset": [_vp],
     "fs_nka_destroy": [_vp],
+    "fs_fvm_geometry": [C.POINTER(FvmMesh), _dp, _dp, _dp],
+    "fs_fvm_boundary": [_vp, C.POINTER(FvmMesh), C.c_int, C.c_int, C.c_double, _vp],
+    "fs_fvm_coef_constant": [_vp, C.POINTER(FvmMesh), C.c_double, _vp, _vp, _vp],
+    "fs_fvm_coef_average": [_vp, C.POINTER(FvmMesh), _vp, _vp, _vp, _vp],
+    "fs_fvm_diffusion": [_vp, C.POINTER(FvmMesh), C.c_double, C.c_double, _vp, _vp, _vp, _vp, _vp,
+                         _vp],
+    "fs_fvm_pack": [_vp, C.POINTER(FvmMesh), _vp, _vp],
+    "fs_fvm_unpack": [_vp, C.POINTER(FvmMesh), _vp, _vp],
+    "fs_fvm_operator_create": [_vp, C.POINTER(FvmOperatorSettings), _vp, _vp, _vp, _vp,
+                               C.POINTER(_vp)],
+    "fs_fvm_operator_info": [_vp, C.POINTER(C.c_int), C.POINTER(_i64)],
     "fs_mm_read": [C.c_char_p, C.POINTER(_vp)],
     "fs_mm_shape": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(C.c_int)],
     "fs_mm_rows": [_vp, _i64, _i64, _vp, _vp, _vp, C.POINTER(_i64)],

@@ -28,11 +28,12 @@ INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr",
+              "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr",
               "-I", str(INCLUDE), "-I", str(CSRC)]
 
 CU_SOURCES = ["context.cu", "spmv.cu", "krylov.cu", "gmres.cu", "batched.cu", "blockcg.cu",
-              "adjoint.cu", "noalloc.cu", "matrix_market.cu", "nka.cu"]
+              "adjoint.cu", "noalloc.cu", "matrix_market.cu", "nka.cu", "fvm.cu"]
 
 
 def _nvcc() -> str:

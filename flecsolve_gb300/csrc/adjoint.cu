@@ -161,6 +161,7 @@ FS_API int fs_fv_assemble(fs_csr Ah, int dim, int64_t n, fs_vec facesh, double s
 	Vec *c = reinterpret_cast<Vec *>(facesh);
 	if (!ok_csr(A) || !ok_vec(c))
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_fv_assemble"));
 	Ctx *ctx = A->ctx;
 	if (dim != 2 && dim != 3)
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_fv_assemble: dim must be 2 or 3");
@@ -205,6 +206,7 @@ FS_API int fs_csr_value_grad(fs_csr Ah, fs_vec lamh, fs_vec xh, fs_vec gh) {
 	    *g = reinterpret_cast<Vec *>(gh);
 	if (!ok_csr(A) || !ok_vec(lam) || !ok_vec(x) || !ok_vec(g))
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_csr_value_grad"));
 	if (lam->n != A->nrows || x->n != A->ncols || g->n != A->nnz || lam->dtype != FS_F64 ||
 	    x->dtype != FS_F64 || g->dtype != FS_F64)
 		return set_err(A->ctx, FS_ERR_SIZE_MISMATCH, "fs_csr_value_grad: sizes do not match A");
@@ -221,6 +223,7 @@ FS_API int fs_csr_transpose(fs_csr Ah, fs_csr *out) {
 	Csr *A = reinterpret_cast<Csr *>(Ah);
 	if (!ok_csr(A) || !out)
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_csr_transpose"));
 	Ctx *ctx = A->ctx;
 	FS_TRY(ensure_transpose(A));
 	FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // the CSC value gather

@@ -278,6 +278,7 @@ extern "C" FS_API int fs_batch_cg_solve(fs_ctx h, const fs_krylov_settings *s, f
 	Vec *b = reinterpret_cast<Vec *>(bh), *x = reinterpret_cast<Vec *>(xh);
 	if (!ok_ctx(ctx) || !ok_csr(A) || !ok_vec(b) || !ok_vec(x) || !s || !sys_offsets || !infos)
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_batch_cg_solve"));
 	if (nsys < 1 || sys_offsets[0] != 0 || sys_offsets[nsys] != A->nrows || A->nrows != A->ncols ||
 	    b->n != A->nrows || x->n != A->nrows || b->dtype != FS_F64 || x->dtype != FS_F64)
 		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_batch_cg_solve: offsets/sizes do not match");

@@ -641,6 +641,7 @@ int block_cg_entry(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah, const fs_pr
 	Vec *B = reinterpret_cast<Vec *>(bh), *X = reinterpret_cast<Vec *>(xh);
 	if (!ok_ctx(ctx) || !ok_csr(A) || !ok_vec(B) || !ok_vec(X) || !s || !infos)
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "block_cg_entry"));
 	if (nrhs != kS)
 		return set_err(ctx, FS_ERR_UNSUPPORTED, "block CG: this build takes %d right-hand sides", kS);
 	const int64_t n = A->nrows;

@@ -69,6 +69,9 @@ constexpr int kCodingPatterns = 1;
 constexpr int kCodingSym = 2;   // row patterns + symmetric storage (diagonal, upper diagonals)
 constexpr int kMaxSym = 4;      // positive column offsets of the symmetric storage
 
+struct FvmOp;
+void destroy_fvm(FvmOp *op);
+
 struct Csr {
 	int magic = kMagicCsr;
 	Ctx *ctx = nullptr;
@@ -121,6 +124,9 @@ struct Csr {
 	bool t_valid = false;
 	bool t_vals_valid = false;
 	std::vector<int> h_rowptr; // host copy of offsets (parcsr splitting)
+	// matrix-free finite-volume operator (no rows, columns or values stored;
+	// only the operator applies and the Jacobi diagonal are available)
+	FvmOp *fvm = nullptr;
 };
 
 // index format an SpMV on A uses (the requested one, or the next one the
@@ -164,6 +170,13 @@ int set_err(Ctx *ctx, int status, const char *fmt, ...);
 	} while (0)
 
 int check_launch(Ctx *ctx, const char *what);
+
+// The calls that need stored rows, columns or values refuse a matrix-free
+// operator
+inline int reject_matrix_free(const Csr *A, const char *what) {
+	return A->fvm ? set_err(A->ctx, FS_ERR_INVALID_ARG, "%s: not available for a matrix-free operator", what)
+	              : FS_OK;
+}
 
 // Programmatic dependent launch: a kernel launched with launch_pdl may be
 // scheduled while the previous kernel on the stream is still finishing (its

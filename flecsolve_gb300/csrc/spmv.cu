@@ -333,6 +333,7 @@ __global__ void gather_kernel(int64_t n, const int *__restrict__ perm,
 
 int ensure_transpose(Csr *A) {
 	Ctx *ctx = A->ctx;
+	FS_TRY(reject_matrix_free(A, "transpose"));
 	if (!A->t_valid) {
 		const int64_t n = A->nrows, m = A->ncols, nnz = A->nnz;
 		std::vector<int> hcol(nnz);
@@ -559,6 +560,7 @@ FS_API int fs_csr_index_coding(fs_csr h, int enable, int *active) {
 	Csr *A = reinterpret_cast<Csr *>(h);
 	if (!ok_csr(A))
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_csr_index_coding"));
 	if (enable > kCodingSym)
 		return set_err(A->ctx, FS_ERR_INVALID_ARG, "fs_csr_index_coding: enable must be -1, 0, 1 or 2");
 	if (enable >= 0)
@@ -591,6 +593,7 @@ FS_API int fs_csr_destroy(fs_csr h) {
 	                (void *)A->t_blk, (void *)A->t_blkinfo})
 		if (p)
 			cudaFree(p);
+	destroy_fvm(A->fvm);
 	A->magic = 0;
 	delete A;
 	return FS_OK;
@@ -610,6 +613,7 @@ FS_API int fs_csr_update_values(fs_csr h, const double *val) {
 	Csr *A = reinterpret_cast<Csr *>(h);
 	if (!ok_csr(A))
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_csr_update_values"));
 	if (A->nnz > 0 && !val)
 		return FS_ERR_INVALID_ARG;
 	if (A->nnz > 0)
@@ -624,6 +628,7 @@ FS_API int fs_csr_update_values_device(fs_csr h, const double *dval) {
 	Csr *A = reinterpret_cast<Csr *>(h);
 	if (!ok_csr(A))
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_csr_update_values_device"));
 	if (A->nnz > 0 && !dval)
 		return FS_ERR_INVALID_ARG;
 	if (A->nnz > 0 && dval != A->val)
@@ -637,6 +642,7 @@ FS_API int fs_csr_values_device_ptr(fs_csr h, double **dval) {
 	Csr *A = reinterpret_cast<Csr *>(h);
 	if (!ok_csr(A) || !dval)
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_csr_values_device_ptr"));
 	*dval = A->val;
 	// the caller may write through the pointer: derived data is rebuilt
 	invalidate_values(A);
@@ -716,6 +722,7 @@ FS_API int fs_parcsr_spmv(fs_csr h, int parts, fs_vec xh, fs_vec yh) {
 	Vec *x = reinterpret_cast<Vec *>(xh), *y = reinterpret_cast<Vec *>(yh);
 	if (!ok_csr(A) || !ok_vec(x) || !ok_vec(y))
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_parcsr_spmv"));
 	Ctx *ctx = A->ctx;
 	if (parts < 1 || parts > A->nrows)
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_parcsr_spmv: parts must be in [1, nrows]");
@@ -734,6 +741,7 @@ FS_API int fs_csr_spmv_transpose(fs_csr h, fs_vec xh, fs_vec yh) {
 	Vec *x = reinterpret_cast<Vec *>(xh), *y = reinterpret_cast<Vec *>(yh);
 	if (!ok_csr(A) || !ok_vec(x) || !ok_vec(y))
 		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_csr_spmv_transpose"));
 	if (x->n != A->nrows || y->n != A->ncols || x->dtype != FS_F64 || y->dtype != FS_F64)
 		return set_err(A->ctx, FS_ERR_SIZE_MISMATCH, "fs_csr_spmv_transpose: FP64 vectors of A^T shape required");
 	if (x == y)

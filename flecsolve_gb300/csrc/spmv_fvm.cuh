@@ -1,0 +1,174 @@
+// Matrix-free finite-volume diffusion operator, applied where the solvers
+// apply a matrix.
+//
+// The operator is the reference's volume diffusion with its boundary
+// operators (flecsolve/physics/volume_diffusion/diffusion.hh:109-193,
+// physics/boundary/dirichlet.hh:49-63, physics/boundary/neumann.hh:49-74):
+//   v = -beta div(b grad u) + alpha vol a u
+// on the logical cells of an nx x ny x nz mesh, written as the sum of face
+// fluxes  f = t (u_hi - u_lo),  t = b (dA / dx)  per face.  A vector holds
+// the logical cells only (r = i + nx (j + ny k), the order of the reference
+// vectors' degrees of freedom); the boundary layer is not stored: a
+// neighbour outside the mesh is the ghost value the boundary operator would
+// have written, the Dirichlet value or, for a Neumann face, the cell's own
+// value minus (nd dx) q.  Per cell the kernel evaluates the same IEEE
+// operations in the same order as the reference's three tasks (flux, surface
+// sum, volume term), so v is identical bit for bit to the reference's apply
+// on a field with those boundary values.
+//
+// Face transmissibilities t are stored per axis in the reference's face
+// layout ((nz+1) x (ny+1) x (nx+1), [k][j][i], face i between cells i and
+// i + 1 of the padded cell index), or are one constant per axis.  One thread
+// per cell of a 256-cell segment of an x line, segments strided over a
+// persistent grid: neighbouring lines and planes are re-read from L1/L2, so
+// a sweep reads u, the three face arrays and a (when stored) about once.
+#pragma once
+
+namespace fsg {
+
+constexpr int kFvmThreads = 256;
+
+// face order of the boundary arrays: x low, x high, y low, y high, z low,
+// z high
+enum { kFvmBcNone = 0, kFvmBcDirichlet = 1, kFvmBcNeumann = 2 };
+
+template<class V>
+struct FvmDev {
+	const V *__restrict__ t[3];  // per axis face transmissibilities, or null
+	V tc[3];                     // ... the constant ones
+	const V *__restrict__ av;    // (alpha vol) a per logical cell, or null
+	V avc;                       // ... the constant
+	V neg_beta;                  // -beta
+	V ghost_val[6];              // Dirichlet: the value; Neumann: the shift
+	int ghost_kind[6];
+	int nx, ny, nz;
+};
+
+struct FvmOp {
+	int nx = 0, ny = 0, nz = 0;
+	double beta = 1.0, alpha = 0.0;
+	double dx[3] = {1, 1, 1}, dA[3] = {1, 1, 1}, vol = 1.0, c[3] = {1, 1, 1};  // c = dA / dx
+	int bc_kind[6] = {0, 0, 0, 0, 0, 0};
+	double bc_value[6] = {0, 0, 0, 0, 0, 0};
+	double ghost[6] = {0, 0, 0, 0, 0, 0};  // Dirichlet value or Neumann shift (nd dx) q
+	double tc[3] = {0, 0, 0};              // constant transmissibilities
+	double avc = 0.0;                      // constant (alpha vol) a
+	double *t64[3] = {nullptr, nullptr, nullptr};
+	float *t32[3] = {nullptr, nullptr, nullptr};
+	double *av64 = nullptr;
+	float *av32 = nullptr;
+	bool affine = false;  // a boundary term that does not vanish at u = 0
+	template<class V>
+	FvmDev<V> dev() const {
+		FvmDev<V> d;
+		for (int a = 0; a < 3; ++a) {
+			if constexpr (sizeof(V) == 8)
+				d.t[a] = t64[a];
+			else
+				d.t[a] = t32[a];
+			d.tc[a] = (V)tc[a];
+		}
+		if constexpr (sizeof(V) == 8)
+			d.av = av64;
+		else
+			d.av = av32;
+		d.avc = (V)avc;
+		d.neg_beta = (V)(-beta);
+		for (int f = 0; f < 6; ++f) {
+			d.ghost_kind[f] = bc_kind[f];
+			d.ghost_val[f] = (V)ghost[f];
+		}
+		d.nx = nx;
+		d.ny = ny;
+		d.nz = nz;
+		return d;
+	}
+};
+
+// the value of the boundary cell beyond face f of a cell whose value is u
+template<class V>
+__device__ __forceinline__ V fvm_ghost(const FvmDev<V> &A, int f, V u) {
+	return A.ghost_kind[f] == kFvmBcDirichlet ? A.ghost_val[f] : sub_rn(u, A.ghost_val[f]);
+}
+
+template<class V>
+__device__ __forceinline__ V fvm_t(const FvmDev<V> &A, int axis, int64_t idx) {
+	return A.t[axis] ? __ldg(A.t[axis] + idx) : A.tc[axis];
+}
+
+// v at logical cell (i, j, k), r its index, with u read through the gather
+template<class V, class G>
+__device__ __forceinline__ V fvm_cell(const FvmDev<V> &A, const G &g, int i, int j, int k, int r) {
+	const int nx = A.nx, ny = A.ny, nz = A.nz;
+	const int64_t fx = (int64_t)nx + 1, fxy = fx * (ny + 1);
+	const V uc = g.at(r);
+	const V uw = i > 0 ? g.at(r - 1) : fvm_ghost(A, 0, uc);
+	const V ue = i + 1 < nx ? g.at(r + 1) : fvm_ghost(A, 1, uc);
+	const V us = j > 0 ? g.at(r - nx) : fvm_ghost(A, 2, uc);
+	const V un = j + 1 < ny ? g.at(r + nx) : fvm_ghost(A, 3, uc);
+	const int64_t plane = (int64_t)nx * ny;
+	const V ud = k > 0 ? g.at(r - plane) : fvm_ghost(A, 4, uc);
+	const V uu = k + 1 < nz ? g.at(r + plane) : fvm_ghost(A, 5, uc);
+	// face indices in the padded face layout; the cell is (i+1, j+1, k+1)
+	const int64_t ix = ((int64_t)(k + 1) * (ny + 1) + (j + 1)) * fx + i;      // x face i, low
+	const int64_t iy = ((int64_t)(k + 1) * (ny + 1) + j) * fx + (i + 1);      // y face j, low
+	const int64_t iz = ((int64_t)k * (ny + 1) + (j + 1)) * fx + (i + 1);      // z face k, low
+	const V fx_hi = mul_rn(fvm_t(A, 0, ix + 1), sub_rn(ue, uc));
+	const V fx_lo = mul_rn(fvm_t(A, 0, ix), sub_rn(uc, uw));
+	const V fy_hi = mul_rn(fvm_t(A, 1, iy + fx), sub_rn(un, uc));
+	const V fy_lo = mul_rn(fvm_t(A, 1, iy), sub_rn(uc, us));
+	const V fz_hi = mul_rn(fvm_t(A, 2, iz + fxy), sub_rn(uu, uc));
+	const V fz_lo = mul_rn(fvm_t(A, 2, iz), sub_rn(uc, ud));
+	const V du = add_rn(add_rn(sub_rn(fx_hi, fx_lo), sub_rn(fy_hi, fy_lo)), sub_rn(fz_hi, fz_lo));
+	const V av = A.av ? __ldg(A.av + r) : A.avc;
+	return add_rn(mul_rn(A.neg_beta, du), mul_rn(av, uc));
+}
+
+template<class V, class G, class Epi>
+__global__ void __launch_bounds__(kFvmThreads)
+spmv_fvm_kernel(FvmDev<V> A, G g_in, Epi epi) {
+	constexpr int NV = Epi::NV;
+	__shared__ double red[128];
+	pdl_wait();
+	pdl_trigger();
+	if (epi.skip())
+		return;
+	G g = g_in;
+	g.init();
+	Acc<V, NV> acc;
+	acc.init();
+	const int segs = (A.nx + kFvmThreads - 1) / kFvmThreads;
+	const int64_t ntile = (int64_t)segs * A.ny * A.nz;
+	for (int64_t t = blockIdx.x; t < ntile; t += gridDim.x) {
+		const int line = (int)(t / segs), seg = (int)(t - (int64_t)line * segs);
+		const int i = seg * kFvmThreads + (int)threadIdx.x;
+		if (i < A.nx) {
+			const int j = line % A.ny, k = line / A.ny;
+			const int r = line * A.nx + i;
+			epi.row(r, fvm_cell(A, g, i, j, k, r), acc);
+		}
+	}
+	if constexpr (NV > 0) {
+		acc.to_part(epi.part, red);
+		if (last_block(epi.counter)) {
+			double sums[NV];
+			sum_partials<NV>(epi.part, gridDim.x, sums, red);
+			if (threadIdx.x == 0) {
+				epi.finish(sums);
+				*epi.counter = 0;
+			}
+		}
+	}
+}
+
+template<class V, class G, class Epi>
+static inline int launch_spmv_fvm(Ctx *ctx, const FvmOp *op, const G &g, const Epi &epi) {
+	const int segs = (op->nx + kFvmThreads - 1) / kFvmThreads;
+	const int64_t ntile = (int64_t)segs * op->ny * op->nz;
+	const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntile, (int64_t)ctx->sms * 8));
+	return check_launch_rc(ctx, launch_pdl(ctx->stream, spmv_fvm_kernel<V, G, Epi>, grid, kFvmThreads, 0,
+	                                       op->dev<V>(), g, epi),
+	                       "spmv (finite-volume stencil)");
+}
+
+}  // namespace fsg

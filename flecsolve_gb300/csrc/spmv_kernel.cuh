@@ -179,6 +179,8 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 
 // x gather, optionally scaled on the fly by a diagonal (y = A D x, used for
 // right Jacobi preconditioning without materialising D x)
@@ -420,6 +422,7 @@ static inline int launch_spmv_as(Ctx *ctx, const CsrDev<V> &d, const V *x, const
 
 #include "spmv_pat.cuh"
 #include "spmv_sym.cuh"
+#include "spmv_fvm.cuh"
 
 namespace fsg {
 
@@ -430,6 +433,12 @@ template<class V, bool EXACT, bool SCALE, class Epi>
 static inline int launch_spmv(Ctx *ctx, const Csr *A, const V *vals, const V *x,
                               const V *dscale, const Epi &epi) {
 	constexpr bool F32 = std::is_same_v<V, float>;
+	if (A->fvm) {  // matrix-free finite-volume operator
+		if constexpr (SCALE)
+			return launch_spmv_fvm<V>(ctx, A->fvm, GatherScale<V>{x, dscale}, epi);
+		else
+			return launch_spmv_fvm<V>(ctx, A->fvm, GatherX<V>{x}, epi);
+	}
 	const int coding = active_coding(A, F32);
 	const bool own_vals = vals == (F32 ? (const V *)A->val32 : (const V *)A->val);
 	if (coding == kCodingSym && own_vals) {

@@ -442,6 +442,81 @@ FS_API int fs_nka_apply(fs_nka k, fs_vec f, fs_vec u, fs_solve_info *info);
 FS_API int fs_nka_reset(fs_nka k);
 FS_API int fs_nka_destroy(fs_nka k);
 
+/* ------------------------------------------- finite-volume physics ----
+ * The structured-mesh physics operators of flecsolve/physics/: boundary
+ * operators, face-coefficient setters and the volume diffusion operator
+ *   v = -beta div(b grad u) + alpha vol a u
+ * (volume_diffusion/diffusion.hh:59-262), on the device.
+ *
+ * Mesh: n[0] x n[1] x n[2] (x, y, z) logical cells on the box [box[a][0],
+ * box[a][1]] per axis, with one layer of boundary cells on every side, as
+ * the reference's fvm_narray with boundary depth 1 (physics/test/
+ * test_setup.hh:47-74).  Spacing, face areas and cell volume follow the
+ * specialization (physics/specializations/fvm_narray.hh:233-289):
+ * dx = |hi - lo| / (n + 1).
+ *  - a cell field is (n[2]+2)(n[1]+2)(n[0]+2) doubles, [k][j][i] with i
+ *    fastest, logical cells 1..n per axis;
+ *  - a face field (one per axis) is (n[2]+1)(n[1]+1)(n[0]+1) doubles in the
+ *    same order; face i of an axis lies between cells i and i+1 of it;
+ *  - a vector of logical cells (the solvers' vectors) is n[0] n[1] n[2]
+ *    doubles or floats, i fastest (the reference vectors' degrees of
+ *    freedom).
+ * Every field is an FP64 fs_vec of the context's device. */
+enum {
+	FS_FVM_X_LOW = 0, FS_FVM_X_HIGH = 1, FS_FVM_Y_LOW = 2,
+	FS_FVM_Y_HIGH = 3, FS_FVM_Z_LOW = 4, FS_FVM_Z_HIGH = 5
+};
+enum { FS_BC_NONE = 0, FS_BC_DIRICHLET = 1, FS_BC_NEUMANN = 2 };
+typedef struct {
+	int64_t n[3];
+	double box[3][2];
+} fs_fvm_mesh;
+/* dx, face areas dA (normal_dA) and the cell volume of the mesh (any may be
+ * NULL) */
+FS_API int fs_fvm_geometry(const fs_fvm_mesh *m, double dx[3], double dA[3], double *volume);
+/* bc<dirichlet, axis, boundary> / bc<neumann, ...>::apply on the cell field
+ * u (boundary/dirichlet.hh:49-63: the boundary cells get `value`;
+ * boundary/neumann.hh:49-74: they get the neighbouring cell minus
+ * (nd dx) value, nd = +1 on a low face, -1 on a high one) */
+FS_API int fs_fvm_boundary(fs_ctx ctx, const fs_fvm_mesh *m, int face, int kind, double value, fs_vec u);
+/* coefficient<constant_coefficient> / coefficient<average_coefficient>::
+ * apply (volume_diffusion/coefficient.hh:84-177): the face fields get
+ * `value`, or the average 0.5 (u_hi + u_lo) of the cells either side */
+FS_API int fs_fvm_coef_constant(fs_ctx ctx, const fs_fvm_mesh *m, double value, fs_vec bx, fs_vec by,
+                                fs_vec bz);
+FS_API int fs_fvm_coef_average(fs_ctx ctx, const fs_fvm_mesh *m, fs_vec u, fs_vec bx, fs_vec by, fs_vec bz);
+/* diffusion::apply (diffusion.hh:83-107, 109-193): v on the logical cells
+ * from the cell fields a, u and the face fields b (its boundary cells are
+ * left as they are); the same values as the reference bit for bit */
+FS_API int fs_fvm_diffusion(fs_ctx ctx, const fs_fvm_mesh *m, double beta, double alpha, fs_vec a, fs_vec bx,
+                            fs_vec by, fs_vec bz, fs_vec u, fs_vec v);
+/* the logical cells of a cell field as a vector, and back */
+FS_API int fs_fvm_pack(fs_ctx ctx, const fs_fvm_mesh *m, fs_vec field, fs_vec x);
+FS_API int fs_fvm_unpack(fs_ctx ctx, const fs_fvm_mesh *m, fs_vec x, fs_vec field);
+
+/* Matrix-free operator: the expression op_expr(six boundary operators,
+ * a face coefficient, diffusion) as an operator on vectors of logical cells,
+ * returned as an fs_csr handle that stores no rows.  fs_csr_spmv,
+ * fs_csr_residual, fs_csr_diag_inv, fs_csr_shape, fs_csr_destroy and every
+ * Krylov solver (FP64, FP32 and mixed) accept it; the calls that need stored
+ * values (updates, transposes, index formats, parcsr, block and batched
+ * solves) return FS_ERR_INVALID_ARG.  Per cell the apply gives the values
+ * fs_fvm_diffusion gives on a field whose boundary cells the six boundary
+ * operators set.  A Dirichlet value or Neumann flux other than 0 makes the
+ * operator affine (A(0) != 0), as the reference's is. */
+typedef struct {
+	fs_fvm_mesh mesh;
+	double beta, alpha;
+	int bc_kind[6];      /* per face (FS_FVM_*): FS_BC_DIRICHLET or FS_BC_NEUMANN */
+	double bc_value[6];  /* boundary_value / flux_value                          */
+	double a_value;      /* the cell coefficient a when the field a is NULL      */
+	double b_value;      /* the face coefficient when the face fields are NULL   */
+} fs_fvm_operator_settings;
+FS_API int fs_fvm_operator_create(fs_ctx ctx, const fs_fvm_operator_settings *s, fs_vec a, fs_vec bx,
+                                  fs_vec by, fs_vec bz, fs_csr *out);
+/* whether the operator is affine, and its logical cells per axis */
+FS_API int fs_fvm_operator_info(fs_csr A, int *affine, int64_t n[3]);
+
 #ifdef __cplusplus
 }
 #endif

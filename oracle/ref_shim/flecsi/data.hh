@@ -14,3 +14,4 @@ namespace data { enum class layout { dense, single };
 template<class T, data::layout L = data::layout::dense> struct field;
 template<class T> struct topology;
 }
+namespace flecsi::topo { template<auto S> using id = std::size_t; }

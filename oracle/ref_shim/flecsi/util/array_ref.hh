@@ -24,7 +24,14 @@ template<class T, std::size_t D> struct mdcolex {
   mdcolex(T* p, std::array<std::size_t, D> s) : p(p), s(s) {}
   T& operator()(std::size_t i, std::size_t j) const { return p[i + s[0]*j]; }
 };
-template<class T> struct iota_view { T b, e; iota_view(T b, T e):b(b),e(e){} };
+template<class T> struct iota_view {
+  T b, e; iota_view(T b, T e):b(b),e(e){}
+  struct iterator { T v; T operator*() const { return v; } iterator& operator++() { ++v; return *this; }
+    bool operator!=(const iterator& o) const { return v != o.v; } };
+  iterator begin() const { return {b}; } iterator end() const { return {e}; }
+  std::size_t size() const { return e - b; } T front() const { return b; } T back() const { return e - 1; }
+};
+template<class R, class F> struct transform_view { transform_view(R, F) {} };
 // 2-D view used by NKA's normal-equation matrix (solvers/nka.hh:468-484):
 // h[i] is row i, h[i][j] an element; only read back through the same view
 template<class T, std::size_t D> struct mdspan;
