@@ -144,6 +144,14 @@ def pcg_iter_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, kind="fp64"):
     return spmv_bytes(nrows, nnz, val_bytes, coding, nblk) + extra * nrows * val_bytes
 
 
+def fvm_apply_bytes(n, val_bytes):
+    """Algorithmic bytes of one matrix-free finite-volume apply on an n^3 mesh
+    with face-coefficient fields: u read once, v written once, and each of
+    the three face-transmissibility arrays read once (n^2 (n+1) faces per
+    axis)."""
+    return val_bytes * (2 * n ** 3 + 3 * n * n * (n + 1))
+
+
 def _traffic_from_profiles(kernel_key):
     p = ROOT / "profiles" / "traffic.json"
     if p.exists():
@@ -249,7 +257,8 @@ def run_suite(args):
     (BiCGSTAB and GMRES(30), FP64 and mixed); 512 independent 2-D diffusion
     systems in one batched launch against the same solver run system by
     system on a sample; block CG on 16 right-hand sides of the 128^3
-    Laplacian against 16 separate solves; the adjoint gradient of
+    Laplacian against 16 separate solves; the diffusion3d-256 problem as the
+    matrix-free finite-volume operator (applies and PCG); the adjoint gradient of
     ||x - x_target||^2 at 128^3 and backward-Euler heat 64^3 x 200 steps
     differentiated with checkpoints every 20."""
     import flecsolve_gb300 as fs
@@ -370,6 +379,42 @@ def run_suite(args):
                 its.append(info.iters)
             res[name] = {"s": tot, "iters_max": max(its), "iters_sum": sum(its)}
         out["laplace3d-128x16"] = res
+    if want("fvm") or want("fvm-apply"):
+        # the matrix-free finite-volume operator on the diffusion3d-256
+        # problem: the generator's face coefficients as face fields, Dirichlet
+        # 0 on every face and dA/dx = 1 (box [0, n+1]^3) give the same
+        # operator as the assembled matrix
+        from flecsolve_gb300 import physics as ph
+        n = 256
+        A, b = P.workload(f"diffusion3d-{n}")
+        N = A.nrows
+        mesh = ph.fvm_mesh(ctx, (n, n, n), [(0.0, float(n + 1))] * 3)
+        fields = mesh.face_fields(P.faces_to_fields(n, P.faces_lognormal(3, n, seed=2)))
+        Amf = ph.op_expr(*[ph.bc(ph.dirichlet(0.0), f // 2, f % 2) for f in range(6)],
+                         ph.diffusion(mesh, None, fields, 1.0, 0.0)).matrix_free()
+        del fields
+        peak, peak_kind = _peaks()
+        res = {"rows": N, "problem": "diffusion3d-256 as a matrix-free operator (face fields, Dirichlet 0)"}
+        for dt, vbytes in (("f64", 8), ("f32", 4)):
+            ms = spmv_events_ms(fs, ctx, Amf, N, dt, reps=20)
+            nbytes = fvm_apply_bytes(n, vbytes)
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            res["apply_" + dt] = {"ms": ms, "gbs": gbs, "frac": gbs / peak, "peak": peak,
+                                  "peak_source": f"hbm_gbs of {peak_kind}", "algorithmic_bytes": nbytes}
+        S = A.to_scipy()
+        x = P.uniform(5, N)
+        y = fs.Vector(ctx, N)
+        Amf.apply(fs.Vector(ctx, x), y)
+        ref = S @ x
+        res["max_rel_diff_vs_matrix"] = float(np.abs(y.numpy() - ref).max() / np.abs(ref).max())
+        if want("fvm"):
+            vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, N)
+            for name, ns in (("pcg_fp64", fs.cg), ("pcg_mixed", fs.mixed_cg)):
+                slv = ns.solver(ns.settings(maxiter=20000, rtol=1e-8))(Amf, fs.op.jacobi)
+                s, info = _timed_solve(ctx, slv, vb, vx)
+                res[name] = {"s": s, "iters": info.iters, "status": info.status,
+                             "true_relres": _relres(S, b, vx.numpy())}
+        out["fvm-diffusion3d-256"] = res
     if want("adjoint"):
         n = 128
         system = ad.DiffusionSolve(ctx, 3, n, rtol=1e-8)

@@ -204,7 +204,7 @@ __global__ void k_fvm_dinv(FvmDev<double> A, double beta, double *__restrict__ d
 		const int64_t iy = ((int64_t)(k + 1) * (A.ny + 1) + j) * fx + (i + 1);
 		const int64_t iz = ((int64_t)k * (A.ny + 1) + (j + 1)) * fx + (i + 1);
 		auto tf = [&](int face, bool boundary, int axis, int64_t idx) {
-			return boundary && A.ghost_kind[face] == kFvmBcNeumann ? 0.0 : fvm_t(A, axis, idx);
+			return boundary && A.ghost_kind[face] == kFvmBcNeumann ? 0.0 : (A.t[axis] ? A.t[axis][idx] : A.tc[axis]);
 		};
 		const double sx = __dadd_rn(tf(0, i == 0, 0, ix), tf(1, i + 1 == A.nx, 0, ix + 1));
 		const double sy = __dadd_rn(tf(2, j == 0, 1, iy), tf(3, j + 1 == A.ny, 1, iy + fx));

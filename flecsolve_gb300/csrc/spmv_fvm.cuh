@@ -91,40 +91,51 @@ __device__ __forceinline__ V fvm_ghost(const FvmDev<V> &A, int f, V u) {
 	return A.ghost_kind[f] == kFvmBcDirichlet ? A.ghost_val[f] : sub_rn(u, A.ghost_val[f]);
 }
 
-template<class V>
-__device__ __forceinline__ V fvm_t(const FvmDev<V> &A, int axis, int64_t idx) {
-	return A.t[axis] ? __ldg(A.t[axis] + idx) : A.tc[axis];
+template<class V, bool TF>
+__device__ __forceinline__ V fvm_t(const FvmDev<V> &A, int axis, int idx) {
+	if constexpr (TF)
+		return __ldg(A.t[axis] + idx);
+	else
+		return A.tc[axis];
 }
 
-// v at logical cell (i, j, k), r its index, with u read through the gather
-template<class V, class G>
+// v at logical cell (i, j, k), r its index, with u read through the gather.
+// TF: face transmissibility fields (else constants); AV: a cell field of
+// (alpha vol) a (else a constant).  Indices fit in int (the cell field of the
+// mesh has fewer than 2^31 entries).
+template<class V, bool TF, bool AV, class G>
 __device__ __forceinline__ V fvm_cell(const FvmDev<V> &A, const G &g, int i, int j, int k, int r) {
 	const int nx = A.nx, ny = A.ny, nz = A.nz;
-	const int64_t fx = (int64_t)nx + 1, fxy = fx * (ny + 1);
+	const int fx = nx + 1, fxy = fx * (ny + 1), plane = nx * ny;
 	const V uc = g.at(r);
 	const V uw = i > 0 ? g.at(r - 1) : fvm_ghost(A, 0, uc);
 	const V ue = i + 1 < nx ? g.at(r + 1) : fvm_ghost(A, 1, uc);
 	const V us = j > 0 ? g.at(r - nx) : fvm_ghost(A, 2, uc);
 	const V un = j + 1 < ny ? g.at(r + nx) : fvm_ghost(A, 3, uc);
-	const int64_t plane = (int64_t)nx * ny;
 	const V ud = k > 0 ? g.at(r - plane) : fvm_ghost(A, 4, uc);
 	const V uu = k + 1 < nz ? g.at(r + plane) : fvm_ghost(A, 5, uc);
 	// face indices in the padded face layout; the cell is (i+1, j+1, k+1)
-	const int64_t ix = ((int64_t)(k + 1) * (ny + 1) + (j + 1)) * fx + i;      // x face i, low
-	const int64_t iy = ((int64_t)(k + 1) * (ny + 1) + j) * fx + (i + 1);      // y face j, low
-	const int64_t iz = ((int64_t)k * (ny + 1) + (j + 1)) * fx + (i + 1);      // z face k, low
-	const V fx_hi = mul_rn(fvm_t(A, 0, ix + 1), sub_rn(ue, uc));
-	const V fx_lo = mul_rn(fvm_t(A, 0, ix), sub_rn(uc, uw));
-	const V fy_hi = mul_rn(fvm_t(A, 1, iy + fx), sub_rn(un, uc));
-	const V fy_lo = mul_rn(fvm_t(A, 1, iy), sub_rn(uc, us));
-	const V fz_hi = mul_rn(fvm_t(A, 2, iz + fxy), sub_rn(uu, uc));
-	const V fz_lo = mul_rn(fvm_t(A, 2, iz), sub_rn(uc, ud));
+	const int ix = ((k + 1) * (ny + 1) + (j + 1)) * fx + i;  // x face i, low
+	const int iy = ix + 1 - fx;                               // y face j, low
+	const int iz = ix + 1 - fxy;                              // z face k, low
+	const V fx_hi = mul_rn(fvm_t<V, TF>(A, 0, ix + 1), sub_rn(ue, uc));
+	const V fx_lo = mul_rn(fvm_t<V, TF>(A, 0, ix), sub_rn(uc, uw));
+	const V fy_hi = mul_rn(fvm_t<V, TF>(A, 1, iy + fx), sub_rn(un, uc));
+	const V fy_lo = mul_rn(fvm_t<V, TF>(A, 1, iy), sub_rn(uc, us));
+	const V fz_hi = mul_rn(fvm_t<V, TF>(A, 2, iz + fxy), sub_rn(uu, uc));
+	const V fz_lo = mul_rn(fvm_t<V, TF>(A, 2, iz), sub_rn(uc, ud));
 	const V du = add_rn(add_rn(sub_rn(fx_hi, fx_lo), sub_rn(fy_hi, fy_lo)), sub_rn(fz_hi, fz_lo));
-	const V av = A.av ? __ldg(A.av + r) : A.avc;
+	V av;
+	if constexpr (AV)
+		av = __ldg(A.av + r);
+	else
+		av = A.avc;
 	return add_rn(mul_rn(A.neg_beta, du), mul_rn(av, uc));
 }
 
-template<class V, class G, class Epi>
+// One thread per cell of a 256-cell segment of an x line; CTAs stride over
+// the segments, the (segment, j, k) position advanced by additions only.
+template<class V, bool TF, bool AV, class G, class Epi>
 __global__ void __launch_bounds__(kFvmThreads)
 spmv_fvm_kernel(FvmDev<V> A, G g_in, Epi epi) {
 	constexpr int NV = Epi::NV;
@@ -138,14 +149,28 @@ spmv_fvm_kernel(FvmDev<V> A, G g_in, Epi epi) {
 	Acc<V, NV> acc;
 	acc.init();
 	const int segs = (A.nx + kFvmThreads - 1) / kFvmThreads;
-	const int64_t ntile = (int64_t)segs * A.ny * A.nz;
-	for (int64_t t = blockIdx.x; t < ntile; t += gridDim.x) {
-		const int line = (int)(t / segs), seg = (int)(t - (int64_t)line * segs);
+	const int G0 = (int)gridDim.x;
+	// position of tile blockIdx.x and the step G0 as (segment, j, k)
+	int seg = (int)blockIdx.x % segs, line = (int)blockIdx.x / segs;
+	int j = line % A.ny, k = line / A.ny;
+	const int dseg = G0 % segs, dline = G0 / segs;
+	const int dj = dline % A.ny, dk = dline / A.ny;
+	while (k < A.nz) {
 		const int i = seg * kFvmThreads + (int)threadIdx.x;
 		if (i < A.nx) {
-			const int j = line % A.ny, k = line / A.ny;
-			const int r = line * A.nx + i;
-			epi.row(r, fvm_cell(A, g, i, j, k, r), acc);
+			const int r = (k * A.ny + j) * A.nx + i;
+			epi.row(r, fvm_cell<V, TF, AV>(A, g, i, j, k, r), acc);
+		}
+		seg += dseg;
+		j += dj;
+		k += dk;
+		if (seg >= segs) {
+			seg -= segs;
+			++j;
+		}
+		if (j >= A.ny) {
+			j -= A.ny;
+			++k;
 		}
 	}
 	if constexpr (NV > 0) {
@@ -161,14 +186,24 @@ spmv_fvm_kernel(FvmDev<V> A, G g_in, Epi epi) {
 	}
 }
 
-template<class V, class G, class Epi>
-static inline int launch_spmv_fvm(Ctx *ctx, const FvmOp *op, const G &g, const Epi &epi) {
+template<class V, bool TF, bool AV, class G, class Epi>
+static inline int launch_spmv_fvm_as(Ctx *ctx, const FvmOp *op, const G &g, const Epi &epi) {
 	const int segs = (op->nx + kFvmThreads - 1) / kFvmThreads;
 	const int64_t ntile = (int64_t)segs * op->ny * op->nz;
 	const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntile, (int64_t)ctx->sms * 8));
-	return check_launch_rc(ctx, launch_pdl(ctx->stream, spmv_fvm_kernel<V, G, Epi>, grid, kFvmThreads, 0,
+	return check_launch_rc(ctx, launch_pdl(ctx->stream, spmv_fvm_kernel<V, TF, AV, G, Epi>, grid, kFvmThreads, 0,
 	                                       op->dev<V>(), g, epi),
 	                       "spmv (finite-volume stencil)");
+}
+
+template<class V, class G, class Epi>
+static inline int launch_spmv_fvm(Ctx *ctx, const FvmOp *op, const G &g, const Epi &epi) {
+	const bool tf = op->t64[0] != nullptr, av = op->av64 != nullptr;
+	if (tf)
+		return av ? launch_spmv_fvm_as<V, true, true>(ctx, op, g, epi)
+		          : launch_spmv_fvm_as<V, true, false>(ctx, op, g, epi);
+	return av ? launch_spmv_fvm_as<V, false, true>(ctx, op, g, epi)
+	          : launch_spmv_fvm_as<V, false, false>(ctx, op, g, epi);
 }
 
 }  // namespace fsg

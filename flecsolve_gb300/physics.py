@@ -199,14 +199,19 @@ class coefficient:
 
 class diffusion:
     """``diffusion<Vec>`` (volume_diffusion/diffusion.hh:209-250): applied to
-    (u, v), v = -beta div(b grad u) + alpha vol a u on the logical cells."""
+    (u, v), v = -beta div(b grad u) + alpha vol a u on the logical cells.
+    ``a`` is a cell field or a number (a field of that value)."""
 
-    def __init__(self, mesh: fvm_mesh, a: Vector, faces, beta: float = 1.0, alpha: float = 0.0):
-        self.mesh, self.a, self.faces = mesh, a, list(faces)
+    def __init__(self, mesh: fvm_mesh, a, faces, beta: float = 1.0, alpha: float = 0.0):
+        self.mesh, self.faces = mesh, list(faces)
+        self.a = a if isinstance(a, Vector) else None
+        self.a_value = 1.0 if isinstance(a, Vector) or a is None else float(a)
         self.beta, self.alpha = float(beta), float(alpha)
 
     def apply(self, u: Vector, v: Vector):
         m = self.mesh
+        if self.a is None:
+            self.a = m.cell_field(self.a_value)
         bx, by, bz = (f.h for f in self.faces)
         check(lib().fs_fvm_diffusion(m.ctx.h, C.byref(m._m), self.beta, self.alpha, self.a.h, bx, by, bz, u.h,
                                      v.h), m.ctx.h, "fs_fvm_diffusion")
@@ -253,6 +258,7 @@ class op_expr:
         s = _lib.FvmOperatorSettings()
         s.mesh = m._m
         s.beta, s.alpha = d.beta, d.alpha
+        s.a_value = d.a_value
         for f in range(6):
             s.bc_kind[f] = bcs[f].spec.kind
             s.bc_value[f] = bcs[f].spec.value
@@ -267,7 +273,8 @@ class op_expr:
             faces = None
         h = C.c_void_p()
         fh = [None, None, None] if faces is None else [f.h for f in faces]
-        check(lib().fs_fvm_operator_create(m.ctx.h, C.byref(s), d.a.h, fh[0], fh[1], fh[2], C.byref(h)),
+        ah = d.a.h if d.a is not None else None
+        check(lib().fs_fvm_operator_create(m.ctx.h, C.byref(s), ah, fh[0], fh[1], fh[2], C.byref(h)),
               m.ctx.h, "fs_fvm_operator_create")
         A = CSR(m.ctx, None, _handle=h)
         A.mesh = m

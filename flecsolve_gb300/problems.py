@@ -122,6 +122,21 @@ def faces_lognormal(dim: int, n: int, seed: int, sigma: float = 1.0,
     return (f, cells) if return_cells else f
 
 
+def faces_to_fields(n: int, faces: np.ndarray):
+    """The 3-D face coefficients of the generator's layout as the three face
+    fields of a finite-volume mesh with boundary layers ((n+1)^3 each,
+    [k][j][i]; x face f of a line between cells f and f+1 counting the
+    boundary cell): with dA/dx = 1 and Dirichlet 0 on every face the
+    diffusion operator on those fields is ``assemble_diffusion(3, n, faces)``."""
+    m = n * n * (n + 1)
+    cx, cy, cz = faces[:m], faces[m:2 * m], faces[2 * m:]
+    out = [np.zeros((n + 1, n + 1, n + 1)) for _ in range(3)]
+    out[0][1:, 1:, :] = cx.reshape(n, n, n + 1)
+    out[1][1:, :, 1:] = cy.reshape(n, n + 1, n)
+    out[2][:, 1:, 1:] = cz.reshape(n + 1, n, n)
+    return out
+
+
 def assemble_diffusion(dim: int, n: int, faces: np.ndarray, name: str = "") -> CSR:
     L = lib()
     N = int(L.fsp_grid_rows(dim, n))
