@@ -24,6 +24,7 @@
 #pragma once
 
 #include <array>
+#include <tuple>
 #include <cmath>
 #include <cstdint>
 #include <iterator>
@@ -397,6 +398,9 @@ public:
 		      ctx_, "fs_csr_create");
 	}
 	device_csr(device_csr &&o) noexcept : ctx_(o.ctx_), h_(o.h_) { o.h_ = nullptr; }
+	// takes ownership of an operator handle the library made (the
+	// matrix-free physics operator, physics::op_expr::matrix_free)
+	static device_csr adopt(fs_ctx c, fs_csr h) { return device_csr(c, h); }
 	// from a host CSR as mat::io::matrix_market produces it
 	template<class H, class = decltype(std::declval<const H &>().rowptr)>
 	device_csr(const context &c, const H &A) : ctx_(c.get()) {
@@ -430,6 +434,7 @@ public:
 	}
 
 private:
+	device_csr(fs_ctx c, fs_csr h) : ctx_(c), h_(h) {}
 	std::pair<std::size_t, std::size_t> shape() const {
 		int64_t r, c;
 		check(fs_csr_shape(h_, &r, &c, nullptr), ctx_, "shape");
@@ -749,5 +754,212 @@ using cg_solver = detail::krylov_solver<cg::settings, FS_CG_MIXED>;
 using bicgstab_solver = detail::krylov_solver<bicgstab::settings, FS_BICGSTAB_MIXED>;
 using gmres_solver = detail::krylov_solver<gmres::settings, FS_GMRES_MIXED>;
 }  // namespace mixed
+
+
+// ----------------------------------------------------------- physics ----
+// The structured-mesh physics operators of flecsolve/physics/ over device
+// fields (fs_fvm_* of fsgpu.h).  Spelled as the reference spells them, with
+// the mesh passed where the reference takes it from the field's topology:
+//   bc<dirichlet, x_axis, boundary_low>::create({1e-9}, m)
+//   coefficient<constant_coefficient>::create({1.0}, faces, m)
+//   diffusion::create({a, faces, beta, alpha}, m)
+//   op_expr(ops...).apply(u, v)  /  op_expr(ops...).matrix_free()
+namespace physics {
+
+enum axis { x_axis = 0, y_axis = 1, z_axis = 2 };
+enum domain { boundary_low = 0, boundary_high = 1 };
+
+// fvm_narray with boundary depth 1 on one color (physics/test/
+// test_setup.hh:47-74): cells with one boundary layer, faces (n+1)^3 per axis
+class fvm_mesh {
+public:
+	fvm_mesh(const context &c, std::array<int64_t, 3> extents,
+	         std::array<std::array<double, 2>, 3> box = {{{0.0, 1.0}, {0.0, 1.0}, {0.0, 1.0}}})
+		: ctx_(c.get()) {
+		for (int a = 0; a < 3; ++a) {
+			m_.n[a] = extents[(std::size_t)a];
+			m_.box[a][0] = box[(std::size_t)a][0];
+			m_.box[a][1] = box[(std::size_t)a][1];
+		}
+		check(fs_fvm_geometry(&m_, dx_, dA_, &vol_), ctx_, "fs_fvm_geometry");
+	}
+	const fs_fvm_mesh &get() const { return m_; }
+	fs_ctx ctx() const { return ctx_; }
+	std::size_t cells() const { return (std::size_t)((m_.n[0] + 2) * (m_.n[1] + 2) * (m_.n[2] + 2)); }
+	std::size_t faces() const { return (std::size_t)((m_.n[0] + 1) * (m_.n[1] + 1) * (m_.n[2] + 1)); }
+	std::size_t dofs() const { return (std::size_t)(m_.n[0] * m_.n[1] * m_.n[2]); }
+	double dx(axis a) const { return dx_[a]; }
+	double normal_dA(axis a) const { return dA_[a]; }
+	double volume() const { return vol_; }
+	vec::device_vec cell_field(const context &c, double v = 0.0) const {
+		vec::device_vec f(c, cells());
+		f.set_scalar(v);
+		return f;
+	}
+	std::array<vec::device_vec, 3> face_fields(const context &c, double v = 0.0) const {
+		std::array<vec::device_vec, 3> out{vec::device_vec(c, faces()), vec::device_vec(c, faces()),
+		                                   vec::device_vec(c, faces())};
+		for (auto &f : out)
+			f.set_scalar(v);
+		return out;
+	}
+	// the logical cells of a cell field as a vector (i fastest), and back
+	void pack(const vec::device_vec &field, vec::device_vec &x) const {
+		check(fs_fvm_pack(ctx_, &m_, field.handle(), x.handle()), ctx_, "fs_fvm_pack");
+	}
+	void unpack(const vec::device_vec &x, vec::device_vec &field) const {
+		check(fs_fvm_unpack(ctx_, &m_, x.handle(), field.handle()), ctx_, "fs_fvm_unpack");
+	}
+
+private:
+	fs_ctx ctx_;
+	fs_fvm_mesh m_{};
+	double dx_[3], dA_[3], vol_ = 0.0;
+};
+
+// operator_parameters<dirichlet<Vec>> / <neumann<Vec>>
+// (boundary/dirichlet.hh:35-38, boundary/neumann.hh:31-34)
+struct dirichlet {
+	double boundary_value = 0.0;
+	static constexpr int kind = FS_BC_DIRICHLET;
+	double value() const { return boundary_value; }
+};
+struct neumann {
+	double flux_value = 0.0;
+	static constexpr int kind = FS_BC_NEUMANN;
+	double value() const { return flux_value; }
+};
+
+// bc<Spec, Axis, Boundary> (boundary/bc_base.hh:29-57)
+template<class Spec, int Axis, int Boundary>
+struct bc {
+	Spec params;
+	const fvm_mesh *m;
+	static constexpr int face = 2 * Axis + Boundary;
+	static bc create(Spec p, const fvm_mesh &mesh) { return bc{p, &mesh}; }
+	void apply(vec::device_vec &u, vec::device_vec &) const {
+		check(fs_fvm_boundary(m->ctx(), &m->get(), face, Spec::kind, params.value(), u.handle()), m->ctx(),
+		      "fs_fvm_boundary");
+	}
+};
+
+// operator_parameters<constant_coefficient> / <average_coefficient>
+// (volume_diffusion/coefficient.hh:66-71, 119-123)
+struct constant_coefficient {
+	double coeff_value = 1.0;
+};
+struct average_coefficient {
+	double dummy_value = 1.0;
+};
+
+// coefficient<Spec, Vec> (coefficient.hh:47-61): sets the face fields
+template<class Spec>
+struct coefficient {
+	Spec params;
+	std::array<vec::device_vec, 3> *faces;
+	const fvm_mesh *m;
+	static coefficient create(Spec p, std::array<vec::device_vec, 3> &f, const fvm_mesh &mesh) {
+		return coefficient{p, &f, &mesh};
+	}
+	void apply(vec::device_vec &u, vec::device_vec &) const {
+		auto &f = *faces;
+		if constexpr (std::is_same_v<Spec, average_coefficient>)
+			check(fs_fvm_coef_average(m->ctx(), &m->get(), u.handle(), f[0].handle(), f[1].handle(),
+			                          f[2].handle()),
+			      m->ctx(), "fs_fvm_coef_average");
+		else
+			check(fs_fvm_coef_constant(m->ctx(), &m->get(), params.coeff_value, f[0].handle(), f[1].handle(),
+			                           f[2].handle()),
+			      m->ctx(), "fs_fvm_coef_constant");
+	}
+};
+
+// diffusion<Vec> (volume_diffusion/diffusion.hh:209-250):
+// v = -beta div(b grad u) + alpha vol a u on the logical cells
+struct diffusion {
+	struct params {
+		vec::device_vec *a;
+		std::array<vec::device_vec, 3> *faces;
+		double beta = 1.0, alpha = 0.0;
+	};
+	params p;
+	const fvm_mesh *m;
+	static diffusion create(params p, const fvm_mesh &mesh) { return diffusion{p, &mesh}; }
+	void apply(vec::device_vec &u, vec::device_vec &v) const {
+		auto &f = *p.faces;
+		check(fs_fvm_diffusion(m->ctx(), &m->get(), p.beta, p.alpha, p.a->handle(), f[0].handle(),
+		                       f[1].handle(), f[2].handle(), u.handle(), v.handle()),
+		      m->ctx(), "fs_fvm_diffusion");
+	}
+};
+
+namespace detail {
+// what matrix_free collects from the expression's operators
+struct mf_parts {
+	fs_fvm_operator_settings s{};
+	int nbc = 0, ncoef = 0, ndiff = 0;
+	bool constant = false;
+	const diffusion *d = nullptr;
+};
+template<class Spec, int Axis, int Boundary>
+void collect(mf_parts &c, const bc<Spec, Axis, Boundary> &o) {
+	c.s.bc_kind[o.face] = Spec::kind;
+	c.s.bc_value[o.face] = o.params.value();
+	++c.nbc;
+}
+template<class Spec>
+void collect(mf_parts &c, const coefficient<Spec> &o) {
+	if constexpr (std::is_same_v<Spec, average_coefficient>)
+		check(FS_ERR_INVALID_ARG, nullptr, "matrix_free: an average coefficient is nonlinear");
+	else {
+		c.s.b_value = o.params.coeff_value;
+		c.constant = true;
+	}
+	++c.ncoef;
+}
+inline void collect(mf_parts &c, const diffusion &o) {
+	c.d = &o;
+	c.s.beta = o.p.beta;
+	c.s.alpha = o.p.alpha;
+	++c.ndiff;
+}
+}  // namespace detail
+
+// op_expr(multivariable<...>, ops...) (expressions/operator_expression.hh:
+// 55-143): applies its operators in order
+template<class... Ops>
+struct op_expr_t {
+	std::tuple<Ops...> ops;
+	void apply(vec::device_vec &u, vec::device_vec &v) const {
+		std::apply([&](const auto &...o) { (o.apply(u, v), ...); }, ops);
+	}
+	// the expression (one boundary operator per face, at most one constant
+	// coefficient setter, one diffusion operator) as an operator on vectors
+	// of logical cells for the Krylov solvers
+	mat::csr matrix_free() const {
+		detail::mf_parts c;
+		std::apply([&](const auto &...o) { (detail::collect(c, o), ...); }, ops);
+		if (c.nbc != 6 || c.ndiff != 1 || c.ncoef > 1)
+			check(FS_ERR_INVALID_ARG, nullptr, "matrix_free: six boundary operators, one diffusion");
+		for (int f = 0; f < 6; ++f)
+			if (c.s.bc_kind[f] == FS_BC_NONE)
+				check(FS_ERR_INVALID_ARG, nullptr, "matrix_free: one boundary operator per face");
+		const fvm_mesh *m = c.d->m;
+		c.s.mesh = m->get();
+		auto &f = *c.d->p.faces;
+		fs_csr h = nullptr;
+		check(fs_fvm_operator_create(m->ctx(), &c.s, c.d->p.a->handle(), c.constant ? nullptr : f[0].handle(),
+		                             c.constant ? nullptr : f[1].handle(), c.constant ? nullptr : f[2].handle(),
+		                             &h),
+		      m->ctx(), "fs_fvm_operator_create");
+		return mat::csr(mat::device_csr::adopt(m->ctx(), h));
+	}
+};
+template<class... Ops>
+op_expr_t<Ops...> op_expr(Ops... ops) {
+	return {std::tuple<Ops...>(std::move(ops)...)};
+}
+
+}  // namespace physics
 
 }  // namespace flecsolve

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "flecsolve_gb300/flecsolve.hh"
@@ -272,6 +273,59 @@ int main() {
 			}
 			expect(threw, "matrix_market: a missing file raises FS_ERR_IO");
 		}
+	}
+	{
+		// physics: the finite-volume operators on fields, as
+		// physics/test/fvm_diffusion.cc builds them, and the same expression
+		// as the matrix-free operator of a CG solve
+		using namespace physics;
+		const context &pc = ctx;
+		fvm_mesh m(pc, {12, 10, 8}, {{{0.0, 1.0}, {0.0, 2.0}, {0.0, 0.5}}});
+		const std::size_t N = m.dofs();
+		auto faces = m.face_fields(pc);
+		auto a = m.cell_field(pc, 1.0);
+		auto expr = op_expr(bc<dirichlet, x_axis, boundary_low>::create({0.0}, m),
+		                    bc<dirichlet, x_axis, boundary_high>::create({0.0}, m),
+		                    bc<neumann, y_axis, boundary_low>::create({0.0}, m),
+		                    bc<neumann, y_axis, boundary_high>::create({0.0}, m),
+		                    bc<neumann, z_axis, boundary_low>::create({0.0}, m),
+		                    bc<neumann, z_axis, boundary_high>::create({0.0}, m),
+		                    coefficient<constant_coefficient>::create({2.0}, faces, m),
+		                    diffusion::create({&a, &faces, 1.0, 0.25}, m));
+		std::vector<double> xs(N);
+		fsp_uniform(11, (int64_t)N, -1.0, 1.0, xs.data());
+		vec::device_vec x(pc, xs), y(pc, N), px(pc, N);
+		auto u = m.cell_field(pc), v = m.cell_field(pc);
+		m.unpack(x, u);
+		expr.apply(u, v);
+		m.pack(v, px);
+		auto A = expr.matrix_free();
+		A.apply(x, y);
+		auto hy = y.download(), hv = px.download();
+		bool same = true;
+		for (std::size_t i = 0; i < N; ++i)
+			same = same && std::memcmp(&hy[i], &hv[i], sizeof(double)) == 0;
+		expect(same, "physics: the matrix-free operator equals op_expr(bc..., coefficient, diffusion) bit for bit");
+		// zero-flux faces, no source: a constant field has no flux
+		auto u1 = m.cell_field(pc, 3.0), v1 = m.cell_field(pc);
+		auto neu = op_expr(bc<neumann, x_axis, boundary_low>::create({0.0}, m),
+		                   bc<neumann, x_axis, boundary_high>::create({0.0}, m),
+		                   bc<neumann, y_axis, boundary_low>::create({0.0}, m),
+		                   bc<neumann, y_axis, boundary_high>::create({0.0}, m),
+		                   bc<neumann, z_axis, boundary_low>::create({0.0}, m),
+		                   bc<neumann, z_axis, boundary_high>::create({0.0}, m),
+		                   coefficient<constant_coefficient>::create({1.0}, faces, m),
+		                   diffusion::create({&a, &faces, 1.0, 0.0}, m));
+		neu.apply(u1, v1);
+		vec::device_vec pv(pc, N);
+		m.pack(v1, pv);
+		expect(pv.l2norm().get() == 0.0, "physics: zero-flux boundaries give no flux for a constant field");
+		vec::device_vec b(pc, xs), sol(pc, N);
+		auto info = cg::solver(cg::settings{2000, 1e-8f, 0.f, true}, cg::make_work(b))(op::ref(A), jacobi)(b, sol);
+		vec::device_vec r(pc, N);
+		A.residual(b, sol, r);
+		expect(info.success() && r.l2norm().get() <= 1e-8 * b.l2norm().get() * 1.01,
+		       "physics: jacobi cg on the matrix-free operator converged");
 	}
 	std::printf("%d failure(s)\n", failures);
 	return failures;
