@@ -74,12 +74,36 @@ class FvmOperatorSettings(C.Structure):
                 ("a_value", C.c_double), ("b_value", C.c_double)]
 
 
+class BdfSettings(C.Structure):
+    _fields_ = [("initial_time", C.c_double), ("final_time", C.c_double), ("max_steps", C.c_int),
+                ("max_dt", C.c_double), ("min_dt", C.c_double), ("initial_dt", C.c_double),
+                ("use_predictor", C.c_int), ("use_initial_predictor", C.c_int),
+                ("has_source_term", C.c_int), ("combine_timestep_estimators", C.c_int),
+                ("predictor", C.c_int), ("timestep_strategy", C.c_int),
+                ("dt_cut_lower_bound", C.c_double), ("dt_growth_upper_bound", C.c_double),
+                ("number_of_time_intervals", C.c_int), ("integrator", C.c_int),
+                ("starting_integrator", C.c_int), ("calculate_time_trunc_error", C.c_int),
+                ("time_trunc_err_norm", C.c_int), ("target_relative_change", C.c_double),
+                ("use_pi_controller", C.c_int), ("pi_controller_type", C.c_int),
+                ("control_timestep_variation", C.c_int), ("time_error_scaling", C.c_int),
+                ("time_rtol", C.c_double), ("time_atol", C.c_double),
+                ("num_problem_scales", C.c_int), ("problem_scale", C.c_double)]
+
+
+class BdfState(C.Structure):
+    _fields_ = [("current_time", C.c_double), ("current_dt", C.c_double), ("final_time", C.c_double),
+                ("current_step", C.c_int), ("num_step_rejects", C.c_int), ("solver_success", C.c_int),
+                ("solver_iters", C.c_int), ("gamma", C.c_double)]
+
+
 class Precond(C.Structure):
     _fields_ = [("kind", C.c_int), ("diag", C.c_void_p), ("op", C.c_void_p)]
 
 
 DIAG_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_double)
 RESIDUAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p)
+RHS_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)
+TIME_SOLVE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_int))
 
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -156,6 +180,16 @@ _PROTOS = {
     "fs_fvm_operator_create": [_vp, C.POINTER(FvmOperatorSettings), _vp, _vp, _vp, _vp,
                                C.POINTER(_vp)],
     "fs_fvm_operator_info": [_vp, C.POINTER(C.c_int), C.POINTER(_i64)],
+    "fs_bdf_settings_default": [C.POINTER(BdfSettings)],
+    "fs_bdf_create": [_vp, C.POINTER(BdfSettings), _i64, RHS_FN, _vp, TIME_SOLVE_FN, _vp, C.POINTER(_vp)],
+    "fs_bdf_create_linear": [_vp, C.POINTER(BdfSettings), _vp, C.c_int, C.POINTER(KrylovSettings),
+                             C.POINTER(Precond), C.POINTER(_vp)],
+    "fs_bdf_advance": [_vp, C.c_double, C.c_int, _vp, _vp],
+    "fs_bdf_check_solution": [_vp, C.POINTER(C.c_int)],
+    "fs_bdf_update": [_vp],
+    "fs_bdf_get_next_dt": [_vp, C.c_int, C.POINTER(C.c_double)],
+    "fs_bdf_state_get": [_vp, C.POINTER(BdfState)],
+    "fs_bdf_destroy": [_vp],
     "fs_mm_read": [C.c_char_p, C.POINTER(_vp)],
     "fs_mm_shape": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(C.c_int)],
     "fs_mm_rows": [_vp, _i64, _i64, _vp, _vp, _vp, C.POINTER(_i64)],

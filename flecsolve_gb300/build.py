@@ -33,7 +33,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "-I", str(INCLUDE), "-I", str(CSRC)]
 
 CU_SOURCES = ["context.cu", "spmv.cu", "krylov.cu", "gmres.cu", "batched.cu", "blockcg.cu",
-              "adjoint.cu", "noalloc.cu", "matrix_market.cu", "nka.cu", "fvm.cu"]
+              "adjoint.cu", "noalloc.cu", "matrix_market.cu", "nka.cu", "fvm.cu",
+              "bdf.cu"]
 
 
 def _nvcc() -> str:

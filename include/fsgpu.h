@@ -517,6 +517,82 @@ FS_API int fs_fvm_operator_create(fs_ctx ctx, const fs_fvm_operator_settings *s,
 /* whether the operator is affine, and its logical cells per axis */
 FS_API int fs_fvm_operator_info(fs_csr A, int *affine, int64_t n[3]);
 
+/* ------------------------------------------------- BDF integrator ----
+ * bdf::integrator of flecsolve/time-integrators/bdf.hh:49-777 for
+ * u' = f(u): backward Euler, Crank-Nicolson and variable-step BDF2-6 with
+ * AB2 / leapfrog / forward-Euler predictors, truncation-error estimates and
+ * the PI / deadbeat step controllers.  The controller runs on the host; every
+ * vector operation (predictor, source term, error estimate, history) and the
+ * solve of the time operator u - gamma f(u) = rhs run on the device.
+ * Settings are bdf::settings (bdf_parameters.hh:35-112) with the enums of
+ * bdf_parameters.hh:16-24 in their declaration order. */
+typedef struct fs_bdf_s *fs_bdf;
+enum { FS_BDF_CN = 0, FS_BDF_BE = 1, FS_BDF_BDF2 = 2, FS_BDF_BDF3 = 3, FS_BDF_BDF4 = 4,
+       FS_BDF_BDF5 = 5, FS_BDF_BDF6 = 6 };
+enum { FS_BDF_AB2 = 0, FS_BDF_LEAPFROG = 1 };
+enum { FS_BDF_TRUNCATION_ERROR = 0, FS_BDF_CONSTANT = 1, FS_BDF_FINAL_CONSTANT = 2,
+       FS_BDF_LIMIT_RELATIVE_CHANGE = 3 };
+enum { FS_BDF_H211B = 0, FS_BDF_PC4_7 = 1, FS_BDF_PC11 = 2, FS_BDF_DEADBEAT = 3 };
+enum { FS_BDF_FIXED_RESOLUTION = 0, FS_BDF_FIXED_SCALING = 1 };
+enum { FS_NORM_INF = 0, FS_NORM_L2 = 1, FS_NORM_L1 = 2 };  /* vec::norm_type */
+typedef struct {
+	/* time_integrator::base_settings (parameters.hh:21-28) */
+	double initial_time, final_time;
+	int max_steps;
+	double max_dt, min_dt, initial_dt;
+	/* bdf::settings */
+	int use_predictor, use_initial_predictor, has_source_term, combine_timestep_estimators;
+	int predictor;                 /* FS_BDF_AB2 / FS_BDF_LEAPFROG */
+	int timestep_strategy;         /* FS_BDF_TRUNCATION_ERROR ... */
+	double dt_cut_lower_bound, dt_growth_upper_bound;
+	int number_of_time_intervals;
+	int integrator, starting_integrator;  /* FS_BDF_CN ... FS_BDF_BDF6 */
+	int calculate_time_trunc_error;
+	int time_trunc_err_norm;       /* FS_NORM_* (inf, else the l2 norm) */
+	double target_relative_change;
+	int use_pi_controller, pi_controller_type, control_timestep_variation;
+	int time_error_scaling;        /* FS_BDF_FIXED_RESOLUTION / _SCALING */
+	double time_rtol, time_atol;
+	int num_problem_scales;        /* 0 or 1: problem_scales of one component */
+	double problem_scale;
+} fs_bdf_settings;
+/* the option defaults of bdf::options (bdf_parameters.hh:121-156); the
+ * options without a default there (times, max_steps, predictor, strategy,
+ * integrators) are set to -1 and must be given */
+FS_API int fs_bdf_settings_default(fs_bdf_settings *s);
+/* the time operator of a general problem: f = f(u) (apply_rhs,
+ * operator_adapter.hh:40-43), and the solve of x - gamma f(x) = rhs from the
+ * initial guess in x (the integrator's solver); *success as
+ * solve_info::success() */
+typedef int (*fs_rhs_fn)(void *user, fs_vec u, fs_vec f);
+typedef int (*fs_time_solve_fn)(void *user, double gamma, fs_vec rhs, fs_vec x, int *success);
+/* bdf::integrator(bdf::parameters(settings, op, make_work(x), solver)) for
+ * vectors of n doubles.  Invalid settings return FS_ERR_BREAKDOWN (the
+ * reference asserts in settings::validate, bdf_parameters.hh:57-110). */
+FS_API int fs_bdf_create(fs_ctx ctx, const fs_bdf_settings *s, int64_t n, fs_rhs_fn rhs, void *rhs_user,
+                         fs_time_solve_fn solve, void *solve_user, fs_bdf *out);
+/* A linear problem f(u) = J u: the time operator I - gamma J is kept as a
+ * CSR with J's pattern (J must store its diagonal), its values rewritten on
+ * the device whenever gamma changes, and solved by a Krylov solver bound to
+ * it (method, settings and preconditioner as fs_krylov_create). */
+FS_API int fs_bdf_create_linear(fs_ctx ctx, const fs_bdf_settings *s, fs_csr J, int method,
+                                const fs_krylov_settings *ks, const fs_precond *P, fs_bdf *out);
+/* integrator::advance / check_solution / update / get_next_dt
+ * (bdf.hh:74-213): out = the solution at t + dt from curr (curr != out) */
+FS_API int fs_bdf_advance(fs_bdf b, double dt, int first_step, fs_vec curr, fs_vec out);
+FS_API int fs_bdf_check_solution(fs_bdf b, int *passed);
+FS_API int fs_bdf_update(fs_bdf b);
+FS_API int fs_bdf_get_next_dt(fs_bdf b, int good_solution, double *dt);
+typedef struct {
+	double current_time, current_dt, final_time;
+	int current_step, num_step_rejects;
+	int solver_success;     /* of the last advance */
+	int solver_iters;       /* of the last advance (linear form) */
+	double gamma;           /* the time operator's scaling of the last step */
+} fs_bdf_state;
+FS_API int fs_bdf_state_get(fs_bdf b, fs_bdf_state *out);
+FS_API int fs_bdf_destroy(fs_bdf b);
+
 #ifdef __cplusplus
 }
 #endif
