@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstdint>
 #include <iterator>
+#include <limits>
 #include <functional>
 #include <memory>
 #include <stdexcept>
@@ -961,5 +962,202 @@ op_expr_t<Ops...> op_expr(Ops... ops) {
 }
 
 }  // namespace physics
+
+
+// ------------------------------------------------- time integrators ----
+// time_integrator::bdf (flecsolve/time-integrators/bdf.hh,
+// bdf_parameters.hh) over device vectors (fs_bdf_* of fsgpu.h), spelled as
+// the reference's test uses it (time-integrators/test/implicit.cc:77-113):
+//   bdf::integrator ti(bdf::parameters(s, F, bdf::make_work(x), solver));
+//   ti.advance(dt, first_step, x, xnew); ti.check_solution(); ti.update();
+//   ti.get_next_dt(good);
+// F provides apply_rhs(u, f) and set_scaling(gamma); solver.apply(b, x)
+// returns a solve_info.  bdf::linear_integrator keeps the time operator
+// I - gamma J of a linear f(u) = J u on the device with a bound Krylov solver.
+namespace time_integrator {
+namespace bdf {
+
+enum class method { cn, be, bdf2, bdf3, bdf4, bdf5, bdf6 };
+enum class predictor { ab2, leapfrog };
+enum class strategy { truncation_error, constant, final_constant, limit_relative_change };
+enum class controller { H211b, pc4_7, pc11, deadbeat };
+enum class error_scaling { fixed_resolution, fixed_scaling };
+enum class norm_type { inf, l2, l1 };
+
+// bdf::settings with time_integrator::base_settings (parameters.hh:21-28,
+// bdf_parameters.hh:35-55); defaults as bdf::options (bdf_parameters.hh:
+// 121-156); the options that have none there must be set
+struct settings {
+	double initial_time = std::nan(""), final_time = std::nan("");
+	int max_steps = -1;
+	double max_dt = std::numeric_limits<double>::max();
+	double min_dt = std::numeric_limits<double>::min();
+	double initial_dt = 0.0;
+	bool use_predictor = true, use_initial_predictor = true, has_source_term = false;
+	bool combine_timestep_estimators = false;
+	bdf::predictor predictor = bdf::predictor::leapfrog;
+	bdf::strategy timestep_strategy = bdf::strategy::truncation_error;
+	double dt_cut_lower_bound = 0.58754407, dt_growth_upper_bound = 1.702;
+	int number_of_time_intervals = 100;
+	bdf::method integrator = bdf::method::bdf2, starting_integrator = bdf::method::cn;
+	bool calculate_time_trunc_error = false;
+	norm_type time_trunc_err_norm = norm_type::inf;
+	double target_relative_change = 0.0;
+	bool use_pi_controller = true;
+	controller pi_controller_type = controller::pc4_7;
+	bool control_timestep_variation = false;
+	error_scaling time_error_scaling = error_scaling::fixed_scaling;
+	double time_rtol = 1e-9, time_atol = 1e-15;
+	std::vector<double> problem_scales;
+
+	fs_bdf_settings to_c() const {
+		fs_bdf_settings c;
+		fs_bdf_settings_default(&c);
+		c.initial_time = initial_time;
+		c.final_time = final_time;
+		c.max_steps = max_steps;
+		c.max_dt = max_dt;
+		c.min_dt = min_dt;
+		c.initial_dt = initial_dt;
+		c.use_predictor = use_predictor;
+		c.use_initial_predictor = use_initial_predictor;
+		c.has_source_term = has_source_term;
+		c.combine_timestep_estimators = combine_timestep_estimators;
+		c.predictor = (int)predictor;
+		c.timestep_strategy = (int)timestep_strategy;
+		c.dt_cut_lower_bound = dt_cut_lower_bound;
+		c.dt_growth_upper_bound = dt_growth_upper_bound;
+		c.number_of_time_intervals = number_of_time_intervals;
+		c.integrator = (int)integrator;
+		c.starting_integrator = (int)starting_integrator;
+		c.calculate_time_trunc_error = calculate_time_trunc_error;
+		c.time_trunc_err_norm = (int)time_trunc_err_norm;
+		c.target_relative_change = target_relative_change;
+		c.use_pi_controller = use_pi_controller;
+		c.pi_controller_type = (int)pi_controller_type;
+		c.control_timestep_variation = control_timestep_variation;
+		c.time_error_scaling = (int)time_error_scaling;
+		c.time_rtol = time_rtol;
+		c.time_atol = time_atol;
+		if (problem_scales.size() > 1)
+			check(FS_ERR_UNSUPPORTED, nullptr, "bdf: problem scales of one component");
+		c.num_problem_scales = (int)problem_scales.size();
+		c.problem_scale = problem_scales.empty() ? 0.0 : problem_scales[0];
+		return c;
+	}
+};
+
+// make_work(x): the integrator allocates its work on the device
+struct work {
+	fs_ctx ctx;
+	std::size_t n;
+};
+inline work make_work(const vec::device_vec &x) { return {x.ctx(), x.local_size()}; }
+
+template<class O, class S>
+struct parameters {
+	settings s;
+	op::handle<O> F;
+	work w;
+	op::handle<S> solver;
+	parameters(const settings &s, op::handle<O> F, work w, op::handle<S> solver)
+		: s(s), F(F), w(w), solver(solver) {}
+};
+
+class integrator_base {
+public:
+	integrator_base(const integrator_base &) = delete;
+	~integrator_base() {
+		if (h_)
+			fs_bdf_destroy(h_);
+	}
+	void advance(double dt, bool first_step, const vec::device_vec &curr, vec::device_vec &out) {
+		check(fs_bdf_advance(h_, dt, first_step ? 1 : 0, curr.handle(), out.handle()), ctx_, "bdf advance");
+	}
+	bool check_solution() {
+		int ok = 0;
+		check(fs_bdf_check_solution(h_, &ok), ctx_, "bdf check_solution");
+		return ok != 0;
+	}
+	void update() { check(fs_bdf_update(h_), ctx_, "bdf update"); }
+	double get_next_dt(bool good) {
+		double dt = 0.0;
+		check(fs_bdf_get_next_dt(h_, good ? 1 : 0, &dt), ctx_, "bdf get_next_dt");
+		return dt;
+	}
+	double get_current_time() const { return state().current_time; }
+	double get_final_time() const { return state().final_time; }
+	double get_current_dt() const { return state().current_dt; }
+	int get_current_step() const { return state().current_step; }
+	int num_step_rejects() const { return state().num_step_rejects; }
+	double get_time_operator_scaling() const { return state().gamma; }
+
+protected:
+	integrator_base() = default;
+	fs_bdf_state state() const {
+		fs_bdf_state st;
+		check(fs_bdf_state_get(h_, &st), ctx_, "bdf state");
+		return st;
+	}
+	fs_ctx ctx_ = nullptr;
+	fs_bdf h_ = nullptr;
+};
+
+// bdf::integrator(bdf::parameters(s, F, make_work(x), solver))
+template<class O, class S>
+class integrator : public integrator_base {
+public:
+	explicit integrator(parameters<O, S> p) : p_(std::make_unique<parameters<O, S>>(std::move(p))) {
+		ctx_ = p_->w.ctx;
+		fs_bdf_settings c = p_->s.to_c();
+		check(fs_bdf_create(ctx_, &c, (int64_t)p_->w.n, &rhs_tr, p_.get(), &solve_tr, p_.get(), &h_), ctx_,
+		      "fs_bdf_create");
+	}
+
+private:
+	static int rhs_tr(void *user, fs_vec u, fs_vec f) {
+		auto *p = static_cast<parameters<O, S> *>(user);
+		try {
+			auto U = vec::device_vec::view(p->w.ctx, u), Fv = vec::device_vec::view(p->w.ctx, f);
+			p->F.get().apply_rhs(U, Fv);
+			return FS_OK;
+		}
+		catch (...) {
+			return FS_ERR_INVALID_ARG;
+		}
+	}
+	static int solve_tr(void *user, double gamma, fs_vec b, fs_vec x, int *success) {
+		auto *p = static_cast<parameters<O, S> *>(user);
+		try {
+			p->F.get().set_scaling(gamma);
+			auto B = vec::device_vec::view(p->w.ctx, b), X = vec::device_vec::view(p->w.ctx, x);
+			solve_info info = p->solver.get().apply(B, X);
+			*success = info.success() ? 1 : 0;
+			return FS_OK;
+		}
+		catch (...) {
+			return FS_ERR_INVALID_ARG;
+		}
+	}
+	std::unique_ptr<parameters<O, S>> p_;
+};
+template<class O, class S>
+integrator(parameters<O, S>) -> integrator<O, S>;
+
+// f(u) = J u with the time operator I - gamma J on the device, solved by a
+// Krylov solver bound to it (method FS_CG ... FS_GMRES_MIXED)
+class linear_integrator : public integrator_base {
+public:
+	linear_integrator(const settings &s, const mat::csr &J, int method, const fs_krylov_settings &ks,
+	                  bool jacobi = false) {
+		ctx_ = J.ctx();
+		fs_bdf_settings c = s.to_c();
+		fs_precond P{jacobi ? FS_PRECOND_JACOBI : FS_PRECOND_NONE, nullptr, nullptr};
+		check(fs_bdf_create_linear(ctx_, &c, J.handle(), method, &ks, &P, &h_), ctx_, "fs_bdf_create_linear");
+	}
+};
+
+}  // namespace bdf
+}  // namespace time_integrator
 
 }  // namespace flecsolve

@@ -327,6 +327,104 @@ int main() {
 		expect(info.success() && r.l2norm().get() <= 1e-8 * b.l2norm().get() * 1.01,
 		       "physics: jacobi cg on the matrix-free operator converged");
 	}
+	{
+		// time_integrator::bdf as time-integrators/test/implicit.cc drives it:
+		// the decay u' = -u from 3 at implicit.cfg's settings
+		using namespace time_integrator;
+		struct rate_op {
+			double lambda, gamma = 1.0;
+			void apply_rhs(const vec::device_vec &x, vec::device_vec &y) const { y.scale(lambda, x); }
+			void set_scaling(double g) { gamma = g; }
+		};
+		struct rate_solver {
+			op::handle<rate_op> F;
+			solve_info apply(const vec::device_vec &b, vec::device_vec &x) const {
+				const double rhs = b.min().get();
+				x.set_scalar(rhs / (1. - F.get().lambda * F.get().gamma));
+				solve_info i;
+				i.status = solve_info::stop_reason::converged_atol;
+				return i;
+			}
+		};
+		auto run = [&](bdf::method m, int &steps, int &rejects, double &err) {
+			bdf::settings s;
+			s.initial_time = 0.0;
+			s.final_time = 1.0;
+			s.initial_dt = 0.5;
+			s.max_steps = 1000;
+			s.min_dt = 0.001;
+			s.max_dt = 0.5;
+			s.timestep_strategy = bdf::strategy::truncation_error;
+			s.integrator = m;
+			s.starting_integrator = bdf::method::cn;
+			s.time_trunc_err_norm = bdf::norm_type::inf;
+			s.predictor = bdf::predictor::leapfrog;
+			s.problem_scales = {1.};
+			s.time_rtol = 1e-7;
+			s.time_atol = 1e-5;
+			s.time_error_scaling = bdf::error_scaling::fixed_resolution;
+			auto F = op::make_shared<rate_op>(rate_op{-1.0});
+			auto solver = op::make_shared<rate_solver>(rate_solver{F});
+			vec::device_vec x(ctx, 1), xnew(ctx, 1);
+			bdf::integrator ti(bdf::parameters(s, F, bdf::make_work(x), solver));
+			x.set_scalar(3.0);
+			double dt = ti.get_current_dt();
+			bool first = true;
+			while (ti.get_current_time() < ti.get_final_time()) {
+				ti.advance(dt, first, x, xnew);
+				const bool good = ti.check_solution();
+				if (good) {
+					ti.update();
+					std::swap(x, xnew);
+					first = false;
+				}
+				dt = ti.get_next_dt(good);
+			}
+			steps = ti.get_current_step();
+			rejects = ti.num_step_rejects();
+			err = std::abs(3.0 * std::exp(-1.0) - x.max().get());
+		};
+		int steps = 0, rejects = 0;
+		double err = 1.0;
+		run(bdf::method::bdf2, steps, rejects, err);
+		expect(err < 1e-3 && steps <= 49 && rejects <= 7, "bdf2: implicit.cc expectations (err < 1e-3, <= 49 steps, <= 7 rejects)");
+		run(bdf::method::bdf5, steps, rejects, err);
+		expect(err < 1e-7 && steps == 48 && rejects == 14, "bdf5: implicit.cc expectations (err < 1e-7, 48 steps, 14 rejects)");
+		// the heat equation u' = -A u, backward Euler with the device time operator
+		host_csr H = diffusion(2, 16, false);
+		for (auto &v : H.val)
+			v = -v;
+		mat::csr J(ctx, H.n, H.n, H.rp, H.col, H.val);
+		bdf::settings hs;
+		hs.initial_time = 0.0;
+		hs.final_time = 0.1;
+		hs.initial_dt = 0.01;
+		hs.max_dt = 0.01;
+		hs.max_steps = 100;
+		hs.timestep_strategy = bdf::strategy::constant;
+		hs.integrator = hs.starting_integrator = bdf::method::be;
+		hs.problem_scales = {1.};
+		fs_krylov_settings ks;
+		fs_krylov_settings_default(&ks);
+		ks.base = {1000, 1e-12f, 0.f, 0};
+		bdf::linear_integrator ht(hs, J, FS_CG, ks, true);
+		vec::device_vec u(ctx, H.n), unew(ctx, H.n);
+		u.set_scalar(1.0);
+		double dt = ht.get_current_dt();
+		bool first = true;
+		while (ht.get_current_time() < ht.get_final_time()) {
+			ht.advance(dt, first, u, unew);
+			const bool good = ht.check_solution();
+			if (good) {
+				ht.update();
+				std::swap(u, unew);
+				first = false;
+			}
+			dt = ht.get_next_dt(good);
+		}
+		expect(std::abs(ht.get_current_time() - 0.1) < 1e-12 && u.max().get() < 1.0 && u.min().get() > 0.0,
+		       "bdf linear form: backward-Euler heat reaches the final time, decaying and positive");
+	}
 	std::printf("%d failure(s)\n", failures);
 	return failures;
 }
