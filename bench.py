@@ -258,7 +258,9 @@ def run_suite(args):
     systems in one batched launch against the same solver run system by
     system on a sample; block CG on 16 right-hand sides of the 128^3
     Laplacian against 16 separate solves; the diffusion3d-256 problem as the
-    matrix-free finite-volume operator (applies and PCG); the adjoint gradient of
+    matrix-free finite-volume operator (applies and PCG); NKA with a CG
+    preconditioner at 128^3; BDF2 heat at 128^3 with the device time operator;
+    the adjoint gradient of
     ||x - x_target||^2 at 128^3 and backward-Euler heat 64^3 x 200 steps
     differentiated with checkpoints every 20."""
     import flecsolve_gb300 as fs
@@ -415,6 +417,77 @@ def run_suite(args):
                 res[name] = {"s": s, "iters": info.iters, "status": info.status,
                              "true_relres": _relres(S, b, vx.numpy())}
         out["fvm-diffusion3d-256"] = res
+    if want("nka"):
+        # NKA with a CG preconditioner set up as solvers/test/nka.cc does (b = 1,
+        # x0 = 3, nka.cfg: max_dim 5, angle 0.2) on the 128^3 log-normal
+        # diffusion operator, with the preconditioner's CG at 100 iterations
+        # (the test's 11 suit its 64^2 Poisson problem) and atol 1e-3
+        # (||b|| = 1448)
+        A, _ = P.workload("diffusion3d-128")
+        dA = fs.CSR(ctx, A)
+        vb = fs.Vector(ctx, np.ones(A.nrows))
+        pre = fs.cg.solver(fs.cg.settings(maxiter=100, rtol=1e-9, atol=1e-9, use_zero_guess=True),
+                           fs.cg.make_work(vb))(dA)
+        s_nka = fs.nka.settings(maxiter=500, atol=1e-3, max_dim=5, angle_tol=0.2, use_zero_guess=False)
+        res = {"rows": A.nrows, "nnz": A.nnz}
+        for rep in range(2):  # the first solve warms up the preconditioner's graphs
+            vx = fs.Vector(ctx, np.full(A.nrows, 3.0))
+            slv = fs.nka.solver(s_nka, fs.nka.make_work(vb, 10))(dA, pre)
+            ctx.sync()
+            t0 = time.perf_counter()
+            info = slv(vb, vx)
+            ctx.sync()
+            t = time.perf_counter() - t0
+        res["nka_cg100"] = {"s": t, "iters": info.iters, "status": info.status,
+                           "s_per_iteration": t / max(info.iters, 1),
+                           "true_res": float(np.linalg.norm(np.ones(A.nrows) - A.to_scipy() @ vx.numpy()))}
+        out["nka-diffusion3d-128"] = res
+    if want("bdf"):
+        # BDF2 with the truncation-error controller on the heat equation
+        # u' = -A u (A the 128^3 log-normal diffusion operator, u0 U[0,1]):
+        # the time operator I + gamma A on the device, mixed-precision Jacobi
+        # CG as the time solver; the host controller's share of the wall time
+        from flecsolve_gb300.time_integrator import bdf
+        A, _ = P.workload("diffusion3d-128")
+        J = fs.CSR(ctx, P.CSR(A.nrows, A.ncols, A.rowptr, A.col, -A.val))
+        st = bdf.settings(**{"initial-time": 0.0, "final-time": 2.0, "initial-dt": 1e-3, "max-dt": 0.5,
+                             "max-steps": 10000, "timestep-selection-strategy": "truncation-error",
+                             "integrator": "BDF2", "starting-integrator": "CN", "predictor": "leapfrog",
+                             "trunc-error-rtol": 1e-4, "trunc-error-atol": 1e-6,
+                             "time-error-scaling": "fixed-resolution", "time-trunc-error-norm": "inf"})
+        res = {"rows": A.nrows, "problem": "u' = -A u, diffusion3d-128, t in [0, 2]"}
+        for rep in range(2):  # the first run warms up the solver's graphs
+            ti = bdf.linear(st, J, fs.mixed_cg.settings(maxiter=20000, rtol=1e-8, use_zero_guess=False),
+                            P=fs.op.jacobi)
+            x, xn = fs.Vector(ctx, P.uniform(17, A.nrows, 0.0, 1.0)), fs.Vector(ctx, A.nrows)
+            ctx.sync()
+            t0 = time.perf_counter()
+            dt, first, attempts, iters = ti.get_current_dt(), True, 0, 0
+            while ti.get_current_time() < ti.get_final_time():
+                ti.advance(dt, first, x, xn)
+                iters += ti.last_solver_iters()
+                attempts += 1
+                good = ti.check_solution()
+                if good:
+                    ti.update()
+                    x, xn = xn, x
+                    first = False
+                dt = ti.get_next_dt(good)
+            ctx.sync()
+            t = time.perf_counter() - t0
+        res["bdf2_mixed_cg"] = {"s": t, "steps": ti.get_current_step(), "rejects": ti.num_step_rejects(),
+                                "attempts": attempts, "krylov_iters": iters,
+                                "s_per_attempt": t / max(attempts, 1)}
+        # the same number of Krylov iterations as plain solves: the time
+        # solver's share of the wall time
+        vb, vx = fs.Vector(ctx, P.uniform(3, A.nrows)), fs.Vector(ctx, A.nrows)
+        Tm = P.CSR(A.nrows, A.ncols, A.rowptr, A.col, A.val * 0.01)
+        Tm.val[Tm.col == np.repeat(np.arange(A.nrows), np.diff(A.rowptr))] += 1.0
+        slv = fs.mixed_cg.solver(fs.mixed_cg.settings(maxiter=20000, rtol=1e-8))(fs.CSR(ctx, Tm), fs.op.jacobi)
+        s1, info1 = _timed_solve(ctx, slv, vb, vx)
+        res["time_operator_solve_probe"] = {"s": s1, "iters": info1.iters,
+                                            "s_per_krylov_iter": s1 / max(info1.iters, 1)}
+        out["bdf-heat-diffusion3d-128"] = res
     if want("adjoint"):
         n = 128
         system = ad.DiffusionSolve(ctx, 3, n, rtol=1e-8)

@@ -53,14 +53,43 @@ constexpr int kMaxHist = 6;
 int memory_size(int m) { return m == FS_BDF_CN ? 1 : m; }  // bdf.cc:5-8
 int order(int m) { return m == FS_BDF_CN ? 2 : m == FS_BDF_BE ? 1 : m; }  // bdf.cc:10-21
 
-// T.val = (diagonal ? 1 : 0) - gamma J.val, one thread per row
+// The time operator I - gamma J from J's values, one thread per row:
+// T.val = (diagonal ? 1 : 0) - gamma J.val, its FP32 copy and the Jacobi
+// diagonal 1 / T_ii, so that no derived array has to be rebuilt before the
+// solve
 __global__ void k_time_operator(int n, const int *__restrict__ rowptr, const int *__restrict__ col,
-                                const double *__restrict__ jval, double gamma, double *__restrict__ tval) {
-	for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+                                const double *__restrict__ jval, double gamma, double *__restrict__ tval,
+                                float *__restrict__ tval32, double *__restrict__ dinv,
+                                float *__restrict__ dinv32) {
+	for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+		double d = 0.0;
 		for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) {
 			const double t = -(gamma * jval[k]);
-			tval[k] = col[k] == r ? 1.0 + t : t;
+			const double v = col[k] == r ? 1.0 + t : t;
+			tval[k] = v;
+			tval32[k] = (float)v;
+			if (col[k] == r)
+				d = 1.0 / v;
 		}
+		dinv[r] = d;
+		dinv32[r] = (float)d;
+	}
+}
+
+// The scaled difference of the solution x and its prediction y
+// (bdf.hh:648-687): sc = rtol x + atol (fixed resolution) or (x + s) rtol
+// (fixed scaling), sf = (x - y) / sc, each operation rounded as the vector
+// operations round it
+__global__ void k_scaled_diff(int64_t n, const double *__restrict__ x, const double *__restrict__ y,
+                              int fixed_scaling, double rtol, double atol_or_scale, double *__restrict__ sc,
+                              double *__restrict__ sf) {
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const double xi = x[i];
+		const double c = fixed_scaling ? __dmul_rn(__dadd_rn(xi, atol_or_scale), rtol)
+		                               : __dadd_rn(__dmul_rn(rtol, xi), atol_or_scale);
+		sc[i] = c;
+		sf[i] = __ddiv_rn(__dsub_rn(xi, y[i]), c);
+	}
 }
 
 struct Bdf {
@@ -125,9 +154,11 @@ struct Bdf {
 		if (!(t_gamma == gamma)) {
 			Csr *Tc = reinterpret_cast<Csr *>(T);
 			k_time_operator<<<grid_for(ctx, J->nrows, 256, 4), 256, 0, ctx->stream>>>(
-				(int)J->nrows, J->rowptr, J->col, J->val, gamma, Tc->val);
+				(int)J->nrows, J->rowptr, J->col, J->val, gamma, Tc->val, Tc->val32, Tc->dinv, Tc->dinv32);
 			FS_TRY(check_launch(ctx, "bdf time operator"));
 			invalidate_values(Tc);
+			Tc->val32_valid = true;
+			Tc->dinv_valid = true;
 			t_gamma = gamma;
 		}
 		fs_solve_info info;
@@ -306,21 +337,15 @@ struct Bdf {
 		return ef;
 	}
 	int scaled_lte_norm(fs_vec x, fs_vec y, double *out) {
-		fs_vec sc = v(W_SCRATCH), sf = v(W_SCRATCH_FN);
-		if (s.time_error_scaling == FS_BDF_FIXED_RESOLUTION) {
-			FS_TRY(fs_vec_scale(s.time_rtol, x, sc));
-			FS_TRY(fs_vec_add_scalar(sc, s.time_atol, sc));
-		}
-		else {
-			FS_TRY(fs_vec_zero(sc));
-			FS_TRY(fs_vec_add_scalar(x, s.problem_scale, sc));
-			FS_TRY(fs_vec_scale_self(s.time_rtol, sc));
-		}
-		FS_TRY(fs_vec_subtract(x, y, sf));
-		FS_TRY(fs_vec_divide(sf, sc, sf));
-		*out = norm(sf);
+		const bool fs = s.time_error_scaling == FS_BDF_FIXED_SCALING;
+		k_scaled_diff<<<grid_for(ctx, n, 256, 4), 256, 0, ctx->stream>>>(
+			n, dptr(x), dptr(y), fs ? 1 : 0, s.time_rtol, fs ? s.problem_scale : s.time_atol, dptr(v(W_SCRATCH)),
+			dptr(v(W_SCRATCH_FN)));
+		FS_TRY(check_launch(ctx, "bdf error estimate"));
+		*out = norm(v(W_SCRATCH_FN));
 		return FS_OK;
 	}
+	static double *dptr(fs_vec h) { return static_cast<double *>(reinterpret_cast<Vec *>(h)->d); }
 	int temporal_truncation_error() {
 		if (step > 0 || (first_step && s.use_initial_predictor)) {
 			alpha = current_dt / old_dt;
@@ -668,6 +693,16 @@ FS_API int fs_bdf_create_linear(fs_ctx h, const fs_bdf_settings *s, fs_csr Jh, i
 	FS_TRY(make(ctx, s, n, &b));
 	b->J = J;
 	int st = fs_csr_create(h, n, n, nnz, rp64.data(), col.data(), 4, val.data(), &b->T);
+	if (st == FS_OK) {
+		// row patterns, not symmetric storage: the values change every time
+		// the step changes, and k_time_operator writes every array the
+		// pattern and column-id formats read
+		Csr *Tc = reinterpret_cast<Csr *>(b->T);
+		Tc->coding = kCodingPatterns;
+		st = ensure_val32(Tc);
+		if (st == FS_OK)
+			st = ensure_dinv(Tc);
+	}
 	if (st == FS_OK) {
 		fs_precond none{FS_PRECOND_NONE, nullptr, nullptr};
 		st = fs_krylov_create(h, method, ks, b->T, P ? P : &none, &b->ks);

@@ -142,6 +142,9 @@ inline int active_coding(const Csr *A, bool f32 = false) {
 // derived data of A's values (float copy, Jacobi diagonal, CSC values,
 // symmetric storage) is stale: rebuilt on next use
 void invalidate_values(Csr *A);
+// FP32 values and the Jacobi diagonal, built on first use (spmv.cu)
+int ensure_val32(Csr *A);
+int ensure_dinv(Csr *A);
 // build the symmetric storage of A's current values for FP64 or FP32 SpMVs
 // when the format is requested and the values are symmetric (setup path: may
 // allocate and synchronise; never called during stream capture)

@@ -941,21 +941,49 @@ static void clear_graphs(Solver *s) {
 	s->graphs.clear();
 }
 
+// Iterations per graph launch.  A launch records k iterations; those after
+// convergence still launch their kernels, which return at once.  So a solve
+// starts with short launches and doubles them while it runs, up to the
+// configured count: a solve that converges in a few iterations (an inner or
+// time-step solve) launches few idle iterations, and a long one soon runs at
+// full length.  After a restart of the recurrences the next launch is sized
+// to the length of the segment that just ended.
+struct Chunk {
+	static constexpr int kFirst = 4;
+	int kmax, k;
+	explicit Chunk(int kmax_) : kmax(kmax_), k(std::min(kFirst, kmax_)) {}
+	void grow() { k = std::min(kmax, 2 * k); }
+	void restart(int64_t segment) {
+		int c = kFirst;
+		while (c < segment && c < kmax)
+			c *= 2;
+		k = std::min(c, kmax);
+	}
+};
+
 // Common loop driver: launch the captured k-iteration body until the device
-// says done; call the user diagnostic for every new history entry.
+// says done; call the user diagnostic for every new history entry.  `*k` is
+// the iteration count the body records, `code` + 2 k its graph key.
 struct LoopSpec {
 	Vec *x;
 	GraphKey key;
 	int (*body)(Solver *, void *);
 	void *arg;
 	int (*on_restart)(Solver *, void *);  // BiCGSTAB restart handler
+	int *k;
+	int code;
 };
 
 static int run_loop(Solver *s, const LoopSpec &L, int *user_stop) {
 	*user_stop = 0;
 	int64_t seen = 0;
+	Chunk chunk(*L.k);
 	for (;;) {
-		FS_TRY(graph_run(s, L.key, L.body, L.arg));
+		*L.k = chunk.k;
+		GraphKey key = L.key;
+		key.k = L.code + 2 * chunk.k;
+		FS_TRY(graph_run(s, key, L.body, L.arg));
+		chunk.grow();
 		FS_TRY(read_state(s));
 		KState &h = *s->hst;
 		int64_t nh = s->method == FS_BICGSTAB ? (int64_t)h.nhist : h.iter;
@@ -1099,7 +1127,7 @@ static int cg_apply64(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	int user_stop = 0;
 	if (!s->hst->done) {
 		CgArgs args{b, x, k_default(s)};
-		LoopSpec L{x, {b->d, x->d, args.k * 2 + PK}, PK ? cg_body64<1> : cg_body64<0>, &args, nullptr};
+		LoopSpec L{x, {b->d, x->d, 0}, PK ? cg_body64<1> : cg_body64<0>, &args, nullptr, &args.k, PK};
 		FS_TRY(run_loop(s, L, &user_stop));
 	}
 	KState &h = *s->hst;
@@ -1309,9 +1337,10 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	}
 	int user_stop = 0;
 	int64_t seen = 0;
-	const int k = k_default(s) > 1 ? k_default(s) : 32;
-	RcArgs args{b, x, k, delta};
-	GraphKey key{b->d, x->d, 2000 + k * 2 + PK};
+	Chunk chunk(k_default(s) > 1 ? k_default(s) : 32);
+	RcArgs args{b, x, chunk.k, delta};
+	GraphKey key{b->d, x->d, 0};
+	int64_t seg_start = 0;  // iteration of the last replacement
 	auto body = PK ? rc_body<1> : rc_body<0>;
 	auto fold = [&]() -> int {
 		// the last iteration's solution step is still pending
@@ -1319,8 +1348,16 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 		return check_launch(ctx, "reliable fold");
 	};
 	while (!s->hst->done) {
+		args.k = chunk.k;
+		key.k = 2000 + 2 * chunk.k + PK;
 		FS_TRY(graph_run(s, key, body, &args));
 		FS_TRY(read_state(s));
+		if (s->hst->flags & KF_RELIABLE) {
+			chunk.restart(s->hst->iter - seg_start);
+			seg_start = s->hst->iter;
+		}
+		else
+			chunk.grow();
 		if (s->hst->flags & KF_RELIABLE) {
 			FS_TRY(fold());
 			FS_TRY(true_residual());
@@ -1460,8 +1497,8 @@ static int bicgstab_apply64(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	int user_stop = 0;
 	if (!s->hst->done) {
 		BiArgs args{b, x, k_default(s)};
-		LoopSpec L{x, {b->d, x->d, 100 + args.k * 2 + PK}, PK ? bi_body64<1> : bi_body64<0>, &args,
-		           bi_restart};
+		LoopSpec L{x, {b->d, x->d, 0}, PK ? bi_body64<1> : bi_body64<0>, &args, bi_restart, &args.k,
+		           100 + PK};
 		FS_TRY(run_loop(s, L, &user_stop));
 	}
 	KState &h = *s->hst;
