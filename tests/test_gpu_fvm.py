@@ -118,6 +118,40 @@ def test_matrix_free_full_size_against_oracle(ctx):
     assert np.array_equal(_bits(y.numpy()), _bits(want))
 
 
+@pytest.mark.parametrize("n", [(40, 9, 17), (33, 8, 1), (64, 3, 20)])
+@pytest.mark.parametrize("faces_as_fields", [True, False])
+def test_matrix_free_plane_marching_against_oracle(ctx, n, faces_as_fields):
+    """meshes at least a warp wide take the plane-marching kernel: partial x
+    and y tiles, a partial last z chunk, one-plane meshes, every boundary kind,
+    face fields or a constant, a cell term; FP64 bit for bit, FP32 to 2e-6"""
+    box = [[0.0, 2.0], [0.0, 1.0], [-1.0, 1.0]]
+    rng = np.random.default_rng(sum(n))
+    b = [np.exp(rng.normal(size=O.face_fields(n)[0].shape)) for _ in range(3)] if faces_as_fields else None
+    a = np.exp(rng.normal(size=O.cell_field(n).shape))
+    kinds = [O.NEUMANN, O.DIRICHLET, O.DIRICHLET, O.NEUMANN, O.NEUMANN, O.DIRICHLET]
+    vals = [0.25, -0.5, 1.0, 0.0, 2.0, -1.5]
+    x = rng.normal(size=n[0] * n[1] * n[2])
+    want = O.matrix_free_apply(n, box, 1.2, 0.3, kinds, vals, a, b, x, b_value=2.5)
+    mesh = ph.fvm_mesh(ctx, n, box)
+    faces = mesh.face_fields(b if faces_as_fields else 0.0)
+    ops = [ph.bc(_spec(k, v), f // 2, f % 2) for f, (k, v) in enumerate(zip(kinds, vals))]
+    if not faces_as_fields:
+        ops.append(ph.coefficient(ph.constant_coefficient(2.5), faces))
+    ops.append(ph.diffusion(mesh, mesh.cell_field(a), faces, 1.2, 0.3))
+    A = ph.op_expr(*ops).matrix_free()
+    y = fs.Vector(ctx, x.size)
+    A.apply(fs.Vector(ctx, x), y)
+    assert np.array_equal(_bits(y.numpy()), _bits(want))
+    y32 = fs.Vector(ctx, x.size, "f32")
+    A.apply(fs.Vector(ctx, x.astype(np.float32), "f32"), y32)
+    assert np.linalg.norm(y32.numpy() - want) / np.linalg.norm(want) < 2e-6
+    # the residual epilogue through the same kernel
+    bb = rng.normal(size=x.size)
+    vb, vx, rv = fs.Vector(ctx, bb), fs.Vector(ctx, x), fs.Vector(ctx, x.size)
+    fs.api.check(fs.api.lib().fs_csr_residual(A.h, vb.h, vx.h, rv.h), ctx.h)
+    assert np.allclose(rv.numpy(), bb - want, rtol=0, atol=1e-12 * np.abs(want).max())
+
+
 @pytest.mark.parametrize("name", sorted(META["cg"]))
 def test_cg_matches_reference(ctx, name):
     m = META["cg"][name]
