@@ -244,7 +244,8 @@ class op_expr:
         one coefficient setter with a constant (or none: the diffusion
         operator's face fields are used as they are) and one diffusion
         operator.  Returns a :class:`CSR`-compatible operator that stores no
-        matrix."""
+        matrix; it copies the face and cell coefficients at creation, so later
+        changes to those fields need a new operator."""
         ops = self.flat()
         bcs = {o.face: o for o in ops if isinstance(o, bc)}
         coefs = [o for o in ops if isinstance(o, coefficient)]

@@ -134,6 +134,7 @@ class _Bdf:
                                                  C.byref(ks), C.byref(P), C.byref(h)),
                       self.ctx.h, "fs_bdf_create_linear")
                 self._cbs = ()
+                self._J = J  # the integrator reads J's values at every step
             else:
                 op, solver, ctx = params.op, params.solver, self.ctx
 

@@ -1145,7 +1145,8 @@ template<class O, class S>
 integrator(parameters<O, S>) -> integrator<O, S>;
 
 // f(u) = J u with the time operator I - gamma J on the device, solved by a
-// Krylov solver bound to it (method FS_CG ... FS_GMRES_MIXED)
+// Krylov solver bound to it (method FS_CG ... FS_GMRES_MIXED); J is read at
+// every step and must outlive the integrator
 class linear_integrator : public integrator_base {
 public:
 	linear_integrator(const settings &s, const mat::csr &J, int method, const fs_krylov_settings &ks,

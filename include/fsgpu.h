@@ -512,6 +512,9 @@ typedef struct {
 	double a_value;      /* the cell coefficient a when the field a is NULL      */
 	double b_value;      /* the face coefficient when the face fields are NULL   */
 } fs_fvm_operator_settings;
+/* The face and cell coefficients are copied (as transmissibilities t = b dA /
+ * dx and (alpha vol) a) when the operator is created; the fields may be
+ * destroyed afterwards, and changing them needs a new operator. */
 FS_API int fs_fvm_operator_create(fs_ctx ctx, const fs_fvm_operator_settings *s, fs_vec a, fs_vec bx,
                                   fs_vec by, fs_vec bz, fs_csr *out);
 /* whether the operator is affine, and its logical cells per axis */
@@ -574,7 +577,8 @@ FS_API int fs_bdf_create(fs_ctx ctx, const fs_bdf_settings *s, int64_t n, fs_rhs
 /* A linear problem f(u) = J u: the time operator I - gamma J is kept as a
  * CSR with J's pattern (J must store its diagonal), its values rewritten on
  * the device whenever gamma changes, and solved by a Krylov solver bound to
- * it (method, settings and preconditioner as fs_krylov_create). */
+ * it (method, settings and preconditioner as fs_krylov_create).  J is read at
+ * every step and must outlive the integrator. */
 FS_API int fs_bdf_create_linear(fs_ctx ctx, const fs_bdf_settings *s, fs_csr J, int method,
                                 const fs_krylov_settings *ks, const fs_precond *P, fs_bdf *out);
 /* integrator::advance / check_solution / update / get_next_dt
