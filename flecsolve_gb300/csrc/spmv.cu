@@ -283,20 +283,20 @@ int ensure_sym(Csr *A, bool f32) {
 // ------------------------------------------------------ parcsr split --
 
 // y_i = (sum over owned columns) + (sum over ghost columns), each summed in
-// CSR order, row blocks [floor(N c / P), floor(N (c+1) / P)).
+// CSR order.  Row blocks as flecsi::util::equal_map makes them (FleCSI 2.4,
+// flecsi/util/color_map.hh, restated): blocks of q = n / P rows, the first
+// r = n % P one row longer; row i is in block i / (q + 1) below (q + 1) r and
+// in block r + (i - (q + 1) r) / q above.
 template<bool EXACT>
 __global__ void parcsr_kernel(int n, int parts, const int *__restrict__ rp,
                               const int *__restrict__ col, const double *__restrict__ val,
                               const double *__restrict__ x, double *__restrict__ y) {
+	const int q = n / parts, rem = n % parts;
+	const int brk = (q + 1) * rem;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		// colour of row i: the largest c with floor(n c / P) <= i
-		long long c = ((long long)i * parts + parts - 1) / n;
-		while (c > 0 && ((long long)n * c) / parts > i)
-			--c;
-		while (c + 1 < parts && ((long long)n * (c + 1)) / parts <= i)
-			++c;
-		const int lo = (int)(((long long)n * c) / parts);
-		const int hi = (int)(((long long)n * (c + 1)) / parts);
+		const int c = i < brk ? i / (q + 1) : rem + (i - brk) / q;
+		const int lo = c * q + (c < rem ? c : rem);
+		const int hi = lo + q + (c < rem ? 1 : 0);
 		double yd = 0.0, yo = 0.0;
 		for (int k = rp[i]; k < rp[i + 1]; ++k) {
 			const int j = col[k];

@@ -220,10 +220,12 @@ FS_API int fs_csr_spmv_transpose(fs_csr A, fs_vec x, fs_vec y);
 FS_API int fs_csr_diag_inv(fs_csr A, fs_vec dinv);
 
 /* Row-block distributed SpMV of mat::parcsr (flecsolve/matrices/parcsr.hh:
- * 60-91, topo/csr.hh:482-618): rows are split into `parts` contiguous blocks,
- * each row's owned-column (diag block) and ghost-column (offd block) entries
- * are summed separately and added, y = y_diag + y_offd.  All parts live on
- * this device. */
+ * 60-91, topo/csr.hh:482-618): rows are split into `parts` contiguous blocks
+ * as flecsi::util::equal_map splits them (parcsr.hh:149-151: blocks of
+ * nrows / parts rows, the first nrows % parts one row longer), each row's
+ * owned-column (diag block) and ghost-column (offd block) entries are summed
+ * separately and added, y = y_diag + y_offd.  All parts live on this
+ * device. */
 FS_API int fs_parcsr_spmv(fs_csr A, int parts, fs_vec x, fs_vec y);
 
 /* ---------------------------------------------------------- solvers --- */

@@ -598,18 +598,28 @@ done:
 
 /* ------------------------------------------------ parallel CSR SpMV --- */
 
+/* The first row of colour c when N rows are split into `parts` colours as
+ * flecsi::util::equal_map splits them (FleCSI 2.4, flecsi/util/color_map.hh,
+ * a dependency absent from the reference; its published rule restated here):
+ * blocks of q = N / parts rows, the first r = N % parts of them one row
+ * longer, so block c starts at c q + min(c, r). */
+static int64_t or_equal_map_start(int64_t N, int parts, int64_t c) {
+	const int64_t q = N / parts, r = N % parts;
+	return c * q + (c < r ? c : r);
+}
+
 /* mat::parcsr spmv over a row-block partition into `parts` colours
- * (flecsolve/matrices/parcsr.hh:60-91, topo/csr.hh:482-618): for every row
- * the owned-column entries (diag block) and the ghost-column entries (offd
- * block) are summed separately, each left to right in CSR order, and then
- * y = y_diag + y_offd (the y.add(y, tmp) of parcsr.hh:67).  Row blocks
- * follow flecsi::util::equal_map: block c owns rows [c*N/parts ...). */
+ * (flecsolve/matrices/parcsr.hh:60-91, 146-156, topo/csr.hh:482-618): for
+ * every row the owned-column entries (diag block) and the ghost-column
+ * entries (offd block) are summed separately, each left to right in CSR
+ * order, and then y = y_diag + y_offd (the y.add(y, tmp) of parcsr.hh:67).
+ * Row blocks are the equal_map blocks above (parcsr.hh:149-151). */
 OR_API void or_parcsr_spmv(const or_csr *A, int parts, const double *x,
                            double *y) {
 	int64_t N = A->nrows;
 	for (int c = 0; c < parts; ++c) {
-		int64_t r0 = (int64_t)((__int128)N * c / parts);
-		int64_t r1 = (int64_t)((__int128)N * (c + 1) / parts);
+		int64_t r0 = or_equal_map_start(N, parts, c);
+		int64_t r1 = or_equal_map_start(N, parts, c + 1);
 		for (int64_t i = r0; i < r1; ++i) {
 			double yd = 0., yo = 0.;
 			for (int64_t off = A->rowptr[i]; off < A->rowptr[i + 1]; ++off) {

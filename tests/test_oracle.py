@@ -97,6 +97,31 @@ def test_oracle_parcsr_single_part_equals_csr():
     assert np.allclose(y3, O.spmv(A, x), rtol=1e-14, atol=1e-14)
 
 
+def test_oracle_parcsr_blocks_follow_equal_map():
+    """rows split as flecsi::util::equal_map (parcsr.hh:149-151): blocks of
+    N // parts rows, the first N % parts one row longer; each row sums its
+    owned and its ghost columns separately, in CSR order"""
+    A, _ = P.workload("convdiff3d-8")  # 512 rows: 3 parts of 171, 171, 170
+    x = P.uniform(7, A.nrows)
+    for parts in (3, 5, 512):
+        q, r = divmod(A.nrows, parts)
+        starts = [c * q + min(c, r) for c in range(parts + 1)]
+        assert starts[-1] == A.nrows
+        want = np.empty(A.nrows)
+        for c in range(parts):
+            lo, hi = starts[c], starts[c + 1]
+            for i in range(lo, hi):
+                yd = yo = 0.0
+                for k in range(A.rowptr[i], A.rowptr[i + 1]):
+                    j = A.col[k]
+                    if lo <= j < hi:
+                        yd += A.val[k] * x[j]
+                    else:
+                        yo += A.val[k] * x[j]
+                want[i] = yd + yo
+        assert np.array_equal(O.parcsr_spmv(A, parts, x), want)
+
+
 def test_oracle_edge_cases():
     A, b = P.workload("poisson2d-8")
     # zero right-hand side with zero guess: converged immediately (cg.hh:77-82)
