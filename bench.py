@@ -55,6 +55,20 @@ def _dist():
     return ws, rank, local
 
 
+def max_over_ranks(values, ws):
+    """The element-wise maximum of `values` over the ranks of the process
+    group (every rank gets it); `values` unchanged on one rank.  The replicas'
+    per-step times are combined this way: the job takes as long as its
+    slowest rank."""
+    if ws <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(values), dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -577,12 +591,7 @@ def run_ours(args, ws, rank, local):
     x_64 = vx.numpy()
 
     # max over ranks of the per-step time
-    if ws > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([ms_mx, ms_64], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_mx, ms_64 = float(t[0]), float(t[1])
+    ms_mx, ms_64 = max_over_ranks([ms_mx, ms_64], ws)
 
     # SpMV kernel alone (the dominant kernel), CUDA events on the same stream
     spmv64_ms = spmv_events_ms(fs, ctx, dA, n, "f64")
