@@ -765,6 +765,9 @@ using gmres_solver = detail::krylov_solver<gmres::settings, FS_GMRES_MIXED>;
 //   coefficient<constant_coefficient>::create({1.0}, faces, m)
 //   diffusion::create({a, faces, beta, alpha}, m)
 //   op_expr(ops...).apply(u, v)  /  op_expr(ops...).matrix_free()
+// The operators hold pointers to the mesh and to the fields they were created
+// with, which must outlive them; the matrix-free operator copies what it needs
+// when it is made.
 namespace physics {
 
 enum axis { x_axis = 0, y_axis = 1, z_axis = 2 };
