@@ -90,6 +90,25 @@ def test_reference_closed_forms_coefficients_and_boundaries():
     assert np.all(u[1:-1, 0, 1:-1] == 1.0) and np.all(u[1:-1, -1, 1:-1] == 1.0)
 
 
+def test_neumann_flux_matches_a_linear_field():
+    """u = s x (x the cell centre along x) with Neumann flux s on both x faces
+    and zero flux on the others: the boundary cells continue the line
+    (neumann.hh:59-72: u_ghost = u_next - (nd dx) q, nd = +1 low, -1 high),
+    so every cell's net flux is zero"""
+    n, box, slope = (7, 4, 3), [[0.0, 2.0], [0.0, 1.0], [0.0, 1.0]], 1.75
+    dx = O.geometry(n, box)[0][0]
+    u = O.cell_field(n)
+    u[...] = slope * dx * np.arange(n[0] + 2)[None, None, :]
+    kinds, vals = [O.NEUMANN] * 6, [slope, slope, 0.0, 0.0, 0.0, 0.0]
+    v = O.cell_field(n)
+    b = O.face_fields(n)
+    u_in = u.copy()
+    O.apply_expr(n, box, 1.0, 0.0, kinds, vals, 1, 2.0, u, O.cell_field(n, 1.0), v, b)
+    assert np.allclose(u[1:-1, 1:-1, 0], u_in[1:-1, 1:-1, 0], rtol=0, atol=1e-14)
+    assert np.allclose(u[1:-1, 1:-1, -1], u_in[1:-1, 1:-1, -1], rtol=0, atol=1e-14)
+    assert np.abs(v[1:-1, 1:-1, 1:-1]).max() < 1e-12
+
+
 def test_geometry_follows_the_specialization():
     dx, dA, vol, c = O.geometry((8, 4, 2), [[0.0, 1.0], [0.0, 2.0], [-1.0, 1.0]])
     assert dx == [1.0 / 9, 2.0 / 5, 2.0 / 3]
