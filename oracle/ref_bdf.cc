@@ -21,7 +21,8 @@
 //         strategy, controller, error scaling, norm (0 inf, 1 l2, 2 l1),
 //         use_pi_controller, control_timestep_variation
 //   double initial_time, final_time, initial_dt, max_dt, min_dt,
-//          trunc_rtol, trunc_atol, problem_scale, dt_cut_lower_bound
+//          trunc_rtol, trunc_atol, problem_scale, dt_cut_lower_bound,
+//          target_relative_change
 //   int32 max_steps
 //   rate:  double lambda, ic, int64 n (vector length)
 //   heat:  int64 n, nnz; int64 rowptr[n+1]; int32 col[nnz];
@@ -204,10 +205,10 @@ int main(int argc, char ** argv) {
 	if (!f)
 		return 2;
 	int32_t e[10];
-	double d[9];
+	double d[10];
 	int32_t max_steps;
 	rd(f, e, 10);
-	rd(f, d, 9);
+	rd(f, d, 10);
 	rd(f, &max_steps, 1);
 
 	bdf::settings s{};
@@ -236,7 +237,7 @@ int main(int argc, char ** argv) {
 	s.dt_cut_lower_bound = d[8];
 	s.dt_growth_upper_bound = 1.702;
 	s.number_of_time_intervals = 100;
-	s.target_relative_change = 0.0;
+	s.target_relative_change = d[9];
 	s.time_rtol = d[5];
 	s.time_atol = d[6];
 	s.problem_scales = {d[7]};

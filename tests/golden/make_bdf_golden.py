@@ -68,6 +68,8 @@ CASES = {
     "rate_bdf2_final_constant": dict(IMPLICIT, problem="rate", method="BDF2", strategy="final-constant",
                                      initial_dt=0.01, max_dt=0.1),
     "rate_bdf2_nopi": dict(IMPLICIT, problem="rate", method="BDF2", pi=False, control_var=True),
+    "rate_bdf2_relchange": dict(IMPLICIT, problem="rate", method="BDF2", strategy="limit-relative-change",
+                                initial_dt=0.01, target=1e-2),
     "heat_bdf2": dict(IMPLICIT, problem="heat", method="BDF2", final_time=0.2, initial_dt=1e-3, max_dt=0.05,
                       rtol=1e-4, atol=1e-6),
     "heat_be_constant": dict(IMPLICIT, problem="heat", method="BE", starting="BE", strategy="constant",
@@ -84,8 +86,9 @@ def run(c):
             f.write(struct.pack("<10i", 0 if c["problem"] == "rate" else 1, M[c["method"]], M[c["starting"]],
                                 PRED[c["predictor"]], STRAT[c["strategy"]], CTRL[c["controller"]],
                                 SCAL[c["scaling"]], NORM[c["norm"]], int(c["pi"]), int(c["control_var"])))
-            f.write(struct.pack("<9d", c["initial_time"], c["final_time"], c["initial_dt"], c["max_dt"],
-                                c["min_dt"], c["rtol"], c["atol"], c["problem_scale"], c["dt_cut"]))
+            f.write(struct.pack("<10d", c["initial_time"], c["final_time"], c["initial_dt"], c["max_dt"],
+                                c["min_dt"], c["rtol"], c["atol"], c["problem_scale"], c["dt_cut"],
+                                c.get("target", 0.0)))
             f.write(struct.pack("<i", c["max_steps"]))
             if c["problem"] == "rate":
                 f.write(struct.pack("<2dq", RATE["lam"], RATE["ic"], RATE["n"]))

@@ -7,7 +7,8 @@ step, the reference's time, dt and acceptance, and its final solution:
   interface) at implicit.cfg's two settings and at settings covering BE, CN,
   BDF2-6, the AB2 / leapfrog / forward-Euler predictors, the H211b / PC.4.7 /
   PC11 / deadbeat controllers, both error scalings, both norms and the
-  constant / final-constant strategies: the same accept / reject sequence,
+  constant / final-constant / limit-relative-change strategies: the same
+  accept / reject sequence,
   steps and rejects, times, steps and the solution to 1e-6; CN reaching
   max_steps (where the reference asserts) the same attempts up to that
   point; BDF6, whose coefficient typo makes the reference reject every step
@@ -48,7 +49,7 @@ def _settings(c):
         "problem-scales": [c["problem_scale"]], "trunc-error-rtol": c["rtol"], "trunc-error-atol": c["atol"],
         "time-error-scaling": c["scaling"], "pi-controller-type": c["controller"],
         "use-pi-controller": c["pi"], "control-timestep-variation": c["control_var"],
-        "dt-cut-lower-bound": c["dt_cut"]})
+        "dt-cut-lower-bound": c["dt_cut"], "target-relative-change": c.get("target", 0.0)})
 
 
 class Rate:
