@@ -5,8 +5,14 @@ Workload (default): 3-D variable-coefficient diffusion on a 256^3 grid
 (sigma = 1, seed 2) with harmonic face averaging, RHS U[-1, 1] (seed 3),
 Jacobi-preconditioned CG to rtol 1e-8, zero initial guess.  A "step" is one
 full solve.  The headline `value` is the time-to-rtol of the mixed-precision
-refined PCG (FP32 inner iterations, FP64 residual / update / stopping test);
-the plain FP64 GPU PCG is timed the same way and their ratio is reported.
+refined PCG: FP64 iterations until the residual is below 3e-3 ||b|| (the
+first decades, where the solution's large components form), then FP32
+recurrences with FP64 residual replacement, FP64 update and FP64 stopping
+test.  That solve ends within 1e-8 of the FP64 PCG's iterate; the same
+solver with FP32 recurrences from the first iteration is timed too, with
+its distance.  The plain FP64 GPU PCG is timed the same way and their
+ratio is reported, with every result's forward error against a tight FP64
+solve (rtol 1e-12).
 
 The matrix (1.7 GB FP64) is larger than L2 (129 MB), so no flush is needed
 between steps.  Timing: CUDA events on the library's stream around exactly
@@ -15,10 +21,13 @@ timed region.  `e2e` times the same solve through the public C ABI with the
 right-hand side uploaded from pinned host memory and the solution downloaded
 every step.
 
-`--impl reference` times the reference's own CPU algorithm instead (the
-oracle restatement, pinned bit-exact to the reference's templates) on a
-bounded sample of PCG iterations of the same workload and projects the
-time-to-rtol with the reference's iteration count for this workload.
+`--impl reference` runs ONE complete solve of the reference's own serial
+Jacobi-PCG (its unmodified templates, compiled by `make -C oracle ref` into
+oracle/_ref/ref_driver; without that build, the oracle restatement pinned
+bit-exact to it) on the host, one core (the reference's serial path), with a
+time stamp at every iteration.  Its W + K steps are W + K consecutive chunks
+of that solve's iterations (the first chunk includes the set-up); the
+`value` is the measured wall time of the whole solve.
 """
 from __future__ import annotations
 
@@ -176,6 +185,40 @@ def _traffic_from_profiles(kernel_key):
     return None
 
 
+def bench_config(wl, nrows, nnz, ws):
+    """The `config` of both arms' lines (the same dict, so that the two
+    lines are comparable key for key)."""
+    what = (f"{wl} variable-coefficient diffusion, log-normal sigma=1, harmonic faces"
+            if wl.startswith("diffusion3d") else wl)
+    return {"workload": f"{what}, Jacobi PCG rtol 1e-8",
+            "rows": nrows, "nnz": nnz, "parallelism": "replicas" if ws > 1 else "single",
+            "l2": "inputs larger than L2 (matrix 1.7 GB), no flush"}
+
+
+def host_description():
+    """The host the CPU legs ran on: logical CPUs and the CPU model."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                             text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None:
+        try:
+            for ln in Path("/proc/cpuinfo").read_text().splitlines():
+                if ln.lower().startswith("model name"):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    import platform
+    return {"nproc": os.cpu_count(), "cpu_model": model, "machine": platform.machine()}
+
+
 def reference_iters(workload):
     p = ROOT / "tests" / "golden" / "full_size.json"
     if p.exists():
@@ -188,20 +231,62 @@ def reference_iters(workload):
 
 # ------------------------------------------------------------ CPU side --
 
-def cpu_sample(A, b, seconds_target=15.0, max_iters=60):
-    """Time the oracle (the reference's serial PCG restated in C) on a bounded
-    number of iterations of the workload; returns seconds per iteration."""
+def _ref_driver():
+    p = ROOT / "oracle" / "_ref" / "ref_driver"
+    return p if p.exists() else None
+
+
+def reference_timeline(A, b, maxiter, rtol=1e-8):
+    """Run the reference's serial Jacobi-PCG on (A, b) once, from a zero
+    guess, with a wall-clock time stamp at every iteration (taken in its
+    diagnostic, which the reference's CG calls once per iteration).
+
+    Returns (kind, stamps, total, status, iters): stamps[i] = seconds from the
+    start of the solver call to the end of iteration i + 1, total = wall time
+    of the whole call.  kind "reference": the reference's own templates
+    (oracle/_ref/ref_driver, compiled from its headers); kind "port": the
+    oracle restatement, pinned bit-exact to them, where that build is
+    absent."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle as O
-    # one short probe to size the sample
+    drv = _ref_driver()
+    if drv is not None:
+        import tempfile
+        with tempfile.TemporaryDirectory() as td:
+            fin, fout, ftim = (os.path.join(td, f) for f in ("in.bin", "out.bin", "t.bin"))
+            O.write_problem(fin, A, b, np.zeros(A.nrows))
+            env = dict(os.environ, REF_DRIVER_TIMES=ftim)
+            subprocess.run([str(drv), fin, fout, "cg", str(int(maxiter)), repr(float(rtol)), "1",
+                            "jacobi"], check=True, env=env, stdout=subprocess.PIPE,
+                           stderr=subprocess.PIPE)
+            raw = open(ftim, "rb").read()
+            head = np.fromfile(fout, np.int32, 3)
+        ns = int(np.frombuffer(raw, np.int64, 1, 0)[0])
+        stamps = np.frombuffer(raw, np.float64, ns, 8).copy()
+        total = float(np.frombuffer(raw, np.float64, 1, 8 + 8 * ns)[0])
+        return "reference", stamps, total, O.STATUS[int(head[0])], int(head[1])
+    stamps = []
     t0 = time.perf_counter()
-    O.solve("cg", A, b, maxiter=2, rtol=1e-30)
-    probe = (time.perf_counter() - t0) / 2
+
+    def stamp(x, res):
+        stamps.append(time.perf_counter() - t0)
+        return False
+    r = O.solve("cg", A, b, maxiter=int(maxiter), rtol=rtol, diag=stamp)
+    total = time.perf_counter() - t0
+    return "port", np.array(stamps), total, r.status, r.iters
+
+
+def cpu_sample(A, b, seconds_target=15.0, max_iters=60):
+    """Time a bounded number of iterations of the reference's serial PCG on
+    the workload (the reference driver when built, else the oracle port);
+    returns (seconds per iteration, iterations timed, kind)."""
+    kind, st, total, _, _ = reference_timeline(A, b, 2, rtol=1e-30)
+    probe = float(st[-1] - st[0]) if len(st) > 1 else total
     iters = int(max(3, min(max_iters, seconds_target / max(probe, 1e-6))))
-    t0 = time.perf_counter()
-    O.solve("cg", A, b, maxiter=iters, rtol=1e-30)
-    dt = time.perf_counter() - t0
-    return dt / iters, iters
+    kind, st, total, _, _ = reference_timeline(A, b, iters, rtol=1e-30)
+    # per iteration: from the end of the first iteration to the end of the
+    # last (the set-up before the first is not part of an iteration)
+    return float(st[-1] - st[0]) / max(1, len(st) - 1), len(st) - 1, kind
 
 
 # ------------------------------------------------------------ GPU side --
@@ -558,9 +643,13 @@ def run_ours(args, ws, rank, local):
     vx = fs.Vector(ctx, n)
     s64 = fs.cg.settings(maxiter=args.maxiter, rtol=1e-8, use_zero_guess=True)
     smx = fs.mixed_cg.settings(maxiter=args.maxiter, rtol=1e-8, use_zero_guess=True,
-                               inner_rtol=args.inner_rtol, refine=args.refine)
+                               inner_rtol=args.inner_rtol, refine=args.refine,
+                               fp64_head=args.fp64_head)
+    smx0 = fs.mixed_cg.settings(maxiter=args.maxiter, rtol=1e-8, use_zero_guess=True,
+                                inner_rtol=args.inner_rtol, refine=args.refine, fp64_head=0.0)
     cg64 = fs.cg.solver(s64, fs.cg.make_work(vb))(fs.op.ref(dA), fs.op.jacobi)
     cgmx = fs.mixed_cg.solver(smx, fs.mixed_cg.make_work(vb))(fs.op.ref(dA), fs.op.jacobi)
+    cgmx0 = fs.mixed_cg.solver(smx0, fs.mixed_cg.make_work(vb))(fs.op.ref(dA), fs.op.jacobi)
 
     def barrier():
         if ws > 1:
@@ -589,9 +678,16 @@ def run_ours(args, ws, rank, local):
     x_mx = vx.numpy()
     ms_64, info_64, launches_64 = timed(cg64, args.steps, max(1, args.warmup // 3), "fp64")
     x_64 = vx.numpy()
+    ms_mx0, info_mx0, _ = timed(cgmx0, args.steps, max(1, args.warmup // 3), "mixed-fp32-start")
+    x_mx0 = vx.numpy()
+    # a tight FP64 solve (rtol 1e-12, untimed): the forward error of each result
+    tight = fs.cg.solver(fs.cg.settings(maxiter=args.maxiter, rtol=1e-12, use_zero_guess=True),
+                         fs.cg.make_work(vb))(fs.op.ref(dA), fs.op.jacobi)
+    info_t = tight(vb, vx)
+    x_t = vx.numpy()
 
     # max over ranks of the per-step time
-    ms_mx, ms_64 = max_over_ranks([ms_mx, ms_64], ws)
+    ms_mx, ms_64, ms_mx0 = max_over_ranks([ms_mx, ms_64, ms_mx0], ws)
 
     # SpMV kernel alone (the dominant kernel), CUDA events on the same stream
     spmv64_ms = spmv_events_ms(fs, ctx, dA, n, "f64")
@@ -605,7 +701,8 @@ def run_ours(args, ws, rank, local):
     gbs32 = b32 / (spmv32_ms * 1e-3) / 1e9
     # whole mixed iteration: two kernels when the SpMV stages windows
     it_bytes = pcg_iter_bytes(n, nnz, 4, coding, dA.nblk(), "reliable")
-    it_s = ms_mx * 1e-3 / max(1, info_mx.iters)
+    # the FP32 iteration: from the solve with FP32 recurrences from the start
+    it_s = ms_mx0 * 1e-3 / max(1, info_mx0.iters)
 
     # e2e: through the public API with host buffers
     import torch
@@ -632,9 +729,26 @@ def run_ours(args, ws, rank, local):
     # accuracy of the headline result against the FP64 GPU solve, and the
     # true FP64 relative residual of both
     sys.path.insert(0, str(ROOT / "oracle"))
-    relres_mx = float(np.linalg.norm(b - A.to_scipy() @ x_mx) / np.linalg.norm(b))
-    relres_64 = float(np.linalg.norm(b - A.to_scipy() @ x_64) / np.linalg.norm(b))
-    err_vs_fp64 = float(np.linalg.norm(x_mx - x_64) / np.linalg.norm(x_64))
+    S = A.to_scipy()
+
+    def relres(x):
+        return float(np.linalg.norm(b - S @ x) / np.linalg.norm(b))
+
+    def rel(x, y):
+        return float(np.linalg.norm(x - y) / np.linalg.norm(y))
+    relres_mx, relres_64, relres_mx0 = relres(x_mx), relres(x_64), relres(x_mx0)
+    err_vs_fp64 = rel(x_mx, x_64)
+    # the reference's own solution of this workload at 1024 rows
+    vs_ref = None
+    fsz = ROOT / "tests" / "golden" / "full_size.json"
+    if fsz.exists():
+        ref = json.loads(fsz.read_text()).get(wl, {}).get("cg")
+        if ref:
+            idx = np.asarray(ref["x_sample_index"])
+            xs = np.asarray(ref["x_sample"])
+            vs_ref = {"fp64_pcg": rel(x_64[idx], xs), "mixed_pcg": rel(x_mx[idx], xs),
+                      "reference_iters": ref["iters"],
+                      "what": "relative distance to the reference's own solution at 1024 sampled rows"}
 
     out = {
         "metric": METRIC,
@@ -649,16 +763,22 @@ def run_ours(args, ws, rank, local):
         "vs_baseline": None,
         "dtype": "f32-inner/f64-refine",
         "data": "synthetic (seeded generator, no dataset)",
-        "config": {"workload": f"{wl} variable-coefficient diffusion, log-normal sigma=1, "
-                               f"harmonic faces, Jacobi PCG rtol 1e-8",
-                   "rows": n, "nnz": nnz, "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "inputs larger than L2 (matrix 1.7 GB), no flush"},
+        "config": bench_config(wl, n, nnz, ws),
         "fp64_pcg": {"s": ms_64 * 1e-3, "iters": info_64.iters, "status": info_64.status,
-                     "true_relres": relres_64, "launches_per_step": launches_64 / args.steps},
+                     "true_relres": relres_64, "launches_per_step": launches_64 / args.steps,
+                     "forward_err_vs_tight_fp64": rel(x_64, x_t)},
         "mixed_pcg": {"s": ms_mx * 1e-3, "iters": info_mx.iters, "outer": info_mx.restarts,
                       "status": info_mx.status, "true_relres": relres_mx,
-                      "rel_err_vs_fp64_gpu": err_vs_fp64, "refine": args.refine,
+                      "rel_err_vs_fp64_gpu": err_vs_fp64,
+                      "forward_err_vs_tight_fp64": rel(x_mx, x_t),
+                      "fp64_head": args.fp64_head, "refine": args.refine,
                       "inner_rtol": args.inner_rtol or ("library default (0.1)" if args.refine == "reliable" else "library default (1e-4)")},
+        "mixed_pcg_fp32_from_start": {
+            "s": ms_mx0 * 1e-3, "iters": info_mx0.iters, "status": info_mx0.status,
+            "true_relres": relres_mx0, "rel_err_vs_fp64_gpu": rel(x_mx0, x_64),
+            "forward_err_vs_tight_fp64": rel(x_mx0, x_t), "speedup_vs_fp64": ms_64 / ms_mx0},
+        "tight_fp64_solve": {"rtol": 1e-12, "iters": info_t.iters, "status": info_t.status},
+        "vs_reference_solution": vs_ref,
         "speedup_mixed_vs_fp64": ms_64 / ms_mx,
         "spmv_hbm_gbs": {"f64": gbs64, "f32": gbs32, "f64_ms": spmv64_ms, "f32_ms": spmv32_ms},
         "roofline": {"bound": "hbm",
@@ -675,7 +795,8 @@ def run_ours(args, ws, rank, local):
         "roofline_mixed_iteration": {"bytes_per_iteration": it_bytes, "s_per_iteration": it_s,
                                      "achieved": it_bytes / it_s / 1e9, "peak": peak,
                                      "frac": it_bytes / it_s / 1e9 / peak,
-                                     "kernels_per_iteration": 3},
+                                     "kernels_per_iteration": 3,
+                                     "from": "mixed_pcg_fp32_from_start (every iteration FP32)"},
         "e2e": {"value": e2e_ms * 1e-3, "unit": "s", "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 8 * n},
         "gpu_launches": launches_mx,
@@ -683,51 +804,71 @@ def run_ours(args, ws, rank, local):
         "setup": {"generate_s": gen_s},
     }
     if rank == 0 and not args.no_cpu:
-        per_it, its = cpu_sample(A, b, args.cpu_seconds)
+        per_it, its, kind = cpu_sample(A, b, args.cpu_seconds)
         ref_it = reference_iters(wl) or info_64.iters
-        out["cpu_baseline"] = {"value": per_it * ref_it, "unit": "s", "cores": 1, "kind": "port",
-                               "sample": f"{its} Jacobi-PCG iterations of {wl} timed with the "
-                                         f"oracle (reference serial PCG restated in C, pinned "
-                                         f"bit-exact to the reference), {per_it:.4f} s/iter x "
-                                         f"{ref_it} reference iterations"}
+        what = ("the reference's serial Jacobi-PCG (its own templates, oracle/_ref/ref_driver)"
+                if kind == "reference" else
+                "the oracle (the reference's serial PCG restated in C, pinned bit-exact to it)")
+        out["cpu_baseline"] = {"value": per_it * ref_it, "unit": "s", "cores": 1, "kind": kind,
+                               "projected": True, "host": host_description(),
+                               "sample": f"{its} Jacobi-PCG iterations of {wl} timed with {what}: "
+                                         f"{per_it:.4f} s/iter x {ref_it} reference iterations "
+                                         f"(a projection; `bench.py --impl reference` times the "
+                                         f"complete solve)"}
     return out
 
 
 def run_reference(args, ws, rank, local):
+    """One complete solve of the reference's serial Jacobi-PCG, split into
+    the W + K steps the contract times (see the module docstring)."""
     from flecsolve_gb300 import problems as P
     wl = args.workload
     A, b = P.workload(wl)
-    ref_it = reference_iters(wl)
-    samples = []
-    for i in range(args.warmup + args.steps):
-        per_it, its = cpu_sample(A, b, args.cpu_seconds / 2, max_iters=40)
-        if i >= args.warmup:
-            samples.append(per_it)
-    per_it = statistics.median(samples)
-    iters = ref_it if ref_it else None
-    val = per_it * iters if iters else per_it
+    kind, stamps, total, status, iters = reference_timeline(A, b, args.maxiter)
+    nst = len(stamps)
+    nsteps = args.warmup + args.steps
+    # chunk boundaries over the iterations; chunk c ends at iteration e_c
+    ends = [max(1, round((c + 1) * nst / nsteps)) for c in range(nsteps)]
+    chunk_s = []
+    prev = 0.0
+    for e in ends:
+        t = float(stamps[e - 1]) if nst else total
+        chunk_s.append(t - prev)
+        prev = t
+    timed = chunk_s[args.warmup:]
+    ms_per_step = 1e3 * sum(timed) / max(1, len(timed))
+    what = ("the reference's own serial Jacobi-PCG templates (flecsolve/solvers/cg.hh over "
+            "vec::seq_vec and mat::csr<double>), compiled from its headers into "
+            "oracle/_ref/ref_driver" if kind == "reference" else
+            "the oracle (the reference's serial PCG restated in C, pinned bit-exact to it; "
+            "the reference build is absent on this host)")
+    sample = (f"one complete solve of {wl} to rtol 1e-8 ({iters} iterations, {status}) with "
+              f"{what}, one core (the reference's serial path); the {nsteps} steps are "
+              f"{nsteps} consecutive chunks of its iterations, the first with the set-up; "
+              f"value = the measured wall time of the whole solve")
     return {
         "impl": "reference",
         "metric": METRIC,
-        "value": val,
-        "unit": "s" if iters else "s/iteration",
+        "value": total,
+        "unit": "s",
         "n_gpus": ws,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": val * 1e3,
+        "ms_per_step": ms_per_step,
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded generator, no dataset)",
-        "config": {"workload": f"{wl} variable-coefficient diffusion, Jacobi PCG rtol 1e-8",
-                   "rows": A.nrows, "nnz": A.nnz},
-        "cpu_baseline": {"value": val, "unit": "s", "cores": 1, "kind": "port",
-                         "sample": f"median per-iteration time of bounded PCG samples "
-                                   f"(<= 40 iterations each) of the oracle, the reference's "
-                                   f"serial PCG restated in C (single-threaded as the "
-                                   f"reference's seq path), x {iters} reference iterations"},
-        "e2e": {"value": val, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": bench_config(wl, A.nrows, A.nnz, ws),
+        "step": "a chunk of consecutive iterations of one complete solve (value: that solve)",
+        "reference_solve": {"s": total, "iters": iters, "status": status,
+                            "s_per_iteration": (float(stamps[-1] - stamps[0]) / max(1, nst - 1)
+                                                if nst > 1 else None),
+                            "chunk_s": chunk_s},
+        "cpu_baseline": {"value": total, "unit": "s", "cores": 1, "kind": kind,
+                         "projected": False, "host": host_description(), "sample": sample},
+        "e2e": {"value": total, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
@@ -742,6 +883,9 @@ def main():
     ap.add_argument("--inner-rtol", dest="inner_rtol", type=float, default=0.0,
                     help="replacement factor (reliable) / inner tolerance (restart); 0 = library default")
     ap.add_argument("--refine", default="reliable", choices=["restart", "reliable"])
+    ap.add_argument("--fp64-head", dest="fp64_head", type=float, default=3e-3,
+                    help="mixed CG: FP64 iterations until the residual is below this "
+                         "fraction of ||b|| (0 = FP32 recurrences from the start)")
     ap.add_argument("--cpu-seconds", dest="cpu_seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
     ap.add_argument("--mode", default="solve", choices=["solve", "spmv", "suite"],

@@ -54,7 +54,8 @@ class KrylovSettings(C.Structure):
     _fields_ = [("base", SolverSettings), ("max_krylov_dim", C.c_int),
                 ("pre_side", C.c_int), ("restart", C.c_int), ("ortho", C.c_int),
                 ("k_readback", C.c_int), ("refine", C.c_int),
-                ("inner_rtol", C.c_double), ("max_outer", C.c_int)]
+                ("inner_rtol", C.c_double), ("max_outer", C.c_int),
+                ("fp64_head", C.c_double)]
 
 
 class NkaSettings(C.Structure):

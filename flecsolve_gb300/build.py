@@ -6,7 +6,10 @@
 * ``_build/libfsgpu.so`` -- the CUDA kernels, the device solver loops and the
   C ABI declared in ``include/fsgpu.h``, compiled for sm_103a only.
 * ``oracle/`` -- the CPU checker (``make -C oracle``), and the reference
-  driver when the reference headers are present.
+  drivers when the reference library is available: given by the
+  ``FLECSOLVE_REF`` environment variable (a flecsolve checkout, which is then
+  also staged into the git-ignored ``baseline/_ref``), or already staged
+  there.
 
 Everything is compiled directly with gcc / nvcc (no cmake), translation units
 in parallel, so a cold build takes about a minute.
@@ -110,7 +113,11 @@ def build_cpp_tests(force: bool = False) -> Path:
 
 
 def build_oracle() -> None:
-    _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"])
+    oracle = str(ROOT / "oracle")
+    ref = os.environ.get("FLECSOLVE_REF")
+    if ref:
+        _run(["make", "-s", "-C", oracle, "stage", f"REF={Path(ref).resolve()}"])
+    _run(["make", "-s", f"-j{max(1, min(8, os.cpu_count() or 1))}", "-C", oracle, "ref"])
 
 
 def build_all(force: bool = False, verbose: bool = False) -> None:

@@ -437,6 +437,22 @@ k_rel_finish(int64_t n, const float *__restrict__ r, const float *__restrict__ d
 	}
 }
 
+// The FP64 head of a reliable-update CG has reached its tolerance: the same
+// Krylov process continues at the final tolerance with FP32 recurrences.
+__global__ void k_head_switch(KState *st, double rtol) {
+	st->rtol = rtol;
+	st->tol = rtol * st->bnorm;
+	st->done = 0;
+	st->status = FS_STATUS_UNKNOWN;
+	st->info_iters = 0;
+	st->flags = 0;
+	st->alpha_x = 0.0;
+}
+
+__global__ void k_to_f32(int64_t n, const double *__restrict__ s, float *__restrict__ d) {
+	FOR_EACH(i, n) d[i] = (float)s[i];
+}
+
 // r64 = b - A x, r32 = (float) r64, st->res = ||r64|| (FP64)
 struct EpiRelResidual {
 	static constexpr int NV = 1;
@@ -1303,51 +1319,118 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	const float *dinv = s->dinv32();
 	const int maxiter = s->set.base.maxiter;
 	const double delta = s->set.inner_rtol > 0 ? s->set.inner_rtol : 0.1;
+	const double rtol = (double)s->set.base.rtol;
+	const bool head = s->set.fp64_head > rtol;
 	FS_TRY(solver_hist(s, std::max(1, maxiter)));
-	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, maxiter));
-	FS_TRY(solver_norms(s, b, x, !zg, 0));
-	if (zg) {
-		k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
-		FS_TRY(check_launch(ctx, "fill"));
-	}
-	k_fill<float><<<G, kThreads, 0, ctx->stream>>>(n, xs, 0.f);
-	FS_TRY(check_launch(ctx, "fill"));
 	auto true_residual = [&]() -> int {
 		return launch_spmv<double, false, false>(
 			ctx, s->A, s->A->val, (const double *)x->d, nullptr,
 			EpiRelResidual{(const double *)b->d, r32, s->st, s->part, s->counter});
 	};
-	FS_TRY(true_residual());
-	if (PK)
-		k_cg_start<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, p32, s->st, s->part,
-		                                                     s->counter);
-	else
-		k_cg_start<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, p32, s->st, s->part,
-		                                                     s->counter);
-	FS_TRY(check_launch(ctx, "cg start f32"));
-	FS_TRY(read_state(s));
-	const double res0 = s->hst->res0;
-	{
+	int user_stop = 0;
+	bool head_stop = false;  // the user stopped the FP64 head: x is final
+	int64_t seen = 0;
+	const int G4 = grid_for(ctx, (n + 3) / 4, kThreads, 8);
+	if (head) {
+		// FP64 PCG (the cg_apply64 iteration) to fp64_head * ||b||
+		const size_t n64 = (size_t)((n + 31) / 32 * 32 + 32) * 8;
+		for (int i = 0; i < 3; ++i)
+			if (!s->w64[i])
+				FS_TRY(dalloc(s, (void **)&s->w64[i], n64));
+		double *r64 = s->w64[0], *p64 = s->w64[1];
+		const int PK64 = s->dinv64() ? 1 : 0;
+		FS_TRY(init_state(s, s->st, s->set.fp64_head, maxiter));
+		FS_TRY(solver_norms(s, b, x, !zg, 0));
+		if (zg) {
+			k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
+			FS_TRY(check_launch(ctx, "fill"));
+			k_copy<double><<<G, kThreads, 0, ctx->stream>>>(n, (const double *)b->d, r64);
+			FS_TRY(check_launch(ctx, "copy"));
+		}
+		else {
+			FS_TRY(launch_spmv<double, false, false>(ctx, s->A, s->A->val, (const double *)x->d,
+			                                         nullptr, EpiResidual<double>{(const double *)b->d, r64}));
+		}
+		if (PK64)
+			k_cg_start<double, 1><<<G, kThreads, 0, ctx->stream>>>(n, r64, s->dinv64(), p64, s->st,
+			                                                      s->part, s->counter);
+		else
+			k_cg_start<double, 0><<<G, kThreads, 0, ctx->stream>>>(n, r64, nullptr, p64, s->st,
+			                                                      s->part, s->counter);
+		FS_TRY(check_launch(ctx, "cg start"));
+		FS_TRY(read_state(s));
+		if (!s->hst->done) {
+			CgArgs args{b, x, k_default(s)};
+			LoopSpec L{x, {b->d, x->d, 0}, PK64 ? cg_body64<1> : cg_body64<0>, &args, nullptr,
+			           &args.k, 4000 + PK64};
+			FS_TRY(run_loop(s, L, &user_stop));
+		}
+		seen = s->hst->iter;
+		head_stop = user_stop != 0;
+		const bool go_on = !user_stop && s->hst->status == FS_CONVERGED_RTOL;
+		if (go_on) {
+			// continue the same process: the direction in FP32, the residual
+			// replaced by the FP64 b - A x, beta from the last FP64 rho
+			k_head_switch<<<1, 1, 0, ctx->stream>>>(s->st, rtol);
+			FS_TRY(check_launch(ctx, "head switch"));
+			k_to_f32<<<G, kThreads, 0, ctx->stream>>>(n, p64, p32);
+			FS_TRY(check_launch(ctx, "direction to f32"));
+			k_fill<float><<<G, kThreads, 0, ctx->stream>>>(n, xs, 0.f);
+			FS_TRY(check_launch(ctx, "fill"));
+			FS_TRY(true_residual());
+			if (PK)
+				k_rel_finish<1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, s->st, s->part, s->counter);
+			else
+				k_rel_finish<0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, s->st, s->part,
+				                                                s->counter);
+			FS_TRY(check_launch(ctx, "head finish"));
+			if (PK)
+				k_cg_dir_x<1><<<G4, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, xs, s->st);
+			else
+				k_cg_dir_x<0><<<G4, kThreads, 0, ctx->stream>>>(n, p32, r32, nullptr, xs, s->st);
+			FS_TRY(check_launch(ctx, "cg direction f32"));
+		}
+		// otherwise (user stop, maxiter, non-finite) the FP64 loop's verdict
+		// stands and x holds its iterate
+		FS_TRY(read_state(s));
+	}
+	else {
+		FS_TRY(init_state(s, s->st, rtol, maxiter));
+		FS_TRY(solver_norms(s, b, x, !zg, 0));
+		if (zg) {
+			k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
+			FS_TRY(check_launch(ctx, "fill"));
+		}
+		k_fill<float><<<G, kThreads, 0, ctx->stream>>>(n, xs, 0.f);
+		FS_TRY(check_launch(ctx, "fill"));
+		FS_TRY(true_residual());
+		if (PK)
+			k_cg_start<float, 1><<<G, kThreads, 0, ctx->stream>>>(n, r32, dinv, p32, s->st, s->part,
+			                                                     s->counter);
+		else
+			k_cg_start<float, 0><<<G, kThreads, 0, ctx->stream>>>(n, r32, nullptr, p32, s->st,
+			                                                     s->part, s->counter);
+		FS_TRY(check_launch(ctx, "cg start f32"));
+		FS_TRY(read_state(s));
 		// reference level for the first replacement = the initial residual
 		KState h = *s->hst;
-		h.aux[1] = res0;
+		h.aux[1] = h.res0;
 		FS_CUDA_TRY(ctx, cudaMemcpyAsync(&s->st->aux[1], &h.aux[1], sizeof(double),
 		                                 cudaMemcpyHostToDevice, ctx->stream));
 		FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
 	}
-	int user_stop = 0;
-	int64_t seen = 0;
+	const double res0 = s->hst->res0;
 	Chunk chunk(k_default(s) > 1 ? k_default(s) : 32);
 	RcArgs args{b, x, chunk.k, delta};
 	GraphKey key{b->d, x->d, 0};
-	int64_t seg_start = 0;  // iteration of the last replacement
+	int64_t seg_start = s->hst->iter;  // iteration of the last replacement
 	auto body = PK ? rc_body<1> : rc_body<0>;
 	auto fold = [&]() -> int {
 		// the last iteration's solution step is still pending
 		k_rel_fold_pending<<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, xs, p32, s->st);
 		return check_launch(ctx, "reliable fold");
 	};
-	while (!s->hst->done) {
+	while (!s->hst->done && !user_stop) {
 		args.k = chunk.k;
 		key.k = 2000 + 2 * chunk.k + PK;
 		FS_TRY(graph_run(s, key, body, &args));
@@ -1369,7 +1452,6 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 			FS_TRY(check_launch(ctx, "reliable finish"));
 			// the direction from the replaced residual; alpha_x is 0 here, so
 			// xs (cleared by the fold) stays 0
-			const int G4 = grid_for(ctx, (n + 3) / 4, kThreads, 8);
 			if (PK)
 				k_cg_dir_x<1><<<G4, kThreads, 0, ctx->stream>>>(n, p32, r32, dinv, xs, s->st);
 			else
@@ -1391,7 +1473,7 @@ static int cg_apply_reliable(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 				break;
 		}
 	}
-	if (user_stop)
+	if (user_stop && !head_stop)
 		FS_TRY(fold());
 	KState &h = *s->hst;
 	s->hhist_count = std::min<int64_t>(h.iter, s->hist_cap);

@@ -300,6 +300,13 @@ typedef struct {
 	                        replacements (0 = 0.1 for CG and batched CG,
 	                        1e-2 for BiCGSTAB)                              */
 	int max_outer;       /* restart: maximum refinement steps            */
+	/* reliable mixed CG: FP64 iterations until the residual is below
+	   fp64_head * ||b||, then FP32 recurrences with FP64 replacement for the
+	   rest of the same Krylov process (0 = FP32 from the first iteration).
+	   The solution's large components form in the first decades of residual
+	   reduction; computing them in FP64 keeps the result's distance to the
+	   FP64 solve's iterate far below FP32 rounding. */
+	double fp64_head;
 } fs_krylov_settings;
 
 /* Fill `s` with the reference defaults (gmres.hh:414-418) and device defaults. */

@@ -94,9 +94,34 @@ static int call_diag(or_diag *d, const double *x, int64_t n, double res) {
 
 /* ------------------------------------------------------ vector ops --- */
 
+/* Summation order of the reductions.  0 (default): the reference's serial
+ * left-to-right loop.  The others exist only to measure how far a solver's
+ * iteration count moves when the same sums are taken in another valid
+ * order, as a parallel reduction takes them:
+ *   1: blocks of 4096 products summed left to right, then the block sums
+ *      left to right (a two-level reduction);
+ *   2: right to left. */
+static int dot_order = 0;
+OR_API void or_set_dot_order(int order) { dot_order = order; }
+
 /* seq.hh:282-295, res += x_i * y_i left to right */
 static double dot(int64_t n, const double *x, const double *y) {
 	double res = 0.0;
+	if (dot_order == 1) {
+		for (int64_t b = 0; b < n; b += 4096) {
+			const int64_t e = b + 4096 < n ? b + 4096 : n;
+			double part = 0.0;
+			for (int64_t i = b; i < e; ++i)
+				part += x[i] * y[i];
+			res += part;
+		}
+		return res;
+	}
+	if (dot_order == 2) {
+		for (int64_t i = n - 1; i >= 0; --i)
+			res += x[i] * y[i];
+		return res;
+	}
 	for (int64_t i = 0; i < n; ++i)
 		res += x[i] * y[i];
 	return res;

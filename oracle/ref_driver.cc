@@ -17,7 +17,13 @@
 // Output file:
 //   int32 status, iters, restarts; float res0, res, sol0, sol, rhs;
 //   int64 nhist; double hist[nhist]; double x[n]
+// Timing (bench.py's reference arm): with REF_DRIVER_TIMES=<file> set, the
+// diagnostic also takes a steady-clock time stamp at every call (the
+// reference's loops call it once per iteration), and the driver writes
+//   int64 nstamp; double seconds_since_solve_start[nstamp]; double total
+// where total is the wall time of the whole solver call (set-up included).
 #include <array>
+#include <chrono>
 #include <cstdio>
 #include <cstdint>
 #include <cstdlib>
@@ -44,10 +50,16 @@ void rd(std::FILE * f, T * p, std::size_t n) {
 		throw std::runtime_error("short read");
 }
 
+using clk = std::chrono::steady_clock;
+
 struct recorder {
 	std::vector<double> * hist;
+	std::vector<double> * stamps; // null unless timing was asked for
+	clk::time_point t0;
 	template<class V>
 	bool operator()(const V &, double r) const {
+		if (stamps)
+			stamps->push_back(std::chrono::duration<double>(clk::now() - t0).count());
 		hist->push_back(r);
 		return false;
 	}
@@ -117,10 +129,12 @@ int main(int argc, char ** argv) {
 	const bool zero_guess = std::atoi(argv[6]) != 0;
 	const bool jacobi = std::string(argv[7]) == "jacobi";
 
-	std::vector<double> hist;
-	recorder diag{&hist};
+	std::vector<double> hist, stamps;
+	const char * times_path = std::getenv("REF_DRIVER_TIMES");
+	recorder diag{&hist, times_path ? &stamps : nullptr, clk::now()};
 	solve_info info;
 	int assert_failed = 0;
+	diag.t0 = clk::now();
 	try {
 		if (which == "cg") {
 			cg::settings s{maxiter, rtol, 0.f, zero_guess};
@@ -160,6 +174,17 @@ int main(int argc, char ** argv) {
 	catch (const std::runtime_error & e) {
 		std::fprintf(stderr, "assert: %s\n", e.what());
 		assert_failed = 1;
+	}
+	const double total = std::chrono::duration<double>(clk::now() - diag.t0).count();
+	if (times_path) {
+		std::FILE * t = std::fopen(times_path, "wb");
+		if (!t)
+			return 5;
+		int64_t ns = static_cast<int64_t>(stamps.size());
+		std::fwrite(&ns, sizeof(int64_t), 1, t);
+		std::fwrite(stamps.data(), sizeof(double), stamps.size(), t);
+		std::fwrite(&total, sizeof(double), 1, t);
+		std::fclose(t);
 	}
 
 	std::FILE * o = std::fopen(argv[2], "wb");

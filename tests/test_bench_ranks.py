@@ -62,3 +62,30 @@ def test_reference_arm_runs_on_rank_zero_only():
                        text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip() == ""
+
+
+def test_reference_arm_times_one_complete_solve():
+    """The reference arm's steps are consecutive chunks of one complete
+    solve: the K timed steps fit inside the measured solve, and the solve is
+    the reference's (its iteration count for the workload)."""
+    import json
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                        "--workload", "poisson2d-64", "--steps", "4", "--warmup", "3"],
+                       cwd=str(ROOT), capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "s"
+    assert line["ms_per_step"] * line["steps"] <= line["value"] * 1e3 * (1 + 1e-9)
+    solve = line["reference_solve"]
+    assert solve["status"] == "converged_rtol"
+    assert len(solve["chunk_s"]) == 7
+    assert abs(sum(solve["chunk_s"]) - line["value"]) <= 0.05 * line["value"] + 1e-3
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle as O
+    sys.path.insert(0, str(ROOT))
+    from flecsolve_gb300 import problems as P
+    A, b = P.workload("poisson2d-64")
+    assert solve["iters"] == O.solve("cg", A, b, maxiter=20000, rtol=1e-8).iters
+    assert line["cpu_baseline"]["kind"] == ("reference" if O.ref_available() else "port")
+    assert line["cpu_baseline"]["projected"] is False
+    assert line["config"]["rows"] == A.nrows and line["config"]["nnz"] == A.nnz
