@@ -22,11 +22,12 @@ STATUS_NAMES = {0: "ok", 1: "bad handle", 2: "size mismatch", 3: "out of memory"
 ERR_BAD_HANDLE, ERR_SIZE_MISMATCH, ERR_OUT_OF_MEMORY, ERR_CUDA = 1, 2, 3, 4
 ERR_NON_FINITE, ERR_BREAKDOWN, ERR_INVALID_ARG, ERR_NO_DEVICE, ERR_UNSUPPORTED = 5, 6, 7, 8, 9
 ERR_IO = 10
+ERR_CALLBACK = 11
 
 F64, F32 = 0, 1
 BC_NONE, BC_DIRICHLET, BC_NEUMANN = 0, 1, 2
-CG, BICGSTAB, GMRES, CG_MIXED, BICGSTAB_MIXED, GMRES_MIXED = 0, 1, 2, 3, 4, 5
-PRECOND_NONE, PRECOND_JACOBI, PRECOND_DIAG, PRECOND_CSR = 0, 1, 2, 3
+CG, BICGSTAB, GMRES, CG_MIXED, BICGSTAB_MIXED, GMRES_MIXED, FCG = 0, 1, 2, 3, 4, 5, 6
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_DIAG, PRECOND_CSR, PRECOND_SOLVER = 0, 1, 2, 3, 4
 LEFT, RIGHT = 0, 1
 ORTHO_CGS2, ORTHO_MGS, ORTHO_AUTO = 0, 1, 2
 REFINE_RESTART, REFINE_RELIABLE = 0, 1
@@ -98,11 +99,13 @@ class BdfState(C.Structure):
 
 
 class Precond(C.Structure):
-    _fields_ = [("kind", C.c_int), ("diag", C.c_void_p), ("op", C.c_void_p)]
+    _fields_ = [("kind", C.c_int), ("diag", C.c_void_p), ("op", C.c_void_p),
+                ("solver", C.c_void_p)]
 
 
 DIAG_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_double)
 RESIDUAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p)
+OP_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)
 RHS_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)
 TIME_SOLVE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_int))
 
@@ -200,6 +203,7 @@ _PROTOS = {
                          C.POINTER(Precond), C.POINTER(_vp)],
     "fs_krylov_destroy": [_vp],
     "fs_krylov_set_diagnostic": [_vp, DIAG_FN, _vp],
+    "fs_shell_create": [_vp, C.c_int64, C.c_int64, OP_FN, _vp, C.POINTER(_vp)],
     "fs_krylov_settings_get": [_vp, C.POINTER(KrylovSettings)],
     "fs_krylov_settings_set": [_vp, C.POINTER(KrylovSettings)],
     "fs_krylov_apply": [_vp, _vp, _vp, C.POINTER(SolveInfo)],

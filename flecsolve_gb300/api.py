@@ -32,7 +32,8 @@ from ._lib import check, lib
 
 __all__ = ["Context", "Vector", "Multi", "CSR", "SolveInfo", "Future", "op", "vec", "mat",
            "batch_cg", "batch_tuning", "block_cg",
-           "cg", "bicgstab", "gmres", "mixed_cg", "mixed_bicgstab", "mixed_gmres"]
+           "cg", "bicgstab", "gmres", "fcg", "mixed_cg", "mixed_bicgstab", "mixed_gmres",
+           "Shell"]
 
 
 class Context:
@@ -461,6 +462,42 @@ class Multi:
 
 # ------------------------------------------------------------- op:: ----
 
+class Shell(CSR):
+    """``op::make_shell(f)`` (operators/shell.hh:26-95): a caller-defined
+    operator ``f(x, y)`` that writes ``y = Op(x)`` on FP64 device vectors of
+    ``ctx`` (through any Vector / CSR / solver call).  Usable wherever an
+    operator goes: ``apply``, residuals, and every solver as A or as the
+    preconditioner.  An exception in ``f`` stops the solve with
+    ``FsError`` (FS_ERR_CALLBACK)."""
+
+    def __init__(self, ctx: Context, f, nrows: int, ncols: int = None, var=None):
+        self.ctx = ctx
+        self.var = var
+        self.nrows = int(nrows)
+        self.ncols = int(nrows if ncols is None else ncols)
+        self.error = None
+
+        def _cb(user, xh, yh):
+            xv, yv = (Vector.__new__(Vector) for _ in range(2))
+            for v, hnd in ((xv, xh), (yv, yh)):
+                v.ctx = ctx
+                v.h = C.c_void_p(hnd)
+            try:
+                f(xv, yv)
+                return 0
+            except Exception as e:  # reported through the status code
+                self.error = e
+                return 1
+            finally:
+                xv.h = yv.h = None  # borrowed handles
+
+        self._cb = _lib.OP_FN(_cb)
+        h = C.c_void_p()
+        check(lib().fs_shell_create(ctx.h, self.nrows, self.ncols, self._cb, None, C.byref(h)),
+              ctx.h, "fs_shell_create")
+        self.h = h
+
+
 class _Identity:
     """``op::I`` (operators/shell.hh:317-318)."""
 
@@ -470,7 +507,7 @@ class _Jacobi:
 
 
 op = SimpleNamespace(I=_Identity(), jacobi=_Jacobi(), ref=lambda A: A, cref=lambda A: A,
-                     make_shared=lambda A: A)
+                     make_shared=lambda A: A, make_shell=Shell)
 vec = SimpleNamespace(make=lambda ctx, a, dtype="f64": Vector(ctx, a, dtype), Vector=Vector,
                       multi=Multi)
 mat = SimpleNamespace(csr=CSR)
@@ -537,8 +574,14 @@ class BoundSolver:
             pc.diag = P.h
             self._keep.append(P)
         elif isinstance(P, CSR):
+            # any operator: a stored or matrix-free CSR, or a shell
             pc.kind = _lib.PRECOND_CSR
             pc.op = P.h
+            self._keep.append(P)
+        elif isinstance(P, BoundSolver):
+            # a nested solver (the NKA / flexible-CG pattern)
+            pc.kind = _lib.PRECOND_SOLVER
+            pc.solver = P.h
             self._keep.append(P)
         else:
             raise TypeError(f"unsupported preconditioner {P!r}")
@@ -701,6 +744,7 @@ def _namespace(method, nwork, **defaults):
 cg = _namespace(_lib.CG, 4)                 # flecsolve/solvers/cg.hh:250-270
 bicgstab = _namespace(_lib.BICGSTAB, 8)     # bicgstab.hh:193-216
 gmres = _namespace(_lib.GMRES, 104, max_krylov_dim=-1, pre_side="right", restart=False)  # gmres.hh:366-438
+fcg = _namespace(_lib.FCG, 5)               # cg.hh:145-244, 272-290 (flexible CG)
 mixed_cg = _namespace(_lib.CG_MIXED, 4)     # FP32 inner PCG in FP64 refinement
 mixed_bicgstab = _namespace(_lib.BICGSTAB_MIXED, 8)
 mixed_gmres = _namespace(_lib.GMRES_MIXED, 104, max_krylov_dim=-1, pre_side="right", restart=False)

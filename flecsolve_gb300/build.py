@@ -37,7 +37,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
 
 CU_SOURCES = ["context.cu", "spmv.cu", "krylov.cu", "gmres.cu", "batched.cu", "blockcg.cu",
               "adjoint.cu", "noalloc.cu", "matrix_market.cu", "nka.cu", "fvm.cu",
-              "bdf.cu"]
+              "bdf.cu", "generic.cu"]
 
 
 def _nvcc() -> str:
@@ -112,6 +112,24 @@ def build_cpp_tests(force: bool = False) -> Path:
     return out
 
 
+def build_template_test(force: bool = False):
+    """flecsolve's own solver templates over the device policy
+    (tests/cpp/test_flecsolve_templates.cc), built where a flecsolve checkout
+    is staged (baseline/_ref); None elsewhere."""
+    ref = ROOT / "baseline" / "_ref"
+    if not (ref / "flecsolve").is_dir():
+        return None
+    out = BUILD / "test_flecsolve_templates"
+    src = ROOT / "tests" / "cpp" / "test_flecsolve_templates.cc"
+    deps = [src, INCLUDE / "fsgpu.h", INCLUDE / "flecsolve_gb300" / "flecsolve_device.hh",
+            BUILD / "libfsgpu.so"]
+    if force or _stale(out, deps):
+        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", str(INCLUDE),
+              "-I", str(ROOT / "oracle" / "ref_shim"), "-I", str(ref), str(src), "-o", str(out),
+              "-L", str(BUILD), "-lfsgpu", f"-Wl,-rpath,{BUILD}"])
+    return out
+
+
 def build_oracle() -> None:
     oracle = str(ROOT / "oracle")
     ref = os.environ.get("FLECSOLVE_REF")
@@ -125,6 +143,7 @@ def build_all(force: bool = False, verbose: bool = False) -> None:
     build_oracle()
     build_gpu(force, verbose)
     build_cpp_tests(force)
+    build_template_test(force)
 
 
 if __name__ == "__main__":

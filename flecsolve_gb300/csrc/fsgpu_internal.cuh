@@ -127,7 +127,14 @@ struct Csr {
 	// matrix-free finite-volume operator (no rows, columns or values stored;
 	// only the operator applies and the Jacobi diagonal are available)
 	FvmOp *fvm = nullptr;
+	// caller-defined operator (fs_shell_create): y = shell_fn(shell_user, x,
+	// y); nothing stored
+	fs_op_fn shell_fn = nullptr;
+	void *shell_user = nullptr;
 };
+
+// an operator that stores no rows (matrix-free finite-volume or shell)
+inline bool stores_no_rows(const Csr *A) { return A->fvm || A->shell_fn; }
 
 // index format an SpMV on A uses (the requested one, or the next one the
 // matrix supports)
@@ -177,9 +184,16 @@ int check_launch(Ctx *ctx, const char *what);
 // The calls that need stored rows, columns or values refuse a matrix-free
 // operator
 inline int reject_matrix_free(const Csr *A, const char *what) {
-	return A->fvm ? set_err(A->ctx, FS_ERR_INVALID_ARG, "%s: not available for a matrix-free operator", what)
-	              : FS_OK;
+	return stores_no_rows(A)
+	           ? set_err(A->ctx, FS_ERR_INVALID_ARG,
+	                     "%s: not available for a matrix-free or shell operator", what)
+	           : FS_OK;
 }
+
+// y = A x for a shell operator: the caller's callback, with the context's
+// stream ordered before and after it (a callback may use the legacy stream
+// or its own)
+int shell_apply(const Csr *A, Vec *x, Vec *y);
 
 // Programmatic dependent launch: a kernel launched with launch_pdl may be
 // scheduled while the previous kernel on the stream is still finishing (its

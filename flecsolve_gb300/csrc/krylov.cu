@@ -1790,7 +1790,7 @@ FS_API int fs_krylov_create(fs_ctx h, int method, const fs_krylov_settings *set,
 	if (!ok_ctx(ctx) || !ok_csr(A) || !out || !set)
 		return FS_ERR_BAD_HANDLE;
 	*out = nullptr;
-	if (method < FS_CG || method > FS_GMRES_MIXED)
+	if (method < FS_CG || method > FS_FCG)
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_krylov_create: unknown method %d", method);
 	if (A->nrows != A->ncols)
 		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_krylov_create: operator must be square");
@@ -1811,33 +1811,55 @@ FS_API int fs_krylov_create(fs_ctx h, int method, const fs_krylov_settings *set,
 			s->P.diag = d;
 		}
 		else if (P->kind == FS_PRECOND_CSR) {
-			// a CSR preconditioner is accepted when it is diagonal (the D^-1
-			// operator of util/test/mesh.hh:123-140) and turned into a vector
+			// a CSR preconditioner whose entries are all on the diagonal (the
+			// D^-1 operator of util/test/mesh.hh:123-140) becomes a diagonal
+			// vector fused into the device loops; any other operator is
+			// applied as its own step (generic.cu)
 			Csr *M = reinterpret_cast<Csr *>(P->op);
-			if (!ok_csr(M) || M->nrows != A->nrows) {
+			if (!ok_csr(M) || M->nrows != A->nrows || M->ncols != A->nrows || M->ctx != ctx) {
 				delete s;
 				return set_err(ctx, FS_ERR_BAD_HANDLE, "fs_krylov_create: bad CSR preconditioner");
 			}
-			std::vector<int> hc(M->nnz);
-			if (M->nnz)
-				cudaMemcpy(hc.data(), M->col, M->nnz * sizeof(int), cudaMemcpyDeviceToHost);
-			bool diagonal = true;
-			for (int64_t i = 0; i < M->nrows && diagonal; ++i)
-				for (int k = M->h_rowptr[i]; k < M->h_rowptr[i + 1]; ++k)
-					if (hc[k] != i)
-						diagonal = false;
-			if (!diagonal) {
-				delete s;
-				return set_err(ctx, FS_ERR_UNSUPPORTED,
-				               "fs_krylov_create: only diagonal CSR preconditioners are supported");
+			bool diagonal = !stores_no_rows(M);
+			if (diagonal) {
+				std::vector<int> hc(M->nnz);
+				if (M->nnz)
+					cudaMemcpy(hc.data(), M->col, M->nnz * sizeof(int), cudaMemcpyDeviceToHost);
+				for (int64_t i = 0; i < M->nrows && diagonal; ++i)
+					for (int k = M->h_rowptr[i]; k < M->h_rowptr[i + 1]; ++k)
+						if (hc[k] != i)
+							diagonal = false;
 			}
 			s->P.kind = FS_PRECOND_CSR;
 			s->P.op = M;
+			s->pc_diagonal = diagonal;
+		}
+		else if (P->kind == FS_PRECOND_SOLVER) {
+			Solver *inner = reinterpret_cast<Solver *>(P->solver);
+			if (!ok_slv(inner) || inner->n != A->nrows || inner->ctx != ctx || inner == s) {
+				delete s;
+				return set_err(ctx, FS_ERR_BAD_HANDLE, "fs_krylov_create: bad solver preconditioner");
+			}
+			s->P.solver = inner;
 		}
 		else if (P->kind != FS_PRECOND_NONE && P->kind != FS_PRECOND_JACOBI) {
 			delete s;
 			return set_err(ctx, FS_ERR_INVALID_ARG, "fs_krylov_create: unknown preconditioner kind");
 		}
+	}
+	if (s->P.kind == FS_PRECOND_JACOBI && A->shell_fn) {
+		delete s;
+		return set_err(ctx, FS_ERR_INVALID_ARG,
+		               "fs_krylov_create: Jacobi needs the operator's diagonal; a shell operator stores none");
+	}
+	const bool mixed_method =
+		method == FS_CG_MIXED || method == FS_BICGSTAB_MIXED || method == FS_GMRES_MIXED;
+	if (mixed_method && (A->shell_fn || (s->P.kind == FS_PRECOND_CSR && !s->pc_diagonal) ||
+	                     s->P.kind == FS_PRECOND_SOLVER)) {
+		delete s;
+		return set_err(ctx, FS_ERR_UNSUPPORTED,
+		               "fs_krylov_create: mixed-precision solvers take a stored or matrix-free "
+		               "operator and an identity, Jacobi or diagonal preconditioner");
 	}
 	if (method == FS_GMRES || method == FS_GMRES_MIXED) {
 		int m = set->max_krylov_dim < 0 ? set->base.maxiter : set->max_krylov_dim;
@@ -1848,7 +1870,8 @@ FS_API int fs_krylov_create(fs_ctx h, int method, const fs_krylov_settings *set,
 		}
 	}
 	int st = solver_alloc(s);
-	if (st == FS_OK && (s->P.kind == FS_PRECOND_DIAG || s->P.kind == FS_PRECOND_CSR)) {
+	if (st == FS_OK && (s->P.kind == FS_PRECOND_DIAG ||
+	                    (s->P.kind == FS_PRECOND_CSR && s->pc_diagonal))) {
 		// copy the diagonal into the solver (FP64 + FP32)
 		if (s->P.kind == FS_PRECOND_CSR) {
 			Csr *M = s->P.op;
@@ -1975,6 +1998,8 @@ FS_API int fs_krylov_apply(fs_solver h, fs_vec bh, fs_vec xh, fs_solve_info *inf
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_krylov_apply: b and x must differ");
 	cudaSetDevice(ctx->device);
 	s->mixed_outer = s->mixed_inner = 0;
+	if (needs_generic(s))
+		return generic_apply(s, b, x, info);
 	// the operator's values may have changed since the last apply
 	// (fs_csr_update_values, fs_fv_assemble): derived arrays are rebuilt in
 	// place, so captured graphs stay valid

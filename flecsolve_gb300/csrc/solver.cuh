@@ -7,6 +7,7 @@
 #pragma once
 
 #include <map>
+#include <memory>
 #include <tuple>
 #include <vector>
 
@@ -60,10 +61,13 @@ struct GmState {
 	int pad_;
 };
 
+struct Solver;
+
 struct Precond {
 	int kind = FS_PRECOND_NONE;
 	Vec *diag = nullptr;
 	Csr *op = nullptr;
+	Solver *solver = nullptr;   // FS_PRECOND_SOLVER
 };
 
 struct GraphKey {
@@ -82,6 +86,7 @@ struct Solver {
 	fs_krylov_settings set{};
 	Csr *A = nullptr;
 	Precond P;
+	bool pc_diagonal = false;  // an FS_PRECOND_CSR with only diagonal entries
 	fs_diag_fn diag = nullptr;
 	void *diag_user = nullptr;
 
@@ -116,6 +121,9 @@ struct Solver {
 	int64_t hhist_count = 0;
 	int mixed_outer = 0, mixed_inner = 0;
 	int graph_nodes_launched = 0;
+	// work vectors of the host-stepped loops (generic.cu), as vector handles
+	// the caller's operator callbacks receive
+	std::vector<std::unique_ptr<Vec>> gwork;
 
 	const double *dinv64() const;
 	const float *dinv32() const;
@@ -134,5 +142,10 @@ int solver_norms(Solver *s, Vec *b, Vec *x, bool with_x, int gmres_rule);
 int solver_hist(Solver *s, int cap);
 int ensure_val32(Csr *A);
 int ensure_dinv(Csr *A);
+
+// host-stepped loops for operators and preconditioners the fused device
+// loops do not take (generic.cu)
+bool needs_generic(const Solver *s);
+int generic_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info);
 
 }  // namespace fsg

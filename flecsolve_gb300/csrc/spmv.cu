@@ -167,6 +167,8 @@ __global__ void dinv_kernel(int n, const int *__restrict__ rp, const int *__rest
 int ensure_val32(Csr *A) {
 	if (A->val32_valid)
 		return FS_OK;
+	if (A->shell_fn)
+		return set_err(A->ctx, FS_ERR_UNSUPPORTED, "a shell operator has no FP32 values");
 	Ctx *ctx = A->ctx;
 	if (!A->val32) {
 		size_t padded = (size_t)((A->nnz + 15) / 16 * 16 + 16);
@@ -184,6 +186,8 @@ int ensure_val32(Csr *A) {
 int ensure_dinv(Csr *A) {
 	if (A->dinv_valid)
 		return FS_OK;
+	if (A->shell_fn)
+		return set_err(A->ctx, FS_ERR_INVALID_ARG, "a shell operator has no stored diagonal");
 	Ctx *ctx = A->ctx;
 	if (!A->dinv) {
 		size_t padded = (size_t)((A->nrows + 31) / 32 * 32 + 32);
@@ -409,6 +413,23 @@ int transpose_spmv(Csr *A, const double *x, double *y) {
 	return st;
 }
 
+// y = A x through the caller's callback.  The context's stream is drained
+// first, so x is complete whichever stream or host code the callback reads it
+// from; the callback returns once y is written or its writes are enqueued on
+// the context's stream.
+int shell_apply(const Csr *A, Vec *x, Vec *y) {
+	Ctx *ctx = A->ctx;
+	if (x->dtype != FS_F64 || y->dtype != FS_F64)
+		return set_err(ctx, FS_ERR_UNSUPPORTED, "a shell operator applies to FP64 vectors");
+	if (x->n != A->ncols || y->n != A->nrows)
+		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "shell operator: vector sizes do not match");
+	FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	const int rc = A->shell_fn(A->shell_user, reinterpret_cast<fs_vec>(x), reinterpret_cast<fs_vec>(y));
+	if (rc != 0)
+		return set_err(ctx, FS_ERR_CALLBACK, "shell operator callback returned %d", rc);
+	return FS_OK;
+}
+
 }  // namespace fsg
 
 using namespace fsg;
@@ -580,6 +601,24 @@ FS_API int fs_csr_row_blocks(fs_csr h, int64_t *nblk) {
 	return FS_OK;
 }
 
+FS_API int fs_shell_create(fs_ctx h, int64_t nrows, int64_t ncols, fs_op_fn fn, void *user,
+                           fs_csr *out) {
+	Ctx *ctx = reinterpret_cast<Ctx *>(h);
+	if (!ok_ctx(ctx) || !out)
+		return FS_ERR_BAD_HANDLE;
+	*out = nullptr;
+	if (!fn || nrows < 0 || ncols < 0)
+		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_shell_create: a callback and sizes >= 0 are required");
+	Csr *A = new Csr();
+	A->ctx = ctx;
+	A->nrows = nrows;
+	A->ncols = ncols;
+	A->shell_fn = fn;
+	A->shell_user = user;
+	*out = reinterpret_cast<fs_csr>(A);
+	return FS_OK;
+}
+
 FS_API int fs_csr_destroy(fs_csr h) {
 	Csr *A = reinterpret_cast<Csr *>(h);
 	if (!ok_csr(A))
@@ -661,6 +700,8 @@ FS_API int fs_csr_spmv(fs_csr h, fs_vec xh, fs_vec yh, int mode) {
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_spmv: x and y must differ");
 	if (mode != FS_SPMV_FMA && mode != FS_SPMV_EXACT)
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_spmv: bad mode");
+	if (A->shell_fn)
+		return shell_apply(A, x, y);
 	if (A->nrows == 0)
 		return FS_OK;
 	FS_TRY(ensure_sym(A, x->dtype == FS_F32));
@@ -689,6 +730,11 @@ FS_API int fs_csr_residual(fs_csr h, fs_vec bh, fs_vec xh, fs_vec rh) {
 		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_csr_residual: shapes/dtypes do not match");
 	if (x == r)
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_residual: x and r must differ");
+	if (A->shell_fn) {
+		// op::core::residual (operators/core.hh:129-142): apply, then r = b - r
+		FS_TRY(shell_apply(A, x, r));
+		return fs_vec_subtract(bh, rh, rh);
+	}
 	if (A->nrows == 0)
 		return FS_OK;
 	FS_TRY(ensure_sym(A, x->dtype == FS_F32));

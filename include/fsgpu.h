@@ -48,7 +48,8 @@ enum fs_status {
 	FS_ERR_INVALID_ARG = 7,    /* argument out of range                     */
 	FS_ERR_NO_DEVICE = 8,      /* no usable CUDA device                     */
 	FS_ERR_UNSUPPORTED = 9,    /* valid request this build does not handle  */
-	FS_ERR_IO = 10             /* file missing, unreadable or malformed     */
+	FS_ERR_IO = 10,            /* file missing, unreadable or malformed     */
+	FS_ERR_CALLBACK = 11       /* a caller's operator callback failed       */
 };
 
 /* value types of vectors and matrix values */
@@ -219,6 +220,25 @@ FS_API int fs_csr_spmv_transpose(fs_csr A, fs_vec x, fs_vec y);
 /* dinv_i = 1 / a_ii, the D^-1 operator of flecsolve/util/test/mesh.hh:123-140 */
 FS_API int fs_csr_diag_inv(fs_csr A, fs_vec dinv);
 
+/* Caller-defined operator: op::make_shell / op::base
+ * (flecsolve/operators/shell.hh:26-95, operators/core.hh:29-78).  The
+ * callback computes y = Op(x) for FS_F64 device vectors of the operator's
+ * context, on the host thread that called the library, and returns 0 on
+ * success (anything else stops the caller's solve with FS_ERR_CALLBACK).  It
+ * may call any fs_* function on the context (SpMVs, vector ops, a bound
+ * solver's apply) or launch its own kernels.  The library drains the
+ * context's stream before each call, so x is complete; the callback returns
+ * once y is written, or once the work that writes y is enqueued on the
+ * context's stream (fs_ctx_stream; every fs_* call on the context is).  The
+ * handle is an fs_csr that stores no rows: fs_csr_spmv / fs_csr_residual and
+ * every Krylov solver (as A or as the preconditioner) take it; the calls that
+ * need stored values (value updates, transposes, index formats, parcsr,
+ * batched and block solves, Jacobi of it) return FS_ERR_INVALID_ARG.  Destroy
+ * with fs_csr_destroy. */
+typedef int (*fs_op_fn)(void *user, fs_vec x, fs_vec y);
+FS_API int fs_shell_create(fs_ctx ctx, int64_t nrows, int64_t ncols, fs_op_fn fn, void *user,
+                           fs_csr *out);
+
 /* Row-block distributed SpMV of mat::parcsr (flecsolve/matrices/parcsr.hh:
  * 60-91, topo/csr.hh:482-618): rows are split into `parts` contiguous blocks
  * as flecsi::util::equal_map splits them (parcsr.hh:149-151: blocks of
@@ -253,20 +273,33 @@ enum fs_method {
 	FS_GMRES = 2,        /* op::gmres, gmres.hh:78-241                   */
 	FS_CG_MIXED = 3,     /* FP32 inner PCG inside FP64 refinement        */
 	FS_BICGSTAB_MIXED = 4, /* FP32 BiCGSTAB, FP64 residual replacement   */
-	FS_GMRES_MIXED = 5   /* FP32 Arnoldi cycles, FP64 restart residual   */
+	FS_GMRES_MIXED = 5,  /* FP32 Arnoldi cycles, FP64 restart residual   */
+	FS_FCG = 6           /* op::fcg, flexible CG, cg.hh:145-244          */
 };
 
+/* The preconditioner slot P of krylov_parameters (krylov_parameters.hh:
+ * 41-78): any operator.  Identity, Jacobi and diagonal preconditioners (and
+ * a CSR whose entries are all on the diagonal, the reference's D^-1
+ * operator) are fused into the device loops of every method; any other
+ * operator -- a general CSR, a matrix-free or shell handle, a bound solver
+ * (the NKA / nested-solver pattern of solvers/test/nka.cc:72-80) -- is
+ * applied as its own step of host-stepped loops that follow the reference's
+ * operation order (FP64 methods and FS_FCG; the mixed methods return
+ * FS_ERR_UNSUPPORTED for it). */
 enum fs_precond_kind {
 	FS_PRECOND_NONE = 0,   /* op::I, operators/shell.hh:94-95             */
 	FS_PRECOND_JACOBI = 1, /* D^-1 of A (util/test/mesh.hh:123-140)       */
 	FS_PRECOND_DIAG = 2,   /* caller-given diagonal vector (z_i = d_i r_i) */
-	FS_PRECOND_CSR = 3     /* a CSR operator applied by SpMV               */
+	FS_PRECOND_CSR = 3,    /* an fs_csr operator: z = P r                  */
+	FS_PRECOND_SOLVER = 4  /* a bound solver: z = solve(r) with its own
+	                          settings, operator and preconditioner         */
 };
 
 typedef struct {
 	int kind;            /* enum fs_precond_kind */
 	fs_vec diag;         /* FS_PRECOND_DIAG      */
 	fs_csr op;           /* FS_PRECOND_CSR       */
+	fs_solver solver;    /* FS_PRECOND_SOLVER    */
 } fs_precond;
 
 enum fs_gmres_side { FS_LEFT = 0, FS_RIGHT = 1 };

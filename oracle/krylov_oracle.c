@@ -10,6 +10,7 @@
  *     (flecsolve/matrices/seq.hh:177-193),
  *   - op::core::residual r = b - A x (flecsolve/operators/core.hh:129-142),
  *   - op::cg::apply (flecsolve/solvers/cg.hh:43-139),
+ *   - op::fcg::apply, the flexible CG (flecsolve/solvers/cg.hh:145-244),
  *   - op::bicgstab::apply (flecsolve/solvers/bicgstab.hh:39-187),
  *   - op::gmres::apply / orthogonalize / Givens / back_solve / correct
  *     (flecsolve/solvers/gmres.hh:54-348),
@@ -269,6 +270,99 @@ done:
 	free(z);
 	free(p);
 	free(w);
+	return info->status;
+}
+
+/* ---------------------------------------------------- flexible CG --- */
+
+/* The preconditioner of or_fcg: P itself, or (inner_iters > 0) that many
+ * iterations of Jacobi-PCG on A with P as its preconditioner, from a zero
+ * guess, rtol 0 (a nested cg::solver bound as the preconditioner, the
+ * solvers/test/nka.cc:72-80 pattern) */
+typedef struct {
+	const or_csr *A, *P;
+	int inner_iters;
+} fcg_pc;
+
+static void fcg_papply(const fcg_pc *pc, int64_t n, const double *r, double *z) {
+	if (pc->inner_iters <= 0) {
+		papply(pc->P, n, r, z);
+		return;
+	}
+	or_settings s = {pc->inner_iters, 0.f, 0.f, 1};
+	or_info info;
+	or_cg(&s, pc->A, pc->P, r, z, NULL, &info);
+}
+
+/* flecsolve/solvers/cg.hh:145-244 */
+OR_API int or_fcg(const or_settings *s, const or_csr *A, const or_csr *P, int inner_iters,
+                  const double *b, double *u, or_diag *diag, or_info *info) {
+	int64_t n = A->nrows;
+	memset(info, 0, sizeof(*info));
+	info->status = OR_UNKNOWN;
+	info->res_norm_initial = NAN; /* indeterminate in the reference */
+	fcg_pc pc = {A, P, inner_iters};
+	double *wk = malloc(5 * n * sizeof(double));
+	double *r = wk, *v = wk + n, *w = wk + 2 * n, *q = wk + 3 * n, *d = wk + 4 * n;
+
+	double b_norm = l2norm(n, b);
+	if (b_norm == 0.0)
+		b_norm = 1.0;
+	const double terminate_tol = s->rtol * b_norm;
+	info->rhs_norm = (float)b_norm;
+	if (s->use_zero_guess) {
+		info->sol_norm_initial = 0;
+		setv(n, 0., u);
+		copy(n, b, r);
+	}
+	else {
+		info->sol_norm_initial = (float)l2norm(n, u);
+		residual(A, b, u, r);
+	}
+	double current_res = l2norm(n, r);
+	if (current_res < terminate_tol) {
+		info->res_norm_initial = (float)current_res;
+		info->res_norm_final = (float)current_res;
+		info->status = OR_CONVERGED_RTOL;
+		goto done;
+	}
+	double rho = 0;
+	for (int iter = 0; iter < s->maxiter; iter++) {
+		fcg_papply(&pc, n, r, v);
+		or_spmv(A, v, w);
+		double alpha = dot(n, v, r);
+		double beta = dot(n, v, w);
+		if (iter > 0) {
+			double gamma = dot(n, v, q);
+			axpy(n, (-gamma) / rho, d, v, d);
+			axpy(n, (-gamma) / rho, q, w, q);
+			rho = beta - (gamma * gamma) / rho;
+		}
+		else {
+			copy(n, v, d);
+			copy(n, w, q);
+			rho = beta;
+		}
+		axpy(n, alpha / rho, d, u, u);
+		axpy(n, -alpha / rho, q, r, r);
+		current_res = l2norm(n, r);
+		if (call_diag(diag, u, n, current_res)) {
+			info->iters = iter + 1;
+			info->status = OR_CONVERGED_USER;
+			break;
+		}
+		if (current_res < terminate_tol) {
+			info->iters = iter + 1;
+			info->status = OR_CONVERGED_RTOL;
+			break;
+		}
+	}
+	info->res_norm_final = (float)current_res;
+	info->sol_norm_final = (float)l2norm(n, u);
+	if (info->iters == 0)
+		info->status = OR_DIVERGED_ITERS;
+done:
+	free(wk);
 	return info->status;
 }
 

@@ -165,13 +165,15 @@ def serial_dot(x, y):
 
 def solve(method, A, b, x0=None, *, maxiter=2000, rtol=1e-8,
           use_zero_guess=True, precond="jacobi", krylov_dim=30,
-          side="right", restart=True, diag=None) -> Result:
+          side="right", restart=True, diag=None, inner_iters=0, pmat=None) -> Result:
     """Run the oracle solver.  ``diag(x, res) -> bool`` is the optional user
-    diagnostic; the residual history is always recorded."""
+    diagnostic; the residual history is always recorded.  ``pmat``: a CSR
+    preconditioner operator (instead of ``precond``).  ``inner_iters`` (FCG
+    only): the preconditioner is that many Jacobi-PCG iterations on A."""
     L = lib()
     n = A.nrows
     m = _Mat(A)
-    P = _DinvMat(A) if precond == "jacobi" else None
+    P = _Mat(pmat) if pmat is not None else (_DinvMat(A) if precond == "jacobi" else None)
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
     hist = np.zeros(maxiter + 1)
@@ -192,6 +194,9 @@ def solve(method, A, b, x0=None, *, maxiter=2000, rtol=1e-8,
     elif method == "gmres":
         gs = _GmresSettings(base, int(krylov_dim), 0 if side == "left" else 1, int(bool(restart)))
         L.or_gmres(C.byref(gs), C.byref(m.s), Pp, _dp(b), _dp(x), C.byref(d), C.byref(info))
+    elif method == "fcg":
+        L.or_fcg(C.byref(base), C.byref(m.s), Pp, int(inner_iters), _dp(b), _dp(x), C.byref(d),
+                 C.byref(info))
     else:
         raise ValueError(method)
     return Result(STATUS[info.status], info.iters, info.restarts,
@@ -218,7 +223,7 @@ def write_problem(path, A, b, x0):
 
 def ref_solve(method, A, b, x0=None, *, maxiter=2000, rtol=1e-8,
               use_zero_guess=True, precond="jacobi", krylov_dim=30,
-              side="right", restart=True) -> Result:
+              side="right", restart=True, inner_iters=0) -> Result:
     """Run the reference's own templates (compiled from its headers)."""
     if not ref_available():
         raise RuntimeError("reference driver not built (oracle/_ref/ref_driver)")
@@ -227,8 +232,9 @@ def ref_solve(method, A, b, x0=None, *, maxiter=2000, rtol=1e-8,
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         write_problem(fin, A, b, x0)
+        pname = f"cg{int(inner_iters)}" if inner_iters > 0 else precond
         args = [str(REF_DRIVER), fin, fout, method, str(maxiter), repr(float(rtol)),
-                str(int(bool(use_zero_guess))), precond]
+                str(int(bool(use_zero_guess))), pname]
         if method == "gmres":
             args += [str(krylov_dim), side, str(int(bool(restart)))]
         subprocess.run(args, check=True, stdout=subprocess.PIPE, stderr=subprocess.PIPE)

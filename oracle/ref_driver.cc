@@ -12,8 +12,11 @@
 //   int64 n, int64 nnz, int64 rowptr[n+1], int32 col[nnz], double val[nnz],
 //   double b[n], double x0[n]
 // Command line:
-//   ref_driver <in> <out> <cg|bicgstab|gmres> <maxiter> <rtol> <zero_guess>
-//              <none|jacobi> [krylov_dim left|right restart]
+//   ref_driver <in> <out> <cg|bicgstab|gmres|fcg> <maxiter> <rtol> <zero_guess>
+//              <none|jacobi|cg<k>> [krylov_dim left|right restart]
+// cg<k> (fcg only): the preconditioner is the reference's cg::solver with
+// maxiter k, rtol 0, a zero guess and D^-1, bound as an operator (the
+// nested-solver pattern of flecsolve/solvers/test/nka.cc:72-80).
 // Output file:
 //   int32 status, iters, restarts; float res0, res, sol0, sol, rhs;
 //   int64 nhist; double hist[nhist]; double x[n]
@@ -151,6 +154,21 @@ int main(int argc, char ** argv) {
 				info = bicgstab::solver(s, std::move(w))(op::ref(Aop), op::ref(Pop), diag)(b, x);
 			else
 				info = bicgstab::solver(s, std::move(w))(op::ref(Aop), op::I, diag)(b, x);
+		}
+		else if (which == "fcg") {
+			fcg::settings s{maxiter, rtol, 0.f, zero_guess};
+			vec::seq_work<double, fcg::nwork> w{b};
+			const std::string pname = argv[7];
+			if (pname.rfind("cg", 0) == 0) {
+				cg::settings ps{std::atoi(pname.c_str() + 2), 0.f, 0.f, true};
+				auto inner = cg::solver(ps, vec::seq_work<double, cg::nwork>{b})(op::ref(Aop),
+				                                                               op::ref(Pop));
+				info = fcg::solver(s, std::move(w))(op::ref(Aop), op::ref(inner), diag)(b, x);
+			}
+			else if (jacobi)
+				info = fcg::solver(s, std::move(w))(op::ref(Aop), op::ref(Pop), diag)(b, x);
+			else
+				info = fcg::solver(s, std::move(w))(op::ref(Aop), op::I, diag)(b, x);
 		}
 		else if (which == "gmres") {
 			if (argc < 11)

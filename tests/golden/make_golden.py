@@ -44,6 +44,11 @@ CASES = [
      {"krylov_dim": 10, "use_zero_guess": False, "x0": ("uniform", 12), "rtol": 1e-10}),
     ("convdiff3d-16_gmres_norestart", "convdiff3d-16", "gmres",
      {"krylov_dim": 60, "restart": False, "maxiter": 60, "precond": "none"}),
+    # flexible CG (cg.hh:145-244): Jacobi, none, and a nested reference CG
+    # (5 Jacobi-PCG iterations, rtol 0, zero guess) bound as the preconditioner
+    ("poisson2d-128_fcg", "poisson2d-128", "fcg", {}),
+    ("diffusion3d-16_fcg_noprec", "diffusion3d-16", "fcg", {"precond": "none"}),
+    ("diffusion3d-16_fcg_cg5", "diffusion3d-16", "fcg", {"inner_iters": 5}),
 ]
 
 

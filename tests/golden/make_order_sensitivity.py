@@ -6,8 +6,10 @@ in another order.  This script runs the oracle -- the reference's solvers
 restated in C and pinned to them bit for bit -- on the full-size workloads
 with its reductions taken in two other valid orders (blocks of 4096 then the
 block sums; right to left) and records status and iteration count for each,
-in tests/golden/order_sensitivity.json.  The spread is the part of an
-iteration-count difference that comes from summation order alone.  Hours of
+in tests/golden/order_sensitivity.json, with the solution at the rows that
+tests/golden/full_size.json samples.  The spread is the part of an
+iteration-count (and forward-error) difference that comes from summation
+order alone.  Hours of
 CPU per GMRES run; each spec can run in its own process:
 
     python tests/golden/make_order_sensitivity.py convdiff3d-192:gmres:1
@@ -40,6 +42,8 @@ def run(spec: str) -> None:
     t0 = time.time()
     r = O.solve(method, A, b, maxiter=20000, rtol=1e-8, **SETTINGS[method])
     O.lib().or_set_dot_order(0)
+    full = json.loads((HERE / "full_size.json").read_text())
+    idx = full[wl][method]["x_sample_index"]
     out = HERE / "order_sensitivity.json"
     # several processes may finish at once: read and write under a lock
     with open(HERE / ".order_sensitivity.lock", "w") as lk:
@@ -48,7 +52,7 @@ def run(spec: str) -> None:
         data.setdefault(wl, {}).setdefault(method, {})[str(order)] = {
             "order": ORDERS[order], "status": r.status, "iters": r.iters,
             "restarts": r.restarts, "res_norm_final": r.res_norm_final,
-            "seconds_one_core": time.time() - t0}
+            "x_sample": r.x[idx].tolist(), "seconds_one_core": time.time() - t0}
         out.write_text(json.dumps(data, indent=1, sort_keys=True))
     print(spec, r.status, r.iters, flush=True)
 

@@ -108,3 +108,15 @@ def test_cpp_api_header_compiles_and_links():
     (running it needs a GPU: tests/test_gpu_cpp_api.py)."""
     exe = build.build_cpp_tests()
     assert exe.exists()
+
+
+def test_flecsolve_device_binding_compiles():
+    """include/flecsolve_gb300/flecsolve_device.hh under flecsolve's own
+    solver templates (where a flecsolve checkout is staged): the program that
+    runs them on the GPU builds and links against the library."""
+    from flecsolve_gb300 import build
+    build.build_gpu()
+    exe = build.build_template_test()
+    if exe is None:
+        pytest.skip("no flecsolve checkout staged in baseline/_ref")
+    assert exe.exists()

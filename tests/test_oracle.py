@@ -63,6 +63,7 @@ def test_oracle_matches_reference_fixture(name):
     ("cg", {"rtol": 1e-6}),
     ("bicgstab", {"precond": "none"}),
     ("gmres", {"krylov_dim": 7, "side": "left"}),
+    ("fcg", {"inner_iters": 3}),
 ])
 def test_oracle_matches_reference_live(method, kw):
     """Where the reference compiles (this container), compare live on a fresh
