@@ -135,7 +135,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-CODING_NAMES = {0: "colids", 1: "patterns", 2: "symmetric"}
+CODING_NAMES = {0: "colids", 1: "patterns", 2: "symmetric", 3: "grid"}
 
 
 def spmv_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, nsym=3):
@@ -145,13 +145,16 @@ def spmv_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, nsym=3):
     pattern-id byte per row + 16 bytes of warp offsets per 256-row block.
     Symmetric storage (2): the diagonal and `nsym` upper diagonals (3 for a
     7-point operator) + one pattern-id byte per row.  Pattern tables (<= 8 KB)
-    are read once per CTA out of L2 and not counted."""
+    are read once per CTA out of L2 and not counted.  Grid stencil (3): the
+    diagonal and upper diagonals only (rows addressed by grid coordinates)."""
     if coding == 0:
         mat = nnz * val_bytes + 4 * nnz + 4 * (nrows + 1)
     elif coding == 1:
         mat = nnz * val_bytes + nrows + 16 * nblk
-    else:
+    elif coding == 2:
         mat = (nsym + 1) * nrows * val_bytes + nrows
+    else:
+        mat = (nsym + 1) * nrows * val_bytes
     return mat + 2 * nrows * val_bytes
 
 
@@ -321,7 +324,7 @@ def run_spmv_only(args):
     best = dA.index_coding()
     out = {"mode": "spmv", "workload": args.workload, "rows": n, "nnz": nnz,
            "index_coding": CODING_NAMES[best]}
-    for coding in [c for c in (2, 1, 0) if c <= best]:
+    for coding in [c for c in (3, 2, 1, 0) if c <= best]:
         if dA.index_coding(coding) != coding:
             continue
         for dt, vb in (("f64", 8), ("f32", 4)):
@@ -782,7 +785,8 @@ def run_ours(args, ws, rank, local):
         "speedup_mixed_vs_fp64": ms_64 / ms_mx,
         "spmv_hbm_gbs": {"f64": gbs64, "f32": gbs32, "f64_ms": spmv64_ms, "f32_ms": spmv32_ms},
         "roofline": {"bound": "hbm",
-                     "kernel": {2: "spmv_sym_kernel<float> (FP32 CSR SpMV, symmetric storage: diagonal + upper diagonals)",
+                     "kernel": {3: "spmv_grid_kernel<float> (FP32 CSR SpMV, grid stencil: diagonal + upper diagonals addressed by grid coordinates, 16-byte loads)",
+                                2: "spmv_sym_kernel<float> (FP32 CSR SpMV, symmetric storage: diagonal + upper diagonals)",
                                 1: "spmv_pat_kernel<float> (FP32 CSR SpMV, row patterns, warp-specialised)",
                                 0: "spmv_rb_kernel<float> (FP32 CSR SpMV, int32 column ids)"}[coding],
                      "achieved": gbs32, "peak": peak, "unit": "GB/s", "frac": gbs32 / peak,

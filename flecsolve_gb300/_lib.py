@@ -162,6 +162,7 @@ _PROTOS = {
     "fs_csr_values_device_ptr": [_vp, C.POINTER(_vp)],
     "fs_csr_index_coding": [_vp, C.c_int, C.POINTER(C.c_int)],
     "fs_csr_row_blocks": [_vp, C.POINTER(_i64)],
+    "fs_csr_grid_dims": [_vp, C.POINTER(_i64)],
     "fs_csr_spmv": [_vp, _vp, _vp, C.c_int],
     "fs_csr_residual": [_vp, _vp, _vp, _vp],
     "fs_csr_spmv_transpose": [_vp, _vp, _vp],

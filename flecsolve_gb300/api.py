@@ -323,21 +323,22 @@ class CSR:
         check(lib().fs_csr_row_blocks(self.h, C.byref(n)), self.ctx.h)
         return n.value
 
-    CODINGS = {"colids": 0, "patterns": 1, "symmetric": 2}
+    CODINGS = {"colids": 0, "patterns": 1, "symmetric": 2, "grid": 3}
 
     def index_coding(self, enable=None) -> int:
         """The index format the FP64 SpMV uses: 0 = column ids, 1 = row
         patterns (stencil operators: one pattern id per row, no column ids or
         row offsets read), 2 = row patterns with symmetric storage (the
         diagonal and upper diagonals of a matrix that is symmetric bit for
-        bit).  `enable` switches it: True = the best format the matrix
-        supports, False = column ids, or a mode number / name; a format the
-        matrix (or its current values) does not support falls back to the
-        next one down."""
+        bit), 3 = the symmetric storage of a grid stencil addressed by grid
+        coordinates (no pattern ids, 16-byte loads).  `enable` switches it:
+        True = the best format the matrix supports, False = column ids, or a
+        mode number / name; a format the matrix (or its current values) does
+        not support falls back to the next one down."""
         if enable is None:
             req = -1
         elif isinstance(enable, bool):
-            req = 2 if enable else 0
+            req = 3 if enable else 0
         elif isinstance(enable, str):
             req = self.CODINGS[enable]
         else:
@@ -345,6 +346,12 @@ class CSR:
         a = C.c_int()
         check(lib().fs_csr_index_coding(self.h, req, C.byref(a)), self.ctx.h)
         return a.value
+
+    def grid_dims(self):
+        """(nx, ny, nz) of a grid-stencil matrix, (0, 0, 0) otherwise."""
+        d = (C.c_int64 * 3)()
+        check(lib().fs_csr_grid_dims(self.h, d), self.ctx.h)
+        return tuple(int(v) for v in d)
 
     def values(self) -> np.ndarray:
         """The current values (row order) copied to the host."""
@@ -672,14 +679,18 @@ def _info(i) -> "SolveInfo":
 
 def batch_cg(A: CSR, offsets, b: Vector, x: Vector, maxiter: int, rtol: float,
              use_zero_guess: bool = True, delta: float = 0.0, cluster: int = 0,
-             threads: int = 0):
+             threads: int = 0, fp64_head: float = None):
     """Solve the independent systems on the diagonal blocks of ``A`` (system
     s = rows offsets[s]:offsets[s+1]) in one persistent launch, one thread-
     block cluster per system; returns one :class:`SolveInfo` per system.
-    ``cluster``/``threads`` = 0 lets the autotuner choose."""
+    ``cluster``/``threads`` = 0 lets the autotuner choose; ``fp64_head``: FP64
+    iterations until each system's residual is below that fraction of its
+    ||b|| (None: the library default, 1e-2; 0: FP32 from the start)."""
     off = np.ascontiguousarray(offsets, dtype=np.int64)
     nsys = off.size - 1
     st = _settings(_lib.CG_MIXED, maxiter, rtol, 0.0, use_zero_guess, inner_rtol=delta)
+    if fp64_head is not None:
+        st.fp64_head = float(fp64_head)
     infos = (_lib.SolveInfo * nsys)()
     check(lib().fs_batch_cg_solve(A.ctx.h, C.byref(st), A.h, nsys,
                                   off.ctypes.data_as(C.POINTER(C.c_int64)), b.h, x.h, int(cluster),

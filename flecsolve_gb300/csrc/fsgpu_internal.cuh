@@ -67,6 +67,7 @@ constexpr int kMaxPat = 256;
 constexpr int kCodingColIds = 0;
 constexpr int kCodingPatterns = 1;
 constexpr int kCodingSym = 2;   // row patterns + symmetric storage (diagonal, upper diagonals)
+constexpr int kCodingGrid = 3;  // symmetric storage of a grid stencil: rows addressed by (i, j, k)
 constexpr int kMaxSym = 4;      // positive column offsets of the symmetric storage
 
 struct FvmOp;
@@ -92,7 +93,7 @@ struct Csr {
 	int npat = 0;
 	unsigned char *plen = nullptr;  // nonzeros per pattern
 	short *pwb = nullptr;           // per row block, per 32-row warp: first nonzero - k0
-	int coding = kCodingSym;        // requested format; the next one down when absent
+	int coding = kCodingGrid;       // requested format; the next one down when absent
 	// symmetric storage (square row-pattern matrices whose patterns pair every
 	// offset -d with +d, at most kMaxSym of them): per pattern entry a slot
 	// code (0 diagonal, k + 1 upper offset k, -(k + 1) lower offset k), per
@@ -105,6 +106,10 @@ struct Csr {
 	int2 *stab = nullptr;           // npat x kPatW: {value offset, column offset} from r
 	int nsym = 0;
 	int64_t sym_ld = 0;
+	// grid stencil (0 when the matrix is none): the symmetric storage's
+	// offsets are 1, nx, nx ny (as many as nsym) and row r = i + nx (j + ny k)
+	// holds exactly its neighbours inside the nx x ny x nz grid
+	int grid_nx = 0, grid_ny = 0, grid_nz = 0;
 	double *sym64 = nullptr;
 	float *sym32 = nullptr;
 	unsigned *sym_flag = nullptr;   // device: set by the build when a pair differs
@@ -141,8 +146,9 @@ inline bool stores_no_rows(const Csr *A) { return A->fvm || A->shell_fn; }
 inline int active_coding(const Csr *A, bool f32 = false) {
 	if (!A->pid || A->coding == kCodingColIds)
 		return kCodingColIds;
-	if (A->coding == kCodingSym && (f32 ? A->sym32_valid : A->sym64_valid))
-		return kCodingSym;
+	if (A->coding >= kCodingSym && (f32 ? A->sym32_valid : A->sym64_valid))
+		return A->coding == kCodingGrid && A->grid_nx % 4 == 0 && A->grid_nx > 0 ? kCodingGrid
+		                                                                         : kCodingSym;
 	return kCodingPatterns;
 }
 

@@ -11,6 +11,7 @@
 // Its scratch -- one partial sum per CTA plus a completion counter -- lives in
 // the file-scope array below, which every GPU that loads the library holds
 // until the process exits.  The array caps the number of CTAs, hence n.
+#include <cuda.h>
 #include <mutex>
 
 #include "fsgpu_internal.cuh"
@@ -58,9 +59,60 @@ dot_noalloc_kernel(const double *__restrict__ x, const double *__restrict__ y, i
 	}
 }
 
-// device address of the scratch array, looked up once per device
+// The scratch array's device address belongs to a CUDA context (the device's
+// primary context under the runtime API, or a context the caller made
+// current through the driver API): it is looked up once per context and
+// cached under that context.
+typedef CUresult (*ctx_get_current_fn)(CUcontext *);
 std::mutex g_na_mutex;
-double *g_na_addr[64] = {};
+constexpr int kNaCtxSlots = 64;
+CUcontext g_na_ctx[kNaCtxSlots] = {};
+double *g_na_addr[kNaCtxSlots] = {};
+int g_na_used = 0;
+
+ctx_get_current_fn ctx_get_current() {
+	static ctx_get_current_fn fn = [] {
+		void *p = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) !=
+		        cudaSuccess ||
+		    q != cudaDriverEntryPointSuccess) {
+			cudaGetLastError();
+			p = nullptr;
+		}
+		return reinterpret_cast<ctx_get_current_fn>(p);
+	}();
+	return fn;
+}
+
+// the scratch address in the calling thread's current context (null on error)
+double *scratch_address() {
+	ctx_get_current_fn get = ctx_get_current();
+	if (!get)
+		return nullptr;
+	CUcontext c = nullptr;
+	if (get(&c) != CUDA_SUCCESS)
+		return nullptr;
+	std::lock_guard<std::mutex> lock(g_na_mutex);
+	for (int i = 0; c && i < g_na_used; ++i)
+		if (g_na_ctx[i] == c)
+			return g_na_addr[i];
+	// host code cannot use the symbol itself as a device address; the lookup
+	// also makes the device's primary context current when none is
+	double *p = nullptr;
+	if (cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_scratch) != cudaSuccess || !p) {
+		cudaGetLastError();
+		return nullptr;
+	}
+	if (!c && get(&c) != CUDA_SUCCESS)
+		return nullptr;
+	if (c && g_na_used < kNaCtxSlots) {
+		g_na_ctx[g_na_used] = c;
+		g_na_addr[g_na_used] = p;
+		++g_na_used;
+	}
+	return p;
+}
 
 }  // namespace
 }  // namespace fsg
@@ -74,25 +126,13 @@ extern "C" FS_API int fs_dot_f64_noalloc(const double *x, const double *y, int64
 	if (n > FS_DOT_NOALLOC_MAX_N)
 		return FS_ERR_INVALID_ARG;  // beyond the scratch array's capacity
 	int dev = 0;
-	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+	if (cudaGetDevice(&dev) != cudaSuccess) {
 		cudaGetLastError();
 		return FS_ERR_NO_DEVICE;
 	}
-	double *scratch = nullptr;
-	{
-		std::lock_guard<std::mutex> lock(g_na_mutex);
-		if (!g_na_addr[dev]) {
-			// host code cannot use the symbol itself as a device address
-			double *p = nullptr;
-			cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_scratch);
-			if (e != cudaSuccess || !p) {
-				cudaGetLastError();
-				return FS_ERR_CUDA;
-			}
-			g_na_addr[dev] = p;
-		}
-		scratch = g_na_addr[dev];
-	}
+	double *scratch = scratch_address();
+	if (!scratch)
+		return FS_ERR_CUDA;
 	cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
 	// the array keeps the previous call's contents: the counter must start at 0
 	if (cudaMemsetAsync(scratch + kNaMaxBlocks, 0, sizeof(unsigned), st) != cudaSuccess) {

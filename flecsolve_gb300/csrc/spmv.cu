@@ -136,6 +136,70 @@ static bool sym_slots(const std::vector<int> &ptab, const std::vector<int> &plen
 	return true;
 }
 
+// Grid stencil: the positive offsets are 1, nx and nx ny (one, two or three
+// of them) and every row r = i + nx (j + ny k) holds exactly its neighbours
+// inside the nx x ny x nz grid, in column order.  Rows fall in at most 64
+// boundary classes (i, j, k each at the low end, the high end or inside);
+// every row of a class must carry the class's pattern.
+static bool grid_dims(int64_t n, const std::vector<int> &sofs, const std::vector<unsigned char> &pid,
+                      const std::vector<int> &ptab, const std::vector<int> &plen, int dims[3]) {
+	const int K = (int)sofs.size();
+	if (K < 1 || K > 3 || sofs[0] != 1 || n < 1)
+		return false;
+	int64_t nx = n, ny = 1, nz = 1;
+	if (K >= 2) {
+		nx = sofs[1];
+		if (nx < 2 || n % nx)
+			return false;
+		ny = n / nx;
+	}
+	if (K == 3) {
+		if (sofs[2] % nx || n % sofs[2])
+			return false;
+		ny = sofs[2] / nx;
+		nz = n / sofs[2];
+	}
+	if (nx > (1 << 30) || ny > (1 << 30) || nz > (1 << 30))
+		return false;
+	const int64_t o[3] = {1, nx, nx * ny};
+	int cls_pid[64];
+	std::fill(cls_pid, cls_pid + 64, -1);
+	int64_t r = 0;
+	for (int64_t k = 0; k < nz; ++k)
+		for (int64_t j = 0; j < ny; ++j)
+			for (int64_t i = 0; i < nx; ++i, ++r) {
+				const int64_t c[3] = {i, j, k}, e[3] = {nx, ny, nz};
+				int cls = 0;
+				for (int d = 0; d < 3; ++d)
+					cls = cls * 4 + (c[d] == 0 ? 1 : 0) + (c[d] == e[d] - 1 ? 2 : 0);
+				const int p = pid[r];
+				if (cls_pid[cls] == p)
+					continue;
+				if (cls_pid[cls] >= 0)
+					return false;
+				// the class's pattern: lower neighbours from the far offset in,
+				// the diagonal, upper neighbours
+				int want[kPatW], len = 0;
+				for (int d = K - 1; d >= 0; --d)
+					if (c[d] > 0)
+						want[len++] = (int)-o[d];
+				want[len++] = 0;
+				for (int d = 0; d < K; ++d)
+					if (c[d] < e[d] - 1)
+						want[len++] = (int)o[d];
+				if (len != plen[p])
+					return false;
+				for (int q = 0; q < len; ++q)
+					if (ptab[(size_t)p * kPatW + q] != want[q])
+						return false;
+				cls_pid[cls] = p;
+			}
+	dims[0] = (int)nx;
+	dims[1] = (int)ny;
+	dims[2] = (int)nz;
+	return true;
+}
+
 static std::vector<int4> block_info(const std::vector<int> &blk, const std::vector<int> &rp) {
 	std::vector<int4> info(blk.size() > 0 ? blk.size() - 1 : 0);
 	for (size_t b = 0; b + 1 < blk.size(); ++b)
@@ -245,7 +309,7 @@ __global__ void k_sym_build(int n, const int *__restrict__ rp, const double *__r
 }
 
 int ensure_sym(Csr *A, bool f32) {
-	if (!A->pslot || A->coding != kCodingSym || A->sym_state == 0)
+	if (!A->pslot || A->coding < kCodingSym || A->sym_state == 0)
 		return FS_OK;
 	bool &valid = f32 ? A->sym32_valid : A->sym64_valid;
 	if (valid)
@@ -571,6 +635,12 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 			}
 			A->nsym = (int)sofs.size();
 			A->sym_ld = sym_ld;
+			int dims[3];
+			if (grid_dims(nrows, sofs, pid, ptab, plen, dims)) {
+				A->grid_nx = dims[0];
+				A->grid_ny = dims[1];
+				A->grid_nz = dims[2];
+			}
 		}
 	}
 	*out = reinterpret_cast<fs_csr>(A);
@@ -582,14 +652,25 @@ FS_API int fs_csr_index_coding(fs_csr h, int enable, int *active) {
 	if (!ok_csr(A))
 		return FS_ERR_BAD_HANDLE;
 	FS_TRY(reject_matrix_free(A, "fs_csr_index_coding"));
-	if (enable > kCodingSym)
-		return set_err(A->ctx, FS_ERR_INVALID_ARG, "fs_csr_index_coding: enable must be -1, 0, 1 or 2");
+	if (enable > kCodingGrid)
+		return set_err(A->ctx, FS_ERR_INVALID_ARG,
+		               "fs_csr_index_coding: enable must be -1, 0, 1, 2 or 3");
 	if (enable >= 0)
 		A->coding = enable;
 	if (active) {
 		FS_TRY(ensure_sym(A, false));
 		*active = active_coding(A);
 	}
+	return FS_OK;
+}
+
+FS_API int fs_csr_grid_dims(fs_csr h, int64_t dims[3]) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	if (!ok_csr(A) || !dims)
+		return FS_ERR_BAD_HANDLE;
+	dims[0] = A->grid_nx;
+	dims[1] = A->grid_ny;
+	dims[2] = A->grid_nz;
 	return FS_OK;
 }
 

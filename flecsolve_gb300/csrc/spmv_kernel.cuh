@@ -175,6 +175,21 @@ __device__ __forceinline__ unsigned char ld_stream(const unsigned char *p) {
 	return (unsigned char)v;
 }
 
+// 16 bytes (four floats / two doubles) from a 16-byte aligned address,
+// through the read-only path
+__device__ __forceinline__ void ld_vec16(const float *p, float (&o)[4]) {
+	const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+	o[0] = t.x;
+	o[1] = t.y;
+	o[2] = t.z;
+	o[3] = t.w;
+}
+__device__ __forceinline__ void ld_vec16(const double *p, double (&o)[2]) {
+	const double2 t = __ldg(reinterpret_cast<const double2 *>(p));
+	o[0] = t.x;
+	o[1] = t.y;
+}
+
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
@@ -422,6 +437,7 @@ static inline int launch_spmv_as(Ctx *ctx, const CsrDev<V> &d, const V *x, const
 
 #include "spmv_pat.cuh"
 #include "spmv_sym.cuh"
+#include "spmv_grid.cuh"
 #include "spmv_fvm.cuh"
 
 namespace fsg {
@@ -441,7 +457,13 @@ static inline int launch_spmv(Ctx *ctx, const Csr *A, const V *vals, const V *x,
 	}
 	const int coding = active_coding(A, F32);
 	const bool own_vals = vals == (F32 ? (const V *)A->val32 : (const V *)A->val);
-	if (coding == kCodingSym && own_vals) {
+	if (coding == kCodingGrid && own_vals && grid_aligned<V>(A, x, dscale)) {
+		if constexpr (SCALE)
+			return launch_spmv_grid<V, EXACT>(ctx, A, GatherScale<V>{x, dscale}, epi);
+		else
+			return launch_spmv_grid<V, EXACT>(ctx, A, GatherX<V>{x}, epi);
+	}
+	if (coding >= kCodingSym && own_vals) {
 		if constexpr (SCALE)
 			return launch_spmv_sym<V, EXACT>(ctx, A, GatherScale<V>{x, dscale}, epi);
 		else

@@ -73,6 +73,10 @@ struct GatherX {
 	__device__ V at(int c) const { return __ldg(x + c); }
 	// the same value, read with a 256-byte L2 fetch (contiguous sweeps)
 	__device__ V at_stream(int c) const { return ld_stream(x + c); }
+	// 16 bytes from x + c (c a multiple of 16 / sizeof(V), x 16-byte aligned)
+	template<int W>
+	__device__ void at_vec(int c, V (&o)[W]) const { ld_vec16(x + c, o); }
+	__device__ bool aligned16() const { return ((uintptr_t)x & 15) == 0; }
 };
 
 // y = A D x (right Jacobi preconditioning without materialising D x); the
@@ -83,6 +87,16 @@ struct GatherScale {
 	__device__ void init() {}
 	__device__ V at(int c) const { return mul_rn(__ldg(d + c), __ldg(x + c)); }
 	__device__ V at_stream(int c) const { return mul_rn(ld_stream(d + c), ld_stream(x + c)); }
+	template<int W>
+	__device__ void at_vec(int c, V (&o)[W]) const {
+		V dv[W];
+		ld_vec16(d + c, dv);
+		ld_vec16(x + c, o);
+#pragma unroll
+		for (int q = 0; q < W; ++q)
+			o[q] = mul_rn(dv[q], o[q]);
+	}
+	__device__ bool aligned16() const { return (((uintptr_t)x | (uintptr_t)d) & 15) == 0; }
 };
 
 // Issue the copies of row block `b` (bounds m) into stage `st`; the

@@ -162,14 +162,23 @@ FS_API int fs_csr_values_device_ptr(fs_csr A, double **dval);
  *    most 256 distinct sequences of column offsets c - r (stencil operators),
  *    one byte per row names its sequence; neither column ids nor row offsets
  *    are read.
- *  2 symmetric storage (the default): row patterns of a square matrix whose
- *    values are symmetric bit for bit are read from the diagonal and the upper
- *    diagonals only (a(r, r-d) = a(r-d, r)).  Derived from the current values
- *    and checked whenever they change; an asymmetric matrix uses format 1.
- * enable: 0, 1 or 2 requests a format (a matrix falls back to the best format
- * it supports), -1 leaves it unchanged; *active (may be NULL) = the format the
+ *  2 symmetric storage: row patterns of a square matrix whose values are
+ *    symmetric bit for bit are read from the diagonal and the upper diagonals
+ *    only (a(r, r-d) = a(r-d, r)).  Derived from the current values and
+ *    checked whenever they change; an asymmetric matrix uses format 1.
+ *  3 grid stencil (the default): the symmetric storage of a 1-, 2- or 3-D
+ *    grid stencil (positive offsets 1, nx, nx ny; every row holds exactly its
+ *    neighbours inside the grid, found at creation) with nx a multiple of 4:
+ *    rows are addressed by their grid coordinates, no pattern id is read, and
+ *    16-byte loads serve 4 (FP32) or 2 (FP64) rows.  Other matrices use
+ *    format 2.  Formats 1-3 give the bits of format 0.
+ * enable: 0 .. 3 requests a format (a matrix falls back to the best format it
+ * supports), -1 leaves it unchanged; *active (may be NULL) = the format the
  * FP64 SpMV uses now. */
 FS_API int fs_csr_index_coding(fs_csr A, int enable, int *active);
+/* the grid of a grid-stencil matrix (format 3): dims = {nx, ny, nz}, all 0
+ * when the matrix is none; no counterpart in the reference */
+FS_API int fs_csr_grid_dims(fs_csr A, int64_t dims[3]);
 /* number of SpMV row blocks (at most 256 rows and 1792 nonzeros each, a
  * longer row alone); no counterpart in the reference */
 FS_API int fs_csr_row_blocks(fs_csr A, int64_t *nblk);
@@ -333,12 +342,15 @@ typedef struct {
 	                        replacements (0 = 0.1 for CG and batched CG,
 	                        1e-2 for BiCGSTAB)                              */
 	int max_outer;       /* restart: maximum refinement steps            */
-	/* reliable mixed CG: FP64 iterations until the residual is below
-	   fp64_head * ||b||, then FP32 recurrences with FP64 replacement for the
-	   rest of the same Krylov process (0 = FP32 from the first iteration).
-	   The solution's large components form in the first decades of residual
-	   reduction; computing them in FP64 keeps the result's distance to the
-	   FP64 solve's iterate far below FP32 rounding. */
+	/* reliable mixed CG and batched CG: FP64 iterations until the residual
+	   is below fp64_head * ||b||, then FP32 recurrences with FP64
+	   replacement for the rest of the same Krylov process (default 1e-2;
+	   0 = FP32 from the first iteration).  The solution's large components
+	   form in the first decades of residual reduction.  Computed in FP32,
+	   they cost the iterates orthogonality (up to 13 % more iterations on
+	   2-D log-normal diffusion systems of 256^2) and put the result ~2e-8
+	   from the FP64 solve's iterate at 256^3 (3e-3: 4e-9); the default head
+	   gives the FP64 iteration count on every system tested. */
 	double fp64_head;
 } fs_krylov_settings;
 
@@ -436,9 +448,11 @@ FS_API int fs_block_cg_solve_mixed(fs_ctx ctx, const fs_krylov_settings *s, fs_c
  *  - n <= FS_DOT_NOALLOC_MAX_N (64 Mi elements, one scratch slot per 4096
  *    elements); larger n returns FS_ERR_INVALID_ARG and launches nothing.
  *  - `stream` is a cudaStream_t (NULL = legacy default stream) of the current
- *    device.  The first call on a device looks up the scratch array's device
- *    address (cudaGetSymbolAddress); make that first call before any stream
- *    capture.
+ *    device.  The scratch array's device address belongs to a CUDA context:
+ *    the first call under each context (the device's primary context, or a
+ *    context the caller made current with the driver API) looks it up
+ *    (cudaGetSymbolAddress) and caches it for that context; make that first
+ *    call before any stream capture.
  *  - Every call shares the one scratch array, so calls whose kernels can
  *    overlap on the GPU (different streams without ordering) race.
  *  - The result is deterministic for a given n and agrees with fs_vec_dot to

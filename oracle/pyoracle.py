@@ -247,3 +247,21 @@ def ref_solve(method, A, b, x0=None, *, maxiter=2000, rtol=1e-8,
     return Result(STATUS[int(head[0])], int(head[1]), int(head[2]),
                   float(norms[0]), float(norms[1]), float(norms[2]),
                   float(norms[3]), float(norms[4]), hist, x)
+
+
+def solve_orders(method, A, b, x0=None, **kw):
+    """The oracle solve with its dot products summed in the reference's
+    serial order and in two other valid orders (blocks of 4096 then the block
+    sums; right to left).  The spread of their iteration counts is the part
+    of a count difference that comes from summation order alone (BiCGSTAB
+    and GMRES amplify it)."""
+    L = lib()
+    out = []
+    try:
+        for order in (0, 1, 2):
+            L.or_set_dot_order(order)
+            out.append(solve(method, A, b, x0, **kw))
+    finally:
+        L.or_set_dot_order(0)
+    return out
+

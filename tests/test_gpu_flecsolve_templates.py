@@ -7,8 +7,11 @@ templates produced over the reference's serial vectors.
 The program is built where a flecsolve checkout is staged (baseline/_ref);
 without one these tests are skipped.  Bars: the same status, iterations
 within +-2, the first residual norms handed to the diagnostic within 1e-10,
-the CG / FCG solution within 1e-10 of the reference's, the BiCGSTAB / GMRES
-forward error within 2x the reference's own."""
+the CG solution within 1e-10 of the reference's; the flexible CG, BiCGSTAB
+and GMRES forward error within 2x the reference's own (the flexible CG's
+one-step truncation amplifies the rounding of its dot products: without a
+preconditioner two correct runs that differ only in summation order end
+1.5e-9 apart at 16^3)."""
 import json
 import os
 import subprocess
@@ -76,7 +79,7 @@ def test_reference_templates_on_device(program, name):
     assert np.allclose(hist[:k], g["hist"][:k], rtol=1e-10, atol=0)
     if c["status"] != "converged_rtol":
         return
-    if c["method"] in ("cg", "fcg"):
+    if c["method"] == "cg":
         assert np.linalg.norm(x - g["x"]) <= 1e-10 * np.linalg.norm(g["x"])
     else:
         import scipy.sparse.linalg as spla

@@ -17,10 +17,12 @@ Bars:
   FP64 one: its forward error against a tight FP64 solve (rtol 1e-12) is
   within 1 % of the FP64 iterate's own.
 * BiCGSTAB / GMRES: iterations within the reference's own spread over
-  summation orders (+-2 beyond it); forward error on the sampled rows within
-  2x the reference's own, against a tight FP64 solve.
-* Batched (512 systems): every system converged with true residual <= rtol,
-  iterations within +-3 of the reference's CG on that system alone.
+  summation orders (+-2 beyond it); forward error on the sampled rows,
+  against a tight FP64 solve, within 2x the largest of the reference's own
+  runs under the three summation orders.
+* Batched (512 systems, the default FP64 head to 1e-2 ||b||): every system
+  converged with true residual <= rtol, iterations within +-3 of the
+  reference's CG on that system alone.
 * Block CG (128^3, 16 right-hand sides): every column's true residual <=
   rtol, and its forward error within 2x that of the single-vector FP64 CG.
 """
@@ -124,9 +126,16 @@ def c3(ctx):
     yield dict(A=A, b=b, S=S, dA=dA, vb=vb, vx=vx, x_tight=x_tight)
 
 
-def _sampled_accuracy(ref, x, x_tight):
+def _sampled_accuracy(wl, method, x, x_tight):
+    """Forward error of x on the sampled rows against a tight FP64 solve, and
+    the largest forward error among the reference's own runs: its serial
+    order (full_size.json) and the two other summation orders of the same
+    algorithm (order_sensitivity.json)."""
+    ref = FULL[wl][method]
     idx = np.asarray(ref["x_sample_index"])
-    e_ref = _rel(np.asarray(ref["x_sample"]), x_tight[idx])
+    samples = [ref["x_sample"]] + [v["x_sample"] for v in ORDERS.get(wl, {}).get(method, {}).values()
+                                   if "x_sample" in v]
+    e_ref = max(_rel(np.asarray(xs), x_tight[idx]) for xs in samples)
     return _rel(x[idx], x_tight[idx]), e_ref
 
 
@@ -137,7 +146,7 @@ def test_convdiff3d_192_bicgstab_against_reference(ctx, c3):
     it_ref, bar = _iter_bar("convdiff3d-192", "bicgstab")
     assert abs(info.iters - it_ref) <= bar
     assert _relres(c3["S"], c3["b"], x) <= 1e-8
-    e, e_ref = _sampled_accuracy(ref, x, c3["x_tight"])
+    e, e_ref = _sampled_accuracy("convdiff3d-192", "bicgstab", x, c3["x_tight"])
     assert e <= 2.0 * e_ref + 1e-12
 
 
@@ -157,7 +166,7 @@ def test_convdiff3d_192_gmres30_against_reference(ctx, c3, ortho):
     it_ref, bar = _iter_bar("convdiff3d-192", "gmres")
     assert abs(info.iters - it_ref) <= bar
     assert _relres(c3["S"], c3["b"], x) <= 1e-8
-    e, e_ref = _sampled_accuracy(ref, x, c3["x_tight"])
+    e, e_ref = _sampled_accuracy("convdiff3d-192", "gmres", x, c3["x_tight"])
     assert e <= 2.0 * e_ref + 1e-12
 
 

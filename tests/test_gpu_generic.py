@@ -75,7 +75,14 @@ def test_shell_operator_as_A(ctx, name, ns):
     assert info.status == c["status"]
     assert abs(info.iters - c["iters"]) <= ITER_TOL
     assert len(calls) >= info.iters
-    assert np.linalg.norm(b - A.to_scipy() @ x) / np.linalg.norm(b) <= 1e-8 * 1.01
+    relres = np.linalg.norm(b - A.to_scipy() @ x) / np.linalg.norm(b)
+    if c["kwargs"].get("side") == "left":
+        # left preconditioning stops on the preconditioned residual: the
+        # true residual is bounded by the reference's own
+        ref_relres = np.linalg.norm(b - A.to_scipy() @ g["x"]) / np.linalg.norm(b)
+        assert relres <= 2.0 * ref_relres
+    else:
+        assert relres <= 1e-8 * 1.01
     if ns is fs.cg:
         assert _rel(x, g["x"]) <= 1e-10
     else:
@@ -120,7 +127,12 @@ def test_fcg_against_reference_fixture(ctx, name):
     info = fs.fcg.solver(fs.fcg.settings(maxiter=2000, rtol=1e-8))(dA, prec)(vb, vx)
     assert info.status == c["status"]
     assert abs(info.iters - c["iters"]) <= ITER_TOL
-    assert _rel(vx.numpy(), g["x"]) <= 1e-10
+    # the one-step truncation amplifies the rounding of the dot products
+    # (without a preconditioner two runs that differ only in summation order
+    # end 1.5e-9 apart): forward error within 2x the reference's own
+    import scipy.sparse.linalg as spla
+    xs = spla.spsolve(A.to_scipy().tocsc(), b)
+    assert _rel(vx.numpy(), xs) <= 2.0 * _rel(g["x"], xs) + 1e-12
 
 
 def test_fcg_with_a_bound_cg_as_preconditioner(ctx):

@@ -59,12 +59,26 @@ def test_against_reference_fixture(ctx, name):
                       rtol=kw.pop("rtol", 1e-8), use_zero_guess=kw.pop("use_zero_guess", True))
     g = np.load(GOLD / f"{name}.npz")
     assert info.status == c["status"]
-    assert abs(info.iters - c["iters"]) <= ITER_TOL
     assert _true_relres(A, b, x) <= 1e-8 * 1.01
     if c["method"] == "cg":
+        assert abs(info.iters - c["iters"]) <= ITER_TOL
         assert _rel(x, g["x"]) <= X_RTOL_F64
     else:
+        _order_bar("bicgstab", A, b, info.iters, x0, maxiter=2000, rtol=1e-8, precond=prec,
+                   use_zero_guess=x0 is None)
         _bicgstab_accuracy_bar(A, b, x, g["x"])
+
+
+def _order_bar(method, A, b, iters, x0=None, **kw):
+    """BiCGSTAB and GMRES amplify the rounding of their dot products: the
+    reference's own iteration count moves with the summation order (on the
+    128^2 Poisson system its BiCGSTAB takes 259, 300 or 285 iterations for
+    three valid orders).  The bar: within the range of the reference
+    algorithm's counts over summation orders (the oracle, pinned bit for bit
+    to the reference in its serial order), +-2."""
+    rs = O.solve_orders(method, A, b, x0, **kw)
+    lo, hi = min(r.iters for r in rs), max(r.iters for r in rs)
+    assert lo - ITER_TOL <= iters <= hi + ITER_TOL, (iters, [r.iters for r in rs])
 
 
 def _bicgstab_accuracy_bar(A, b, x, x_ref):
@@ -149,7 +163,7 @@ def test_bicgstab_vs_oracle(ctx, wl, prec):
     r = O.solve("bicgstab", A, b, maxiter=4000, rtol=1e-8, precond=prec)
     info, x, _ = _run(ctx, fs.bicgstab, A, b, P_=prec, maxiter=4000, rtol=1e-8)
     assert info.status == r.status
-    assert abs(info.iters - r.iters) <= ITER_TOL
+    _order_bar("bicgstab", A, b, info.iters, maxiter=4000, rtol=1e-8, precond=prec)
     assert _true_relres(A, b, x) <= 1e-8 * 1.01
     _bicgstab_accuracy_bar(A, b, x, r.x)
 
@@ -207,7 +221,7 @@ def test_mixed_cg_index_formats(ctx, wl):
     dA = fs.CSR(ctx, A)
     vb = fs.Vector(ctx, b)
     res = {}
-    for coding in ("symmetric", "patterns", "colids"):
+    for coding in ("grid", "symmetric", "patterns", "colids"):
         dA.index_coding(coding)
         for rtol in (1e-8, 1e-11):
             vx = fs.Vector(ctx, A.nrows)
@@ -215,7 +229,7 @@ def test_mixed_cg_index_formats(ctx, wl):
                                      fs.mixed_cg.make_work(vb))(fs.op.ref(dA), fs.op.jacobi)
             info = slv(vb, vx)
             res[coding, rtol] = (info, vx.numpy(), slv.mixed_stats())
-    for coding in ("symmetric", "patterns", "colids"):
+    for coding in ("grid", "symmetric", "patterns", "colids"):
         info, x, (outer, inner) = res[coding, 1e-8]
         assert info.status == "converged_rtol"
         assert _true_relres(A, b, x) <= 1e-8
@@ -225,6 +239,7 @@ def test_mixed_cg_index_formats(ctx, wl):
         assert _rel(x2, xs) <= X_RTOL_MIXED
     assert abs(res["patterns", 1e-8][0].iters - res["colids", 1e-8][0].iters) <= 1
     assert abs(res["symmetric", 1e-8][0].iters - res["colids", 1e-8][0].iters) <= 1
+    assert abs(res["grid", 1e-8][0].iters - res["colids", 1e-8][0].iters) <= 1
     # with a diagnostic the loop reads back every iteration and a user stop
     # folds the pending solution step into x
     dA.index_coding("symmetric")
@@ -332,7 +347,7 @@ def test_gmres_cgs2_vs_oracle(ctx, wl):
     r = O.solve("gmres", A, b, maxiter=5000, rtol=1e-8, krylov_dim=30)
     info, x, _ = _run_gmres(ctx, A, b, maxiter=5000, rtol=1e-8, max_krylov_dim=30, restart=True)
     assert info.status == r.status == "converged_rtol"
-    assert abs(info.iters - r.iters) <= ITER_TOL
+    _order_bar("gmres", A, b, info.iters, maxiter=5000, rtol=1e-8, krylov_dim=30)
     _bicgstab_accuracy_bar(A, b, x, r.x)
 
 

@@ -43,10 +43,38 @@ def _pattern_rect(n2, rows, cols):
 
 
 PATTERN_CASES = ["poisson2d-128", "poisson2d-127", "diffusion3d-24", "diffusion3d-23",
-                 "convdiff3d-20", "rect-wide", "rect-tall"]
+                 "convdiff3d-20", "rect-wide", "rect-tall", "line-1000", "box-12x5x7"]
+
+
+def _grid_stencil(nx, ny, nz, seed):
+    """A symmetric diffusion-like stencil on an nx x ny x nz grid (1-D when
+    ny = nz = 1, 2-D when nz = 1) with seeded off-diagonals."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    n = nx * ny * nz
+    dims = [d for d in (nx, ny, nz)]
+    offs = [1, nx, nx * ny]
+    K = 1 if ny == nz == 1 else (2 if nz == 1 else 3)
+    r = np.arange(n)
+    c = np.stack([r % nx, (r // nx) % ny, r // (nx * ny)])
+    rows, cols, vals = [r], [r], [np.full(n, 8.0)]
+    for d in range(K):
+        keep = c[d] < dims[d] - 1
+        v = rng.uniform(-1.0, -0.1, int(keep.sum()))
+        rows += [r[keep], r[keep] + offs[d]]
+        cols += [r[keep] + offs[d], r[keep]]
+        vals += [v, v]
+    M = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(n, n))
+    M.sort_indices()
+    return P.CSR(n, n, M.indptr.astype(np.int64), M.indices.astype(np.int32), M.data)
 
 
 def _pattern_matrix(name):
+    if name == "line-1000":
+        return _grid_stencil(1000, 1, 1, 5)
+    if name == "box-12x5x7":
+        return _grid_stencil(12, 5, 7, 6)
     if name == "rect-wide":
         return _pattern_rect(61, 3001, 61 * 61)   # ncols > nrows, odd sizes
     if name == "rect-tall":
@@ -56,21 +84,29 @@ def _pattern_matrix(name):
 
 @pytest.mark.parametrize("wl", PATTERN_CASES)
 def test_row_pattern_spmv_matches_column_ids(ctx, wl):
-    """Stencil matrices carry row patterns.  The symmetric storage (coding 2:
-    diagonal and upper diagonals, lower entries read from their partners) and
-    the row-pattern SpMV (coding 1, warp-specialised, row offsets from pattern
-    lengths) give the same bits as the one reading column ids (coding 0), in
-    every mode and type, on odd sizes and rectangular matrices.  A matrix that
-    is not symmetric bit for bit falls back to coding 1."""
+    """Stencil matrices carry row patterns.  The grid-stencil kernel (coding
+    3: the symmetric storage addressed by grid coordinates, 16-byte loads),
+    the symmetric storage (coding 2: diagonal and upper diagonals, lower
+    entries read from their partners) and the row-pattern SpMV (coding 1,
+    warp-specialised, row offsets from pattern lengths) give the same bits as
+    the one reading column ids (coding 0), in every mode and type, on odd
+    sizes, 1-, 2- and 3-D grids and rectangular matrices.  A matrix that is
+    not symmetric bit for bit falls back to coding 1, a symmetric one that is
+    not a grid stencil with nx a multiple of 4 to coding 2."""
     A = _pattern_matrix(wl)
     x = P.uniform(43, A.ncols)
     dA = fs.CSR(ctx, A)
     S = A.to_scipy()
     symmetric = A.nrows == A.ncols and (S != S.T).nnz == 0
-    best = 2 if symmetric else 1
+    nx, ny, nz = dA.grid_dims()
+    if wl.startswith(("poisson2d", "diffusion3d", "line", "box")):
+        side = int(wl.split("-")[1].split("x")[0])
+        assert nx == side and nx * ny * nz == A.nrows
+    grid = symmetric and nx > 0 and nx % 4 == 0
+    best = 3 if grid else (2 if symmetric else 1)
     assert dA.index_coding() == best
     out = {}
-    for coding in (2, 1, 0):
+    for coding in (3, 2, 1, 0):
         assert dA.index_coding(coding) == min(coding, best)
         for dt in ("f64", "f32"):
             vx, vy = fs.Vector(ctx, x.astype(np.float32) if dt == "f32" else x, dt), fs.Vector(ctx, A.nrows, dt)
@@ -95,7 +131,7 @@ def test_symmetric_storage_follows_value_changes(ctx):
     A, b = P.workload("diffusion3d-24")
     x = P.uniform(46, A.ncols)
     dA = fs.CSR(ctx, A)
-    assert dA.index_coding() == 2
+    assert dA.index_coding() == 3
     vx, vy = fs.Vector(ctx, x), fs.Vector(ctx, A.nrows)
     vb = fs.Vector(ctx, b)
     slv = fs.bicgstab.solver(fs.bicgstab.settings(maxiter=2000, rtol=1e-8))(dA, fs.op.jacobi)
@@ -104,7 +140,7 @@ def test_symmetric_storage_follows_value_changes(ctx):
         if step == 1:
             M.val[A.rowptr[100] + 1] *= 1.5     # one lower entry no longer matches its partner
         dA.update_values(M.val)
-        assert dA.index_coding() == (1 if step == 1 else 2)
+        assert dA.index_coding() == (1 if step == 1 else 3)
         dA.apply(vx, vy, exact=True)
         assert np.array_equal(vy.numpy(), O.spmv(M, x))
         vsol = fs.Vector(ctx, A.nrows)
@@ -114,11 +150,13 @@ def test_symmetric_storage_follows_value_changes(ctx):
         assert np.linalg.norm(r) <= 1.5e-8 * np.linalg.norm(b)
 
 
-def test_spmv_on_unaligned_wrapped_vectors(ctx):
+@pytest.mark.parametrize("wl", ["diffusion3d-23", "diffusion3d-24"])
+def test_spmv_on_unaligned_wrapped_vectors(ctx, wl):
     """A wrapped device vector that starts on an 8-byte boundary only (a
-    torch view at an odd offset) is gathered element by element: same bits."""
+    torch view at an odd offset) is gathered element by element (the grid
+    kernel's 16-byte loads are not used for it): same bits."""
     torch = pytest.importorskip("torch")
-    A, _ = P.workload("diffusion3d-23")
+    A, _ = P.workload(wl)
     x = P.uniform(45, A.ncols)
     dA = fs.CSR(ctx, A)
     base = torch.zeros(A.ncols + 1, dtype=torch.float64, device="cuda")

@@ -137,3 +137,17 @@ def test_oracle_edge_cases():
     # GMRES validate(): restart = false needs maxiter <= max_krylov_dim
     r = O.solve("gmres", A, b, krylov_dim=5, restart=False, maxiter=10)
     assert r.status == "assert_failed"
+
+
+def test_summation_order_moves_bicgstab_not_cg():
+    """The reference algorithms with their dot products summed in other valid
+    orders (oracle order switch; order 0 is the reference's serial sum): CG's
+    iteration count does not move, BiCGSTAB's does -- the basis of the
+    order-range bars of the BiCGSTAB / GMRES parity tests."""
+    A, b = P.workload("poisson2d-128")
+    cg = [r.iters for r in O.solve_orders("cg", A, b, maxiter=2000, rtol=1e-8)]
+    bi = [r.iters for r in O.solve_orders("bicgstab", A, b, maxiter=2000, rtol=1e-8)]
+    assert cg == [389, 389, 389]
+    assert bi == [259, 300, 285]
+    # order 0 is the reference's own run, bit for bit
+    assert bi[0] == META["cases"]["poisson2d-128_bicgstab"]["iters"]
