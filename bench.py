@@ -416,22 +416,55 @@ def run_suite(args):
         S = A.to_scipy()
         rr = max(_relres(S[off[k]:off[k + 1]], b[off[k]:off[k + 1]], x) for k in range(len(infos)))
         its = [i.iters for i in infos]
-        # the same solver system by system on every 32nd system, scaled to all
-        seq, sample = 0.0, list(range(0, len(infos), 32))
-        for k in sample:
+        # the same solver on every system separately (the single-system mixed
+        # CG, one timed solve each after a warm-up)
+        seq = 0.0
+        for k in range(len(infos)):
             lo, hi = off[k], off[k + 1]
             Ak = P.CSR(int(hi - lo), int(hi - lo), A.rowptr[lo:hi + 1] - A.rowptr[lo],
                        A.col[A.rowptr[lo]:A.rowptr[hi]] - lo, A.val[A.rowptr[lo]:A.rowptr[hi]])
             slv = fs.mixed_cg.solver(fs.mixed_cg.settings(maxiter=20000, rtol=1e-8))(
                 fs.CSR(ctx, Ak), fs.op.jacobi)
             seq += _timed_solve(ctx, slv, fs.Vector(ctx, b[lo:hi]), fs.Vector(ctx, int(hi - lo)))[0]
+        # algorithmic bytes: per row and FP32 iteration of the persistent
+        # kernel, the column-id SpMV (value + column id per nonzero, row offset,
+        # A p written), the update (x32 and r read and written, A p and D^-1
+        # read) and the direction (p read and written, D^-1 and r read); the
+        # FP64 head iterations and replacements are counted as FP32 ones (a
+        # lower bound)
+        rows_it = sum(int(off[k + 1] - off[k]) * its[k] for k in range(len(infos)))
+        nnz_row = A.nnz / A.nrows
+        b_row_it = nnz_row * 8 + 4 + 4 + 24 + 16
+        gbs = rows_it * b_row_it / t / 1e9
+        peak, peak_kind = _peaks()
         out["batch512-diffusion2d"] = {
             "systems": len(infos), "rows": A.nrows, "nnz": A.nnz, "s": t, "cluster": cl,
             "threads": th, "all_converged": all(i.status == "converged_rtol" for i in infos),
             "max_true_relres": rr, "iters_min": min(its), "iters_max": max(its),
-            "iters_sum": int(sum(its)),
-            "one_by_one_s_estimate": seq * len(infos) / len(sample),
-            "one_by_one_sample": f"{len(sample)} systems (every 32nd), mixed CG one solve each"}
+            "iters_sum": int(sum(its)), "row_iterations": rows_it,
+            "roofline": {"bytes_per_row_iteration": b_row_it,
+                         "algorithmic_bytes": rows_it * b_row_it, "achieved_gbs": gbs,
+                         "peak": peak, "frac": gbs / peak, "peak_source": f"hbm_gbs of {peak_kind}"},
+            "one_by_one_s": seq,
+            "one_by_one": "all 512 systems, single-system mixed CG, one timed solve each"}
+    if want("cg-variants"):
+        # the CG loops on the headline workload: FP64 (three kernels, two
+        # reductions per iteration), the single-reduction FP64 variant (two
+        # kernels, one reduction), mixed with and without the FP64 head
+        A, b = P.workload("diffusion3d-256")
+        dA = fs.CSR(ctx, A)
+        vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
+        S = A.to_scipy()
+        res = {"rows": A.nrows}
+        for name, ns, kw in (("cg_fp64", fs.cg, {}), ("cg_fp64_single_reduction", fs.pipelined_cg, {}),
+                             ("cg_mixed_fp64_head_3e-3", fs.mixed_cg, {"fp64_head": 3e-3}),
+                             ("cg_mixed_fp32_from_start", fs.mixed_cg, {"fp64_head": 0.0})):
+            slv = ns.solver(ns.settings(maxiter=20000, rtol=1e-8, **kw))(dA, fs.op.jacobi)
+            sec, info = _timed_solve(ctx, slv, vb, vx)
+            res[name] = {"s": sec, "iters": info.iters, "status": info.status,
+                         "s_per_iteration": sec / max(info.iters, 1),
+                         "true_relres": _relres(S, b, vx.numpy())}
+        out["cg-variants-diffusion3d-256"] = res
     if want("blockcg-mixed"):
         # the mixed block solve alone (profiling): 16 right-hand sides of the
         # 96^3 Laplacian, one warm-up and one timed solve

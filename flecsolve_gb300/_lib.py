@@ -26,7 +26,7 @@ ERR_CALLBACK = 11
 
 F64, F32 = 0, 1
 BC_NONE, BC_DIRICHLET, BC_NEUMANN = 0, 1, 2
-CG, BICGSTAB, GMRES, CG_MIXED, BICGSTAB_MIXED, GMRES_MIXED, FCG = 0, 1, 2, 3, 4, 5, 6
+CG, BICGSTAB, GMRES, CG_MIXED, BICGSTAB_MIXED, GMRES_MIXED, FCG, CG_PIPELINED = 0, 1, 2, 3, 4, 5, 6, 7
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_DIAG, PRECOND_CSR, PRECOND_SOLVER = 0, 1, 2, 3, 4
 LEFT, RIGHT = 0, 1
 ORTHO_CGS2, ORTHO_MGS, ORTHO_AUTO = 0, 1, 2
@@ -163,6 +163,11 @@ _PROTOS = {
     "fs_csr_index_coding": [_vp, C.c_int, C.POINTER(C.c_int)],
     "fs_csr_row_blocks": [_vp, C.POINTER(_i64)],
     "fs_csr_grid_dims": [_vp, C.POINTER(_i64)],
+    "fs_parcsr_create": [_vp, _i64, _i64, _i64, _vp, _vp, _vp, C.POINTER(_vp)],
+    "fs_parcsr_destroy": [_vp],
+    "fs_parcsr_shape": [_vp] + [C.POINTER(_i64)] * 5,
+    "fs_parcsr_ghosts": [_vp, _vp, C.POINTER(_i64)],
+    "fs_parcsr_color_spmv": [_vp, _vp, _vp],
     "fs_csr_spmv": [_vp, _vp, _vp, C.c_int],
     "fs_csr_residual": [_vp, _vp, _vp, _vp],
     "fs_csr_spmv_transpose": [_vp, _vp, _vp],

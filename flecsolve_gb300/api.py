@@ -32,7 +32,7 @@ from ._lib import check, lib
 
 __all__ = ["Context", "Vector", "Multi", "CSR", "SolveInfo", "Future", "op", "vec", "mat",
            "batch_cg", "batch_tuning", "block_cg",
-           "cg", "bicgstab", "gmres", "fcg", "mixed_cg", "mixed_bicgstab", "mixed_gmres",
+           "cg", "bicgstab", "gmres", "fcg", "pipelined_cg", "mixed_cg", "mixed_bicgstab", "mixed_gmres",
            "Shell"]
 
 
@@ -756,6 +756,7 @@ cg = _namespace(_lib.CG, 4)                 # flecsolve/solvers/cg.hh:250-270
 bicgstab = _namespace(_lib.BICGSTAB, 8)     # bicgstab.hh:193-216
 gmres = _namespace(_lib.GMRES, 104, max_krylov_dim=-1, pre_side="right", restart=False)  # gmres.hh:366-438
 fcg = _namespace(_lib.FCG, 5)               # cg.hh:145-244, 272-290 (flexible CG)
+pipelined_cg = _namespace(_lib.CG_PIPELINED, 6)  # cg.hh:43-139, one reduction per iteration
 mixed_cg = _namespace(_lib.CG_MIXED, 4)     # FP32 inner PCG in FP64 refinement
 mixed_bicgstab = _namespace(_lib.BICGSTAB_MIXED, 8)
 mixed_gmres = _namespace(_lib.GMRES_MIXED, 104, max_krylov_dim=-1, pre_side="right", restart=False)

@@ -37,7 +37,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
 
 CU_SOURCES = ["context.cu", "spmv.cu", "krylov.cu", "gmres.cu", "batched.cu", "blockcg.cu",
               "adjoint.cu", "noalloc.cu", "matrix_market.cu", "nka.cu", "fvm.cu",
-              "bdf.cu", "generic.cu"]
+              "bdf.cu", "generic.cu", "parcsr.cu"]
 
 
 def _nvcc() -> str:

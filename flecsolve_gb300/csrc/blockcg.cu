@@ -75,7 +75,30 @@ struct BAcc<float> {
 	__device__ double get() const { return (double)hi + (double)lo; }
 };
 
-// sum over the tile's rows of a[rr][i] * b[rr][j]
+// Thread layout of the block kernels: 256 threads = 16 row slots x 16
+// column lanes (lane j handles column j; a warp covers two rows, 128
+// contiguous bytes of an FP32 block vector).  A CTA step covers kStep rows
+// (kRows per slot), staged in shared memory for the 16 x 16 products.
+constexpr int kRows = 2;
+constexpr int kStep = kTile * kRows;  // 32 rows per CTA step
+
+__device__ __forceinline__ bool bcg_skip(const BcgState *st) {
+	return st->done || (st->flags & BCG_REPLACE);
+}
+
+// sum over the step's rows of a[rr][i] * b[rr][j] (plain FMA; the caller
+// adds the step sum into a compensated running sum)
+template<class V>
+__device__ __forceinline__ V step_dot(const V (*a)[kS], const V (*b)[kS], int i, int j) {
+	V t = 0;
+#pragma unroll
+	for (int rr = 0; rr < kStep; ++rr)
+		t = fma(a[rr][i], b[rr][j], t);
+	return t;
+}
+
+// sum over a 16-row tile of a[rr][i] * b[rr][j] (start and replacement
+// kernels)
 template<class V>
 __device__ __forceinline__ V tile_dot(const V (*a)[kS], const V (*b)[kS], int i, int j) {
 	V t = 0;
@@ -85,106 +108,226 @@ __device__ __forceinline__ V tile_dot(const V (*a)[kS], const V (*b)[kS], int i,
 	return t;
 }
 
-__device__ __forceinline__ bool bcg_skip(const BcgState *st) {
-	return st->done || (st->flags & BCG_REPLACE);
+// The last CTA's fold of the per-CTA partials part[b * stride + t] over the
+// grid: eight interleaved running sums (eight loads in flight per thread),
+// combined in a fixed order -- deterministic for a given grid.
+__device__ __forceinline__ double fold_parts(const double *part, int nb, int stride, int t) {
+	double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+	for (int b = 0; b < nb; b += 8) {
+#pragma unroll
+		for (int u = 0; u < 8; ++u)
+			if (b + u < nb)
+				a[u] += __ldcg(part + (size_t)(b + u) * stride + t);
+	}
+	return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
 }
 
-// x = A^-1 B for the s x s matrix A (row-major), s right-hand sides in B
-// (row-major, overwritten with the solution): Gaussian elimination with
-// partial pivoting.  Returns false on a zero pivot.  Single thread.
-__device__ bool small_solve(double *A, double *B) {
+// X = A^-1 B for the 16 x 16 matrix A with 16 right-hand sides B (both in
+// shared memory, row-major, padded rows; B overwritten with the solution):
+// Gaussian elimination with partial pivoting by all 256 threads of the CTA.
+// Returns false (the same in every thread) on a zero pivot.
+struct SmallLs {
+	double A[kS][kS + 1], B[kS][kS + 1];
+	double fac[kS];
+	int piv, ok;
+};
+
+__device__ bool small_solve_par(SmallLs &L) {
+	const int i = threadIdx.x / kS, j = threadIdx.x % kS;
+	if (threadIdx.x == 0)
+		L.ok = 1;
+	__syncthreads();
 	for (int k = 0; k < kS; ++k) {
-		int p = k;
-		double m = fabs(A[k * kS + k]);
-		for (int i = k + 1; i < kS; ++i)
-			if (fabs(A[i * kS + k]) > m) {
-				m = fabs(A[i * kS + k]);
-				p = i;
+		if (threadIdx.x < 32) {
+			const int lane = threadIdx.x;
+			double v = (lane >= k && lane < kS) ? fabs(L.A[lane][k]) : -1.0;
+			int idx = lane;
+#pragma unroll
+			for (int off = 16; off > 0; off >>= 1) {
+				const double ov = __shfl_down_sync(0xffffffffu, v, off);
+				const int oi = __shfl_down_sync(0xffffffffu, idx, off);
+				if (ov > v || (ov == v && oi < idx)) {
+					v = ov;
+					idx = oi;
+				}
 			}
-		if (!(m > 0.0))
+			if (lane == 0) {
+				L.piv = idx;
+				if (!(v > 0.0))
+					L.ok = 0;
+			}
+		}
+		__syncthreads();
+		if (!L.ok)
 			return false;
+		const int p = L.piv;
 		if (p != k) {
-			for (int j = 0; j < kS; ++j) {
-				double t = A[k * kS + j];
-				A[k * kS + j] = A[p * kS + j];
-				A[p * kS + j] = t;
-				t = B[k * kS + j];
-				B[k * kS + j] = B[p * kS + j];
-				B[p * kS + j] = t;
+			if (i == 0) {
+				const double t = L.A[k][j];
+				L.A[k][j] = L.A[p][j];
+				L.A[p][j] = t;
+			}
+			else if (i == 1) {
+				const double t = L.B[k][j];
+				L.B[k][j] = L.B[p][j];
+				L.B[p][j] = t;
 			}
 		}
-		for (int i = k + 1; i < kS; ++i) {
-			const double f = A[i * kS + k] / A[k * kS + k];
-			for (int j = k; j < kS; ++j)
-				A[i * kS + j] -= f * A[k * kS + j];
-			for (int j = 0; j < kS; ++j)
-				B[i * kS + j] -= f * B[k * kS + j];
+		__syncthreads();
+		if (threadIdx.x < kS && (int)threadIdx.x > k)
+			L.fac[threadIdx.x] = L.A[threadIdx.x][k] / L.A[k][k];
+		__syncthreads();
+		if (i > k) {
+			const double f = L.fac[i];
+			if (j >= k)
+				L.A[i][j] -= f * L.A[k][j];
+			L.B[i][j] -= f * L.B[k][j];
 		}
+		__syncthreads();
 	}
-	for (int k = kS - 1; k >= 0; --k)
-		for (int j = 0; j < kS; ++j) {
-			double s = B[k * kS + j];
-			for (int i = k + 1; i < kS; ++i)
-				s -= A[k * kS + i] * B[i * kS + j];
-			B[k * kS + j] = s / A[k * kS + k];
+	for (int k = kS - 1; k >= 0; --k) {
+		if (threadIdx.x < kS) {
+			double s = L.B[k][j];
+			for (int m = k + 1; m < kS; ++m)
+				s -= L.A[k][m] * L.B[m][j];
+			L.B[k][j] = s / L.A[k][k];
 		}
+		__syncthreads();
+	}
 	return true;
 }
 
-// beta = G^-1 G', G = G' (single thread); false on breakdown
-__device__ bool form_beta(BcgState *st) {
-	double Gc[kS * kS];
-	for (int i = 0; i < kS * kS; ++i) {
-		Gc[i] = st->G[i];
-		st->beta[i] = st->Gn[i];
-	}
-	const bool ok = small_solve(Gc, st->beta);
-	for (int i = 0; i < kS * kS; ++i)
-		st->G[i] = st->Gn[i];
+// beta = G^-1 G', G = G' (all threads of the last CTA); false on breakdown
+__device__ bool form_beta(BcgState *st, SmallLs &L) {
+	const int i = threadIdx.x / kS, j = threadIdx.x % kS;
+	L.A[i][j] = st->G[threadIdx.x];
+	L.B[i][j] = st->Gn[threadIdx.x];
+	__syncthreads();
+	const bool ok = small_solve_par(L);
+	if (ok)
+		st->beta[threadIdx.x] = L.B[i][j];
+	st->G[threadIdx.x] = st->Gn[threadIdx.x];
 	return ok;
+}
+
+// The operator for the block SpMM: a grid stencil in symmetric storage (rows
+// addressed by their grid coordinates, every neighbour load independent) or
+// the CSR rows.
+template<class V>
+struct BcgOp {
+	const int *rp, *col;
+	const V *val;
+	const V *S;  // grid: diagonal, upper diagonals (null: CSR)
+	int64_t ld;
+	int nx, ny, nz, K;
+};
+
+// q_j = (A P)[r][j] for lane j, the products in the CSR column order
+template<class V>
+__device__ __forceinline__ V bcg_row(const BcgOp<V> &A, const V *__restrict__ P, int r, int j) {
+	V q = 0;
+	if (A.S) {
+		const int64_t nxy = (int64_t)A.nx * A.ny;
+		const int i = r % A.nx;
+		const int line = r / A.nx;
+		const int jj = A.K >= 2 ? line % A.ny : 0, kk = A.K >= 2 ? line / A.ny : 0;
+		const V *U1 = A.S + A.ld, *U2 = A.S + 2 * A.ld, *U3 = A.S + 3 * A.ld;
+		const bool lz = A.K >= 3 && kk > 0, hz = A.K >= 3 && kk < A.nz - 1;
+		const bool ly = A.K >= 2 && jj > 0, hy = A.K >= 2 && jj < A.ny - 1;
+		const bool lx = i > 0, hx = i < A.nx - 1;
+		// every load first (fixed slots in column order), then the sum
+		const bool has[7] = {lz, ly, lx, true, hx, hy, hz};
+		const int64_t off[7] = {-nxy, -A.nx, -1, 0, 1, A.nx, nxy};
+		V a[7], x[7];
+#pragma unroll
+		for (int t = 0; t < 7; ++t) {
+			a[t] = 0;
+			x[t] = 0;
+			if (has[t]) {
+				const V *U = t == 3 ? A.S : (t < 3 ? (t == 0 ? U3 : t == 1 ? U2 : U1)
+				                                   : (t == 4 ? U1 : t == 5 ? U2 : U3));
+				a[t] = __ldg(U + (t < 3 ? r + off[t] : r));
+				x[t] = __ldg(P + (size_t)(r + off[t]) * kS + j);
+			}
+		}
+#pragma unroll
+		for (int t = 0; t < 7; ++t)
+			if (has[t])
+				q = fma(a[t], x[t], q);
+		return q;
+	}
+	const int k0 = __ldg(A.rp + r), k1 = __ldg(A.rp + r + 1);
+	for (int k = k0; k < k1; k += 8) {
+		// a batch of up to 8 entries: the column ids, then the gathers
+		int c[8];
+		V a[8];
+#pragma unroll
+		for (int t = 0; t < 8; ++t)
+			if (k + t < k1) {
+				c[t] = __ldg(A.col + k + t);
+				a[t] = __ldg(A.val + k + t);
+			}
+		V x[8];
+#pragma unroll
+		for (int t = 0; t < 8; ++t)
+			if (k + t < k1)
+				x[t] = __ldg(P + (size_t)c[t] * kS + j);
+#pragma unroll
+		for (int t = 0; t < 8; ++t)
+			if (k + t < k1)
+				q = fma(a[t], x[t], q);
+	}
+	return q;
 }
 
 // Q = A P and the CTA's part of M = P^T Q; the last CTA forms alpha = M^-1 G
 template<class V>
 __global__ void __launch_bounds__(256)
-k_bcg_spmm(int n, const int *__restrict__ rp, const int *__restrict__ col,
-           const V *__restrict__ val, const V *__restrict__ P, V *__restrict__ Q, BcgState *st,
+k_bcg_spmm(int n, BcgOp<V> A, const V *__restrict__ P, V *__restrict__ Q, BcgState *st,
            double *part, unsigned *counter) {
-	__shared__ V sp[kTile][kS], sq[kTile][kS];
+	__shared__ V sp[kStep][kS], sq[kStep][kS];
+	__shared__ SmallLs L;
 	if (bcg_skip(st))
 		return;
 	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
-	const int ntiles = (n + kTile - 1) / kTile;
+	const int nsteps = (n + kStep - 1) / kStep;
 	BAcc<V> m;
-	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const int r = t * kTile + tr;
-		V q = 0, p = 0;
-		if (r < n) {
-			for (int k = rp[r]; k < rp[r + 1]; ++k)
-				q = fma(val[k], P[(size_t)col[k] * kS + tj], q);
-			Q[(size_t)r * kS + tj] = q;
-			p = P[(size_t)r * kS + tj];
+	for (int t = blockIdx.x; t < nsteps; t += gridDim.x) {
+		V q[kRows], p[kRows];
+#pragma unroll
+		for (int u = 0; u < kRows; ++u) {
+			const int r = t * kStep + u * kTile + tr;
+			q[u] = 0;
+			p[u] = 0;
+			if (r < n) {
+				q[u] = bcg_row(A, P, r, tj);
+				p[u] = __ldg(P + (size_t)r * kS + tj);
+			}
 		}
-		sp[tr][tj] = p;
-		sq[tr][tj] = q;
+#pragma unroll
+		for (int u = 0; u < kRows; ++u) {
+			const int r = t * kStep + u * kTile + tr;
+			if (r < n)
+				Q[(size_t)r * kS + tj] = q[u];
+			sp[u * kTile + tr][tj] = p[u];
+			sq[u * kTile + tr][tj] = q[u];
+		}
 		__syncthreads();
-		m.add(tile_dot<V>(sp, sq, tr, tj));
+		m.add(step_dot<V>(sp, sq, tr, tj));
 		__syncthreads();
 	}
 	part[(size_t)blockIdx.x * 256 + threadIdx.x] = m.get();
 	if (last_block(counter)) {
-		double s = 0.0;
-		for (unsigned b = 0; b < gridDim.x; ++b)
-			s += __ldcg(part + (size_t)b * 256 + threadIdx.x);
+		const double s = fold_parts(part, gridDim.x, 256, threadIdx.x);
 		st->M[threadIdx.x] = s;
+		L.A[tr][tj] = s;
+		L.B[tr][tj] = st->G[threadIdx.x];
 		__syncthreads();
+		const bool ok = small_solve_par(L);
+		if (ok)
+			st->alpha[threadIdx.x] = L.B[tr][tj];
 		if (threadIdx.x == 0) {
-			double Mc[kS * kS];
-			for (int i = 0; i < kS * kS; ++i) {
-				Mc[i] = st->M[i];
-				st->alpha[i] = st->G[i];
-			}
-			if (!small_solve(Mc, st->alpha)) {
+			if (!ok) {
 				st->done = 1;
 				st->status = FS_DIVERGED_BREAKDOWN;
 			}
@@ -205,61 +348,85 @@ __global__ void __launch_bounds__(256)
 k_bcg_update(int n, V *__restrict__ X, const V *__restrict__ P, V *__restrict__ R,
              const V *__restrict__ Q, const V *__restrict__ dinv, BcgState *st, double *part,
              double *part2, unsigned *counter, double tolf, int maxiter, double delta) {
-	__shared__ V sa[kS * kS], sp[kTile][kS], sq[kTile][kS], sr[kTile][kS], sz[kTile][kS];
+	__shared__ V sa[kS][kS];
+	__shared__ V sp[kStep][kS], sq[kStep][kS];
 	__shared__ double cn[kTile][kS];
+	__shared__ SmallLs L;
+	__shared__ int s_beta;
 	if (bcg_skip(st))
 		return;
-	sa[threadIdx.x] = (V)st->alpha[threadIdx.x];
-	__syncthreads();
 	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
-	const int ntiles = (n + kTile - 1) / kTile;
+	sa[tr][tj] = (V)st->alpha[threadIdx.x];
+	__syncthreads();
+	V al[kS];
+#pragma unroll
+	for (int i = 0; i < kS; ++i)
+		al[i] = sa[i][tj];
+	const int nsteps = (n + kStep - 1) / kStep;
 	BAcc<V> g, nr;
-	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const int r = t * kTile + tr;
-		sp[tr][tj] = r < n ? P[(size_t)r * kS + tj] : V(0);
-		sq[tr][tj] = r < n ? Q[(size_t)r * kS + tj] : V(0);
+	for (int t = blockIdx.x; t < nsteps; t += gridDim.x) {
+		V xr[kRows], rr[kRows];
+#pragma unroll
+		for (int u = 0; u < kRows; ++u) {
+			const int r = t * kStep + u * kTile + tr;
+			V pv = 0, qv = 0;
+			xr[u] = 0;
+			rr[u] = 0;
+			if (r < n) {
+				pv = P[(size_t)r * kS + tj];
+				qv = Q[(size_t)r * kS + tj];
+				xr[u] = X[(size_t)r * kS + tj];
+				rr[u] = R[(size_t)r * kS + tj];
+			}
+			sp[u * kTile + tr][tj] = pv;
+			sq[u * kTile + tr][tj] = qv;
+		}
 		__syncthreads();
-		V rv = 0, z = 0;
-		if (r < n) {
-			V x = X[(size_t)r * kS + tj];
-			rv = R[(size_t)r * kS + tj];
+		V zr[kRows];
+#pragma unroll
+		for (int u = 0; u < kRows; ++u) {
+			const int r = t * kStep + u * kTile + tr;
+			const int row = u * kTile + tr;
 #pragma unroll
 			for (int i = 0; i < kS; ++i) {
-				x = fma(sp[tr][i], sa[i * kS + tj], x);
-				rv = fma(-sq[tr][i], sa[i * kS + tj], rv);
+				xr[u] = fma(sp[row][i], al[i], xr[u]);
+				rr[u] = fma(-sq[row][i], al[i], rr[u]);
 			}
-			X[(size_t)r * kS + tj] = x;
-			R[(size_t)r * kS + tj] = rv;
-			z = dinv ? dinv[r] * rv : rv;
-			nr.add(rv * rv);
+			zr[u] = 0;
+			if (r < n) {
+				X[(size_t)r * kS + tj] = xr[u];
+				R[(size_t)r * kS + tj] = rr[u];
+				zr[u] = dinv ? __ldg(dinv + r) * rr[u] : rr[u];
+				nr.add(rr[u] * rr[u]);
+			}
+			else
+				rr[u] = 0;
 		}
-		sr[tr][tj] = rv;
-		sz[tr][tj] = z;
 		__syncthreads();
-		g.add(tile_dot<V>(sz, sr, tr, tj));
+		// the staged P and Q are consumed: reuse them for Z and R
+#pragma unroll
+		for (int u = 0; u < kRows; ++u) {
+			sp[u * kTile + tr][tj] = zr[u];
+			sq[u * kTile + tr][tj] = rr[u];
+		}
+		__syncthreads();
+		g.add(step_dot<V>(sp, sq, tr, tj));
 		__syncthreads();
 	}
 	part[(size_t)blockIdx.x * 256 + threadIdx.x] = g.get();
-	// column norms: fold the 16 row-threads of each column in the block first
+	// column norms: fold the 16 row slots of each column in the block first
 	cn[tr][tj] = nr.get();
 	__syncthreads();
 	if (threadIdx.x < kS) {
 		double c = 0.0;
-		for (int rr = 0; rr < kTile; ++rr)
-			c += cn[rr][threadIdx.x];
+		for (int q = 0; q < kTile; ++q)
+			c += cn[q][threadIdx.x];
 		part2[(size_t)blockIdx.x * kS + threadIdx.x] = c;
 	}
 	if (last_block(counter)) {
-		double s = 0.0;
-		for (unsigned b = 0; b < gridDim.x; ++b)
-			s += __ldcg(part + (size_t)b * 256 + threadIdx.x);
-		st->Gn[threadIdx.x] = s;
-		if (threadIdx.x < kS) {
-			double c = 0.0;
-			for (unsigned b = 0; b < gridDim.x; ++b)
-				c += __ldcg(part2 + (size_t)b * kS + threadIdx.x);
-			st->rnorm[threadIdx.x] = sqrt(c);
-		}
+		st->Gn[threadIdx.x] = fold_parts(part, gridDim.x, 256, threadIdx.x);
+		if (threadIdx.x < kS)
+			st->rnorm[threadIdx.x] = sqrt(fold_parts(part2, gridDim.x, kS, threadIdx.x));
 		__syncthreads();
 		if (threadIdx.x == 0) {
 			const int it = st->iter + 1;
@@ -267,6 +434,7 @@ k_bcg_update(int n, V *__restrict__ X, const V *__restrict__ P, V *__restrict__ 
 			bool finite = true;
 			for (int j = 0; j < kS; ++j)
 				finite = finite && isfinite(st->rnorm[j]);
+			s_beta = 0;
 			if (delta <= 0.0) {
 				bool all = true;
 				for (int j = 0; j < kS; ++j) {
@@ -286,10 +454,8 @@ k_bcg_update(int n, V *__restrict__ X, const V *__restrict__ P, V *__restrict__ 
 					st->done = 1;
 					st->status = FS_DIVERGED_ITERS;
 				}
-				else if (!form_beta(st)) {
-					st->done = 1;
-					st->status = FS_DIVERGED_BREAKDOWN;
-				}
+				else
+					s_beta = 1;
 			}
 			else {
 				bool replace = it >= maxiter || !finite;
@@ -304,13 +470,17 @@ k_bcg_update(int n, V *__restrict__ X, const V *__restrict__ P, V *__restrict__ 
 				}
 				if (replace || worst < delta)
 					st->flags |= BCG_REPLACE;
-				else if (!form_beta(st)) {
-					st->done = 1;
-					st->status = FS_DIVERGED_BREAKDOWN;
-				}
+				else
+					s_beta = 1;
 			}
-			*counter = 0;
 		}
+		__syncthreads();
+		if (s_beta && !form_beta(st, L) && threadIdx.x == 0) {
+			st->done = 1;
+			st->status = FS_DIVERGED_BREAKDOWN;
+		}
+		if (threadIdx.x == 0)
+			*counter = 0;
 	}
 }
 
@@ -319,24 +489,43 @@ template<class V>
 __global__ void __launch_bounds__(256)
 k_bcg_dir(int n, V *__restrict__ P, const V *__restrict__ R, const V *__restrict__ dinv,
           const BcgState *st) {
-	__shared__ V sb[kS * kS], sp[kTile][kS];
+	__shared__ V sb[kS][kS], sp[kStep][kS];
 	if (bcg_skip(st))
 		return;
-	sb[threadIdx.x] = (V)st->beta[threadIdx.x];
 	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
-	const int ntiles = (n + kTile - 1) / kTile;
-	for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-		const int r = t * kTile + tr;
+	sb[tr][tj] = (V)st->beta[threadIdx.x];
+	__syncthreads();
+	V be[kS];
+#pragma unroll
+	for (int i = 0; i < kS; ++i)
+		be[i] = sb[i][tj];
+	const int nsteps = (n + kStep - 1) / kStep;
+	for (int t = blockIdx.x; t < nsteps; t += gridDim.x) {
+		V z[kRows];
+#pragma unroll
+		for (int u = 0; u < kRows; ++u) {
+			const int r = t * kStep + u * kTile + tr;
+			V pv = 0;
+			z[u] = 0;
+			if (r < n) {
+				pv = P[(size_t)r * kS + tj];
+				z[u] = (dinv ? __ldg(dinv + r) : V(1)) * R[(size_t)r * kS + tj];
+			}
+			sp[u * kTile + tr][tj] = pv;
+		}
 		__syncthreads();
-		sp[tr][tj] = r < n ? P[(size_t)r * kS + tj] : V(0);
-		__syncthreads();
-		if (r < n) {
-			V p = (dinv ? dinv[r] : V(1)) * R[(size_t)r * kS + tj];
+#pragma unroll
+		for (int u = 0; u < kRows; ++u) {
+			const int r = t * kStep + u * kTile + tr;
+			const int row = u * kTile + tr;
+			V pn = z[u];
 #pragma unroll
 			for (int i = 0; i < kS; ++i)
-				p = fma(sp[tr][i], sb[i * kS + tj], p);
-			P[(size_t)r * kS + tj] = p;
+				pn = fma(sp[row][i], be[i], pn);
+			if (r < n)
+				P[(size_t)r * kS + tj] = pn;
 		}
+		__syncthreads();
 	}
 }
 
@@ -396,16 +585,10 @@ k_bcg_start(int n, const int *__restrict__ rp, const int *__restrict__ col,
 		part2[(size_t)blockIdx.x * 2 * kS + kS + threadIdx.x] = c2;
 	}
 	if (last_block(counter)) {
-		double s = 0.0;
-		for (unsigned b = 0; b < gridDim.x; ++b)
-			s += __ldcg(part + (size_t)b * 256 + threadIdx.x);
-		st->G[threadIdx.x] = s;
+		st->G[threadIdx.x] = fold_parts(part, gridDim.x, 256, threadIdx.x);
 		if (threadIdx.x < kS) {
-			double c1 = 0.0, c2 = 0.0;
-			for (unsigned b = 0; b < gridDim.x; ++b) {
-				c1 += __ldcg(part2 + (size_t)b * 2 * kS + threadIdx.x);
-				c2 += __ldcg(part2 + (size_t)b * 2 * kS + kS + threadIdx.x);
-			}
+			const double c1 = fold_parts(part2, gridDim.x, 2 * kS, threadIdx.x);
+			const double c2 = fold_parts(part2, gridDim.x, 2 * kS, kS + threadIdx.x);
 			const double bn = sqrt(c1);
 			st->bnorm[threadIdx.x] = bn == 0.0 ? 1.0 : bn;
 			st->rnorm[threadIdx.x] = sqrt(c2);
@@ -444,6 +627,8 @@ k_bcg_true_res(int n, const int *__restrict__ rp, const int *__restrict__ col,
                int maxiter) {
 	__shared__ float sr[kTile][kS], sz[kTile][kS];
 	__shared__ double cr[kTile][kS];
+	__shared__ SmallLs L;
+	__shared__ int s_beta;
 	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
 	const int ntiles = (n + kTile - 1) / kTile;
 	BAcc<float> g;
@@ -477,14 +662,9 @@ k_bcg_true_res(int n, const int *__restrict__ rp, const int *__restrict__ col,
 		part2[(size_t)blockIdx.x * kS + threadIdx.x] = c;
 	}
 	if (last_block(counter)) {
-		double s = 0.0;
-		for (unsigned b = 0; b < gridDim.x; ++b)
-			s += __ldcg(part + (size_t)b * 256 + threadIdx.x);
-		st->Gn[threadIdx.x] = s;
+		st->Gn[threadIdx.x] = fold_parts(part, gridDim.x, 256, threadIdx.x);
 		if (threadIdx.x < kS) {
-			double c = 0.0;
-			for (unsigned b = 0; b < gridDim.x; ++b)
-				c += __ldcg(part2 + (size_t)b * kS + threadIdx.x);
+			const double c = fold_parts(part2, gridDim.x, kS, threadIdx.x);
 			st->rnorm[threadIdx.x] = sqrt(c);
 			st->rlast[threadIdx.x] = sqrt(c);
 		}
@@ -500,6 +680,7 @@ k_bcg_true_res(int n, const int *__restrict__ rp, const int *__restrict__ col,
 			}
 			st->replacements += 1;
 			st->flags &= ~BCG_REPLACE;
+			s_beta = 0;
 			if (all) {
 				st->done = 1;
 				st->status = FS_CONVERGED_RTOL;
@@ -512,12 +693,16 @@ k_bcg_true_res(int n, const int *__restrict__ rp, const int *__restrict__ col,
 				st->done = 1;
 				st->status = FS_DIVERGED_ITERS;
 			}
-			else if (!form_beta(st)) {
-				st->done = 1;
-				st->status = FS_DIVERGED_BREAKDOWN;
-			}
-			*counter = 0;
+			else
+				s_beta = 1;
 		}
+		__syncthreads();
+		if (s_beta && !form_beta(st, L) && threadIdx.x == 0) {
+			st->done = 1;
+			st->status = FS_DIVERGED_BREAKDOWN;
+		}
+		if (threadIdx.x == 0)
+			*counter = 0;
 	}
 }
 
@@ -540,7 +725,9 @@ int block_cg_run(Ctx *ctx, const fs_krylov_settings *s, Csr *A, bool jac, Vec *B
 	if (mixed)
 		FS_TRY(ensure_val32(A));
 	BcgPlan &p = g_bcg[std::make_pair((const Csr *)A, mixed)];
-	const int G = std::max(1, std::min(ctx->sms * 8, (int)((n + kTile - 1) / kTile)));
+	// two 256-thread CTAs per SM: each thread keeps enough loads in flight,
+	// and the last CTA's fold of the partials stays short
+	const int G = std::max(1, std::min(ctx->sms * 2, (int)((n + kStep - 1) / kStep)));
 	const size_t m = (size_t)n * kS;
 	if (p.n != n) {
 		if (p.work) {
@@ -568,6 +755,18 @@ int block_cg_run(Ctx *ctx, const fs_krylov_settings *s, Csr *A, bool jac, Vec *B
 	if (jac)
 		dinv = mixed ? (const V *)A->dinv32 : (const V *)A->dinv;
 	const V *val = mixed ? (const V *)A->val32 : (const V *)A->val;
+	// a grid stencil in symmetric storage: neighbours addressed by the grid
+	// coordinates; anything else: the CSR rows
+	BcgOp<V> op{A->rowptr, A->col, val, nullptr, 0, 0, 0, 0, 0};
+	FS_TRY(ensure_sym(A, mixed));
+	if (A->grid_nx > 0 && active_coding(A, mixed) >= kCodingSym) {
+		op.S = sym_vals<V>(A);
+		op.ld = A->sym_ld;
+		op.nx = A->grid_nx;
+		op.ny = A->grid_ny;
+		op.nz = A->grid_nz;
+		op.K = A->nsym;
+	}
 	const double *b = (const double *)B->d;
 	double *x = (double *)X->d;
 	V *xv = mixed ? Xc : (V *)x;
@@ -588,8 +787,7 @@ int block_cg_run(Ctx *ctx, const fs_krylov_settings *s, Csr *A, bool jac, Vec *B
 	FS_TRY(read_back());
 	while (!p.hst->done) {
 		for (int j = 0; j < k; ++j) {
-			k_bcg_spmm<V><<<G, 256, 0, ctx->stream>>>((int)n, A->rowptr, A->col, val, Pm, Qm, p.st,
-			                                          part, p.counter);
+			k_bcg_spmm<V><<<G, 256, 0, ctx->stream>>>((int)n, op, Pm, Qm, p.st, part, p.counter);
 			FS_TRY(check_launch(ctx, "block cg spmm"));
 			k_bcg_update<V><<<G, 256, 0, ctx->stream>>>((int)n, xv, Pm, R, Qm, dinv, p.st, part,
 			                                            part2, p.counter, tolf, maxiter, delta);

@@ -581,7 +581,10 @@ int generic_apply(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	info->status = FS_STATUS_UNKNOWN;
 	int st = FS_ERR_UNSUPPORTED;
 	switch (s->method) {
-	case FS_CG: st = gen_cg(g, b, x, info); break;
+	case FS_CG:
+	case FS_CG_PIPELINED:  // with a general operator: the reference's CG loop
+		st = gen_cg(g, b, x, info);
+		break;
 	case FS_FCG: st = gen_fcg(g, b, x, info); break;
 	case FS_BICGSTAB: st = gen_bicgstab(g, b, x, info); break;
 	case FS_GMRES: st = gen_gmres(g, b, x, info); break;

@@ -67,13 +67,42 @@ __device__ __forceinline__ void block_multi_sum(const double (&vals)[kChunk], in
 	}
 }
 
-// Last block: out[j] = sum over blocks of part[b*nv + j], in block order.
-__device__ __forceinline__ void fold_multi(const double *part, int nv, double *out) {
-	for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+// Last block: out[j] = sum over blocks of part[b*nv + j].  Every thread sums
+// the blocks b = t, t + blockDim, ... (all nv values of a block are adjacent,
+// so a warp reads contiguous memory), then the block tree combines the
+// threads' sums: a fixed order, so the result is deterministic for a given
+// grid, with every thread's loads in flight at once.
+__device__ __forceinline__ void fold_multi(const double *part, int nv, double *out, double *sh) {
+	double acc[kChunk];
+#pragma unroll
+	for (int j = 0; j < kChunk; ++j)
+		acc[j] = 0.0;
+	for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+#pragma unroll
+		for (int j = 0; j < kChunk; ++j)
+			if (j < nv)
+				acc[j] += __ldcg(part + (size_t)b * nv + j);
+	}
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	const int nw = blockDim.x >> 5;
+	__syncthreads();  // sh was used by the block's own reduction
+#pragma unroll
+	for (int j = 0; j < kChunk; ++j) {
+		if (j < nv) {
+			double v = acc[j];
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1)
+				v += __shfl_down_sync(0xffffffffu, v, o);
+			if (lane == 0)
+				sh[j * 8 + wid] = v;
+		}
+	}
+	__syncthreads();
+	if ((int)threadIdx.x < nv) {
 		double t = 0.0;
-		for (unsigned b = 0; b < gridDim.x; ++b)
-			t += __ldcg(part + (size_t)b * nv + j);
-		out[j] = t;
+		for (int w = 0; w < nw; ++w)
+			t += sh[threadIdx.x * 8 + w];
+		out[threadIdx.x] = t;
 	}
 }
 
@@ -215,7 +244,7 @@ k_gm_dots(int64_t n, const T *__restrict__ V, int64_t ld, int j0, int nj,
 		accd[j] = (double)acc[j];
 	block_multi_sum(accd, nj, part, sh);
 	if (last_block(counter)) {
-		fold_multi(part, nj, g->h1 + j0);
+		fold_multi(part, nj, g->h1 + j0, sh);
 		if (threadIdx.x == 0)
 			*counter = 0;
 	}
@@ -278,7 +307,7 @@ k_gm_project_dots(int64_t n, const T *__restrict__ V, int64_t ld, int kp1, int j
 		accd[j] = (double)acc[j];
 	block_multi_sum(accd, nj, part, sh);
 	if (last_block(counter)) {
-		fold_multi(part, nj, g->h2 + j0);
+		fold_multi(part, nj, g->h2 + j0, sh);
 		if (threadIdx.x == 0)
 			*counter = 0;
 	}

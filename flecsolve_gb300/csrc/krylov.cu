@@ -78,6 +78,11 @@ __global__ void k_copy(int64_t n, const V *__restrict__ s, V *__restrict__ d) {
 	FOR_EACH(i, n) d[i] = s[i];
 }
 
+__global__ void k_mul(int64_t n, const double *__restrict__ a, const double *__restrict__ b,
+                      double *__restrict__ d) {
+	FOR_EACH(i, n) d[i] = a[i] * b[i];
+}
+
 // ---------------------------------------------------------------- CG --
 
 // z = P r (PK 0: identity, 1: diagonal); p = z; rho = z'r; res0 = ||r||
@@ -854,6 +859,7 @@ int solver_alloc(Solver *s) {
 	case FS_BICGSTAB: nw64 = 6; break;
 	case FS_GMRES: nw64 = 3; break;
 	case FS_CG_MIXED: nw64 = 1; nw32 = 5; break;
+	case FS_CG_PIPELINED: nw64 = 5; break;
 	case FS_BICGSTAB_MIXED: nw64 = 1; nw32 = 7; break;
 	case FS_GMRES_MIXED: nw64 = 3; nw32 = 3; break;
 	}
@@ -1168,6 +1174,195 @@ static int cg_apply64(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
 	}
 	if (h.flags & KF_NONFINITE)
 		return set_err(ctx, FS_ERR_NON_FINITE, "CG: non-finite residual norm");
+	return FS_OK;
+}
+
+// ---------------------------------- single-reduction (pipelined) CG --
+//
+// Chronopoulos & Gear (1989): the CG recurrences of cg.hh:43-139 rearranged
+// so that an iteration has ONE grid-wide reduction.  With u = P r and w = A u
+// carried along, the two dots gamma = (r, u) and delta = (w, u) (and the
+// stopping norm ||r||) are all available right after the SpMV w = A u, so they
+// are summed in that kernel's epilogue; the other kernel applies every vector
+// update at once:
+//   p = u + beta p,  s = w + beta s,  x += alpha p,  r -= alpha s,  u = P r
+//   w = A u;  gamma' = (r, u), delta = (w, u), ||r||
+//   beta = gamma' / gamma,  alpha = gamma' / (delta - beta gamma' / alpha)
+// Two kernels and one reduction per iteration instead of three and two, at
+// the price of two more vectors (s, w) streamed: 12 vector accesses in the
+// update instead of 11 over the update and the direction kernels.  The
+// stopping test is the reference's, on ||r|| after the update.
+
+// p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s, u = P r
+template<int PK>
+__global__ void __launch_bounds__(kThreads)
+k_pcg_update(int64_t n, double *__restrict__ x, double *__restrict__ r, double *__restrict__ u,
+             const double *__restrict__ w, double *__restrict__ p, double *__restrict__ s,
+             const double *__restrict__ dinv, const KState *st) {
+	pdl_wait();
+	pdl_trigger();
+	if (stopped(st))
+		return;
+	const double alpha = st->alpha, beta = st->beta;
+	FOR_EACH(i, n) {
+		const double pi = fma(beta, p[i], u[i]);
+		const double si = fma(beta, s[i], w[i]);
+		x[i] = fma(alpha, pi, x[i]);
+		const double ri = fma(-alpha, si, r[i]);
+		p[i] = pi;
+		s[i] = si;
+		r[i] = ri;
+		u[i] = PK ? dinv[i] * ri : ri;
+	}
+}
+
+// w = A u and the iteration's three dots; the last CTA counts the iteration,
+// tests ||r|| and forms beta, alpha (the first call, iter < 0: the start)
+struct EpiPipe {
+	static constexpr int NV = 3;
+	double *w;
+	const double *u, *r;
+	KState *st;
+	double *part;
+	unsigned *counter;
+	double *hist;
+	__device__ bool skip() const { return stopped(st); }
+	template<class A>
+	__device__ void row(int i, double s, A &acc) const {
+		w[i] = s;
+		const double ui = u[i], ri = r[i];
+		acc.add_prod(0, ri, ui);
+		acc.add_prod(1, s, ui);
+		acc.add_prod(2, ri, ri);
+	}
+	__device__ void finish(const double *sm) const {
+		const double gamma = sm[0], delta = sm[1];
+		const double res = sqrt(sm[2]);
+		if (st->aux[0] == 0.0) {
+			// the start (cg.hh:75-90): alpha = gamma / delta, beta = 0
+			st->aux[0] = 1.0;
+			st->res0 = res;
+			st->res = res;
+			st->rho = gamma;
+			st->beta = 0.0;
+			st->alpha = gamma / delta;
+			if (res < st->tol) {
+				st->done = 1;
+				st->status = FS_CONVERGED_RTOL;
+				st->info_iters = 0;
+			}
+			else if (st->maxiter <= 0) {
+				st->done = 1;
+				st->status = FS_DIVERGED_ITERS;
+			}
+			return;
+		}
+		const int it = st->iter + 1;
+		st->iter = it;
+		st->res = res;
+		if (it <= st->hist_cap)
+			hist[it - 1] = res;
+		if (!isfinite(res))
+			st->flags |= KF_NONFINITE;
+		if (res < st->tol) {
+			st->done = 1;
+			st->status = FS_CONVERGED_RTOL;
+			st->info_iters = it;
+		}
+		else if (it >= st->maxiter || (st->flags & KF_NONFINITE)) {
+			st->done = 1;
+			st->status = FS_DIVERGED_ITERS;
+			st->info_iters = 0;
+		}
+		const double beta = gamma / st->rho;
+		st->beta = beta;
+		st->alpha = gamma / (delta - beta * gamma / st->alpha);
+		st->rho = gamma;
+	}
+};
+
+template<int PK>
+static int pcg_body(Solver *s, void *a) {
+	CgArgs *g = (CgArgs *)a;
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	double *r = s->w64[0], *u = s->w64[1], *w = s->w64[2], *p = s->w64[3], *sv = s->w64[4];
+	double *x = (double *)g->x->d;
+	const double *dinv = s->dinv64();
+	const int G = red_grid(ctx, n);
+	for (int k = 0; k < g->k; ++k) {
+		FS_TRY(check_launch_rc(ctx,
+		                       launch_pdl(ctx->stream, k_pcg_update<PK>, G, kThreads, 0, n, x, r, u,
+		                                  (const double *)w, p, sv, dinv, (const KState *)s->st),
+		                       "pipelined cg update"));
+		FS_TRY(launch_spmv<double, false, false>(
+			ctx, s->A, s->A->val, u, nullptr,
+			EpiPipe{w, u, r, s->st, s->part, s->counter, s->hist}));
+	}
+	return FS_OK;
+}
+
+static int cg_apply_pipelined(Solver *s, Vec *b, Vec *x, fs_solve_info *info) {
+	Ctx *ctx = s->ctx;
+	const int64_t n = s->n;
+	const int G = red_grid(ctx, n);
+	const bool zg = s->set.base.use_zero_guess != 0;
+	const int PK = s->dinv64() ? 1 : 0;
+	double *r = s->w64[0], *u = s->w64[1], *w = s->w64[2], *p = s->w64[3], *sv = s->w64[4];
+	FS_TRY(solver_hist(s, std::max(1, s->set.base.maxiter)));
+	FS_TRY(init_state(s, s->st, (double)s->set.base.rtol, s->set.base.maxiter));
+	FS_TRY(solver_norms(s, b, x, !zg, 0));
+	if (zg) {
+		k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, (double *)x->d, 0.0);
+		FS_TRY(check_launch(ctx, "fill"));
+		k_copy<double><<<G, kThreads, 0, ctx->stream>>>(n, (const double *)b->d, r);
+		FS_TRY(check_launch(ctx, "copy"));
+	}
+	else {
+		FS_TRY(launch_spmv<double, false, false>(ctx, s->A, s->A->val, (const double *)x->d, nullptr,
+		                                         EpiResidual<double>{(const double *)b->d, r}));
+	}
+	// u = P r, p = s = 0, then w = A u with the start's dots
+	if (PK)
+		k_mul<<<G, kThreads, 0, ctx->stream>>>(n, s->dinv64(), r, u);
+	else
+		k_copy<double><<<G, kThreads, 0, ctx->stream>>>(n, r, u);
+	FS_TRY(check_launch(ctx, "pipelined cg start"));
+	k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, p, 0.0);
+	k_fill<double><<<G, kThreads, 0, ctx->stream>>>(n, sv, 0.0);
+	FS_TRY(check_launch(ctx, "fill"));
+	FS_TRY(launch_spmv<double, false, false>(ctx, s->A, s->A->val, u, nullptr,
+	                                         EpiPipe{w, u, r, s->st, s->part, s->counter, s->hist}));
+	FS_TRY(read_state(s));
+	int user_stop = 0;
+	if (!s->hst->done) {
+		CgArgs args{b, x, k_default(s)};
+		LoopSpec L{x, {b->d, x->d, 0}, PK ? pcg_body<1> : pcg_body<0>, &args, nullptr, &args.k,
+		           6000 + PK};
+		FS_TRY(run_loop(s, L, &user_stop));
+	}
+	KState &h = *s->hst;
+	s->hhist_count = std::min<int64_t>(h.iter, s->hist_cap);
+	double xn = 0;
+	FS_TRY(sol_norm(s, x, &xn));
+	memset(info, 0, sizeof(*info));
+	info->rhs_norm = (float)h.rhs_norm;
+	info->sol_norm_initial = zg ? 0.f : (float)h.sol0;
+	info->res_norm_initial = (float)h.res0;
+	info->sol_norm_final = (float)xn;
+	info->res_norm_final = (float)h.res;
+	if (user_stop) {
+		info->status = FS_CONVERGED_USER;
+		info->iters = user_stop;
+	}
+	else {
+		info->status = h.status;
+		info->iters = h.info_iters;
+		if (h.iter > 0 && info->iters == 0)
+			info->status = FS_DIVERGED_ITERS;  // cg.hh:135-136
+	}
+	if (h.flags & KF_NONFINITE)
+		return set_err(ctx, FS_ERR_NON_FINITE, "pipelined CG: non-finite residual norm");
 	return FS_OK;
 }
 
@@ -1791,7 +1986,7 @@ FS_API int fs_krylov_create(fs_ctx h, int method, const fs_krylov_settings *set,
 	if (!ok_ctx(ctx) || !ok_csr(A) || !out || !set)
 		return FS_ERR_BAD_HANDLE;
 	*out = nullptr;
-	if (method < FS_CG || method > FS_FCG)
+	if (method < FS_CG || method > FS_CG_PIPELINED)
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_krylov_create: unknown method %d", method);
 	if (A->nrows != A->ncols)
 		return set_err(ctx, FS_ERR_SIZE_MISMATCH, "fs_krylov_create: operator must be square");
@@ -2015,6 +2210,7 @@ FS_API int fs_krylov_apply(fs_solver h, fs_vec bh, fs_vec xh, fs_solve_info *inf
 		FS_TRY(ensure_sym(s->A, true));
 	switch (s->method) {
 	case FS_CG: return cg_apply64(s, b, x, info);
+	case FS_CG_PIPELINED: return cg_apply_pipelined(s, b, x, info);
 	case FS_BICGSTAB: return bicgstab_apply64(s, b, x, info);
 	case FS_GMRES: return gmres_apply(s, b, x, info);
 	case FS_CG_MIXED:

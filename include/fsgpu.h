@@ -72,6 +72,7 @@ typedef struct fs_csr_s *fs_csr;
 typedef struct fs_solver_s *fs_solver;
 typedef struct fs_mm_s *fs_mm;
 typedef struct fs_nka_s *fs_nka;
+typedef struct fs_parcsr_s *fs_parcsr;
 
 /* ----------------------------------------------------------- context --- */
 /* Replaces the FleCSI runtime/scheduler context the reference's vector ops
@@ -257,6 +258,33 @@ FS_API int fs_shell_create(fs_ctx ctx, int64_t nrows, int64_t ncols, fs_op_fn fn
  * device. */
 FS_API int fs_parcsr_spmv(fs_csr A, int parts, fs_vec x, fs_vec y);
 
+/* One color of the distributed operator itself: mat::parcsr over topo::csr
+ * (flecsolve/matrices/parcsr.hh:29-177, topo/csr.hh:413-632), the color's
+ * rows on this device.  From the color's rows (rowptr[nrows + 1], global
+ * column ids gcol, values) and its owned column block [col_begin, col_end)
+ * (the column block of the same color, an equal_map block as in
+ * parcsr.hh:166-169), built as the reference's coloring and init_mats build
+ * it (csr.hh:482-618): the ghost columns are the column ids outside the
+ * owned block, sorted and unique (the colmap, fs_parcsr_ghosts); the diag
+ * part holds the owned entries (column = id - col_begin), the offd part the
+ * ghost entries (column = nown + the ghost's position in the colmap), each
+ * row in input order.
+ * fs_parcsr_color_spmv: y = diag x + offd x (parcsr.hh:60-71) for x holding
+ * the color's columns -- its nown owned values, then one value per ghost in
+ * colmap order, filled by the caller's halo exchange from the owning colors
+ * (topo/csr.hh:240-304).  Each row's diag and offd sums are taken
+ * separately with the reference's row arithmetic and then added: the bits
+ * of fs_parcsr_spmv on the whole matrix. */
+FS_API int fs_parcsr_create(fs_ctx ctx, int64_t col_begin, int64_t col_end, int64_t nrows,
+                            const int64_t *rowptr, const int64_t *gcol, const double *val,
+                            fs_parcsr *out);
+FS_API int fs_parcsr_destroy(fs_parcsr A);
+FS_API int fs_parcsr_shape(fs_parcsr A, int64_t *nrows, int64_t *nown, int64_t *nghost,
+                           int64_t *nnz_diag, int64_t *nnz_offd);
+/* the colmap: *n in = capacity (gids may be NULL to query), out = count */
+FS_API int fs_parcsr_ghosts(fs_parcsr A, int64_t *gids, int64_t *n);
+FS_API int fs_parcsr_color_spmv(fs_parcsr A, fs_vec x, fs_vec y);
+
 /* ---------------------------------------------------------- solvers --- */
 /* solver_settings, flecsolve/solvers/solver_settings.hh:31-36 */
 typedef struct {
@@ -283,7 +311,9 @@ enum fs_method {
 	FS_CG_MIXED = 3,     /* FP32 inner PCG inside FP64 refinement        */
 	FS_BICGSTAB_MIXED = 4, /* FP32 BiCGSTAB, FP64 residual replacement   */
 	FS_GMRES_MIXED = 5,  /* FP32 Arnoldi cycles, FP64 restart residual   */
-	FS_FCG = 6           /* op::fcg, flexible CG, cg.hh:145-244          */
+	FS_FCG = 6,          /* op::fcg, flexible CG, cg.hh:145-244          */
+	FS_CG_PIPELINED = 7  /* op::cg's recurrences rearranged (Chronopoulos
+	                        & Gear) to one grid reduction per iteration    */
 };
 
 /* The preconditioner slot P of krylov_parameters (krylov_parameters.hh:

@@ -377,3 +377,25 @@ def test_mixed_gmres(ctx, wl, ortho):
     assert info.status == "converged_rtol"
     assert _true_relres(A, b, x) <= 1e-8
     assert info.iters <= 1.2 * r.iters + 30
+
+
+@pytest.mark.parametrize("name", ["poisson2d-128_cg", "diffusion3d-16_cg", "poisson2d-128_cg_noprec_x0"])
+def test_pipelined_cg_against_reference_fixture(ctx, name):
+    """The single-reduction CG (the reference's recurrences rearranged,
+    Chronopoulos & Gear): the same iterations (+-2), the same stopping test,
+    and the solution within 1e-10 of the reference's CG."""
+    c = META["cases"][name]
+    A, b = P.workload(c["workload"])
+    kw = dict(c["kwargs"])
+    x0 = P.uniform(int(c["x0"][1]), A.nrows, 0.0, 1.0) if c["x0"] else None
+    prec = kw.pop("precond", "jacobi")
+    info, x, slv = _run(ctx, fs.pipelined_cg, A, b, x0, prec, maxiter=kw.pop("maxiter", 2000),
+                        rtol=kw.pop("rtol", 1e-8), use_zero_guess=kw.pop("use_zero_guess", True))
+    g = np.load(GOLD / f"{name}.npz")
+    assert info.status == c["status"]
+    assert abs(info.iters - c["iters"]) <= ITER_TOL
+    assert _true_relres(A, b, x) <= 1e-8 * 1.01
+    assert _rel(x, g["x"]) <= X_RTOL_F64
+    h = slv.history()
+    assert h.size == info.iters
+    assert np.allclose(h[:20], g["hist"][:20], rtol=1e-9, atol=0)
