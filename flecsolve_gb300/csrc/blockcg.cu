@@ -75,26 +75,8 @@ struct BAcc<float> {
 	__device__ double get() const { return (double)hi + (double)lo; }
 };
 
-// Thread layout of the block kernels: 256 threads = 16 row slots x 16
-// column lanes (lane j handles column j; a warp covers two rows, 128
-// contiguous bytes of an FP32 block vector).  A CTA step covers kStep rows
-// (kRows per slot), staged in shared memory for the 16 x 16 products.
-constexpr int kRows = 2;
-constexpr int kStep = kTile * kRows;  // 32 rows per CTA step
-
 __device__ __forceinline__ bool bcg_skip(const BcgState *st) {
 	return st->done || (st->flags & BCG_REPLACE);
-}
-
-// sum over the step's rows of a[rr][i] * b[rr][j] (plain FMA; the caller
-// adds the step sum into a compensated running sum)
-template<class V>
-__device__ __forceinline__ V step_dot(const V (*a)[kS], const V (*b)[kS], int i, int j) {
-	V t = 0;
-#pragma unroll
-	for (int rr = 0; rr < kStep; ++rr)
-		t = fma(a[rr][i], b[rr][j], t);
-	return t;
 }
 
 // sum over a 16-row tile of a[rr][i] * b[rr][j] (start and replacement
@@ -120,6 +102,66 @@ __device__ __forceinline__ double fold_parts(const double *part, int nb, int str
 				a[u] += __ldcg(part + (size_t)(b + u) * stride + t);
 	}
 	return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+}
+
+// Per-CTA partials: one row of kW doubles per CTA (the 16 x 16 Gram entries,
+// then up to two 16-value column norms).
+constexpr int kW = 256 + 2 * kS;
+constexpr int kGroup = 32;  // CTAs per first-level fold group
+
+// Two-level fold of the CTAs' partial rows part[b * kW + t], t < nval: the
+// last CTA of each group of kGroup CTAs folds the group's rows (in CTA
+// order) into gpart, and the last of those folds the group rows (in group
+// order) into res (shared memory).  Returns true in that one CTA.  A fixed
+// grouping, so the result is deterministic for a given grid; no CTA waits
+// for another.  counters: [0] the groups done, [1 + g] group g's CTAs done.
+__device__ bool fold2(const double *part, double *gpart, unsigned *counters, int nval,
+                      double *res) {
+	__shared__ int s_flag;
+	const int G = gridDim.x, g = blockIdx.x / kGroup, ng = (G + kGroup - 1) / kGroup;
+	const int b0 = g * kGroup, gsize = min(kGroup, G - b0);
+	__threadfence();
+	__syncthreads();
+	if (threadIdx.x == 0)
+		s_flag = atomicAdd(counters + 1 + g, 1u) == (unsigned)(gsize - 1);
+	__syncthreads();
+	if (!s_flag)
+		return false;
+	__threadfence();
+	for (int t = threadIdx.x; t < nval; t += blockDim.x) {
+		double a[4] = {0.0, 0.0, 0.0, 0.0};
+		for (int b = 0; b < gsize; b += 4) {
+#pragma unroll
+			for (int u = 0; u < 4; ++u)
+				if (b + u < gsize)
+					a[u] += __ldcg(part + (size_t)(b0 + b + u) * kW + t);
+		}
+		gpart[(size_t)g * kW + t] = (a[0] + a[1]) + (a[2] + a[3]);
+	}
+	if (threadIdx.x == 0)
+		counters[1 + g] = 0;
+	__threadfence();
+	__syncthreads();
+	if (threadIdx.x == 0)
+		s_flag = atomicAdd(counters, 1u) == (unsigned)(ng - 1);
+	__syncthreads();
+	if (!s_flag)
+		return false;
+	__threadfence();
+	for (int t = threadIdx.x; t < nval; t += blockDim.x) {
+		double a[4] = {0.0, 0.0, 0.0, 0.0};
+		for (int q = 0; q < ng; q += 4) {
+#pragma unroll
+			for (int u = 0; u < 4; ++u)
+				if (q + u < ng)
+					a[u] += __ldcg(gpart + (size_t)(q + u) * kW + t);
+		}
+		res[t] = (a[0] + a[1]) + (a[2] + a[3]);
+	}
+	if (threadIdx.x == 0)
+		counters[0] = 0;
+	__syncthreads();
+	return true;
 }
 
 // X = A^-1 B for the 16 x 16 matrix A with 16 right-hand sides B (both in
@@ -222,116 +264,225 @@ struct BcgOp {
 	int nx, ny, nz, K;
 };
 
-// q_j = (A P)[r][j] for lane j, the products in the CSR column order
+// ---------------------------------------------------------------------
+// Register-blocked layout of the iteration kernels.  Row phase: a thread
+// owns a quad of 4 columns of one row (64 rows per 256-thread step; a warp
+// reads 8 rows x 64 contiguous bytes of a block vector with 16-byte loads).
+// The 16 x 16 coefficient matrices (alpha, beta) are read 16 bytes at a
+// time from shared memory, the step's rows of P / Q / Z / R are staged in
+// shared memory (rows padded to kLd values: 16-byte aligned, the 8 rows of a
+// warp on distinct banks).  Gram phase: thread (g, a, b) accumulates the 4 x 4
+// block [4a, 4a+4) x [4b, 4b+4) of the product over the step rows g, g + 16,
+// g + 32, g + 48 (one plain step sum per entry, then a compensated running
+// sum); at the end the 16 row groups are folded in a fixed order.
+constexpr int kQ = 4;
+constexpr int kQRows = 256 / (kS / kQ);  // 64 rows per step
+constexpr int kLd = kS + 4;
+
+__device__ __forceinline__ void ld4(const float *p, float (&o)[4]) {
+	const float4 t = *reinterpret_cast<const float4 *>(p);
+	o[0] = t.x;
+	o[1] = t.y;
+	o[2] = t.z;
+	o[3] = t.w;
+}
+__device__ __forceinline__ void ld4(const double *p, double (&o)[4]) {
+	const double2 t0 = *reinterpret_cast<const double2 *>(p);
+	const double2 t1 = *reinterpret_cast<const double2 *>(p + 2);
+	o[0] = t0.x;
+	o[1] = t0.y;
+	o[2] = t1.x;
+	o[3] = t1.y;
+}
+__device__ __forceinline__ void st4(float *p, const float (&o)[4]) {
+	*reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
+}
+__device__ __forceinline__ void st4(double *p, const double (&o)[4]) {
+	*reinterpret_cast<double2 *>(p) = make_double2(o[0], o[1]);
+	*reinterpret_cast<double2 *>(p + 2) = make_double2(o[2], o[3]);
+}
 template<class V>
-__device__ __forceinline__ V bcg_row(const BcgOp<V> &A, const V *__restrict__ P, int r, int j) {
-	V q = 0;
+__device__ __forceinline__ void ldg4(const V *p, V (&o)[4]) {
+	if constexpr (sizeof(V) == 4) {
+		const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+		o[0] = t.x;
+		o[1] = t.y;
+		o[2] = t.z;
+		o[3] = t.w;
+	}
+	else {
+		const double2 t0 = __ldg(reinterpret_cast<const double2 *>(p));
+		const double2 t1 = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+		o[0] = t0.x;
+		o[1] = t0.y;
+		o[2] = t1.x;
+		o[3] = t1.y;
+	}
+}
+
+// Gram accumulation of one step: m[a'][b'] += sum over the group's rows of
+// za[row][4a + a'] * zb[row][4b + b'] (plain step sums, compensated across
+// steps)
+template<class V>
+struct GramAcc {
+	BAcc<V> m[kQ][kQ];
+	__device__ void step(const V (*za)[kLd], const V (*zb)[kLd], int g, int a, int b) {
+		V t[kQ][kQ];
+#pragma unroll
+		for (int i = 0; i < kQ; ++i)
+#pragma unroll
+			for (int j = 0; j < kQ; ++j)
+				t[i][j] = 0;
+#pragma unroll
+		for (int rr = 0; rr < kQRows / 16; ++rr) {
+			const int row = g + 16 * rr;
+			V u[kQ], w[kQ];
+			ld4(&za[row][kQ * a], u);
+			ld4(&zb[row][kQ * b], w);
+#pragma unroll
+			for (int i = 0; i < kQ; ++i)
+#pragma unroll
+				for (int j = 0; j < kQ; ++j)
+					t[i][j] = fma(u[i], w[j], t[i][j]);
+		}
+#pragma unroll
+		for (int i = 0; i < kQ; ++i)
+#pragma unroll
+			for (int j = 0; j < kQ; ++j)
+				m[i][j].add(t[i][j]);
+	}
+	// the CTA's 16 x 16 sums into part row b (entry i * 16 + j); red holds
+	// 8 x 256 doubles of shared memory.  Row groups g and g + 1 share a warp
+	// (xor-16 shuffle), the 8 warps' sums are then folded in warp order.
+	__device__ void to_part(double *part, double (*red)[256], int g, int a, int b) {
+		const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+		__syncthreads();
+#pragma unroll
+		for (int i = 0; i < kQ; ++i)
+#pragma unroll
+			for (int j = 0; j < kQ; ++j) {
+				double v = m[i][j].get();
+				v += __shfl_xor_sync(0xffffffffu, v, 16);
+				if (lane < 16)
+					red[warp][(kQ * a + i) * kS + kQ * b + j] = v;
+			}
+		__syncthreads();
+		double t = 0.0;
+#pragma unroll
+		for (int w = 0; w < 8; ++w)
+			t += red[w][threadIdx.x];
+		part[(size_t)blockIdx.x * kW + threadIdx.x] = t;
+	}
+};
+
+// q[c] = (A P)[r][4 cq + c], the products in the CSR column order
+template<class V>
+__device__ __forceinline__ void bcg_row4(const BcgOp<V> &A, const V *__restrict__ P, int r, int cq,
+                                         V (&q)[kQ]) {
+#pragma unroll
+	for (int c = 0; c < kQ; ++c)
+		q[c] = 0;
 	if (A.S) {
 		const int64_t nxy = (int64_t)A.nx * A.ny;
 		const int i = r % A.nx;
 		const int line = r / A.nx;
 		const int jj = A.K >= 2 ? line % A.ny : 0, kk = A.K >= 2 ? line / A.ny : 0;
 		const V *U1 = A.S + A.ld, *U2 = A.S + 2 * A.ld, *U3 = A.S + 3 * A.ld;
-		const bool lz = A.K >= 3 && kk > 0, hz = A.K >= 3 && kk < A.nz - 1;
-		const bool ly = A.K >= 2 && jj > 0, hy = A.K >= 2 && jj < A.ny - 1;
-		const bool lx = i > 0, hx = i < A.nx - 1;
-		// every load first (fixed slots in column order), then the sum
-		const bool has[7] = {lz, ly, lx, true, hx, hy, hz};
+		const bool has[7] = {A.K >= 3 && kk > 0, A.K >= 2 && jj > 0, i > 0, true,
+		                     i < A.nx - 1, A.K >= 2 && jj < A.ny - 1, A.K >= 3 && kk < A.nz - 1};
 		const int64_t off[7] = {-nxy, -A.nx, -1, 0, 1, A.nx, nxy};
-		V a[7], x[7];
+		// all loads issued before any use: an absent neighbour reads row r
+		// itself (an L1 hit) and its products are skipped
+		V a[7], x[7][kQ];
 #pragma unroll
 		for (int t = 0; t < 7; ++t) {
-			a[t] = 0;
-			x[t] = 0;
-			if (has[t]) {
-				const V *U = t == 3 ? A.S : (t < 3 ? (t == 0 ? U3 : t == 1 ? U2 : U1)
-				                                   : (t == 4 ? U1 : t == 5 ? U2 : U3));
-				a[t] = __ldg(U + (t < 3 ? r + off[t] : r));
-				x[t] = __ldg(P + (size_t)(r + off[t]) * kS + j);
-			}
+			const V *U = t == 3 ? A.S : (t < 3 ? (t == 0 ? U3 : t == 1 ? U2 : U1)
+			                                   : (t == 4 ? U1 : t == 5 ? U2 : U3));
+			const int64_t c = has[t] ? r + off[t] : r;
+			a[t] = __ldg(U + (t < 3 ? c : r));
+			ldg4(P + (size_t)c * kS + kQ * cq, x[t]);
 		}
 #pragma unroll
 		for (int t = 0; t < 7; ++t)
 			if (has[t])
-				q = fma(a[t], x[t], q);
-		return q;
+#pragma unroll
+				for (int c = 0; c < kQ; ++c)
+					q[c] = fma(a[t], x[t][c], q[c]);
+		return;
 	}
 	const int k0 = __ldg(A.rp + r), k1 = __ldg(A.rp + r + 1);
-	for (int k = k0; k < k1; k += 8) {
-		// a batch of up to 8 entries: the column ids, then the gathers
-		int c[8];
-		V a[8];
+	for (int k = k0; k < k1; k += 4) {
+		// a batch of up to 4 entries: the column ids, then the gathers
+		int col[4];
+		V a[4];
 #pragma unroll
-		for (int t = 0; t < 8; ++t)
-			if (k + t < k1) {
-				c[t] = __ldg(A.col + k + t);
-				a[t] = __ldg(A.val + k + t);
-			}
-		V x[8];
+		for (int t = 0; t < 4; ++t) {
+			const int kk = k + t < k1 ? k + t : k1 - 1;
+			col[t] = __ldg(A.col + kk);
+			a[t] = __ldg(A.val + kk);
+		}
+		V x[4][kQ];
 #pragma unroll
-		for (int t = 0; t < 8; ++t)
+		for (int t = 0; t < 4; ++t)
+			ldg4(P + (size_t)col[t] * kS + kQ * cq, x[t]);
+#pragma unroll
+		for (int t = 0; t < 4; ++t)
 			if (k + t < k1)
-				x[t] = __ldg(P + (size_t)c[t] * kS + j);
 #pragma unroll
-		for (int t = 0; t < 8; ++t)
-			if (k + t < k1)
-				q = fma(a[t], x[t], q);
+				for (int c = 0; c < kQ; ++c)
+					q[c] = fma(a[t], x[t][c], q[c]);
 	}
-	return q;
 }
 
 // Q = A P and the CTA's part of M = P^T Q; the last CTA forms alpha = M^-1 G
 template<class V>
 __global__ void __launch_bounds__(256)
 k_bcg_spmm(int n, BcgOp<V> A, const V *__restrict__ P, V *__restrict__ Q, BcgState *st,
-           double *part, unsigned *counter) {
-	__shared__ V sp[kStep][kS], sq[kStep][kS];
+           double *part, double *gpart, unsigned *counters) {
+	__shared__ __align__(16) V sp[kQRows][kLd];
+	__shared__ __align__(16) V sq[kQRows][kLd];
+	__shared__ double red[8][256];
 	__shared__ SmallLs L;
+	__shared__ double sres[kW];
 	if (bcg_skip(st))
 		return;
-	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
-	const int nsteps = (n + kStep - 1) / kStep;
-	BAcc<V> m;
+	const int rs = threadIdx.x >> 2, cq = threadIdx.x & 3;
+	const int g = threadIdx.x >> 4, ga = (threadIdx.x >> 2) & 3, gb = threadIdx.x & 3;
+	const int nsteps = (n + kQRows - 1) / kQRows;
+	GramAcc<V> m;
 	for (int t = blockIdx.x; t < nsteps; t += gridDim.x) {
-		V q[kRows], p[kRows];
-#pragma unroll
-		for (int u = 0; u < kRows; ++u) {
-			const int r = t * kStep + u * kTile + tr;
-			q[u] = 0;
-			p[u] = 0;
-			if (r < n) {
-				q[u] = bcg_row(A, P, r, tj);
-				p[u] = __ldg(P + (size_t)r * kS + tj);
-			}
+		const int r = t * kQRows + rs;
+		V q[kQ], p[kQ];
+		if (r < n) {
+			bcg_row4(A, P, r, cq, q);
+			ldg4(P + (size_t)r * kS + kQ * cq, p);
+			st4(Q + (size_t)r * kS + kQ * cq, q);
 		}
+		else {
 #pragma unroll
-		for (int u = 0; u < kRows; ++u) {
-			const int r = t * kStep + u * kTile + tr;
-			if (r < n)
-				Q[(size_t)r * kS + tj] = q[u];
-			sp[u * kTile + tr][tj] = p[u];
-			sq[u * kTile + tr][tj] = q[u];
+			for (int c = 0; c < kQ; ++c)
+				q[c] = p[c] = 0;
 		}
+		st4(&sp[rs][kQ * cq], p);
+		st4(&sq[rs][kQ * cq], q);
 		__syncthreads();
-		m.add(step_dot<V>(sp, sq, tr, tj));
+		m.step(sp, sq, g, ga, gb);
 		__syncthreads();
 	}
-	part[(size_t)blockIdx.x * 256 + threadIdx.x] = m.get();
-	if (last_block(counter)) {
-		const double s = fold_parts(part, gridDim.x, 256, threadIdx.x);
-		st->M[threadIdx.x] = s;
-		L.A[tr][tj] = s;
+	m.to_part(part, red, g, ga, gb);
+	if (fold2(part, gpart, counters, 256, sres)) {
+		const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
+		const double v = sres[threadIdx.x];
+		st->M[threadIdx.x] = v;
+		L.A[tr][tj] = v;
 		L.B[tr][tj] = st->G[threadIdx.x];
 		__syncthreads();
 		const bool ok = small_solve_par(L);
 		if (ok)
 			st->alpha[threadIdx.x] = L.B[tr][tj];
-		if (threadIdx.x == 0) {
-			if (!ok) {
-				st->done = 1;
-				st->status = FS_DIVERGED_BREAKDOWN;
-			}
-			*counter = 0;
+		if (threadIdx.x == 0 && !ok) {
+			st->done = 1;
+			st->status = FS_DIVERGED_BREAKDOWN;
 		}
 	}
 }
@@ -347,86 +498,105 @@ template<class V>
 __global__ void __launch_bounds__(256)
 k_bcg_update(int n, V *__restrict__ X, const V *__restrict__ P, V *__restrict__ R,
              const V *__restrict__ Q, const V *__restrict__ dinv, BcgState *st, double *part,
-             double *part2, unsigned *counter, double tolf, int maxiter, double delta) {
-	__shared__ V sa[kS][kS];
-	__shared__ V sp[kStep][kS], sq[kStep][kS];
-	__shared__ double cn[kTile][kS];
+             double *gpart, unsigned *counters, double tolf, int maxiter, double delta) {
+	__shared__ __align__(16) V sa[kS][kLd];
+	__shared__ __align__(16) V sp[kQRows][kLd];
+	__shared__ __align__(16) V sq[kQRows][kLd];
+	__shared__ double red[8][256];
 	__shared__ SmallLs L;
 	__shared__ int s_beta;
+	__shared__ double sres[kW];
 	if (bcg_skip(st))
 		return;
-	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
-	sa[tr][tj] = (V)st->alpha[threadIdx.x];
+	{
+		const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
+		sa[tr][tj] = (V)st->alpha[threadIdx.x];
+	}
 	__syncthreads();
-	V al[kS];
-#pragma unroll
-	for (int i = 0; i < kS; ++i)
-		al[i] = sa[i][tj];
-	const int nsteps = (n + kStep - 1) / kStep;
-	BAcc<V> g, nr;
+	const int rs = threadIdx.x >> 2, cq = threadIdx.x & 3;
+	const int g = threadIdx.x >> 4, ga = (threadIdx.x >> 2) & 3, gb = threadIdx.x & 3;
+	const int nsteps = (n + kQRows - 1) / kQRows;
+	GramAcc<V> gm;
+	BAcc<V> nr[kQ];
 	for (int t = blockIdx.x; t < nsteps; t += gridDim.x) {
-		V xr[kRows], rr[kRows];
+		const int r = t * kQRows + rs;
+		V p[kQ], q[kQ], x[kQ], rv[kQ];
+		V dr = 0;
+		if (r < n) {
+			ldg4(P + (size_t)r * kS + kQ * cq, p);
+			ldg4(Q + (size_t)r * kS + kQ * cq, q);
+			ld4(X + (size_t)r * kS + kQ * cq, x);
+			ld4(R + (size_t)r * kS + kQ * cq, rv);
+			dr = dinv ? __ldg(dinv + r) : V(1);
+		}
+		else {
 #pragma unroll
-		for (int u = 0; u < kRows; ++u) {
-			const int r = t * kStep + u * kTile + tr;
-			V pv = 0, qv = 0;
-			xr[u] = 0;
-			rr[u] = 0;
-			if (r < n) {
-				pv = P[(size_t)r * kS + tj];
-				qv = Q[(size_t)r * kS + tj];
-				xr[u] = X[(size_t)r * kS + tj];
-				rr[u] = R[(size_t)r * kS + tj];
+			for (int c = 0; c < kQ; ++c)
+				p[c] = q[c] = x[c] = rv[c] = 0;
+		}
+		st4(&sp[rs][kQ * cq], p);
+		st4(&sq[rs][kQ * cq], q);
+		__syncthreads();
+		// x += P[r][:] alpha[:, quad], r -= Q[r][:] alpha[:, quad]
+#pragma unroll
+		for (int i4 = 0; i4 < kS / kQ; ++i4) {
+			V pr[kQ], qr[kQ];
+			ld4(&sp[rs][kQ * i4], pr);
+			ld4(&sq[rs][kQ * i4], qr);
+#pragma unroll
+			for (int ii = 0; ii < kQ; ++ii) {
+				V al[kQ];
+				ld4(&sa[kQ * i4 + ii][kQ * cq], al);
+#pragma unroll
+				for (int c = 0; c < kQ; ++c) {
+					x[c] = fma(pr[ii], al[c], x[c]);
+					rv[c] = fma(-qr[ii], al[c], rv[c]);
+				}
 			}
-			sp[u * kTile + tr][tj] = pv;
-			sq[u * kTile + tr][tj] = qv;
+		}
+		V z[kQ];
+#pragma unroll
+		for (int c = 0; c < kQ; ++c) {
+			z[c] = dr * rv[c];
+			if (r < n)
+				nr[c].add(rv[c] * rv[c]);
+		}
+		if (r < n) {
+			st4(X + (size_t)r * kS + kQ * cq, x);
+			st4(R + (size_t)r * kS + kQ * cq, rv);
+		}
+		else {
+#pragma unroll
+			for (int c = 0; c < kQ; ++c)
+				z[c] = rv[c] = 0;
 		}
 		__syncthreads();
-		V zr[kRows];
-#pragma unroll
-		for (int u = 0; u < kRows; ++u) {
-			const int r = t * kStep + u * kTile + tr;
-			const int row = u * kTile + tr;
-#pragma unroll
-			for (int i = 0; i < kS; ++i) {
-				xr[u] = fma(sp[row][i], al[i], xr[u]);
-				rr[u] = fma(-sq[row][i], al[i], rr[u]);
-			}
-			zr[u] = 0;
-			if (r < n) {
-				X[(size_t)r * kS + tj] = xr[u];
-				R[(size_t)r * kS + tj] = rr[u];
-				zr[u] = dinv ? __ldg(dinv + r) * rr[u] : rr[u];
-				nr.add(rr[u] * rr[u]);
-			}
-			else
-				rr[u] = 0;
-		}
+		// the staged P and Q are consumed: stage Z and R for G' = Z^T R
+		st4(&sp[rs][kQ * cq], z);
+		st4(&sq[rs][kQ * cq], rv);
 		__syncthreads();
-		// the staged P and Q are consumed: reuse them for Z and R
-#pragma unroll
-		for (int u = 0; u < kRows; ++u) {
-			sp[u * kTile + tr][tj] = zr[u];
-			sq[u * kTile + tr][tj] = rr[u];
-		}
-		__syncthreads();
-		g.add(step_dot<V>(sp, sq, tr, tj));
+		gm.step(sp, sq, g, ga, gb);
 		__syncthreads();
 	}
-	part[(size_t)blockIdx.x * 256 + threadIdx.x] = g.get();
-	// column norms: fold the 16 row slots of each column in the block first
-	cn[tr][tj] = nr.get();
+	gm.to_part(part, red, g, ga, gb);
+	// column norms: this thread's 4 columns, folded over the 64 row slots
+	// (in the fold buffer, once every thread has read it)
+	double (*cn)[kS] = reinterpret_cast<double (*)[kS]>(&red[0][0]);
+	__syncthreads();
+#pragma unroll
+	for (int c = 0; c < kQ; ++c)
+		cn[rs][kQ * cq + c] = nr[c].get();
 	__syncthreads();
 	if (threadIdx.x < kS) {
 		double c = 0.0;
-		for (int q = 0; q < kTile; ++q)
+		for (int q = 0; q < kQRows; ++q)
 			c += cn[q][threadIdx.x];
-		part2[(size_t)blockIdx.x * kS + threadIdx.x] = c;
+		part[(size_t)blockIdx.x * kW + 256 + threadIdx.x] = c;
 	}
-	if (last_block(counter)) {
-		st->Gn[threadIdx.x] = fold_parts(part, gridDim.x, 256, threadIdx.x);
+	if (fold2(part, gpart, counters, 256 + kS, sres)) {
+		st->Gn[threadIdx.x] = sres[threadIdx.x];
 		if (threadIdx.x < kS)
-			st->rnorm[threadIdx.x] = sqrt(fold_parts(part2, gridDim.x, kS, threadIdx.x));
+			st->rnorm[threadIdx.x] = sqrt(sres[256 + threadIdx.x]);
 		__syncthreads();
 		if (threadIdx.x == 0) {
 			const int it = st->iter + 1;
@@ -479,8 +649,6 @@ k_bcg_update(int n, V *__restrict__ X, const V *__restrict__ P, V *__restrict__ 
 			st->done = 1;
 			st->status = FS_DIVERGED_BREAKDOWN;
 		}
-		if (threadIdx.x == 0)
-			*counter = 0;
 	}
 }
 
@@ -489,43 +657,50 @@ template<class V>
 __global__ void __launch_bounds__(256)
 k_bcg_dir(int n, V *__restrict__ P, const V *__restrict__ R, const V *__restrict__ dinv,
           const BcgState *st) {
-	__shared__ V sb[kS][kS], sp[kStep][kS];
+	__shared__ __align__(16) V sb[kS][kLd];
+	__shared__ __align__(16) V sp[kQRows][kLd];
 	if (bcg_skip(st))
 		return;
-	const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
-	sb[tr][tj] = (V)st->beta[threadIdx.x];
-	__syncthreads();
-	V be[kS];
-#pragma unroll
-	for (int i = 0; i < kS; ++i)
-		be[i] = sb[i][tj];
-	const int nsteps = (n + kStep - 1) / kStep;
+	{
+		const int tr = threadIdx.x / kS, tj = threadIdx.x % kS;
+		sb[tr][tj] = (V)st->beta[threadIdx.x];
+	}
+	const int rs = threadIdx.x >> 2, cq = threadIdx.x & 3;
+	const int nsteps = (n + kQRows - 1) / kQRows;
 	for (int t = blockIdx.x; t < nsteps; t += gridDim.x) {
-		V z[kRows];
+		const int r = t * kQRows + rs;
+		V p[kQ], pn[kQ];
+		if (r < n) {
+			ld4(P + (size_t)r * kS + kQ * cq, p);
+			ldg4(R + (size_t)r * kS + kQ * cq, pn);
+			const V d = dinv ? __ldg(dinv + r) : V(1);
 #pragma unroll
-		for (int u = 0; u < kRows; ++u) {
-			const int r = t * kStep + u * kTile + tr;
-			V pv = 0;
-			z[u] = 0;
-			if (r < n) {
-				pv = P[(size_t)r * kS + tj];
-				z[u] = (dinv ? __ldg(dinv + r) : V(1)) * R[(size_t)r * kS + tj];
+			for (int c = 0; c < kQ; ++c)
+				pn[c] = d * pn[c];
+		}
+		else {
+#pragma unroll
+			for (int c = 0; c < kQ; ++c)
+				p[c] = pn[c] = 0;
+		}
+		__syncthreads();
+		st4(&sp[rs][kQ * cq], p);
+		__syncthreads();
+#pragma unroll
+		for (int i4 = 0; i4 < kS / kQ; ++i4) {
+			V pr[kQ];
+			ld4(&sp[rs][kQ * i4], pr);
+#pragma unroll
+			for (int ii = 0; ii < kQ; ++ii) {
+				V be[kQ];
+				ld4(&sb[kQ * i4 + ii][kQ * cq], be);
+#pragma unroll
+				for (int c = 0; c < kQ; ++c)
+					pn[c] = fma(pr[ii], be[c], pn[c]);
 			}
-			sp[u * kTile + tr][tj] = pv;
 		}
-		__syncthreads();
-#pragma unroll
-		for (int u = 0; u < kRows; ++u) {
-			const int r = t * kStep + u * kTile + tr;
-			const int row = u * kTile + tr;
-			V pn = z[u];
-#pragma unroll
-			for (int i = 0; i < kS; ++i)
-				pn = fma(sp[row][i], be[i], pn);
-			if (r < n)
-				P[(size_t)r * kS + tj] = pn;
-		}
-		__syncthreads();
+		if (r < n)
+			st4(P + (size_t)r * kS + kQ * cq, pn);
 	}
 }
 
@@ -709,8 +884,9 @@ k_bcg_true_res(int n, const int *__restrict__ rp, const int *__restrict__ col,
 struct BcgPlan {
 	BcgState *st = nullptr, *hst = nullptr;
 	void *work = nullptr;       // P, Q, R (and the FP32 X correction)
-	double *part = nullptr;     // G partials (grid x 256) + norm partials
-	unsigned *counter = nullptr;
+	double *part = nullptr;     // per-CTA partial rows (grid x kW) + norm partials
+	double *gpart = nullptr;    // per-group partial rows of the two-level fold
+	unsigned *counter = nullptr;  // [0] + one per fold group
 	int64_t n = 0;
 };
 std::map<std::pair<const Csr *, bool>, BcgPlan> g_bcg;
@@ -725,24 +901,37 @@ int block_cg_run(Ctx *ctx, const fs_krylov_settings *s, Csr *A, bool jac, Vec *B
 	if (mixed)
 		FS_TRY(ensure_val32(A));
 	BcgPlan &p = g_bcg[std::make_pair((const Csr *)A, mixed)];
-	// two 256-thread CTAs per SM: each thread keeps enough loads in flight,
-	// and the last CTA's fold of the partials stays short
-	const int G = std::max(1, std::min(ctx->sms * 2, (int)((n + kStep - 1) / kStep)));
+	// every kernel on all SMs at its occupancy (resident CTAs per SM), the
+	// partials folded in groups of kGroup CTAs
+	const int nsteps = (int)((n + kQRows - 1) / kQRows);
+	auto grid_of = [&](auto kern) {
+		int nb = 0;
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, 0) != cudaSuccess || nb < 1)
+			nb = 1;
+		return std::max(1, std::min(ctx->sms * std::min(nb, 8), nsteps));
+	};
+	const int G = grid_of(k_bcg_spmm<V>);
+	const int Gu = grid_of(k_bcg_update<V>);
+	const int Gd = grid_of(k_bcg_dir<V>);
 	const size_t m = (size_t)n * kS;
 	if (p.n != n) {
 		if (p.work) {
 			cudaStreamSynchronize(ctx->stream);
 			cudaFree(p.work);
 			cudaFree(p.part);
+			cudaFree(p.gpart);
 			cudaFree(p.counter);
 			cudaFree(p.st);
 			cudaFreeHost(p.hst);
 			p = BcgPlan();
 		}
 		FS_CUDA_TRY(ctx, cudaMalloc(&p.work, sizeof(V) * (mixed ? 4 : 3) * m));
-		FS_CUDA_TRY(ctx, cudaMalloc(&p.part, sizeof(double) * (size_t)ctx->sms * 8 * (256 + 2 * kS)));
-		FS_CUDA_TRY(ctx, cudaMalloc(&p.counter, 64));
-		FS_CUDA_TRY(ctx, cudaMemset(p.counter, 0, 64));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.part, sizeof(double) * (size_t)ctx->sms * 8 * kW));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.gpart,
+		                            sizeof(double) * (size_t)(ctx->sms * 8 / kGroup + 2) * kW));
+		const size_t cbytes = sizeof(unsigned) * (size_t)(ctx->sms * 8 / kGroup + 2);
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.counter, cbytes));
+		FS_CUDA_TRY(ctx, cudaMemset(p.counter, 0, cbytes));
 		FS_CUDA_TRY(ctx, fence_setup_copies());
 		FS_CUDA_TRY(ctx, cudaMalloc(&p.st, sizeof(BcgState)));
 		FS_CUDA_TRY(ctx, cudaMallocHost(&p.hst, sizeof(BcgState)));
@@ -787,12 +976,13 @@ int block_cg_run(Ctx *ctx, const fs_krylov_settings *s, Csr *A, bool jac, Vec *B
 	FS_TRY(read_back());
 	while (!p.hst->done) {
 		for (int j = 0; j < k; ++j) {
-			k_bcg_spmm<V><<<G, 256, 0, ctx->stream>>>((int)n, op, Pm, Qm, p.st, part, p.counter);
+			k_bcg_spmm<V><<<G, 256, 0, ctx->stream>>>((int)n, op, Pm, Qm, p.st, part, p.gpart,
+			                                          p.counter);
 			FS_TRY(check_launch(ctx, "block cg spmm"));
-			k_bcg_update<V><<<G, 256, 0, ctx->stream>>>((int)n, xv, Pm, R, Qm, dinv, p.st, part,
-			                                            part2, p.counter, tolf, maxiter, delta);
+			k_bcg_update<V><<<Gu, 256, 0, ctx->stream>>>((int)n, xv, Pm, R, Qm, dinv, p.st, part,
+			                                             p.gpart, p.counter, tolf, maxiter, delta);
 			FS_TRY(check_launch(ctx, "block cg update"));
-			k_bcg_dir<V><<<G, 256, 0, ctx->stream>>>((int)n, Pm, R, dinv, p.st);
+			k_bcg_dir<V><<<Gd, 256, 0, ctx->stream>>>((int)n, Pm, R, dinv, p.st);
 			FS_TRY(check_launch(ctx, "block cg direction"));
 		}
 		FS_TRY(read_back());

@@ -219,6 +219,17 @@ struct EpiScaleStore {
 __device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
 
+// Loads of a chunk of basis vectors at element i: all kChunk loads are
+// issued before any use (vector indices past `last` repeat `last`, an L1 hit),
+// so one element costs one memory round trip, not one per vector.
+template<class T>
+__device__ __forceinline__ void load_chunk(const T *__restrict__ V, int64_t ld, int j0, int last,
+                                           int64_t i, T (&vr)[kChunk]) {
+#pragma unroll
+	for (int j = 0; j < kChunk; ++j)
+		vr[j] = V[(size_t)min(j0 + j, last) * ld + i];
+}
+
 // CGS2 pass 1: h1_j = v . V_j, j in [j0, j0 + nj)
 template<class T>
 __global__ void __launch_bounds__(kT)
@@ -232,11 +243,13 @@ k_gm_dots(int64_t n, const T *__restrict__ V, int64_t ld, int j0, int nj,
 	for (int j = 0; j < kChunk; ++j)
 		acc[j] = T(0);
 	FOR_EACH(i, n) {
+		T vr[kChunk];
+		load_chunk(V, ld, j0, j0 + nj - 1, i, vr);
 		const T vi = v[i];
 #pragma unroll
 		for (int j = 0; j < kChunk; ++j)
 			if (j < nj)
-				acc[j] = mad(vi, V[(size_t)(j0 + j) * ld + i], acc[j]);
+				acc[j] = mad(vi, vr[j], acc[j]);
 	}
 	double accd[kChunk];
 #pragma unroll
@@ -251,9 +264,9 @@ k_gm_dots(int64_t n, const T *__restrict__ V, int64_t ld, int j0, int nj,
 }
 
 // CGS2 pass 2: (chunk j0 == 0 only) v -= sum_j h1_j V_j over all k + 1
-// vectors, then h2_j = v . V_j for the chunk [j0, j0 + nj).  When all k + 1
-// vectors fit one chunk, each V_j is loaded once and kept in registers for
-// both the update and the dot.
+// vectors, then h2_j = v . V_j for the chunk [j0, j0 + nj).  The update
+// walks the basis a chunk at a time (each chunk's loads issued together); the
+// first chunk's vectors stay in registers for the dots of chunk 0.
 template<class T>
 __global__ void __launch_bounds__(kT)
 k_gm_project_dots(int64_t n, const T *__restrict__ V, int64_t ld, int kp1, int j0, int nj,
@@ -270,36 +283,29 @@ k_gm_project_dots(int64_t n, const T *__restrict__ V, int64_t ld, int kp1, int j
 #pragma unroll
 	for (int j = 0; j < kChunk; ++j)
 		acc[j] = T(0);
-	if (j0 == 0 && kp1 <= kChunk) {
-		FOR_EACH(i, n) {
-			T vr[kChunk];
-			T vi = v[i];
+	FOR_EACH(i, n) {
+		T vr[kChunk];
+		T vi = v[i];
+		if (j0 == 0) {
+			for (int c0 = 0; c0 < kp1; c0 += kChunk) {
+				T vc[kChunk];
+				load_chunk(V, ld, c0, kp1 - 1, i, vc);
 #pragma unroll
-			for (int j = 0; j < kChunk; ++j)
-				if (j < kp1) {
-					vr[j] = V[(size_t)j * ld + i];
-					vi = mad(-hs[j], vr[j], vi);
+				for (int j = 0; j < kChunk; ++j) {
+					if (c0 + j < kp1)
+						vi = mad(-hs[c0 + j], vc[j], vi);
+					if (c0 == 0)
+						vr[j] = vc[j];
 				}
-			v[i] = vi;
-#pragma unroll
-			for (int j = 0; j < kChunk; ++j)
-				if (j < kp1)
-					acc[j] = mad(vi, vr[j], acc[j]);
-		}
-	}
-	else {
-		FOR_EACH(i, n) {
-			T vi = v[i];
-			if (j0 == 0) {
-				for (int j = 0; j < kp1; ++j)
-					vi = mad(-hs[j], V[(size_t)j * ld + i], vi);
-				v[i] = vi;
 			}
-#pragma unroll
-			for (int j = 0; j < kChunk; ++j)
-				if (j < nj)
-					acc[j] = mad(vi, V[(size_t)(j0 + j) * ld + i], acc[j]);
+			v[i] = vi;
 		}
+		else
+			load_chunk(V, ld, j0, j0 + nj - 1, i, vr);
+#pragma unroll
+		for (int j = 0; j < kChunk; ++j)
+			if (j < nj)
+				acc[j] = mad(vi, vr[j], acc[j]);
 	}
 	double accd[kChunk];
 #pragma unroll
@@ -330,8 +336,14 @@ k_gm_project_norm(int64_t n, const T *__restrict__ V, int64_t ld, int kp1,
 	T acc = T(0);
 	FOR_EACH(i, n) {
 		T vi = v[i];
-		for (int j = 0; j < kp1; ++j)
-			vi = mad(-hs[j], V[(size_t)j * ld + i], vi);
+		for (int c0 = 0; c0 < kp1; c0 += kChunk) {
+			T vc[kChunk];
+			load_chunk(V, ld, c0, kp1 - 1, i, vc);
+#pragma unroll
+			for (int j = 0; j < kChunk; ++j)
+				if (c0 + j < kp1)
+					vi = mad(-hs[c0 + j], vc[j], vi);
+		}
 		v[i] = vi;
 		acc = mad(vi, vi, acc);
 	}

@@ -29,8 +29,8 @@ def test_colors_reproduce_parcsr_spmv(ctx, name, colors):
     A = _random(2000, 9) if name == "random" else P.workload(name)[0]
     x = P.uniform(92, A.ncols)
     dA = fs.CSR(ctx, A)
-    y_all = fs.Vector(ctx, A.nrows)
-    fs.api.lib().fs_parcsr_spmv(dA.h, colors, fs.Vector(ctx, x).h, y_all.h)
+    vx, y_all = fs.Vector(ctx, x), fs.Vector(ctx, A.nrows)
+    dA.parcsr_apply(colors, vx, y_all)
     y = np.empty(A.nrows)
     for c in range(colors):
         cr = PC.color_rows(A, c, colors)
