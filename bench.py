@@ -158,6 +158,29 @@ def spmv_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, nsym=3):
     return mat + 2 * nrows * val_bytes
 
 
+def gmres_solve_bytes(nrows, nnz, coding, nblk, iters, restarts, m=30, ortho="cgs2",
+                      basis_bytes=4):
+    """Algorithmic bytes of a right-preconditioned Jacobi GMRES(m) solve of
+    `iters` steps: per step with kp1 = k + 1 basis vectors (k = step mod m)
+    the SpMV in the basis type (x gathered through D^-1: + N s_b) and the
+    orthogonalisation -- staged CGS2: three passes reading v and the kp1
+    vectors, the last writing V_k+1 = (3 (kp1 + 1) + 1) N s_b; MGS: kp1 + 1
+    passes reading v, kp1 of them writing it, 2 kp1 basis reads, then the
+    normalisation (read v, write V_k+1) = (4 kp1 + 3) N s_b.  Per cycle end
+    the FP64 correction (kp1 = m basis vectors, D^-1, x read and written),
+    the FP64 residual SpMV (b read, r written) and basis_0 (read r, write
+    V_0)."""
+    sb, n = basis_bytes, nrows
+    total = 0
+    spmv = spmv_bytes(n, nnz, sb, coding, nblk) + n * sb
+    for it in range(iters):
+        kp1 = it % m + 1
+        ortho_b = (3 * (kp1 + 1) + 1) if ortho == "cgs2" else (4 * kp1 + 3)
+        total += spmv + ortho_b * n * sb
+    cycle = (m * sb + 8 + 16) * n + spmv_bytes(n, nnz, 8, coding, nblk) + 16 * n + (8 + sb) * n
+    return total + (restarts + 1) * cycle
+
+
 def pcg_iter_bytes(nrows, nnz, val_bytes, coding=0, nblk=0, kind="fp64"):
     """Algorithmic bytes of one Jacobi-PCG iteration beyond the SpMV's own
     (B_spmv: matrix data, p read once, w written once).
@@ -334,6 +357,27 @@ def run_spmv_only(args):
             out[dt + "_" + CODING_NAMES[coding]] = {
                 "ms": ms, "gbs": gbs, "frac": gbs / peak, "peak": peak,
                 "peak_source": f"hbm_gbs of {peak_kind}", "algorithmic_bytes": nbytes}
+    if best == 0:
+        # no row patterns: the column-id schedules, one thread per row against
+        # 4 / 8 / 16 / 32 lanes per row, and the autotuner's choice
+        for dt, vb in (("f64", 8), ("f32", 4)):
+            npdt = np.float64 if dt == "f64" else np.float32
+            nbytes = spmv_bytes(n, nnz, vb, 0, dA.nblk())
+            sched = {}
+            for lanes in (0, 4, 8, 16, 32):
+                dA.set_lanes(lanes, npdt)
+                ms = spmv_events_ms(fs, ctx, dA, n, dt, reps=max(1, args.steps))
+                sched["row_per_thread" if lanes == 0 else f"lanes_{lanes}"] = {
+                    "ms": ms, "frac": nbytes / (ms * 1e-3) / 1e9 / peak}
+            dA.set_lanes(-1, npdt)
+            tuned = dA.tune(npdt)
+            ms = spmv_events_ms(fs, ctx, dA, n, dt, reps=max(1, args.steps))
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            out[dt + "_colids_schedules"] = {
+                "tuned_lanes": tuned, "ms": ms, "gbs": gbs, "frac": gbs / peak, "peak": peak,
+                "peak_source": f"hbm_gbs of {peak_kind}", "algorithmic_bytes": nbytes,
+                "rows_nnz_mean": nnz / n, "rows_nnz_max": int(np.diff(A.rowptr).max()),
+                "schedules": sched}
     dA.index_coding(best)
     return out
 
@@ -385,6 +429,18 @@ def run_suite(args):
             s, info = _timed_solve(ctx, slv, vb, vx)
             res[name] = {"s": s, "iters": info.iters, "restarts": info.restarts,
                          "status": info.status, "true_relres": _relres(S, b, vx.numpy())}
+            if name.startswith("gmres") and "max_krylov_dim" in kw:
+                # bandwidth bound of the whole solve (algorithmic bytes / HBM peak)
+                mixed = name.endswith("mixed")
+                ortho = kw.get("ortho", "cgs2" if mixed else "mgs")
+                nbytes = gmres_solve_bytes(A.nrows, A.nnz, dA.index_coding(), dA.nblk(), info.iters,
+                                           info.restarts, kw["max_krylov_dim"], ortho,
+                                           4 if mixed else 8)
+                peak, peak_kind = _peaks()
+                res[name]["roofline"] = {
+                    "algorithmic_bytes": nbytes, "achieved_gbs": nbytes / s / 1e9,
+                    "bound_s": nbytes / (peak * 1e9), "frac": nbytes / (peak * 1e9) / s,
+                    "peak_source": f"hbm_gbs of {peak_kind}", "ortho": ortho}
         out[tag] = res
 
     g30 = dict(max_krylov_dim=30, restart=True)

@@ -163,6 +163,8 @@ _PROTOS = {
     "fs_csr_index_coding": [_vp, C.c_int, C.POINTER(C.c_int)],
     "fs_csr_row_blocks": [_vp, C.POINTER(_i64)],
     "fs_csr_grid_dims": [_vp, C.POINTER(_i64)],
+    "fs_csr_tune": [_vp, C.c_int, C.POINTER(C.c_int)],
+    "fs_csr_set_lanes": [_vp, C.c_int, C.c_int],
     "fs_parcsr_create": [_vp, _i64, _i64, _i64, _vp, _vp, _vp, C.POINTER(_vp)],
     "fs_parcsr_destroy": [_vp],
     "fs_parcsr_shape": [_vp] + [C.POINTER(_i64)] * 5,

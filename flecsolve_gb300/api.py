@@ -244,6 +244,13 @@ class Vector:
         return len(self)
 
 
+def _dtype_code(dtype) -> int:
+    """FS_F32 for float32 / "f32", FS_F64 otherwise."""
+    if isinstance(dtype, str):
+        return _lib.F32 if dtype == "f32" else _lib.F64
+    return _lib.F32 if np.dtype(dtype) == np.float32 else _lib.F64
+
+
 class CSR:
     """Device CSR operator (``op::core<mat::csr<double>>``).  ``var`` is the
     operator's input/output variable (``op::base<Params, ivar, ovar>``,
@@ -352,6 +359,19 @@ class CSR:
         d = (C.c_int64 * 3)()
         check(lib().fs_csr_grid_dims(self.h, d), self.ctx.h)
         return tuple(int(v) for v in d)
+
+    def tune(self, dtype=np.float64) -> int:
+        """Time the column-id SpMV schedules for values of `dtype` and keep
+        the fastest: 0 (one thread per row) or 4 / 8 / 16 / 32 lanes per
+        row.  Returns the choice."""
+        lanes = C.c_int()
+        check(lib().fs_csr_tune(self.h, _dtype_code(dtype), C.byref(lanes)), self.ctx.h, "fs_csr_tune")
+        return lanes.value
+
+    def set_lanes(self, lanes: int, dtype=np.float64) -> None:
+        """Fix the column-id SpMV schedule (-1: tune again on the next SpMV)."""
+        check(lib().fs_csr_set_lanes(self.h, _dtype_code(dtype), int(lanes)), self.ctx.h,
+              "fs_csr_set_lanes")
 
     def values(self) -> np.ndarray:
         """The current values (row order) copied to the host."""

@@ -115,6 +115,9 @@ struct Csr {
 	unsigned *sym_flag = nullptr;   // device: set by the build when a pair differs
 	bool sym64_valid = false, sym32_valid = false;
 	int sym_state = -1;             // -1 not checked since the values changed, 0 no, 1 yes
+	// FMA-mode column-id SpMV kernel per value type (0 FP64, 1 FP32): 0 row
+	// blocks, L lanes per row of the vector kernel, -1 not tuned yet
+	int vec_lanes[2] = {-1, -1};
 	double *dinv = nullptr;    // 1 / a_ii, built on first use
 	float *dinv32 = nullptr;
 	bool dinv_valid = false;
@@ -157,6 +160,9 @@ inline int active_coding(const Csr *A, bool f32 = false) {
 void invalidate_values(Csr *A);
 // FP32 values and the Jacobi diagonal, built on first use (spmv.cu)
 int ensure_val32(Csr *A);
+// lanes per row of the FMA-mode column-id SpMV for A's values of one type (0:
+// the row-block kernel); tunes A on first use outside a graph capture
+int spmv_lanes(Ctx *ctx, const Csr *A, bool f32);
 int ensure_dinv(Csr *A);
 // build the symmetric storage of A's current values for FP64 or FP32 SpMVs
 // when the format is requested and the values are symmetric (setup path: may

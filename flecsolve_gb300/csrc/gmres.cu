@@ -567,6 +567,11 @@ __global__ void k_gm_mixed_cycle_end(KState *st) {
 }
 
 }  // namespace
+}  // namespace fsg
+
+#include "gmres_staged.cuh"
+
+namespace fsg {
 
 // ---------------------------------------------------------------- host --
 
@@ -621,6 +626,15 @@ int gm_step(Solver *s, int k) {
 			                                       s->counter, s->hist);
 			FS_TRY(check_launch(ctx, "gmres mgs"));
 		}
+	}
+	else if (kp1 <= kStagedMax && s->gm_map_base == (const void *)B.V) {
+		// staged CGS2: three passes, the last one writes V_{k+1}
+		OrthoArgs<T> oa{B.v, B.V + (size_t)kp1 * ld, n, kp1, staged_stages(kp1), staged_stride(kp1),
+		                g, s->st, s->part, s->counter, s->hist, ctx->dev_err};
+		const BasisMaps &map = *reinterpret_cast<const BasisMaps *>(s->gm_map);
+		FS_TRY((staged_pass<T, 1>(ctx, oa, map)));
+		FS_TRY((staged_pass<T, 2>(ctx, oa, map)));
+		return staged_pass<T, 3>(ctx, oa, map);
 	}
 	else {
 		for (int j0 = 0; j0 < kp1; j0 += kChunk) {
@@ -721,6 +735,21 @@ int gmres_run(Solver *s, Vec *b, Vec *x, fs_solve_info *info, bool mixed) {
 		for (auto &kv : s->graphs)
 			cudaGraphExecDestroy(kv.second.exec);
 		s->graphs.clear();
+	}
+	{
+		// the staged CGS2 passes read the basis through a tensor map (encoded
+		// on the host, once per basis, type and shape); without one the
+		// register passes run
+		const int key[3] = {(int)sizeof(T), cols, (int)(n & 0x7fffffff)};
+		if (s->gm_map_base != s->basis || memcmp(key, s->gm_map_key, sizeof key) != 0) {
+			s->gm_map_base = nullptr;
+			static_assert(sizeof(BasisMaps) <= sizeof(s->gm_map), "tensor map storage");
+			if (encode_basis_maps<T>(reinterpret_cast<BasisMaps *>(s->gm_map), (const T *)s->basis,
+			                         n, ld, cols)) {
+				s->gm_map_base = s->basis;
+				memcpy(s->gm_map_key, key, sizeof key);
+			}
+		}
 	}
 	FS_CUDA_TRY(ctx, cudaMemsetAsync(s->hdev, 0, sizeof(GmState), ctx->stream));
 	FS_TRY(solver_hist(s, std::max(1, maxiter)));

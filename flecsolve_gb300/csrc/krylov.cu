@@ -886,8 +886,16 @@ int solver_alloc(Solver *s) {
 	}
 	if (s->P.kind == FS_PRECOND_JACOBI)
 		FS_TRY(ensure_dinv(s->A));
-	if (s->method == FS_CG_MIXED || s->method == FS_BICGSTAB_MIXED || s->method == FS_GMRES_MIXED)
+	const bool mixed =
+		s->method == FS_CG_MIXED || s->method == FS_BICGSTAB_MIXED || s->method == FS_GMRES_MIXED;
+	if (mixed)
 		FS_TRY(ensure_val32(s->A));
+	// choose the column-id SpMV schedule now, outside any graph capture
+	if (!stores_no_rows(s->A)) {
+		spmv_lanes(ctx, s->A, false);
+		if (mixed)
+			spmv_lanes(ctx, s->A, true);
+	}
 	return FS_OK;
 }
 
@@ -915,7 +923,8 @@ int graph_run(Solver *s, const GraphKey &key_in, int (*body)(Solver *, void *), 
 	// are part of the key, so a format that changes with the values (the
 	// symmetric storage) or by request gets its own capture
 	GraphKey key = key_in;
-	key.fmt = active_coding(s->A, false) * 4 + active_coding(s->A, true);
+	key.fmt = active_coding(s->A, false) * 4 + active_coding(s->A, true) +
+	          16 * (s->A->vec_lanes[0] + 1) + 1024 * (s->A->vec_lanes[1] + 1);
 	const auto gkey = std::make_pair((const Csr *)s->A, key);
 	auto it = s->graphs.find(gkey);
 	if (it == s->graphs.end()) {

@@ -97,6 +97,11 @@ struct Solver {
 	float *w32[12] = {};
 	double *basis = nullptr;          // GMRES: (m + 1) x n, column j contiguous
 	size_t basis_bytes = 0;
+	// tensor maps of the basis for the staged CGS2 passes (four CUtensorMap)
+	// and what they were encoded for (null base: none)
+	alignas(64) unsigned char gm_map[4 * 128];
+	const void *gm_map_base = nullptr;
+	int gm_map_key[3] = {0, 0, 0};    // element size, columns, n (low 31 bits)
 	double *hdev = nullptr;           // GMRES: dot results scratch
 	KState *st = nullptr;             // device
 	KState *hst = nullptr;            // pinned mirror

@@ -494,11 +494,143 @@ int shell_apply(const Csr *A, Vec *x, Vec *y) {
 	return FS_OK;
 }
 
+// ------------------------------------------------ vector-SpMV tuning --
+
+// lanes per row from the mean row length (0: the row-block kernel)
+static int lanes_from_mean(const Csr *A) {
+	const double mean = A->nrows > 0 ? (double)A->nnz / (double)A->nrows : 0.0;
+	if (mean < 16.0)
+		return 0;
+	return mean < 32.0 ? 4 : mean < 64.0 ? 8 : mean < 128.0 ? 16 : 32;
+}
+
+// mean time of `reps` FMA-mode SpMVs y = A x with `lanes` (0: row blocks)
+template<class V>
+static int time_lanes(Ctx *ctx, const Csr *A, const V *vals, const V *x, V *y, int lanes,
+                      float *ms) {
+	auto once = [&]() -> int {
+		if (lanes > 0)
+			return launch_spmv_vec<V, false>(ctx, A, vals, x, (const V *)nullptr, EpiStore<V>{y},
+			                                 lanes);
+		CsrDev<V> d{A->rowptr, A->col, vals, A->blkinfo, A->nblk, ctx->dev_err};
+		return launch_spmv_as<V, false, false>(ctx, d, x, (const V *)nullptr, EpiStore<V>{y});
+	};
+	constexpr int reps = 5;
+	FS_TRY(once());
+	FS_TRY(once());
+	cudaEvent_t e0, e1;
+	if (cudaEventCreate(&e0) != cudaSuccess)
+		return set_err(ctx, FS_ERR_CUDA, "spmv tuning: event creation failed");
+	if (cudaEventCreate(&e1) != cudaSuccess) {
+		cudaEventDestroy(e0);
+		return set_err(ctx, FS_ERR_CUDA, "spmv tuning: event creation failed");
+	}
+	int rc = cudaEventRecord(e0, ctx->stream) == cudaSuccess ? FS_OK : FS_ERR_CUDA;
+	for (int i = 0; i < reps && rc == FS_OK; ++i)
+		rc = once();
+	if (rc == FS_OK && (cudaEventRecord(e1, ctx->stream) != cudaSuccess ||
+	                    cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(ms, e0, e1) != cudaSuccess))
+		rc = set_err(ctx, FS_ERR_CUDA, "spmv tuning: timing failed");
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	return rc;
+}
+
+// Time the row-block kernel and the vector kernel with 4, 8, 16 and 32
+// lanes per row on A's values of one type; *best = the fastest
+static int tune_lanes(Ctx *ctx, Csr *A, bool f32, int *best) {
+	if (f32)
+		FS_TRY(ensure_val32(A));
+	const size_t vb = f32 ? 4 : 8;
+	void *x = nullptr, *y = nullptr;
+	if (cudaMalloc(&x, (size_t)(A->ncols + 32) * vb) != cudaSuccess ||
+	    cudaMalloc(&y, (size_t)(A->nrows + 32) * vb) != cudaSuccess) {
+		cudaGetLastError();
+		if (x)
+			cudaFree(x);
+		return set_err(ctx, FS_ERR_OUT_OF_MEMORY, "spmv tuning: scratch allocation failed");
+	}
+	int rc = cudaMemsetAsync(x, 0, (size_t)(A->ncols + 32) * vb, ctx->stream) == cudaSuccess
+	             ? FS_OK
+	             : FS_ERR_CUDA;
+	float best_ms = 0.f;
+	*best = 0;
+	for (int lanes : {0, 4, 8, 16, 32}) {
+		if (rc != FS_OK)
+			break;
+		float ms = 0.f;
+		rc = f32 ? time_lanes<float>(ctx, A, A->val32, (const float *)x, (float *)y, lanes, &ms)
+		         : time_lanes<double>(ctx, A, A->val, (const double *)x, (double *)y, lanes, &ms);
+		if (rc == FS_OK && (lanes == 0 || ms < best_ms)) {
+			best_ms = ms;
+			*best = lanes;
+		}
+	}
+	cudaStreamSynchronize(ctx->stream);
+	cudaFree(x);
+	cudaFree(y);
+	return rc;
+}
+
+int spmv_lanes(Ctx *ctx, const Csr *A, bool f32) {
+	// stencil operators keep the row formats (all of them give the same bits)
+	if (A->pid || A->nrows == 0 || stores_no_rows(A))
+		return 0;
+	Csr *M = const_cast<Csr *>(A);
+	int &lanes = M->vec_lanes[f32 ? 1 : 0];
+	if (lanes >= 0)
+		return lanes;
+	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+	if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+		cudaGetLastError();
+		return lanes_from_mean(A);
+	}
+	int best = 0;
+	if (tune_lanes(ctx, M, f32, &best) != FS_OK) {
+		cudaGetLastError();
+		best = lanes_from_mean(A);
+	}
+	lanes = best;
+	return lanes;
+}
+
 }  // namespace fsg
 
 using namespace fsg;
 
 extern "C" {
+
+FS_API int fs_csr_tune(fs_csr h, int dtype, int *lanes) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	if (!ok_csr(A))
+		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_csr_tune"));
+	if (dtype != FS_F64 && dtype != FS_F32)
+		return set_err(A->ctx, FS_ERR_INVALID_ARG, "fs_csr_tune: dtype must be FS_F64 or FS_F32");
+	const bool f32 = dtype == FS_F32;
+	int best = 0;
+	if (!A->pid && A->nrows > 0) {
+		FS_TRY(tune_lanes(A->ctx, A, f32, &best));
+		A->vec_lanes[f32 ? 1 : 0] = best;
+	}
+	if (lanes)
+		*lanes = best;
+	return FS_OK;
+}
+
+FS_API int fs_csr_set_lanes(fs_csr h, int dtype, int lanes) {
+	Csr *A = reinterpret_cast<Csr *>(h);
+	if (!ok_csr(A))
+		return FS_ERR_BAD_HANDLE;
+	FS_TRY(reject_matrix_free(A, "fs_csr_set_lanes"));
+	if (dtype != FS_F64 && dtype != FS_F32)
+		return set_err(A->ctx, FS_ERR_INVALID_ARG, "fs_csr_set_lanes: dtype must be FS_F64 or FS_F32");
+	if (lanes != -1 && lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+		return set_err(A->ctx, FS_ERR_INVALID_ARG,
+		               "fs_csr_set_lanes: lanes must be -1, 0, 4, 8, 16 or 32");
+	A->vec_lanes[dtype == FS_F32 ? 1 : 0] = lanes;
+	return FS_OK;
+}
 
 FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
                          const int64_t *rowptr, const void *col, int index_bytes,

@@ -439,6 +439,7 @@ static inline int launch_spmv_as(Ctx *ctx, const CsrDev<V> &d, const V *x, const
 #include "spmv_sym.cuh"
 #include "spmv_grid.cuh"
 #include "spmv_fvm.cuh"
+#include "spmv_vec.cuh"
 
 namespace fsg {
 
@@ -474,6 +475,11 @@ static inline int launch_spmv(Ctx *ctx, const Csr *A, const V *vals, const V *x,
 			return launch_spmv_pat<V, EXACT>(ctx, A, vals, GatherScale<V>{x, dscale}, epi);
 		else
 			return launch_spmv_pat<V, EXACT>(ctx, A, vals, GatherX<V>{x}, epi);
+	}
+	if constexpr (!EXACT) {
+		const int lanes = spmv_lanes(ctx, A, F32);
+		if (lanes > 0)
+			return launch_spmv_vec<V, SCALE, Epi>(ctx, A, vals, x, dscale, epi, lanes);
 	}
 	CsrDev<V> d{A->rowptr, A->col, vals, A->blkinfo, A->nblk, ctx->dev_err};
 	return launch_spmv_as<V, EXACT, SCALE, Epi>(ctx, d, x, dscale, epi);

@@ -184,6 +184,31 @@ def convdiff3d(n: int, seed: int = 4, pe_max: float = 5.0,
 
 
 # Workloads named by what they are (sizes and seeds of the benchmark suite).
+def powerlaw(n: int, seed: int = 9, xmin: int = 16, alpha: float = 1.6, cap: int = 2048) -> CSR:
+    """Irregular n x n matrix with power-law row lengths: a row holds
+    min(cap, floor(xmin u^(-1/alpha))) entries (u ~ U[0, 1), seed), the
+    first on the diagonal, the others at uniform random columns (seed + 1;
+    an accidental diagonal moves one column right) with values U[-1, 1]
+    (seed + 2); the diagonal is 1 + the sum of the row's other magnitudes,
+    so the matrix is strictly diagonally dominant."""
+    u = uniform(seed, n, 0.0, 1.0)
+    lens = np.minimum(cap, np.floor(xmin * np.maximum(u, 1e-300) ** (-1.0 / alpha)))
+    lens = np.minimum(lens, n).astype(np.int64)
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(lens, out=rowptr[1:])
+    nnz = int(rowptr[-1])
+    rows = np.repeat(np.arange(n, dtype=np.int64), lens)
+    col = randint(seed + 1, nnz, 0, n - 1)
+    col = np.where(col == rows, (col + 1) % n, col)
+    val = uniform(seed + 2, nnz, -1.0, 1.0)
+    starts = rowptr[:-1]
+    col[starts] = np.arange(n)
+    off = np.abs(val)
+    off[starts] = 0.0
+    val[starts] = 1.0 + np.add.reduceat(off, starts)
+    return CSR(n, n, rowptr, col.astype(np.int32), val, f"powerlaw-{n}")
+
+
 def workload(name: str):
     """Return (A, b) for a named workload.
 
@@ -191,6 +216,8 @@ def workload(name: str):
     ``diffusion3d-256``    3-D log-normal diffusion 256^3 (faces seed 2,
                            RHS U[-1,1] seed 3)
     ``convdiff3d-192``     3-D upwind convection-diffusion 192^3 (seed 4),
+                           RHS U[-1,1] seed 3
+    ``powerlaw-2097152``   irregular rows (:func:`powerlaw`, seed 9), n rows,
                            RHS U[-1,1] seed 3
     Any size suffix works (e.g. ``diffusion3d-48``).
     """
@@ -210,6 +237,9 @@ def workload(name: str):
         b = uniform(6, A.nrows)
     elif kind == "convdiff3d":
         A = convdiff3d(n, seed=4)
+        b = uniform(3, A.nrows)
+    elif kind == "powerlaw":
+        A = powerlaw(n)
         b = uniform(3, A.nrows)
     else:
         raise ValueError(f"unknown workload {name}")

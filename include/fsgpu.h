@@ -183,6 +183,19 @@ FS_API int fs_csr_grid_dims(fs_csr A, int64_t dims[3]);
 /* number of SpMV row blocks (at most 256 rows and 1792 nonzeros each, a
  * longer row alone); no counterpart in the reference */
 FS_API int fs_csr_row_blocks(fs_csr A, int64_t *nblk);
+/* Kernel of the FMA-mode column-id SpMV for values of `dtype` (no
+ * counterpart in the reference; a schedule choice of this library): 0 the
+ * row-block kernel (one thread per row), 4 / 8 / 16 / 32 the vector kernel
+ * with that many lanes per row.  Matrices with row patterns (stencil
+ * operators, formats 1-3) always keep the row formats; EXACT mode always
+ * sums each row in one thread, in the reference's order.
+ * fs_csr_tune times every candidate on the context's stream (synchronising
+ * it) and keeps the fastest; an untuned matrix is tuned by its first SpMV
+ * outside a CUDA-graph capture (inside one, the mean row length chooses).
+ * *lanes (may be NULL) = the choice.  fs_csr_set_lanes fixes the choice; -1
+ * drops it so that the next SpMV tunes again. */
+FS_API int fs_csr_tune(fs_csr A, int dtype, int *lanes);
+FS_API int fs_csr_set_lanes(fs_csr A, int dtype, int lanes);
 
 /* ---------------------------------------------- MatrixMarket input ----
  * Host only: no context or device needed.  Reads a MatrixMarket coordinate

@@ -105,6 +105,16 @@ static int call_diag(or_diag *d, const double *x, int64_t n, double res) {
 static int dot_order = 0;
 OR_API void or_set_dot_order(int order) { dot_order = order; }
 
+/* Contraction switch (a checker option, default off): 1 fuses every
+ * product into the sum or update it feeds -- the SpMV row sums, the dots and
+ * the axpy updates -- as fma(a, b, c) with one rounding, the arithmetic of
+ * the device's FMA kernels.  Off is the reference's separately rounded
+ * products.  It measures how far an iteration count moves with that
+ * rounding alone. */
+static int contract = 0;
+OR_API void or_set_contract(int on) { contract = on; }
+#define OR_MAC(a, b, c) (contract ? fma((a), (b), (c)) : (a) * (b) + (c))
+
 /* seq.hh:282-295, res += x_i * y_i left to right */
 static double dot(int64_t n, const double *x, const double *y) {
 	double res = 0.0;
@@ -113,18 +123,18 @@ static double dot(int64_t n, const double *x, const double *y) {
 			const int64_t e = b + 4096 < n ? b + 4096 : n;
 			double part = 0.0;
 			for (int64_t i = b; i < e; ++i)
-				part += x[i] * y[i];
+				part = OR_MAC(x[i], y[i], part);
 			res += part;
 		}
 		return res;
 	}
 	if (dot_order == 2) {
 		for (int64_t i = n - 1; i >= 0; --i)
-			res += x[i] * y[i];
+			res = OR_MAC(x[i], y[i], res);
 		return res;
 	}
 	for (int64_t i = 0; i < n; ++i)
-		res += x[i] * y[i];
+		res = OR_MAC(x[i], y[i], res);
 	return res;
 }
 /* seq.hh:221-247 with p = 2: sqrt(scalar_prod(x, x)) */
@@ -133,7 +143,7 @@ static double l2norm(int64_t n, const double *x) { return sqrt(dot(n, x, x)); }
 static void axpy(int64_t n, double alpha, const double *x, const double *y,
                  double *z) {
 	for (int64_t i = 0; i < n; ++i)
-		z[i] = alpha * x[i] + y[i];
+		z[i] = OR_MAC(alpha, x[i], y[i]);
 }
 static void copy(int64_t n, const double *s, double *d) {
 	memcpy(d, s, (size_t)n * sizeof(double));
@@ -155,7 +165,7 @@ OR_API void or_spmv(const or_csr *A, const double *x, double *y) {
 	for (int64_t i = 0; i < A->nrows; ++i) {
 		y[i] = 0.;
 		for (int64_t off = A->rowptr[i]; off < A->rowptr[i + 1]; ++off)
-			y[i] += A->val[off] * x[A->col[off]];
+			y[i] = OR_MAC(A->val[off], x[A->col[off]], y[i]);
 	}
 }
 

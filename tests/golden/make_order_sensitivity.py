@@ -13,6 +13,10 @@ order alone.  Hours of
 CPU per GMRES run; each spec can run in its own process:
 
     python tests/golden/make_order_sensitivity.py convdiff3d-192:gmres:1
+
+The variant "fma" keeps the serial order and fuses every product into the sum
+or update it feeds (convdiff3d-192:gmres:fma): the rounding of the device's
+FMA kernels, which a change of summation order does not show.
 """
 from __future__ import annotations
 
@@ -31,17 +35,22 @@ import pyoracle as O  # noqa: E402
 
 SETTINGS = {"cg": {}, "bicgstab": {}, "gmres": {"krylov_dim": 30, "side": "right",
                                                  "restart": True}}
-ORDERS = {1: "blocks of 4096, then the block sums", 2: "right to left"}
+ORDERS = {"1": "blocks of 4096, then the block sums", "2": "right to left",
+          "fma": "serial, every product fused into its sum or update (one rounding, as in "
+                 "the device's FMA kernels)"}
 
 
 def run(spec: str) -> None:
     wl, method, order = spec.split(":")
-    order = int(order)
     A, b = P.workload(wl)
-    O.lib().or_set_dot_order(order)
+    if order == "fma":
+        O.lib().or_set_contract(1)
+    else:
+        O.lib().or_set_dot_order(int(order))
     t0 = time.time()
     r = O.solve(method, A, b, maxiter=20000, rtol=1e-8, **SETTINGS[method])
     O.lib().or_set_dot_order(0)
+    O.lib().or_set_contract(0)
     full = json.loads((HERE / "full_size.json").read_text())
     idx = full[wl][method]["x_sample_index"]
     out = HERE / "order_sensitivity.json"
@@ -49,7 +58,7 @@ def run(spec: str) -> None:
     with open(HERE / ".order_sensitivity.lock", "w") as lk:
         fcntl.flock(lk, fcntl.LOCK_EX)
         data = json.loads(out.read_text()) if out.exists() else {}
-        data.setdefault(wl, {}).setdefault(method, {})[str(order)] = {
+        data.setdefault(wl, {}).setdefault(method, {})[order] = {
             "order": ORDERS[order], "status": r.status, "iters": r.iters,
             "restarts": r.restarts, "res_norm_final": r.res_norm_final,
             "x_sample": r.x[idx].tolist(), "seconds_one_core": time.time() - t0}

@@ -347,8 +347,10 @@ def test_gmres_validate_rejects_reference_asserts(ctx):
         _run_gmres(ctx, A, b, maxiter=1000, max_krylov_dim=101, restart=True)
 
 
-@pytest.mark.parametrize("wl", ["convdiff3d-24", "diffusion3d-20"])
+@pytest.mark.parametrize("wl", ["convdiff3d-24", "diffusion3d-20", "convdiff3d-13", "convdiff3d-7"])
 def test_gmres_cgs2_vs_oracle(ctx, wl):
+    # odd sizes: a last tile of the staged passes that ends inside an element
+    # pair (FP32) and a problem smaller than one tile
     A, b = P.workload(wl)
     r = O.solve("gmres", A, b, maxiter=5000, rtol=1e-8, krylov_dim=30)
     info, x, _ = _run_gmres(ctx, A, b, maxiter=5000, rtol=1e-8, max_krylov_dim=30, restart=True)
@@ -372,7 +374,7 @@ def test_mixed_bicgstab(ctx, wl):
 
 
 @pytest.mark.parametrize("ortho", ["auto", "mgs"])
-@pytest.mark.parametrize("wl", ["convdiff3d-24", "diffusion3d-20"])
+@pytest.mark.parametrize("wl", ["convdiff3d-24", "diffusion3d-20", "convdiff3d-13", "convdiff3d-7"])
 def test_mixed_gmres(ctx, wl, ortho):
     """FP32 Arnoldi cycles re-anchored on the FP64 residual at every restart:
     converges on the FP64 residual with the FP64 iteration count +- a few."""

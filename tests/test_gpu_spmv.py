@@ -293,3 +293,77 @@ def test_matrix_market_operator_on_device(ctx):
     info = slv(vb, vs)
     assert info.status == ref.status and abs(info.iters - ref.iters) <= 2
     assert np.linalg.norm(vs.numpy() - ref.x) <= 1e-10 * np.linalg.norm(ref.x)
+
+
+@pytest.mark.parametrize("lanes", [0, 4, 8, 16, 32])
+def test_vector_spmv_schedules_on_power_law_rows(ctx, lanes):
+    """Irregular rows (16 to 2048 nonzeros, random columns): every column-id
+    schedule in FMA mode within the FMA bound of the reference's row sums,
+    the same bits on every run; EXACT mode stays the reference's serial
+    order whatever the schedule."""
+    A = P.powerlaw(20000)
+    x = P.uniform(11, A.ncols)
+    dA = fs.CSR(ctx, A)
+    assert dA.index_coding() == 0
+    dA.set_lanes(lanes)
+    vx, vy = fs.Vector(ctx, x), fs.Vector(ctx, A.nrows)
+    ref = O.spmv(A, x)
+    dA.apply(vx, vy)
+    y1 = vy.numpy()
+    import scipy.sparse as sp
+
+    def csr(vals):
+        # duplicate column ids stay separate entries (no scipy cast, which
+        # would sum them first)
+        return sp.csr_matrix((vals, A.col, A.rowptr), shape=(A.nrows, A.ncols))
+
+    nnz_row = np.diff(A.rowptr)
+    bound = 2 * nnz_row * np.finfo(np.float64).eps * (csr(np.abs(A.val)) @ np.abs(x))
+    assert (np.abs(y1 - ref) <= bound).all()
+    dA.apply(vx, vy)
+    assert np.array_equal(vy.numpy(), y1)
+    dA.apply(vx, vy, exact=True)
+    assert np.array_equal(vy.numpy(), ref)
+    # FP32 values
+    x32 = x.astype(np.float32)
+    dA.set_lanes(lanes, np.float32)
+    vx32, vy32 = fs.Vector(ctx, x32, "f32"), fs.Vector(ctx, A.nrows, "f32")
+    dA.apply(vx32, vy32)
+    v32 = A.val.astype(np.float32).astype(np.float64)
+    ref32 = csr(v32) @ x32.astype(np.float64)
+    b32 = 2 * nnz_row * np.finfo(np.float32).eps * (csr(np.abs(v32)) @ np.abs(x32.astype(np.float64)))
+    assert (np.abs(vy32.numpy() - ref32) <= b32).all()
+
+
+def test_spmv_autotuner_picks_a_schedule(ctx):
+    A = P.powerlaw(50000)
+    dA = fs.CSR(ctx, A)
+    for dt in (np.float64, np.float32):
+        lanes = dA.tune(dt)
+        assert lanes in (0, 4, 8, 16, 32)
+    with pytest.raises(fs.api._lib.FsError):
+        dA.set_lanes(3)
+    # stencil operators keep their row formats
+    B, _ = P.workload("poisson2d-64")
+    assert fs.CSR(ctx, B).tune() == 0
+
+
+@pytest.mark.parametrize("lanes", [0, 8, 32])
+@pytest.mark.parametrize("method", ["bicgstab", "gmres"])
+def test_solvers_over_vector_spmv(ctx, lanes, method):
+    """The fused solver epilogues on the vector kernel: BiCGSTAB and GMRES(30)
+    on a diagonally dominant power-law matrix, iterations within 2 of the
+    oracle's, true residual at the tolerance."""
+    A, b = P.workload("powerlaw-20000")
+    dA = fs.CSR(ctx, A)
+    dA.set_lanes(lanes)
+    ns = getattr(fs, method)
+    kw = dict(max_krylov_dim=30, restart=True) if method == "gmres" else {}
+    vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
+    slv = ns.solver(ns.settings(maxiter=500, rtol=1e-10, use_zero_guess=True, **kw))(dA, fs.op.jacobi)
+    info = slv(vb, vx)
+    ref = O.solve(method, A, b, maxiter=500, rtol=1e-10)
+    assert info.status == ref.status == "converged_rtol"
+    assert abs(info.iters - ref.iters) <= 2
+    x = vx.numpy()
+    assert np.linalg.norm(b - A.to_scipy() @ x) <= 1.01e-10 * np.linalg.norm(b)
