@@ -364,10 +364,11 @@ def run_spmv_only(args):
             npdt = np.float64 if dt == "f64" else np.float32
             nbytes = spmv_bytes(n, nnz, vb, 0, dA.nblk())
             sched = {}
-            for lanes in (0, 4, 8, 16, 32):
+            for lanes in (0, 4, 8, 16, 32, 1):
                 dA.set_lanes(lanes, npdt)
                 ms = spmv_events_ms(fs, ctx, dA, n, dt, reps=max(1, args.steps))
-                sched["row_per_thread" if lanes == 0 else f"lanes_{lanes}"] = {
+                name = {0: "row_per_thread", 1: "binned_by_length"}.get(lanes, f"lanes_{lanes}")
+                sched[name] = {
                     "ms": ms, "frac": nbytes / (ms * 1e-3) / 1e9 / peak}
             dA.set_lanes(-1, npdt)
             tuned = dA.tune(npdt)
@@ -418,6 +419,10 @@ def run_suite(args):
 
     def want(k):
         return only is None or k in only
+
+    def asked(k):
+        # profiling parts: only when named
+        return only is not None and k in only
 
     def krylov(tag, A, b, cases):
         dA = fs.CSR(ctx, A)
@@ -521,6 +526,27 @@ def run_suite(args):
                          "s_per_iteration": sec / max(info.iters, 1),
                          "true_relres": _relres(S, b, vx.numpy())}
         out["cg-variants-diffusion3d-256"] = res
+    if asked("gmres-profile"):
+        # profiling: two restart cycles (60 steps) of the mixed GMRES(30) on
+        # the 192^3 convection-diffusion system
+        A, b = P.workload("convdiff3d-192")
+        dA = fs.CSR(ctx, A)
+        vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
+        slv = fs.mixed_gmres.solver(fs.mixed_gmres.settings(maxiter=60, rtol=1e-8, max_krylov_dim=30,
+                                                            restart=True))(dA, fs.op.jacobi)
+        info = slv(vb, vx)
+        ctx.sync()
+        out["convdiff3d-192-mixed-gmres-60"] = {"iters": info.iters, "status": info.status}
+    if asked("batched-profile"):
+        # profiling: 64 systems of side 96..160 in one launch, cluster 2 x 512
+        # threads (no autotuning launches)
+        A, off, b, _ = P.batch_diffusion2d(nsys=64, side_lo=96, side_hi=160)
+        dA = fs.CSR(ctx, A)
+        vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
+        infos = fs.batch_cg(dA, off, vb, vx, maxiter=20000, rtol=1e-8, cluster=2, threads=512)
+        ctx.sync()
+        out["batch64-diffusion2d-96-160"] = {"rows": A.nrows, "nnz": A.nnz,
+                                             "iters_sum": int(sum(i.iters for i in infos))}
     if want("blockcg-mixed"):
         # the mixed block solve alone (profiling): 16 right-hand sides of the
         # 96^3 Laplacian, one warm-up and one timed solve

@@ -362,8 +362,8 @@ class CSR:
 
     def tune(self, dtype=np.float64) -> int:
         """Time the column-id SpMV schedules for values of `dtype` and keep
-        the fastest: 0 (one thread per row) or 4 / 8 / 16 / 32 lanes per
-        row.  Returns the choice."""
+        the fastest: 0 (one thread per row), 4 / 8 / 16 / 32 lanes per row,
+        or 1 (lanes per row by row-length class).  Returns the choice."""
         lanes = C.c_int()
         check(lib().fs_csr_tune(self.h, _dtype_code(dtype), C.byref(lanes)), self.ctx.h, "fs_csr_tune")
         return lanes.value
@@ -705,7 +705,7 @@ def batch_cg(A: CSR, offsets, b: Vector, x: Vector, maxiter: int, rtol: float,
     block cluster per system; returns one :class:`SolveInfo` per system.
     ``cluster``/``threads`` = 0 lets the autotuner choose; ``fp64_head``: FP64
     iterations until each system's residual is below that fraction of its
-    ||b|| (None: the library default, 1e-2; 0: FP32 from the start)."""
+    ||b|| (None: the library default, 3e-3; 0: FP32 from the start)."""
     off = np.ascontiguousarray(offsets, dtype=np.int64)
     nsys = off.size - 1
     st = _settings(_lib.CG_MIXED, maxiter, rtol, 0.0, use_zero_guess, inner_rtol=delta)

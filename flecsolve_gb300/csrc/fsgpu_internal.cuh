@@ -116,8 +116,14 @@ struct Csr {
 	bool sym64_valid = false, sym32_valid = false;
 	int sym_state = -1;             // -1 not checked since the values changed, 0 no, 1 yes
 	// FMA-mode column-id SpMV kernel per value type (0 FP64, 1 FP32): 0 row
-	// blocks, L lanes per row of the vector kernel, -1 not tuned yet
+	// blocks, L = 4..32 lanes per row of the vector kernel, 1 the vector
+	// kernel with rows binned by length, -1 not tuned yet
 	int vec_lanes[2] = {-1, -1};
+	// the binned schedule (built on first use): row ids grouped by length
+	// class, one warp task {first slot, lanes | rows << 8} per 32 / lanes rows
+	int *bin_rows = nullptr;
+	int2 *bin_task = nullptr;
+	int bin_ntask = 0;
 	double *dinv = nullptr;    // 1 / a_ii, built on first use
 	float *dinv32 = nullptr;
 	bool dinv_valid = false;

@@ -1984,7 +1984,7 @@ FS_API int fs_krylov_settings_default(fs_krylov_settings *s) {
 	s->refine = FS_REFINE_RELIABLE;
 	s->inner_rtol = 0.0;  // per-method default
 	s->max_outer = 64;
-	s->fp64_head = 1e-2;
+	s->fp64_head = 3e-3;
 	return FS_OK;
 }
 

@@ -536,11 +536,53 @@ static int time_lanes(Ctx *ctx, const Csr *A, const V *vals, const V *x, V *y, i
 	return rc;
 }
 
-// Time the row-block kernel and the vector kernel with 4, 8, 16 and 32
-// lanes per row on A's values of one type; *best = the fastest
+// The binned schedule of the vector SpMV: rows by length class (<= 8, <= 32,
+// <= 128 nonzeros, longer: 4, 8, 16, 32 lanes), longest class first, each
+// class in row order, cut into warp tasks of 32 / lanes rows
+static int ensure_bins(Csr *A) {
+	if (A->bin_task || A->nrows == 0)
+		return FS_OK;
+	const std::vector<int> &rp = A->h_rowptr;
+	std::vector<int> cls[4];
+	for (int64_t r = 0; r < A->nrows; ++r) {
+		const int len = rp[r + 1] - rp[r];
+		cls[len <= 8 ? 0 : len <= 32 ? 1 : len <= 128 ? 2 : 3].push_back((int)r);
+	}
+	std::vector<int> rows;
+	std::vector<int2> task;
+	rows.reserve(A->nrows);
+	for (int c = 3; c >= 0; --c) {
+		const int L = 4 << c, per = 32 / L;
+		const int base = (int)rows.size();
+		for (size_t i = 0; i < cls[c].size(); i += per)
+			task.push_back(make_int2(base + (int)i, L | (int)(std::min<size_t>(per, cls[c].size() - i) << 8)));
+		rows.insert(rows.end(), cls[c].begin(), cls[c].end());
+	}
+	if (cudaMalloc(&A->bin_rows, rows.size() * sizeof(int)) != cudaSuccess ||
+	    cudaMalloc(&A->bin_task, task.size() * sizeof(int2)) != cudaSuccess ||
+	    cudaMemcpy(A->bin_rows, rows.data(), rows.size() * sizeof(int), cudaMemcpyHostToDevice) !=
+	        cudaSuccess ||
+	    cudaMemcpy(A->bin_task, task.data(), task.size() * sizeof(int2), cudaMemcpyHostToDevice) !=
+	        cudaSuccess ||
+	    fence_setup_copies() != cudaSuccess) {
+		cudaGetLastError();
+		cudaFree(A->bin_rows);
+		cudaFree(A->bin_task);
+		A->bin_rows = nullptr;
+		A->bin_task = nullptr;
+		return set_err(A->ctx, FS_ERR_OUT_OF_MEMORY, "spmv: binned schedule allocation failed");
+	}
+	A->bin_ntask = (int)task.size();
+	return FS_OK;
+}
+
+// Time the row-block kernel, the vector kernel with 4, 8, 16 and 32 lanes
+// per row and the binned vector kernel on A's values of one type; *best =
+// the fastest
 static int tune_lanes(Ctx *ctx, Csr *A, bool f32, int *best) {
 	if (f32)
 		FS_TRY(ensure_val32(A));
+	FS_TRY(ensure_bins(A));
 	const size_t vb = f32 ? 4 : 8;
 	void *x = nullptr, *y = nullptr;
 	if (cudaMalloc(&x, (size_t)(A->ncols + 32) * vb) != cudaSuccess ||
@@ -555,7 +597,7 @@ static int tune_lanes(Ctx *ctx, Csr *A, bool f32, int *best) {
 	             : FS_ERR_CUDA;
 	float best_ms = 0.f;
 	*best = 0;
-	for (int lanes : {0, 4, 8, 16, 32}) {
+	for (int lanes : {0, 4, 8, 16, 32, 1}) {
 		if (rc != FS_OK)
 			break;
 		float ms = 0.f;
@@ -625,9 +667,12 @@ FS_API int fs_csr_set_lanes(fs_csr h, int dtype, int lanes) {
 	FS_TRY(reject_matrix_free(A, "fs_csr_set_lanes"));
 	if (dtype != FS_F64 && dtype != FS_F32)
 		return set_err(A->ctx, FS_ERR_INVALID_ARG, "fs_csr_set_lanes: dtype must be FS_F64 or FS_F32");
-	if (lanes != -1 && lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+	if (lanes != -1 && lanes != 0 && lanes != 1 && lanes != 4 && lanes != 8 && lanes != 16 &&
+	    lanes != 32)
 		return set_err(A->ctx, FS_ERR_INVALID_ARG,
-		               "fs_csr_set_lanes: lanes must be -1, 0, 4, 8, 16 or 32");
+		               "fs_csr_set_lanes: lanes must be -1, 0, 1, 4, 8, 16 or 32");
+	if (lanes == 1 && !A->pid)
+		FS_TRY(ensure_bins(A));
 	A->vec_lanes[dtype == FS_F32 ? 1 : 0] = lanes;
 	return FS_OK;
 }
@@ -842,7 +887,7 @@ FS_API int fs_csr_destroy(fs_csr h) {
 	                (void *)A->pid, (void *)A->ptab, (void *)A->pwb, (void *)A->plen, (void *)A->pslot, (void *)A->pinv,
 	                (void *)A->sofs, (void *)A->stab, (void *)A->sym64, (void *)A->sym32, (void *)A->sym_flag,
 	                (void *)A->t_colptr, (void *)A->t_row, (void *)A->t_perm, (void *)A->t_val,
-	                (void *)A->t_blk, (void *)A->t_blkinfo})
+	                (void *)A->t_blk, (void *)A->t_blkinfo, (void *)A->bin_rows, (void *)A->bin_task})
 		if (p)
 			cudaFree(p);
 	destroy_fvm(A->fvm);

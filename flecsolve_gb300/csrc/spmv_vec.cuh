@@ -12,9 +12,11 @@
 // the warps stride over the rows in a fixed order, so every row has one owner
 // and the fused reductions of the epilogue are deterministic.
 //
-// The row-block kernel sums each row in one thread (the reference's order,
-// the only form of EXACT mode).  With long rows its blocks hold few rows, so
-// most of its threads idle while one thread walks a row gather by gather.
+// A fixed L serves rows of one length well; the binned schedule below serves
+// rows of many lengths.  The row-block kernel sums each row in one thread
+// (the reference's order, the only form of EXACT mode); with long rows its
+// blocks hold few rows, so most of its threads idle while one thread walks a
+// row gather by gather.
 #pragma once
 
 namespace fsg {
@@ -85,6 +87,97 @@ spmv_vec_kernel(const int *__restrict__ rowptr, const int *__restrict__ col,
 	}
 }
 
+// Binned schedule: the rows grouped by length class (at most 8, 32, 128
+// nonzeros, longer) into warp tasks of 32 / L rows of one class, L = 4, 8,
+// 16, 32 lanes per row (a long row has a whole warp, short ones share it), so
+// the rows of a warp finish together; tasks are taken in a fixed order.
+// rows: row ids by class; task: {first slot in rows, L | (rows << 8)}.
+template<class V, bool SCALE, class Epi>
+__global__ void __launch_bounds__(kVecThreads)
+spmv_bin_kernel(const int *__restrict__ rowptr, const int *__restrict__ col,
+                const V *__restrict__ val, const int *__restrict__ rows,
+                const int2 *__restrict__ task, int ntask, const V *__restrict__ x,
+                const V *__restrict__ dscale, Epi epi) {
+	constexpr int NV = Epi::NV;
+	__shared__ double red[128];
+	pdl_wait();
+	pdl_trigger();
+	if (epi.skip())
+		return;
+	Acc<V, NV> acc;
+	acc.init();
+	const int lane = threadIdx.x & 31;
+	const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+	const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+	for (int t = warp; t < ntask; t += nwarps) {
+		const int2 d = __ldg(task + t);
+		const int L = d.y & 0xff, cnt = d.y >> 8;  // the same for the whole warp
+		const int grp = lane / L, sub = lane & (L - 1);
+		int r = -1;
+		V s = V(0);
+		if (grp < cnt) {
+			r = __ldg(rows + d.x + grp);
+			const int k0 = __ldg(rowptr + r), k1 = __ldg(rowptr + r + 1);
+			int k = k0 + sub;
+			for (; k + 3 * L < k1; k += 4 * L) {
+				V a[4], xv[4];
+				int c[4];
+#pragma unroll
+				for (int j = 0; j < 4; ++j) {
+					a[j] = __ldg(val + k + j * L);
+					c[j] = __ldg(col + k + j * L);
+				}
+#pragma unroll
+				for (int j = 0; j < 4; ++j)
+					xv[j] = xg<V, SCALE>(x, dscale, c[j]);
+#pragma unroll
+				for (int j = 0; j < 4; ++j)
+					s = fma(a[j], xv[j], s);
+			}
+			for (; k < k1; k += L)
+				s = fma(__ldg(val + k), xg<V, SCALE>(x, dscale, __ldg(col + k)), s);
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1)
+			if (o < L)
+				s += __shfl_xor_sync(0xffffffffu, s, o);
+		if (sub == 0 && r >= 0)
+			epi.row(r, s, acc);
+	}
+	if constexpr (NV > 0) {
+		acc.to_part(epi.part, red);
+		if (last_block(epi.counter)) {
+			double sums[NV];
+			sum_partials<NV>(epi.part, gridDim.x, sums, red);
+			if (threadIdx.x == 0) {
+				epi.finish(sums);
+				*epi.counter = 0;
+			}
+		}
+	}
+}
+
+template<class V, bool SCALE, class Epi>
+static inline int launch_spmv_bin(Ctx *ctx, const Csr *A, const V *vals, const V *x,
+                                  const V *dscale, const Epi &epi) {
+	static int per_sm = 0;  // resident CTAs per SM of this instantiation
+	auto kern = spmv_bin_kernel<V, SCALE, Epi>;
+	if (per_sm == 0) {
+		int nb = 0;
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kVecThreads, 0) != cudaSuccess ||
+		    nb < 1)
+			nb = 1;
+		per_sm = nb;
+	}
+	constexpr int warps_per_cta = kVecThreads / 32;
+	const int need = (A->bin_ntask + warps_per_cta - 1) / warps_per_cta;
+	const int grid = std::max(1, std::min(need, ctx->sms * std::min(per_sm, 8)));
+	return check_launch_rc(ctx, launch_pdl(ctx->stream, kern, grid, kVecThreads, 0, A->rowptr,
+	                                       A->col, vals, (const int *)A->bin_rows,
+	                                       (const int2 *)A->bin_task, A->bin_ntask, x, dscale, epi),
+	                       "spmv (vector, rows binned by length)");
+}
+
 template<class V, int L, bool SCALE, class Epi>
 static inline int launch_spmv_vec_l(Ctx *ctx, const Csr *A, const V *vals, const V *x,
                                     const V *dscale, const Epi &epi) {
@@ -109,6 +202,7 @@ template<class V, bool SCALE, class Epi>
 static inline int launch_spmv_vec(Ctx *ctx, const Csr *A, const V *vals, const V *x,
                                   const V *dscale, const Epi &epi, int lanes) {
 	switch (lanes) {
+	case 1: return launch_spmv_bin<V, SCALE, Epi>(ctx, A, vals, x, dscale, epi);
 	case 4: return launch_spmv_vec_l<V, 4, SCALE, Epi>(ctx, A, vals, x, dscale, epi);
 	case 8: return launch_spmv_vec_l<V, 8, SCALE, Epi>(ctx, A, vals, x, dscale, epi);
 	case 16: return launch_spmv_vec_l<V, 16, SCALE, Epi>(ctx, A, vals, x, dscale, epi);

@@ -186,7 +186,8 @@ FS_API int fs_csr_row_blocks(fs_csr A, int64_t *nblk);
 /* Kernel of the FMA-mode column-id SpMV for values of `dtype` (no
  * counterpart in the reference; a schedule choice of this library): 0 the
  * row-block kernel (one thread per row), 4 / 8 / 16 / 32 the vector kernel
- * with that many lanes per row.  Matrices with row patterns (stencil
+ * with that many lanes per row, 1 the vector kernel with the rows binned by
+ * length (4 to 32 lanes per row by class).  Matrices with row patterns (stencil
  * operators, formats 1-3) always keep the row formats; EXACT mode always
  * sums each row in one thread, in the reference's order.
  * fs_csr_tune times every candidate on the context's stream (synchronising
@@ -387,13 +388,14 @@ typedef struct {
 	int max_outer;       /* restart: maximum refinement steps            */
 	/* reliable mixed CG and batched CG: FP64 iterations until the residual
 	   is below fp64_head * ||b||, then FP32 recurrences with FP64
-	   replacement for the rest of the same Krylov process (default 1e-2;
+	   replacement for the rest of the same Krylov process (default 3e-3;
 	   0 = FP32 from the first iteration).  The solution's large components
 	   form in the first decades of residual reduction.  Computed in FP32,
-	   they cost the iterates orthogonality (up to 13 % more iterations on
-	   2-D log-normal diffusion systems of 256^2) and put the result ~2e-8
-	   from the FP64 solve's iterate at 256^3 (3e-3: 4e-9); the default head
-	   gives the FP64 iteration count on every system tested. */
+	   they cost the iterates orthogonality (up to 118 more iterations than
+	   FP64 on 2-D log-normal diffusion systems of 256^2; 90 with a head of
+	   1e-2) and put the result 1.8e-8 from the FP64 solve's iterate at
+	   256^3 (1e-2: 1.2e-8).  The default head gives 4e-9 there and the FP64
+	   iteration count within 2 on all 512 batched systems. */
 	double fp64_head;
 } fs_krylov_settings;
 

@@ -20,8 +20,8 @@ Bars:
   summation orders (+-2 beyond it); forward error on the sampled rows,
   against a tight FP64 solve, within 2x the largest of the reference's own
   runs under the three summation orders.
-* Batched (512 systems, the default FP64 head to 1e-2 ||b||): every system
-  converged with true residual <= rtol, iterations within +-3 of the
+* Batched (512 systems, the default FP64 head to 3e-3 ||b||): every system
+  converged with true residual <= rtol, iterations within +-2 of the
   reference's CG on that system alone.
 * Block CG (128^3, 16 right-hand sides): every column's true residual <=
   rtol, and its forward error within 2x that of the single-vector FP64 CG.
@@ -192,7 +192,7 @@ def test_batched_512_systems_against_reference(ctx):
         assert inf.status == gold["status"][k] == "converged_rtol", (k, inf)
         rr = np.linalg.norm(b[lo:hi] - S[lo:hi] @ x) / np.linalg.norm(b[lo:hi])
         assert rr <= 1e-8, (k, rr)
-        assert abs(inf.iters - gold["iters"][k]) <= 3, (k, inf.iters, gold["iters"][k])
+        assert abs(inf.iters - gold["iters"][k]) <= ITER_TOL, (k, inf.iters, gold["iters"][k])
 
 
 @pytest.mark.parametrize("mixed", [False, True])

@@ -295,7 +295,7 @@ def test_matrix_market_operator_on_device(ctx):
     assert np.linalg.norm(vs.numpy() - ref.x) <= 1e-10 * np.linalg.norm(ref.x)
 
 
-@pytest.mark.parametrize("lanes", [0, 4, 8, 16, 32])
+@pytest.mark.parametrize("lanes", [0, 1, 4, 8, 16, 32])
 def test_vector_spmv_schedules_on_power_law_rows(ctx, lanes):
     """Irregular rows (16 to 2048 nonzeros, random columns): every column-id
     schedule in FMA mode within the FMA bound of the reference's row sums,
@@ -340,7 +340,7 @@ def test_spmv_autotuner_picks_a_schedule(ctx):
     dA = fs.CSR(ctx, A)
     for dt in (np.float64, np.float32):
         lanes = dA.tune(dt)
-        assert lanes in (0, 4, 8, 16, 32)
+        assert lanes in (0, 1, 4, 8, 16, 32)
     with pytest.raises(fs.api._lib.FsError):
         dA.set_lanes(3)
     # stencil operators keep their row formats
@@ -348,7 +348,7 @@ def test_spmv_autotuner_picks_a_schedule(ctx):
     assert fs.CSR(ctx, B).tune() == 0
 
 
-@pytest.mark.parametrize("lanes", [0, 8, 32])
+@pytest.mark.parametrize("lanes", [0, 1, 8, 32])
 @pytest.mark.parametrize("method", ["bicgstab", "gmres"])
 def test_solvers_over_vector_spmv(ctx, lanes, method):
     """The fused solver epilogues on the vector kernel: BiCGSTAB and GMRES(30)
