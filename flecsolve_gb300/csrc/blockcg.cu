@@ -10,10 +10,12 @@
 //   alpha = M^-1 G
 //   X += P alpha,  R -= Q alpha,  Z = D^-1 R,  G' = Z^T R, ||R_j||
 //   beta = G^-1 G',  P = Z + P beta,  G = G'
-// Gram products: each CTA walks 16-row tiles; thread (i, j) of the 256 sums
-// P[r][i] Q[r][j] over the tile's rows, adds that tile sum to its running
-// sum, and the per-CTA sums are folded in CTA order by the last CTA
-// (deterministic).
+// Gram products: each CTA walks 64-row steps; thread (g, a, b) of the 256
+// accumulates the 4 x 4 block [4a, 4a+4) x [4b, 4b+4) over the step's rows
+// g, g + 16, g + 32, g + 48 (register blocking: 16-byte loads, 16 FMAs per
+// pair of loads), adds that step sum to its running sum, and the per-CTA
+// sums are folded in a fixed two-level order (groups of 32 CTAs, then the
+// groups), so the result is deterministic for a given grid.
 //
 // Two precisions share the kernels (template V):
 //  * FP64 (fs_block_cg_solve): every vector and the matrix in FP64.  On this

@@ -119,6 +119,9 @@ struct Csr {
 	// blocks, L = 4..32 lanes per row of the vector kernel, 1 the vector
 	// kernel with rows binned by length, -1 not tuned yet
 	int vec_lanes[2] = {-1, -1};
+	// a transposed view (CSC arrays of another CSR, no host offsets): its
+	// column-id schedule follows the mean row length, untimed
+	bool view = false;
 	// the binned schedule (built on first use): row ids grouped by length
 	// class, one warp task {first slot, lanes | rows << 8} per 32 / lanes rows
 	int *bin_rows = nullptr;

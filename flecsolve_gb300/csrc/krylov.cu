@@ -2244,6 +2244,7 @@ FS_API int fs_krylov_apply_transpose(fs_solver h, fs_vec bh, fs_vec xh, fs_solve
 	if (!s->AT) {
 		s->AT = new Csr();
 		s->AT->ctx = A->ctx;
+		s->AT->view = true;
 	}
 	Csr *T = s->AT;
 	T->nrows = A->ncols;

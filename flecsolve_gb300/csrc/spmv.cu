@@ -457,6 +457,7 @@ int transpose_spmv(Csr *A, const double *x, double *y) {
 	FS_TRY(ensure_transpose(A));
 	Csr T;  // a view sharing the CSC arrays
 	T.ctx = A->ctx;
+	T.view = true;
 	T.nrows = A->ncols;
 	T.ncols = A->nrows;
 	T.nnz = A->nnz;
@@ -543,6 +544,8 @@ static int ensure_bins(Csr *A) {
 	if (A->bin_task || A->nrows == 0)
 		return FS_OK;
 	const std::vector<int> &rp = A->h_rowptr;
+	if ((int64_t)rp.size() != A->nrows + 1)
+		return set_err(A->ctx, FS_ERR_INVALID_ARG, "spmv: no host row offsets for the binned schedule");
 	std::vector<int> cls[4];
 	for (int64_t r = 0; r < A->nrows; ++r) {
 		const int len = rp[r + 1] - rp[r];
@@ -618,6 +621,8 @@ int spmv_lanes(Ctx *ctx, const Csr *A, bool f32) {
 	// stencil operators keep the row formats (all of them give the same bits)
 	if (A->pid || A->nrows == 0 || stores_no_rows(A))
 		return 0;
+	if (A->view)
+		return lanes_from_mean(A);
 	Csr *M = const_cast<Csr *>(A);
 	int &lanes = M->vec_lanes[f32 ? 1 : 0];
 	if (lanes >= 0)
