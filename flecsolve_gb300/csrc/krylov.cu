@@ -444,6 +444,12 @@ k_rel_finish(int64_t n, const float *__restrict__ r, const float *__restrict__ d
 
 // The FP64 head of a reliable-update CG has reached its tolerance: the same
 // Krylov process continues at the final tolerance with FP32 recurrences.
+// After k >= 1 head iterations the next direction is z_k + beta_k p_{k-1}
+// (beta_k from the replaced residual's rho over the head's last rho).  When
+// the initial residual was already below the head's tolerance (k = 0, a
+// warm start), the start kernel's p = z_0 is the first direction itself:
+// beta must be 0 (rho_old = inf), or the direction would be scaled and the
+// next ones would lose conjugacy.
 __global__ void k_head_switch(KState *st, double rtol) {
 	st->rtol = rtol;
 	st->tol = rtol * st->bnorm;
@@ -452,6 +458,8 @@ __global__ void k_head_switch(KState *st, double rtol) {
 	st->info_iters = 0;
 	st->flags = 0;
 	st->alpha_x = 0.0;
+	if (st->iter == 0)
+		st->rho_old = INFINITY;
 }
 
 __global__ void k_to_f32(int64_t n, const double *__restrict__ s, float *__restrict__ d) {

@@ -6,9 +6,10 @@
 // (L = 4, 8, 16 or 32, chosen per matrix and precision by the autotuner of
 // spmv.cu, or from the mean row length while a graph is being captured).
 // The lanes stride over the row's nonzeros -- value and column loads
-// coalesced across the group, four nonzeros per lane in flight, the x
-// gathers independent of each other -- and a fixed xor tree over the group
-// adds the lanes' sums.  A warp takes 32 / L consecutive rows per step and
+// coalesced across the group and marked streaming (read once: evicted first,
+// so that x, gathered at random columns, keeps its place in L2), four
+// nonzeros per lane in flight, the x gathers independent of each other --
+// and a fixed xor tree over the group adds the lanes' sums.  A warp takes 32 / L consecutive rows per step and
 // the warps stride over the rows in a fixed order, so every row has one owner
 // and the fused reductions of the epilogue are deterministic.
 //
@@ -54,8 +55,8 @@ spmv_vec_kernel(const int *__restrict__ rowptr, const int *__restrict__ col,
 				int c[4];
 #pragma unroll
 				for (int j = 0; j < 4; ++j) {
-					a[j] = __ldg(val + k + j * L);
-					c[j] = __ldg(col + k + j * L);
+					a[j] = __ldcs(val + k + j * L);
+					c[j] = __ldcs(col + k + j * L);
 				}
 #pragma unroll
 				for (int j = 0; j < 4; ++j)
@@ -65,7 +66,7 @@ spmv_vec_kernel(const int *__restrict__ rowptr, const int *__restrict__ col,
 					s = fma(a[j], xv[j], s);
 			}
 			for (; k < k1; k += L)
-				s = fma(__ldg(val + k), xg<V, SCALE>(x, dscale, __ldg(col + k)), s);
+				s = fma(__ldcs(val + k), xg<V, SCALE>(x, dscale, __ldcs(col + k)), s);
 		}
 		// every lane of the warp reaches the tree (rows past n add zeros)
 #pragma unroll
@@ -124,8 +125,8 @@ spmv_bin_kernel(const int *__restrict__ rowptr, const int *__restrict__ col,
 				int c[4];
 #pragma unroll
 				for (int j = 0; j < 4; ++j) {
-					a[j] = __ldg(val + k + j * L);
-					c[j] = __ldg(col + k + j * L);
+					a[j] = __ldcs(val + k + j * L);
+					c[j] = __ldcs(col + k + j * L);
 				}
 #pragma unroll
 				for (int j = 0; j < 4; ++j)
@@ -135,7 +136,7 @@ spmv_bin_kernel(const int *__restrict__ rowptr, const int *__restrict__ col,
 					s = fma(a[j], xv[j], s);
 			}
 			for (; k < k1; k += L)
-				s = fma(__ldg(val + k), xg<V, SCALE>(x, dscale, __ldg(col + k)), s);
+				s = fma(__ldcs(val + k), xg<V, SCALE>(x, dscale, __ldcs(col + k)), s);
 		}
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1)

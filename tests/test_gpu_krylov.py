@@ -214,6 +214,23 @@ def test_mixed_cg_refinement(ctx, wl):
     assert _rel(x3, xs) <= X_RTOL_MIXED
 
 
+@pytest.mark.parametrize("eps", [1e-2, 1e-4, 1e-6])
+@pytest.mark.parametrize("head", [0.0, 3e-3, 1e-2])
+def test_mixed_cg_warm_start(ctx, eps, head):
+    """A guess near the solution (initial residual above, near or below the
+    FP64 head's tolerance): the mixed CG takes the oracle's FP64 CG count
+    +-2 from the same guess, whether the head runs or not."""
+    A, b = P.workload("diffusion3d-24")
+    xs = O.solve("cg", A, b, maxiter=20000, rtol=1e-13).x
+    x0 = xs + eps * P.uniform(5, A.nrows)
+    ref = O.solve("cg", A, b, x0, maxiter=20000, rtol=1e-8, use_zero_guess=False)
+    info, x, _ = _run(ctx, fs.mixed_cg, A, b, x0=x0, maxiter=20000, rtol=1e-8,
+                      use_zero_guess=False, fp64_head=head)
+    assert info.status == ref.status == "converged_rtol"
+    assert abs(info.iters - ref.iters) <= ITER_TOL, (info.iters, ref.iters)
+    assert _true_relres(A, b, x) <= 1e-8
+
+
 @pytest.mark.parametrize("wl", ["diffusion3d-40", "poisson2d-127", "diffusion3d-23"])
 def test_mixed_cg_index_formats(ctx, wl):
     """The mixed CG on a stencil matrix with each SpMV format (symmetric
