@@ -467,7 +467,7 @@ def run_suite(args):
         dA = fs.CSR(ctx, A)
         vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
         fs.batch_cg(dA, off, vb, vx, maxiter=20000, rtol=1e-8)  # autotune + warm
-        cl, th = fs.batch_tuning(dA, off)
+        cl, th, nbig = fs.batch_schedule(dA, off)
         ctx.sync()
         ctx.record(6)
         infos = fs.batch_cg(dA, off, vb, vx, maxiter=20000, rtol=1e-8)
@@ -500,7 +500,8 @@ def run_suite(args):
         peak, peak_kind = _peaks()
         out["batch512-diffusion2d"] = {
             "systems": len(infos), "rows": A.nrows, "nnz": A.nnz, "s": t, "cluster": cl,
-            "threads": th, "all_converged": all(i.status == "converged_rtol" for i in infos),
+            "threads": th, "systems_owning_a_cluster": nbig,
+            "all_converged": all(i.status == "converged_rtol" for i in infos),
             "max_true_relres": rr, "iters_min": min(its), "iters_max": max(its),
             "iters_sum": int(sum(its)), "row_iterations": rows_it,
             "roofline": {"bytes_per_row_iteration": b_row_it,

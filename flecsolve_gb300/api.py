@@ -699,22 +699,29 @@ def _info(i) -> "SolveInfo":
 
 def batch_cg(A: CSR, offsets, b: Vector, x: Vector, maxiter: int, rtol: float,
              use_zero_guess: bool = True, delta: float = 0.0, cluster: int = 0,
-             threads: int = 0, fp64_head: float = None):
+             threads: int = 0, fp64_head: float = None, cluster_systems: int = None):
     """Solve the independent systems on the diagonal blocks of ``A`` (system
     s = rows offsets[s]:offsets[s+1]) in one persistent launch, one thread-
     block cluster per system; returns one :class:`SolveInfo` per system.
     ``cluster``/``threads`` = 0 lets the autotuner choose; ``fp64_head``: FP64
     iterations until each system's residual is below that fraction of its
-    ||b|| (None: the library default, 3e-3; 0: FP32 from the start)."""
+    ||b|| (None: the library default, 3e-3; 0: FP32 from the start).
+    ``cluster_systems`` (with explicit sizes): that many of the largest
+    systems own a cluster, every other system one CTA."""
     off = np.ascontiguousarray(offsets, dtype=np.int64)
     nsys = off.size - 1
     st = _settings(_lib.CG_MIXED, maxiter, rtol, 0.0, use_zero_guess, inner_rtol=delta)
     if fp64_head is not None:
         st.fp64_head = float(fp64_head)
     infos = (_lib.SolveInfo * nsys)()
-    check(lib().fs_batch_cg_solve(A.ctx.h, C.byref(st), A.h, nsys,
-                                  off.ctypes.data_as(C.POINTER(C.c_int64)), b.h, x.h, int(cluster),
-                                  int(threads), infos), A.ctx.h, "fs_batch_cg_solve")
+    offp = off.ctypes.data_as(C.POINTER(C.c_int64))
+    if cluster_systems is None:
+        check(lib().fs_batch_cg_solve(A.ctx.h, C.byref(st), A.h, nsys, offp, b.h, x.h, int(cluster),
+                                      int(threads), infos), A.ctx.h, "fs_batch_cg_solve")
+    else:
+        check(lib().fs_batch_cg_solve_split(A.ctx.h, C.byref(st), A.h, nsys, offp, b.h, x.h,
+                                            int(cluster), int(threads), int(cluster_systems), infos),
+              A.ctx.h, "fs_batch_cg_solve_split")
     return [_info(i) for i in infos]
 
 
@@ -741,6 +748,16 @@ def batch_tuning(A: CSR, offsets):
     check(lib().fs_batch_tuning(A.ctx.h, A.h, off.size - 1, off.ctypes.data_as(C.POINTER(C.c_int64)),
                                 C.byref(c), C.byref(t)), A.ctx.h, "fs_batch_tuning")
     return c.value, t.value
+
+
+def batch_schedule(A: CSR, offsets):
+    """(cluster size, threads per CTA, systems that own a cluster) the
+    autotuner chose for this partition."""
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    c, t, nb = C.c_int(), C.c_int(), C.c_int()
+    check(lib().fs_batch_schedule(A.ctx.h, A.h, off.size - 1, off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                  C.byref(c), C.byref(t), C.byref(nb)), A.ctx.h, "fs_batch_schedule")
+    return c.value, t.value, nb.value
 
 
 class _SolverFactory:

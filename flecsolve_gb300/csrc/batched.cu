@@ -2,12 +2,18 @@
 // launch.
 //
 // The systems are the diagonal blocks of one block-diagonal CSR matrix
-// (rows [off[s], off[s+1]) couple only among themselves).  One thread-block
-// cluster owns one system and runs its whole Jacobi-PCG loop without leaving
-// the kernel: each CTA of the cluster owns a contiguous slice of the
-// system's rows, the per-iteration reductions are folded through distributed
-// shared memory (every CTA reads the cluster's partials in rank order, so all
-// CTAs obtain the same bits), and hardware cluster barriers order the phases.
+// (rows [off[s], off[s+1]) couple only among themselves).  A team owns one
+// system and runs its whole Jacobi-PCG loop without leaving the kernel:
+//  * the `nbig` largest systems each get a whole thread-block cluster: each
+//    CTA owns a contiguous slice of the system's rows, the per-iteration
+//    reductions are folded through distributed shared memory (every CTA
+//    reads the cluster's partials in rank order, so all CTAs obtain the same
+//    bits), and hardware cluster barriers order the phases;
+//  * every other system gets one CTA of a cluster (the cluster's CTAs run
+//    independent systems; block reductions and block barriers only).
+// The split keeps the largest systems -- the batch's critical path: the most
+// rows and the most iterations -- from running on one SM while the small
+// ones finish elsewhere.
 // A system stops on its own convergence test; the rest of the grid keeps
 // working (per-system convergence masks without any host round trip).
 //
@@ -39,6 +45,7 @@ namespace {
 
 struct BatchArgs {
 	int nsys;
+	int nbig;                // systems 0..nbig-1 of `order` own a whole cluster
 	const int *order;        // system processed by cluster c (largest first)
 	const int64_t *off;      // row offsets, nsys + 1
 	const int *rowptr;
@@ -87,19 +94,53 @@ __device__ __forceinline__ void cluster_sum(double (&v)[NV], double *sh_tree,
 		v[k] = t[k];
 }
 
+// sum over the team: the cluster (team > 1) or the CTA alone (team == 1)
+template<int NV>
+__device__ __forceinline__ void team_sum(double (&v)[NV], double *sh_tree, double (*slots)[4],
+                                         int ph, cgrp::cluster_group &cl, int team) {
+	if (team > 1) {
+		cluster_sum<NV>(v, sh_tree, slots, ph, cl);
+		return;
+	}
+	block_sum<NV>(v, sh_tree);
+	if (threadIdx.x == 0)
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			slots[ph & 1][k] = v[k];
+	__syncthreads();
+#pragma unroll
+	for (int k = 0; k < NV; ++k)
+		v[k] = slots[ph & 1][k];
+}
+
+// the team's writes to global memory visible to the whole team
+__device__ __forceinline__ void team_sync(cgrp::cluster_group &cl, int team) {
+	__threadfence();
+	if (team > 1)
+		cl.sync();
+	else
+		__syncthreads();
+}
+
 __global__ void __launch_bounds__(1024)
 k_batch_cg(BatchArgs a) {
 	cgrp::cluster_group cl = cgrp::this_cluster();
 	const int crank = (int)cl.block_rank();
 	const int csize = (int)cl.num_blocks();
 	const int cidx = (int)(blockIdx.x / csize);
-	if (cidx >= a.nsys)
-		return;  // uniform across the cluster
-	const int sys = a.order[cidx];
+	// clusters 0..nbig-1: one system each (team = the cluster); then one
+	// system per CTA (team = 1); the choice is uniform across a cluster
+	const bool whole = cidx < a.nbig;
+	const int team = whole ? csize : 1;
+	const int trank = whole ? crank : 0;
+	const int slot = whole ? cidx : a.nbig + (cidx - a.nbig) * csize + crank;
+	if (slot >= a.nsys)
+		return;  // a CTA of the last cluster with no system (team 1 only)
+	const int sys = a.order[slot];
 	const int64_t R0 = a.off[sys], R1 = a.off[sys + 1];
 	const int64_t nrow = R1 - R0;
-	const int64_t chunk = (nrow + csize - 1) / csize;
-	const int64_t lo = chunk * crank, hi = chunk * (crank + 1);
+	const int64_t chunk = (nrow + team - 1) / team;
+	const int64_t lo = chunk * trank, hi = chunk * (trank + 1);
 	const int64_t r0 = R0 + (lo < nrow ? lo : nrow);
 	const int64_t r1 = R0 + (hi < nrow ? hi : nrow);
 	__shared__ double sh_tree[4 * 32];
@@ -117,7 +158,7 @@ k_batch_cg(BatchArgs a) {
 		v2[1] = fma(a.x[i], a.x[i], v2[1]);
 		a.x32[i] = 0.f;
 	}
-	cluster_sum<2>(v2, sh_tree, slots, ph++, cl);
+	team_sum<2>(v2, sh_tree, slots, ph++, cl, team);
 	double bnorm = sqrt(v2[0]);
 	const double rhs_norm = bnorm;
 	if (bnorm == 0.0)
@@ -139,7 +180,7 @@ k_batch_cg(BatchArgs a) {
 			t[0] = fma(ri, ri, t[0]);
 			t[1] = fma((double)r32, (double)(a.dinv32[i] * r32), t[1]);
 		}
-		cluster_sum<2>(t, sh_tree, slots, ph++, cl);
+		team_sum<2>(t, sh_tree, slots, ph++, cl, team);
 		res = sqrt(t[0]);
 		rz = t[1];
 	};
@@ -164,7 +205,7 @@ k_batch_cg(BatchArgs a) {
 			a.p64[i] = zi;
 			t[0] = fma(ri, zi, t[0]);
 		}
-		cluster_sum<1>(t, sh_tree, slots, ph++, cl);
+		team_sum<1>(t, sh_tree, slots, ph++, cl, team);
 		rho = t[0];
 		double rho_old = rho;
 		bool switch_now = false;
@@ -177,7 +218,7 @@ k_batch_cg(BatchArgs a) {
 				a.w64[i] = sum;
 				q[0] = fma(sum, a.p64[i], q[0]);
 			}
-			cluster_sum<1>(q, sh_tree, slots, ph++, cl);
+			team_sum<1>(q, sh_tree, slots, ph++, cl, team);
 			const double alpha = rho / q[0];
 			double u[2] = {0.0, 0.0};
 			for (int64_t i = r0 + tid; i < r1; i += nt) {
@@ -187,7 +228,7 @@ k_batch_cg(BatchArgs a) {
 				u[0] = fma(ri, ri, u[0]);
 				u[1] = fma(ri, a.dinv64[i] * ri, u[1]);
 			}
-			cluster_sum<2>(u, sh_tree, slots, ph++, cl);
+			team_sum<2>(u, sh_tree, slots, ph++, cl, team);
 			iters = it + 1;
 			res = sqrt(u[0]);
 			if (res < tol) {
@@ -205,14 +246,12 @@ k_batch_cg(BatchArgs a) {
 			const double beta = rho / rho_old;
 			for (int64_t i = r0 + tid; i < r1; i += nt)
 				a.p64[i] = fma(beta, a.p64[i], a.dinv64[i] * a.r64[i]);
-			__threadfence();
-			cl.sync();
+			team_sync(cl, team);
 		}
 		if (switch_now) {
 			// the same Krylov process continues in FP32: r replaced by the
 			// FP64 b - A x, the direction p = z + beta p from the last FP64 rho
-			__threadfence();
-			cl.sync();
+			team_sync(cl, team);
 			double rz32 = 0.0;
 			replace(res, rz32);
 			++outer;
@@ -223,8 +262,7 @@ k_batch_cg(BatchArgs a) {
 			rho = rz32;
 			for (int64_t i = r0 + tid; i < r1; i += nt)
 				a.p32[i] = fmaf(bf, (float)a.p64[i], a.dinv32[i] * a.r32[i]);
-			__threadfence();
-			cl.sync();
+			team_sync(cl, team);
 			fp32_start = false;
 		}
 		else if (status != FS_CONVERGED_RTOL) {
@@ -241,8 +279,7 @@ k_batch_cg(BatchArgs a) {
 			for (int64_t i = r0 + tid; i < r1; i += nt)
 				a.p32[i] = a.dinv32[i] * a.r32[i];
 			rho = rz;
-			__threadfence();
-			cl.sync();
+			team_sync(cl, team);
 		}
 		for (int it = iters; it < a.maxiter; ++it) {
 			// w = A p, p . w
@@ -254,7 +291,7 @@ k_batch_cg(BatchArgs a) {
 				a.w32[i] = s;
 				q[0] = fma((double)s, (double)a.p32[i], q[0]);
 			}
-			cluster_sum<1>(q, sh_tree, slots, ph++, cl);
+			team_sum<1>(q, sh_tree, slots, ph++, cl, team);
 			const double alpha = rho / q[0];
 			const float af = (float)alpha;
 			// x32 += alpha p, r -= alpha w, ||r||^2, r . z
@@ -266,7 +303,7 @@ k_batch_cg(BatchArgs a) {
 				u[0] = fma((double)ri, (double)ri, u[0]);
 				u[1] = fma((double)ri, (double)(a.dinv32[i] * ri), u[1]);
 			}
-			cluster_sum<2>(u, sh_tree, slots, ph++, cl);
+			team_sum<2>(u, sh_tree, slots, ph++, cl, team);
 			iters = it + 1;
 			double est = sqrt(u[0]);
 			double rz_new = u[1];
@@ -277,8 +314,7 @@ k_batch_cg(BatchArgs a) {
 					a.x[i] += (double)a.x32[i];
 					a.x32[i] = 0.f;
 				}
-				__threadfence();
-				cl.sync();
+				team_sync(cl, team);
 				replace(res, rz_new);
 				++outer;
 				rmax = res;
@@ -297,15 +333,14 @@ k_batch_cg(BatchArgs a) {
 			const float bf = (float)beta;
 			for (int64_t i = r0 + tid; i < r1; i += nt)
 				a.p32[i] = fmaf(bf, a.p32[i], a.dinv32[i] * a.r32[i]);
-			__threadfence();
-			cl.sync();
+			team_sync(cl, team);
 		}
 	}
 	double xn[1] = {0.0};
 	for (int64_t i = r0 + tid; i < r1; i += nt)
 		xn[0] = fma(a.x[i], a.x[i], xn[0]);
-	cluster_sum<1>(xn, sh_tree, slots, ph++, cl);
-	if (crank == 0 && tid == 0) {
+	team_sum<1>(xn, sh_tree, slots, ph++, cl, team);
+	if (trank == 0 && tid == 0) {
 		fs_solve_info inf;
 		inf.status = status;
 		inf.iters = status == FS_CONVERGED_RTOL ? iters : 0;
@@ -318,7 +353,8 @@ k_batch_cg(BatchArgs a) {
 		a.info[sys] = inf;
 	}
 	// no CTA may leave while a peer can still read its shared slots
-	cl.sync();
+	if (team > 1)
+		cl.sync();
 }
 
 struct BatchPlan {
@@ -330,14 +366,18 @@ struct BatchPlan {
 	double *work64 = nullptr;  // r64, p64, w64 of the FP64 head
 	int nsys = 0;
 	int tuned_cluster = 0, tuned_threads = 0;
+	int tuned_nbig = -1;  // systems that own a whole cluster (-1: all)
 };
 
 // one plan per (matrix, partition); freed with the context process
 std::map<std::pair<const Csr *, std::vector<int64_t>>, BatchPlan> g_plans;
 
+// a.nbig systems own a cluster each; the rest take one CTA each, `cluster`
+// of them per cluster
 int launch_batch(Ctx *ctx, const BatchArgs &a, int nsys, int cluster, int threads) {
+	const int nclusters = a.nbig + (nsys - a.nbig + cluster - 1) / cluster;
 	cudaLaunchConfig_t cfg = {};
-	cfg.gridDim = dim3((unsigned)(nsys * cluster), 1, 1);
+	cfg.gridDim = dim3((unsigned)(nclusters * cluster), 1, 1);
 	cfg.blockDim = dim3((unsigned)threads, 1, 1);
 	cfg.dynamicSmemBytes = 0;
 	cfg.stream = ctx->stream;
@@ -356,15 +396,11 @@ int launch_batch(Ctx *ctx, const BatchArgs &a, int nsys, int cluster, int thread
 	return FS_OK;
 }
 
-}  // namespace
-
-}  // namespace fsg
-
-using namespace fsg;
-
-extern "C" FS_API int fs_batch_cg_solve(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah, int nsys,
-                                        const int64_t *sys_offsets, fs_vec bh, fs_vec xh,
-                                        int cluster_size, int threads, fs_solve_info *infos) {
+// cluster_systems: -1 chooses (with the sizes), else that many of the
+// largest systems own a cluster and the rest one CTA each
+int batch_solve(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah, int nsys, const int64_t *sys_offsets,
+                fs_vec bh, fs_vec xh, int cluster_size, int threads, int cluster_systems,
+                fs_solve_info *infos) {
 	Ctx *ctx = reinterpret_cast<Ctx *>(h);
 	Csr *A = reinterpret_cast<Csr *>(Ah);
 	Vec *b = reinterpret_cast<Vec *>(bh), *x = reinterpret_cast<Vec *>(xh);
@@ -446,12 +482,14 @@ extern "C" FS_API int fs_batch_cg_solve(fs_ctx h, const fs_krylov_settings *s, f
 	a.rtol = s->base.rtol;
 	a.delta = s->inner_rtol > 0 ? s->inner_rtol : 0.1;
 	a.zero_guess = s->base.use_zero_guess ? 1 : 0;
+	a.nbig = cluster_systems >= 0 ? cluster_systems : nsys;
 
 	int cl = cluster_size, th = threads;
 	if (cl == 0 || th == 0) {
 		if (p.tuned_cluster == 0) {
-			// autotuner: time a short capped run of each candidate on this
-			// batch (the solution is restored afterwards) and keep the fastest
+			// autotuner, stage 1: time a short capped run of each cluster /
+			// CTA size (every system a whole cluster) on this batch, keep the
+			// fastest; the solution is restored afterwards
 			std::vector<double> xsave(n);
 			FS_CUDA_TRY(ctx, cudaMemcpy(xsave.data(), x->d, n * 8, cudaMemcpyDeviceToHost));
 			BatchArgs t = a;
@@ -483,23 +521,88 @@ extern "C" FS_API int fs_batch_cg_solve(fs_ctx h, const fs_krylov_settings *s, f
 						p.tuned_threads = tt;
 					}
 				}
+			if (p.tuned_cluster == 0) {
+				cudaEventDestroy(e0);
+				cudaEventDestroy(e1);
+				return set_err(ctx, FS_ERR_CUDA, "batched CG: no launch configuration ran");
+			}
+			// stage 2 (only when the caller fixed neither size): complete
+			// solves -- capped runs cannot see that the largest systems also
+			// need the most iterations -- of the stage-1 winner against
+			// splits where the largest eighth or quarter of the systems own
+			// a cluster of 4 or 8 CTAs and the rest one CTA each
+			p.tuned_nbig = nsys;
+			if (!cluster_size && !threads && nsys >= 8) {
+				struct Cand { int c, t, nbig; };
+				std::vector<Cand> cands = {{p.tuned_cluster, p.tuned_threads, nsys}};
+				for (int c : {8, 4})
+					for (int q : {8, 4})
+						cands.push_back({c, 1024, std::max(1, nsys / q)});
+				cands.push_back({8, 512, std::max(1, nsys / 4)});
+				BatchArgs f = a;
+				f.zero_guess = 1;
+				float best2 = 1e30f;
+				for (const Cand &cd : cands) {
+					f.nbig = cd.nbig;
+					cudaEventRecord(e0, ctx->stream);
+					int st = launch_batch(ctx, f, nsys, cd.c, cd.t);
+					cudaEventRecord(e1, ctx->stream);
+					if (st != FS_OK) {
+						cudaGetLastError();
+						continue;
+					}
+					cudaEventSynchronize(e1);
+					float ms = 0;
+					cudaEventElapsedTime(&ms, e0, e1);
+					if (ms < best2) {
+						best2 = ms;
+						p.tuned_cluster = cd.c;
+						p.tuned_threads = cd.t;
+						p.tuned_nbig = cd.nbig;
+					}
+				}
+			}
 			cudaEventDestroy(e0);
 			cudaEventDestroy(e1);
 			FS_CUDA_TRY(ctx, cudaMemcpy(x->d, xsave.data(), n * 8, cudaMemcpyHostToDevice));
 			FS_CUDA_TRY(ctx, fence_setup_copies());
-			if (p.tuned_cluster == 0)
-				return set_err(ctx, FS_ERR_CUDA, "batched CG: no launch configuration ran");
 		}
 		if (!cl)
 			cl = p.tuned_cluster;
 		if (!th)
 			th = p.tuned_threads;
+		if (!cluster_size && !threads && p.tuned_nbig >= 0 && cluster_systems < 0)
+			a.nbig = p.tuned_nbig;
 	}
 	FS_TRY(launch_batch(ctx, a, nsys, cl, th));
 	FS_CUDA_TRY(ctx, cudaMemcpyAsync(infos, p.d_info, sizeof(fs_solve_info) * nsys, cudaMemcpyDeviceToHost,
 	                                 ctx->stream));
 	FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
 	return FS_OK;
+}
+
+}  // namespace
+}  // namespace fsg
+
+using namespace fsg;
+
+extern "C" FS_API int fs_batch_cg_solve(fs_ctx h, const fs_krylov_settings *s, fs_csr A, int nsys,
+                                        const int64_t *sys_offsets, fs_vec b, fs_vec x,
+                                        int cluster_size, int threads, fs_solve_info *infos) {
+	return batch_solve(h, s, A, nsys, sys_offsets, b, x, cluster_size, threads, -1, infos);
+}
+
+extern "C" FS_API int fs_batch_cg_solve_split(fs_ctx h, const fs_krylov_settings *s, fs_csr A,
+                                              int nsys, const int64_t *sys_offsets, fs_vec b,
+                                              fs_vec x, int cluster_size, int threads,
+                                              int cluster_systems, fs_solve_info *infos) {
+	Ctx *ctx = reinterpret_cast<Ctx *>(h);
+	if (!ok_ctx(ctx))
+		return FS_ERR_BAD_HANDLE;
+	if (cluster_size == 0 || threads == 0 || cluster_systems < 0 || cluster_systems > nsys)
+		return set_err(ctx, FS_ERR_INVALID_ARG,
+		               "fs_batch_cg_solve_split: explicit sizes and 0 <= cluster_systems <= nsys");
+	return batch_solve(h, s, A, nsys, sys_offsets, b, x, cluster_size, threads, cluster_systems, infos);
 }
 
 extern "C" FS_API int fs_batch_tuning(fs_ctx h, fs_csr Ah, int nsys, const int64_t *sys_offsets,
@@ -514,5 +617,17 @@ extern "C" FS_API int fs_batch_tuning(fs_ctx h, fs_csr Ah, int nsys, const int64
 		return set_err(ctx, FS_ERR_INVALID_ARG, "no batched solve has run on this partition");
 	*cluster_size = it->second.tuned_cluster;
 	*threads = it->second.tuned_threads;
+	return FS_OK;
+}
+
+extern "C" FS_API int fs_batch_schedule(fs_ctx h, fs_csr Ah, int nsys, const int64_t *sys_offsets,
+                                        int *cluster_size, int *threads, int *cluster_systems) {
+	FS_TRY(fs_batch_tuning(h, Ah, nsys, sys_offsets, cluster_size, threads));
+	if (!cluster_systems)
+		return FS_ERR_BAD_HANDLE;
+	Csr *A = reinterpret_cast<Csr *>(Ah);
+	std::vector<int64_t> off(sys_offsets, sys_offsets + nsys + 1);
+	const int nbig = g_plans.find(std::make_pair((const Csr *)A, off))->second.tuned_nbig;
+	*cluster_systems = nbig < 0 ? nsys : nbig;
 	return FS_OK;
 }

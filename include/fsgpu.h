@@ -452,13 +452,23 @@ FS_API int fs_fv_face_grad(fs_ctx ctx, int dim, int64_t n, fs_vec lambda, fs_vec
  * (settings->inner_rtol = replacement factor), stopping per system on the
  * FP64 residual (rtol * ||b_s||).  cluster_size (1, 2, 4, 8) and threads per
  * CTA may be 0: an autotuner times the candidates on the first call for this
- * partition and keeps the fastest (fs_batch_tuning reports it).  infos[s]
- * receives system s's solve_info. */
+ * partition and keeps the fastest (fs_batch_tuning reports it).  With both 0
+ * it also tries schedules where only the largest systems own a whole cluster
+ * and every other system one CTA (fs_batch_schedule reports how many own a
+ * cluster).  infos[s] receives system s's solve_info. */
 FS_API int fs_batch_cg_solve(fs_ctx ctx, const fs_krylov_settings *s, fs_csr A, int nsys,
                              const int64_t *sys_offsets, fs_vec b, fs_vec x, int cluster_size,
                              int threads, fs_solve_info *infos);
 FS_API int fs_batch_tuning(fs_ctx ctx, fs_csr A, int nsys, const int64_t *sys_offsets,
                            int *cluster_size, int *threads);
+FS_API int fs_batch_schedule(fs_ctx ctx, fs_csr A, int nsys, const int64_t *sys_offsets,
+                             int *cluster_size, int *threads, int *cluster_systems);
+/* the same solve with an explicit schedule: the cluster_systems largest
+ * systems own a cluster of cluster_size CTAs, every other system one CTA
+ * (cluster_size of them per cluster); sizes must be given */
+FS_API int fs_batch_cg_solve_split(fs_ctx ctx, const fs_krylov_settings *s, fs_csr A, int nsys,
+                                   const int64_t *sys_offsets, fs_vec b, fs_vec x, int cluster_size,
+                                   int threads, int cluster_systems, fs_solve_info *infos);
 
 /* Block Jacobi-PCG for nrhs = 16 right-hand sides of one operator (FP64).
  * No counterpart in the reference (its CG, cg.hh:43-139, takes one

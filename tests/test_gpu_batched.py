@@ -15,13 +15,18 @@ def batch():
     return P.batch_diffusion2d(nsys=24, side_lo=6, side_hi=48, seed=11)
 
 
-@pytest.mark.parametrize("cluster,threads", [(0, 0), (1, 256), (2, 512), (8, 1024)])
-def test_batch_cg_each_system(ctx, batch, cluster, threads):
+@pytest.mark.parametrize("cluster,threads,cluster_systems",
+                         [(0, 0, None), (1, 256, None), (2, 512, None), (8, 1024, None),
+                          (8, 1024, 0), (8, 512, 6), (4, 1024, 23), (2, 256, 24)])
+def test_batch_cg_each_system(ctx, batch, cluster, threads, cluster_systems):
+    """Every schedule: every system a whole cluster, or the largest
+    `cluster_systems` a whole cluster and the others one CTA each (24
+    systems: 0, 6 and 23 own a cluster; a last cluster only partly used)."""
     A, off, b, sides = batch
     dA = fs.CSR(ctx, A)
     vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
     infos = fs.batch_cg(dA, off, vb, vx, maxiter=4000, rtol=1e-8, cluster=cluster,
-                        threads=threads)
+                        threads=threads, cluster_systems=cluster_systems)
     x = vx.numpy()
     S = A.to_scipy()
     for k, inf in enumerate(infos):
@@ -37,6 +42,8 @@ def test_batch_cg_each_system(ctx, batch, cluster, threads):
     if cluster == 0:
         c, t = fs.batch_tuning(dA, off)
         assert c in (1, 2, 4, 8) and t in (256, 512, 1024)
+        c2, t2, nb = fs.batch_schedule(dA, off)
+        assert (c2, t2) == (c, t) and 1 <= nb <= len(infos)
 
 
 def test_batch_rejects_coupled_systems(ctx):
