@@ -1033,7 +1033,7 @@ int block_cg_entry(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah, const fs_pr
 		return FS_ERR_BAD_HANDLE;
 	FS_TRY(reject_matrix_free(A, "block_cg_entry"));
 	if (nrhs != kS)
-		return set_err(ctx, FS_ERR_UNSUPPORTED, "block CG: this build takes %d right-hand sides", kS);
+		return set_err(ctx, FS_ERR_UNSUPPORTED, "block CG: the library takes %d right-hand sides", kS);
 	const int64_t n = A->nrows;
 	if (A->nrows != A->ncols || B->n != n * kS || X->n != n * kS || B->dtype != FS_F64 ||
 	    X->dtype != FS_F64)

@@ -695,7 +695,7 @@ FS_API int fs_csr_create(fs_ctx h, int64_t nrows, int64_t ncols, int64_t nnz,
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_create: index_bytes must be 4 or 8");
 	if (nnz >= (int64_t)1 << 31 || nrows >= (int64_t)1 << 31 || ncols >= (int64_t)1 << 31)
 		return set_err(ctx, FS_ERR_UNSUPPORTED,
-		               "fs_csr_create: this build stores 32-bit offsets (nnz, rows < 2^31)");
+		               "fs_csr_create: the library stores 32-bit offsets (nnz, rows < 2^31)");
 	if (rowptr[0] != 0 || rowptr[nrows] != nnz)
 		return set_err(ctx, FS_ERR_INVALID_ARG, "fs_csr_create: rowptr[0] must be 0 and rowptr[n] = nnz");
 	std::vector<int> rp(nrows + 1);

@@ -47,7 +47,7 @@ enum fs_status {
 	FS_ERR_BREAKDOWN = 6,      /* a solver hit a reference flog_assert      */
 	FS_ERR_INVALID_ARG = 7,    /* argument out of range                     */
 	FS_ERR_NO_DEVICE = 8,      /* no usable CUDA device                     */
-	FS_ERR_UNSUPPORTED = 9,    /* valid request this build does not handle  */
+	FS_ERR_UNSUPPORTED = 9,    /* valid request the library does not handle */
 	FS_ERR_IO = 10,            /* file missing, unreadable or malformed     */
 	FS_ERR_CALLBACK = 11       /* a caller's operator callback failed       */
 };
