@@ -488,19 +488,21 @@ def run_suite(args):
                 fs.CSR(ctx, Ak), fs.op.jacobi)
             seq += _timed_solve(ctx, slv, fs.Vector(ctx, b[lo:hi]), fs.Vector(ctx, int(hi - lo)))[0]
         # algorithmic bytes: per row and FP32 iteration of the persistent
-        # kernel, the column-id SpMV (value + column id per nonzero, row offset,
-        # A p written), the update (x32 and r read and written, A p and D^-1
-        # read) and the direction (p read and written, D^-1 and r read); the
-        # FP64 head iterations and replacements are counted as FP32 ones (a
-        # lower bound)
+        # kernel, the SpMV (grid-stencil storage: the diagonal and two upper
+        # diagonals; column ids: value + column id per nonzero and the row
+        # offset; p read once, A p written), the update (x32 and r read and
+        # written, A p and D^-1 read) and the direction (p read and written,
+        # D^-1 and r read); the FP64 head iterations and replacements are
+        # counted as FP32 ones (a lower bound)
+        fmt = fs.batch_format(dA, off)
         rows_it = sum(int(off[k + 1] - off[k]) * its[k] for k in range(len(infos)))
         nnz_row = A.nnz / A.nrows
-        b_row_it = nnz_row * 8 + 4 + 4 + 24 + 16
+        b_row_it = (12 if fmt == "grid" else nnz_row * 8 + 4) + 4 + 4 + 24 + 16
         gbs = rows_it * b_row_it / t / 1e9
         peak, peak_kind = _peaks()
         out["batch512-diffusion2d"] = {
             "systems": len(infos), "rows": A.nrows, "nnz": A.nnz, "s": t, "cluster": cl,
-            "threads": th, "systems_owning_a_cluster": nbig,
+            "threads": th, "systems_owning_a_cluster": nbig, "storage": fmt,
             "all_converged": all(i.status == "converged_rtol" for i in infos),
             "max_true_relres": rr, "iters_min": min(its), "iters_max": max(its),
             "iters_sum": int(sum(its)), "row_iterations": rows_it,

@@ -12,7 +12,7 @@ from . import build, problems  # noqa: F401
 def __getattr__(name):
     # the CUDA-backed API is imported lazily so that the generators and the
     # build helpers work on hosts without a GPU
-    if name in ("api", "batch_cg", "batch_tuning", "batch_schedule", "block_cg", "Context", "Vector", "Multi", "CSR", "SolveInfo", "op", "vec", "mat", "cg",
+    if name in ("api", "batch_cg", "batch_tuning", "batch_schedule", "batch_format", "block_cg", "Context", "Vector", "Multi", "CSR", "SolveInfo", "op", "vec", "mat", "cg",
                 "bicgstab", "gmres", "fcg", "pipelined_cg", "mixed_cg", "mixed_bicgstab", "mixed_gmres", "nka",
                 "Shell"):
         import importlib

@@ -222,6 +222,7 @@ _PROTOS = {
     "fs_batch_tuning": [_vp, _vp, C.c_int, C.POINTER(_i64), C.POINTER(C.c_int), C.POINTER(C.c_int)],
     "fs_batch_schedule": [_vp, _vp, C.c_int, C.POINTER(_i64), C.POINTER(C.c_int), C.POINTER(C.c_int),
                           C.POINTER(C.c_int)],
+    "fs_batch_format": [_vp, _vp, C.c_int, C.POINTER(_i64), C.POINTER(C.c_int)],
     "fs_batch_cg_solve_split": [_vp, C.POINTER(KrylovSettings), _vp, C.c_int, C.POINTER(_i64), _vp,
                                 _vp, C.c_int, C.c_int, C.c_int, C.POINTER(SolveInfo)],
     "fs_krylov_apply_transpose": [_vp, _vp, _vp, C.POINTER(SolveInfo)],

@@ -760,6 +760,18 @@ def batch_schedule(A: CSR, offsets):
     return c.value, t.value, nb.value
 
 
+def batch_format(A: CSR, offsets) -> str:
+    """The storage the batched kernel reads for this partition (checked on
+    the first solve after the values change): "grid" (every system a
+    symmetric 5-point square-grid stencil: diagonal and upper diagonals) or
+    "csr" (the column ids)."""
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    f = C.c_int()
+    check(lib().fs_batch_format(A.ctx.h, A.h, off.size - 1, off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                C.byref(f)), A.ctx.h, "fs_batch_format")
+    return "grid" if f.value == 1 else "csr"
+
+
 class _SolverFactory:
     """``X::solver(settings, work)``; calling it with (A[, P[, diag]]) binds."""
 

@@ -64,7 +64,103 @@ struct BatchArgs {
 	double delta;
 	double head;             // FP64 iterations until ||r|| < head ||b|| (0: none)
 	int zero_guess;
+	// 2-D grid stencils (every system a 5-point operator on an s x s grid
+	// with symmetric values, found when the plan is made): the diagonal and
+	// the two upper diagonals a(r, r+1), a(r, r+s), FP64 and FP32, and each
+	// system's side; null when the batch is not all grid stencils
+	const int *side;
+	const double *gd64, *gu1_64, *gu2_64;
+	const float *gd32, *gu1_32, *gu2_32;
 };
+
+__device__ __forceinline__ float fmav(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmav(double a, double b, double c) { return fma(a, b, c); }
+
+// Rows r0 + tid, r0 + tid + nt, ... of one system, U at a time: `load`
+// reads every value a row needs into registers for all U rows before `store`
+// writes any of them, so each thread keeps U rows' loads in flight at once
+// (the compiler cannot move a load above a store that it cannot prove
+// disjoint).  The loads are unconditional -- a row past r1 loads row r1 - 1
+// again and is not stored -- so that no branch separates them.
+template<int U, class L, class S>
+__device__ __forceinline__ void rows_batched(int64_t r0, int64_t r1, int tid, int nt, L &&load,
+                                             S &&store) {
+	using T = decltype(load(r0));
+	for (int64_t i0 = r0 + tid; i0 < r1; i0 += (int64_t)U * nt) {
+		T t[U];
+#pragma unroll
+		for (int u = 0; u < U; ++u) {
+			const int64_t i = i0 + (int64_t)u * nt;
+			t[u] = load(i < r1 ? i : r1 - 1);
+		}
+#pragma unroll
+		for (int u = 0; u < U; ++u) {
+			const int64_t i = i0 + (int64_t)u * nt;
+			if (i < r1)
+				store(i, t[u]);
+		}
+	}
+}
+
+// Row sums s_i = sum_k a(i, k) v[k] for the rows r0 + tid, r0 + tid + nt,
+// ... of one system, in column order (the same bits either way), handed to
+// f(i, s_i): from the grid-stencil arrays when the batch has them (no index
+// is read: the coefficient and neighbour loads of a batch of rows are all
+// independent), else from the CSR.
+template<class V, int U, class F>
+__device__ __forceinline__ void row_sums(const BatchArgs &a, const V *val, const V *gd, const V *gu1,
+                                         const V *gu2, const V *__restrict__ v, int sys,
+                                         int64_t R0, int64_t r0, int64_t r1, int tid, int nt, F &&f) {
+	if (a.side && U == 1) {
+		const int sd = a.side[sys];
+		for (int64_t i = r0 + tid; i < r1; i += nt) {
+			const int l = (int)(i - R0), ii = l % sd, jj = l / sd;
+			V sum = V(0);
+			if (jj > 0)
+				sum = fmav(gu2[i - sd], v[i - sd], sum);
+			if (ii > 0)
+				sum = fmav(gu1[i - 1], v[i - 1], sum);
+			sum = fmav(gd[i], v[i], sum);
+			if (ii < sd - 1)
+				sum = fmav(gu1[i], v[i + 1], sum);
+			if (jj < sd - 1)
+				sum = fmav(gu2[i], v[i + sd], sum);
+			f(i, sum);
+		}
+	}
+	else if (a.side) {
+		const int sd = a.side[sys];
+		rows_batched<U>(
+			r0, r1, tid, nt,
+			[&](int64_t i) {
+				// every load from an address inside the system (an absent
+				// neighbour reads row i and its term is not added), so none
+				// waits on a branch
+				const int l = (int)(i - R0), ii = l % sd, jj = l / sd;
+				const bool s_lo = jj > 0, w_lo = ii > 0, w_hi = ii < sd - 1, s_hi = jj < sd - 1;
+				const int64_t is = s_lo ? i - sd : i, iw = w_lo ? i - 1 : i;
+				const int64_t ie = w_hi ? i + 1 : i, in = s_hi ? i + sd : i;
+				const V c0 = gu2[is], x0 = v[is], c1 = gu1[iw], x1 = v[iw], c2 = gd[i], x2 = v[i];
+				const V c3 = gu1[i], x3 = v[ie], c4 = gu2[i], x4 = v[in];
+				V sum = V(0);
+				sum = s_lo ? fmav(c0, x0, sum) : sum;
+				sum = w_lo ? fmav(c1, x1, sum) : sum;
+				sum = fmav(c2, x2, sum);
+				sum = w_hi ? fmav(c3, x3, sum) : sum;
+				sum = s_hi ? fmav(c4, x4, sum) : sum;
+				return sum;
+			},
+			f);
+	}
+	else {
+		for (int64_t i = r0 + tid; i < r1; i += nt) {
+			V sum = V(0);
+			for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k)
+				sum = fmav(val[k], v[a.col[k]], sum);
+			f(i, sum);
+		}
+	}
+}
 
 // sum of NV doubles over the cluster: every CTA block-reduces its values,
 // publishes them in its shared slot for phase `ph`, and after the cluster
@@ -122,8 +218,13 @@ __device__ __forceinline__ void team_sync(cgrp::cluster_group &cl, int team) {
 		__syncthreads();
 }
 
-__global__ void __launch_bounds__(1024)
+// MAXT: the largest CTA the kernel is built for, MINB CTAs of it resident
+// on an SM; U32: FP32 rows per batch of the row loops (FP64: half).  One
+// 1024-thread CTA an SM leaves 64 registers a thread (one row at a time).
+template<int MAXT, int MINB, int U32>
+__global__ void __launch_bounds__(MAXT, MINB)
 k_batch_cg(BatchArgs a) {
+	constexpr int U64 = U32 > 1 ? U32 / 2 : 1;
 	cgrp::cluster_group cl = cgrp::this_cluster();
 	const int crank = (int)cl.block_rank();
 	const int csize = (int)cl.num_blocks();
@@ -170,16 +271,14 @@ k_batch_cg(BatchArgs a) {
 	// ||r64|| and r32 . D^-1 r32 (all CTAs of the cluster get the same)
 	auto replace = [&](double &res, double &rz) {
 		double t[2] = {0.0, 0.0};
-		for (int64_t i = r0 + tid; i < r1; i += nt) {
-			double s = 0.0;
-			for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k)
-				s = fma(a.val64[k], a.x[a.col[k]], s);
-			const double ri = a.b[i] - s;
-			const float r32 = (float)ri;
-			a.r32[i] = r32;
-			t[0] = fma(ri, ri, t[0]);
-			t[1] = fma((double)r32, (double)(a.dinv32[i] * r32), t[1]);
-		}
+		row_sums<double, U64>(a, a.val64, a.gd64, a.gu1_64, a.gu2_64, a.x, sys, R0, r0, r1, tid, nt,
+		                 [&](int64_t i, double s) {
+			                 const double ri = a.b[i] - s;
+			                 const float r32 = (float)ri;
+			                 a.r32[i] = r32;
+			                 t[0] = fma(ri, ri, t[0]);
+			                 t[1] = fma((double)r32, (double)(a.dinv32[i] * r32), t[1]);
+		                 });
 		team_sum<2>(t, sh_tree, slots, ph++, cl, team);
 		res = sqrt(t[0]);
 		rz = t[1];
@@ -195,39 +294,39 @@ k_batch_cg(BatchArgs a) {
 	if (res >= tol && a.head > 0.0 && res >= a.head * bnorm && a.maxiter > 0) {
 		// FP64 head (the cg_apply64 iteration): r64 = b - A x, p = D^-1 r
 		double t[1] = {0.0};
-		for (int64_t i = r0 + tid; i < r1; i += nt) {
-			double sum = 0.0;
-			for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k)
-				sum = fma(a.val64[k], a.x[a.col[k]], sum);
-			const double ri = a.b[i] - sum;
-			a.r64[i] = ri;
-			const double zi = a.dinv64[i] * ri;
-			a.p64[i] = zi;
-			t[0] = fma(ri, zi, t[0]);
-		}
+		row_sums<double, U64>(a, a.val64, a.gd64, a.gu1_64, a.gu2_64, a.x, sys, R0, r0, r1, tid, nt,
+		                 [&](int64_t i, double sum) {
+			                 const double ri = a.b[i] - sum;
+			                 a.r64[i] = ri;
+			                 const double zi = a.dinv64[i] * ri;
+			                 a.p64[i] = zi;
+			                 t[0] = fma(ri, zi, t[0]);
+		                 });
 		team_sum<1>(t, sh_tree, slots, ph++, cl, team);
 		rho = t[0];
 		double rho_old = rho;
 		bool switch_now = false;
 		for (int it = 0; it < a.maxiter; ++it) {
 			double q[1] = {0.0};
-			for (int64_t i = r0 + tid; i < r1; i += nt) {
-				double sum = 0.0;
-				for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k)
-					sum = fma(a.val64[k], a.p64[a.col[k]], sum);
-				a.w64[i] = sum;
-				q[0] = fma(sum, a.p64[i], q[0]);
-			}
+			row_sums<double, U64>(a, a.val64, a.gd64, a.gu1_64, a.gu2_64, a.p64, sys, R0, r0, r1, tid, nt,
+			                 [&](int64_t i, double sum) {
+				                 a.w64[i] = sum;
+				                 q[0] = fma(sum, a.p64[i], q[0]);
+			                 });
 			team_sum<1>(q, sh_tree, slots, ph++, cl, team);
 			const double alpha = rho / q[0];
 			double u[2] = {0.0, 0.0};
-			for (int64_t i = r0 + tid; i < r1; i += nt) {
-				a.x[i] = fma(alpha, a.p64[i], a.x[i]);
-				const double ri = fma(-alpha, a.w64[i], a.r64[i]);
-				a.r64[i] = ri;
-				u[0] = fma(ri, ri, u[0]);
-				u[1] = fma(ri, a.dinv64[i] * ri, u[1]);
-			}
+			struct H5 { double x, p, w, r, d; };
+			rows_batched<U64>(
+				r0, r1, tid, nt,
+				[&](int64_t i) { return H5{a.x[i], a.p64[i], a.w64[i], a.r64[i], a.dinv64[i]}; },
+				[&](int64_t i, const H5 &h) {
+					a.x[i] = fma(alpha, h.p, h.x);
+					const double ri = fma(-alpha, h.w, h.r);
+					a.r64[i] = ri;
+					u[0] = fma(ri, ri, u[0]);
+					u[1] = fma(ri, h.d * ri, u[1]);
+				});
 			team_sum<2>(u, sh_tree, slots, ph++, cl, team);
 			iters = it + 1;
 			res = sqrt(u[0]);
@@ -244,8 +343,9 @@ k_batch_cg(BatchArgs a) {
 				break;
 			}
 			const double beta = rho / rho_old;
-			for (int64_t i = r0 + tid; i < r1; i += nt)
-				a.p64[i] = fma(beta, a.p64[i], a.dinv64[i] * a.r64[i]);
+			rows_batched<U64>(
+				r0, r1, tid, nt, [&](int64_t i) { return make_double3(a.p64[i], a.dinv64[i], a.r64[i]); },
+				[&](int64_t i, const double3 &h) { a.p64[i] = fma(beta, h.x, h.y * h.z); });
 			team_sync(cl, team);
 		}
 		if (switch_now) {
@@ -283,26 +383,33 @@ k_batch_cg(BatchArgs a) {
 		}
 		for (int it = iters; it < a.maxiter; ++it) {
 			// w = A p, p . w
-			double q[1] = {0.0};
-			for (int64_t i = r0 + tid; i < r1; i += nt) {
-				float s = 0.f;
-				for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k)
-					s = fmaf(a.val32[k], a.p32[a.col[k]], s);
-				a.w32[i] = s;
-				q[0] = fma((double)s, (double)a.p32[i], q[0]);
-			}
+			// the FP32 phase's dots: exact FP32 products summed in compensated
+			// FP32 pairs per thread (FP64 accuracy without the FP64 pipe, which
+			// runs at 1/64 of the FP32 rate), FP64 across the team
+			cf32 cq{0.f, 0.f};
+			row_sums<float, U32>(a, a.val32, a.gd32, a.gu1_32, a.gu2_32, a.p32, sys, R0, r0, r1, tid, nt,
+			                [&](int64_t i, float s) {
+				                a.w32[i] = s;
+				                cq.add_prod(s, a.p32[i]);
+			                });
+			double q[1] = {(double)cq.hi + (double)cq.lo};
 			team_sum<1>(q, sh_tree, slots, ph++, cl, team);
 			const double alpha = rho / q[0];
 			const float af = (float)alpha;
 			// x32 += alpha p, r -= alpha w, ||r||^2, r . z
-			double u[2] = {0.0, 0.0};
-			for (int64_t i = r0 + tid; i < r1; i += nt) {
-				a.x32[i] = fmaf(af, a.p32[i], a.x32[i]);
-				const float ri = fmaf(-af, a.w32[i], a.r32[i]);
-				a.r32[i] = ri;
-				u[0] = fma((double)ri, (double)ri, u[0]);
-				u[1] = fma((double)ri, (double)(a.dinv32[i] * ri), u[1]);
-			}
+			cf32 cu0{0.f, 0.f}, cu1{0.f, 0.f};
+			struct S5 { float x, p, w, r, d; };
+			rows_batched<U32>(
+				r0, r1, tid, nt,
+				[&](int64_t i) { return S5{a.x32[i], a.p32[i], a.w32[i], a.r32[i], a.dinv32[i]}; },
+				[&](int64_t i, const S5 &h) {
+					a.x32[i] = fmaf(af, h.p, h.x);
+					const float ri = fmaf(-af, h.w, h.r);
+					a.r32[i] = ri;
+					cu0.add_prod(ri, ri);
+					cu1.add_prod(ri, h.d * ri);
+				});
+			double u[2] = {(double)cu0.hi + (double)cu0.lo, (double)cu1.hi + (double)cu1.lo};
 			team_sum<2>(u, sh_tree, slots, ph++, cl, team);
 			iters = it + 1;
 			double est = sqrt(u[0]);
@@ -331,8 +438,9 @@ k_batch_cg(BatchArgs a) {
 			const double beta = rz_new / rho;
 			rho = rz_new;
 			const float bf = (float)beta;
-			for (int64_t i = r0 + tid; i < r1; i += nt)
-				a.p32[i] = fmaf(bf, a.p32[i], a.dinv32[i] * a.r32[i]);
+			rows_batched<U32>(
+				r0, r1, tid, nt, [&](int64_t i) { return make_float3(a.p32[i], a.dinv32[i], a.r32[i]); },
+				[&](int64_t i, const float3 &h) { a.p32[i] = fmaf(bf, h.x, h.y * h.z); });
 			team_sync(cl, team);
 		}
 	}
@@ -357,6 +465,77 @@ k_batch_cg(BatchArgs a) {
 		cl.sync();
 }
 
+// The grid-stencil storage of a batch, one thread per row: row i of system
+// k (side s, local row l = ii + s jj) must hold exactly the columns
+// i - s, i - 1, i, i + 1, i + s that lie inside the s x s grid, in that
+// order, and its lower entries must equal their partners a(i - s, i),
+// a(i - 1, i) bit for bit; any other row sets *bad.  Writes a(i, i),
+// a(i, i + 1), a(i, i + s) (0 where absent) in FP64 and FP32 at g + {0, ld,
+// 2 ld} + i.
+__global__ void k_batch_grid_build(int64_t n, int nsys, const int64_t *__restrict__ off,
+                                   const int *__restrict__ side, const int *__restrict__ rp,
+                                   const int *__restrict__ col, const double *__restrict__ val,
+                                   double *g64, float *g32, int64_t ld, unsigned *bad) {
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+	     i += (int64_t)gridDim.x * blockDim.x) {
+		// the system holding row i: the last k with off[k] <= i
+		int lo = 0, hi = nsys;
+		while (hi - lo > 1) {
+			const int mid = (lo + hi) / 2;
+			if (off[mid] <= i)
+				lo = mid;
+			else
+				hi = mid;
+		}
+		const int64_t sd = side[lo];
+		const int64_t l = i - off[lo], ii = l % sd, jj = l / sd;
+		int k = rp[i];
+		const int e = rp[i + 1];
+		bool ok = true;
+		double d = 0.0, u1 = 0.0, u2 = 0.0;
+		if (jj > 0) {
+			// partner a(i - s, i): the last entry of row i - s
+			const int q = rp[i - sd + 1] - 1;
+			ok = k < e && col[k] == i - sd && q >= rp[i - sd] &&
+			     __double_as_longlong(val[k]) == __double_as_longlong(val[q]);
+			++k;
+		}
+		if (ok && ii > 0) {
+			// partner a(i - 1, i): row i - 1's entry after its diagonal
+			const int q = rp[i - 1] + (jj > 0) + (ii > 1) + 1;
+			ok = k < e && col[k] == i - 1 && q < rp[i] &&
+			     __double_as_longlong(val[k]) == __double_as_longlong(val[q]);
+			++k;
+		}
+		if (ok) {
+			ok = k < e && col[k] == i;
+			if (ok)
+				d = val[k];
+			++k;
+		}
+		if (ok && ii < sd - 1) {
+			ok = k < e && col[k] == i + 1;
+			if (ok)
+				u1 = val[k];
+			++k;
+		}
+		if (ok && jj < sd - 1) {
+			ok = k < e && col[k] == i + sd;
+			if (ok)
+				u2 = val[k];
+			++k;
+		}
+		if (!ok || k != e)
+			atomicOr(bad, 1u);
+		g64[i] = d;
+		g64[ld + i] = u1;
+		g64[2 * ld + i] = u2;
+		g32[i] = (float)d;
+		g32[ld + i] = (float)u1;
+		g32[2 * ld + i] = (float)u2;
+	}
+}
+
 struct BatchPlan {
 	std::vector<int64_t> off;
 	int64_t *d_off = nullptr;
@@ -367,10 +546,68 @@ struct BatchPlan {
 	int nsys = 0;
 	int tuned_cluster = 0, tuned_threads = 0;
 	int tuned_nbig = -1;  // systems that own a whole cluster (-1: all)
+	// grid-stencil storage (every system a 5-point s x s grid with symmetric
+	// values): per-system sides, diagonal and upper diagonals; `grid` is 1
+	// when it holds for the values of generation `grid_gen`, 0 when not, -1
+	// not checked
+	int *d_side = nullptr;
+	double *g64 = nullptr;
+	float *g32 = nullptr;
+	unsigned *d_bad = nullptr;
+	int grid = -1;
+	unsigned grid_gen = 0;
 };
 
-// one plan per (matrix, partition); freed with the context process
+void free_plan(BatchPlan &p) {
+	for (void *q : {(void *)p.d_off, (void *)p.d_order, (void *)p.d_info, (void *)p.work,
+	                (void *)p.work64, (void *)p.d_side, (void *)p.g64, (void *)p.g32, (void *)p.d_bad})
+		if (q)
+			cudaFree(q);
+}
+
+// one plan per (matrix, partition); freed with the matrix
 std::map<std::pair<const Csr *, std::vector<int64_t>>, BatchPlan> g_plans;
+
+// (re)check the batch for the grid-stencil storage after a change of values
+int ensure_batch_grid(Ctx *ctx, const Csr *A, BatchPlan &p) {
+	if (p.grid >= 0 && p.grid_gen == A->values_gen)
+		return FS_OK;
+	p.grid = 0;
+	p.grid_gen = A->values_gen;
+	const int nsys = p.nsys;
+	std::vector<int> side(nsys);
+	for (int k = 0; k < nsys; ++k) {
+		const int64_t m = p.off[k + 1] - p.off[k];
+		int64_t sd = (int64_t)std::llround(std::sqrt((double)m));
+		while (sd * sd > m)
+			--sd;
+		while ((sd + 1) * (sd + 1) <= m)
+			++sd;
+		if (sd * sd != m || sd > 46340)
+			return FS_OK;  // not a square grid: the CSR row loops
+		side[k] = (int)sd;
+	}
+	const size_t n = (size_t)A->nrows, ld = n + 32;
+	if (!p.d_side) {
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.d_side, sizeof(int) * nsys));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.g64, sizeof(double) * 3 * ld));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.g32, sizeof(float) * 3 * ld));
+		FS_CUDA_TRY(ctx, cudaMalloc(&p.d_bad, sizeof(unsigned)));
+	}
+	FS_CUDA_TRY(ctx, cudaMemcpy(p.d_side, side.data(), sizeof(int) * nsys, cudaMemcpyHostToDevice));
+	FS_CUDA_TRY(ctx, cudaMemsetAsync(p.d_bad, 0, sizeof(unsigned), ctx->stream));
+	if (n > 0) {
+		k_batch_grid_build<<<grid_for(ctx, (int64_t)n, 256, 4), 256, 0, ctx->stream>>>(
+			(int64_t)n, nsys, p.d_off, p.d_side, A->rowptr, A->col, A->val, p.g64, p.g32,
+			(int64_t)ld, p.d_bad);
+		FS_TRY(check_launch(ctx, "batched grid-stencil build"));
+	}
+	unsigned bad = 1;
+	FS_CUDA_TRY(ctx, cudaMemcpyAsync(&bad, p.d_bad, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+	FS_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	p.grid = bad ? 0 : 1;
+	return FS_OK;
+}
 
 // a.nbig systems own a cluster each; the rest take one CTA each, `cluster`
 // of them per cluster
@@ -388,7 +625,9 @@ int launch_batch(Ctx *ctx, const BatchArgs &a, int nsys, int cluster, int thread
 	attr[0].val.clusterDim.z = 1;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
-	cudaError_t e = cudaLaunchKernelEx(&cfg, k_batch_cg, a);
+	cudaError_t e = threads > 512   ? cudaLaunchKernelEx(&cfg, k_batch_cg<1024, 1, 1>, a)
+	                : threads > 256 ? cudaLaunchKernelEx(&cfg, k_batch_cg<512, 1, 4>, a)
+	                                : cudaLaunchKernelEx(&cfg, k_batch_cg<256, 2, 8>, a);
 	if (e != cudaSuccess)
 		return set_err(ctx, FS_ERR_CUDA, "batched CG launch (cluster %d, %d threads): %s", cluster,
 		               threads, cudaGetErrorString(e));
@@ -456,6 +695,7 @@ int batch_solve(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah, int nsys, cons
 	BatchPlan &p = it->second;
 	FS_TRY(ensure_val32(A));
 	FS_TRY(ensure_dinv(A));
+	FS_TRY(ensure_batch_grid(ctx, A, p));
 	const size_t n = (size_t)A->nrows;
 	BatchArgs a;
 	a.nsys = nsys;
@@ -483,43 +723,67 @@ int batch_solve(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah, int nsys, cons
 	a.delta = s->inner_rtol > 0 ? s->inner_rtol : 0.1;
 	a.zero_guess = s->base.use_zero_guess ? 1 : 0;
 	a.nbig = cluster_systems >= 0 ? cluster_systems : nsys;
+	a.side = nullptr;
+	a.gd64 = a.gu1_64 = a.gu2_64 = nullptr;
+	a.gd32 = a.gu1_32 = a.gu2_32 = nullptr;
+	if (p.grid == 1) {
+		const size_t ld = n + 32;
+		a.side = p.d_side;
+		a.gd64 = p.g64;
+		a.gu1_64 = p.g64 + ld;
+		a.gu2_64 = p.g64 + 2 * ld;
+		a.gd32 = p.g32;
+		a.gu1_32 = p.g32 + ld;
+		a.gu2_32 = p.g32 + 2 * ld;
+	}
 
 	int cl = cluster_size, th = threads;
 	if (cl == 0 || th == 0) {
 		if (p.tuned_cluster == 0) {
 			// autotuner, stage 1: time a short capped run of each cluster /
-			// CTA size (every system a whole cluster) on this batch, keep the
-			// fastest; the solution is restored afterwards
+			// CTA size (every system a whole cluster) on this batch and keep
+			// the fastest cluster size for each CTA size; the solution is
+			// restored afterwards
 			std::vector<double> xsave(n);
 			FS_CUDA_TRY(ctx, cudaMemcpy(xsave.data(), x->d, n * 8, cudaMemcpyDeviceToHost));
 			BatchArgs t = a;
 			t.maxiter = std::min(a.maxiter, 40);
 			t.zero_guess = 1;
-			float best = 1e30f;
+			t.nbig = nsys;
+			const int tsizes[3] = {256, 512, 1024};
+			float best_t[3] = {1e30f, 1e30f, 1e30f};
+			int best_c[3] = {0, 0, 0};
 			cudaEvent_t e0, e1;
 			cudaEventCreate(&e0);
 			cudaEventCreate(&e1);
-			for (int c : {1, 2, 4, 8})
-				for (int tt : {256, 512, 1024}) {
-					if (cluster_size && c != cluster_size)
+			auto time_launch = [&](const BatchArgs &args, int c, int tt, float &ms) {
+				cudaEventRecord(e0, ctx->stream);
+				int st = launch_batch(ctx, args, nsys, c, tt);
+				cudaEventRecord(e1, ctx->stream);
+				if (st != FS_OK) {
+					cudaGetLastError();
+					return false;
+				}
+				cudaEventSynchronize(e1);
+				cudaEventElapsedTime(&ms, e0, e1);
+				return true;
+			};
+			for (int ti = 0; ti < 3; ++ti)
+				for (int c : {1, 2, 4, 8}) {
+					if ((cluster_size && c != cluster_size) || (threads && tsizes[ti] != threads))
 						continue;
-					if (threads && tt != threads)
-						continue;
-					cudaEventRecord(e0, ctx->stream);
-					int st = launch_batch(ctx, t, nsys, c, tt);
-					cudaEventRecord(e1, ctx->stream);
-					if (st != FS_OK) {
-						cudaGetLastError();
-						continue;
-					}
-					cudaEventSynchronize(e1);
 					float ms = 0;
-					cudaEventElapsedTime(&ms, e0, e1);
-					if (ms < best) {
-						best = ms;
-						p.tuned_cluster = c;
-						p.tuned_threads = tt;
+					if (time_launch(t, c, tsizes[ti], ms) && ms < best_t[ti]) {
+						best_t[ti] = ms;
+						best_c[ti] = c;
 					}
+				}
+			float best = 1e30f;
+			for (int ti = 0; ti < 3; ++ti)
+				if (best_c[ti] && best_t[ti] < best) {
+					best = best_t[ti];
+					p.tuned_cluster = best_c[ti];
+					p.tuned_threads = tsizes[ti];
 				}
 			if (p.tuned_cluster == 0) {
 				cudaEventDestroy(e0);
@@ -527,34 +791,27 @@ int batch_solve(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah, int nsys, cons
 				return set_err(ctx, FS_ERR_CUDA, "batched CG: no launch configuration ran");
 			}
 			// stage 2 (only when the caller fixed neither size): complete
-			// solves -- capped runs cannot see that the largest systems also
-			// need the most iterations -- of the stage-1 winner against
-			// splits where the largest eighth or quarter of the systems own
-			// a cluster of 4 or 8 CTAs and the rest one CTA each
+			// solves -- capped runs see neither that the largest systems
+			// need the most iterations nor how the FP64 head and the FP32
+			// phase share the time -- of each CTA size's stage-1 winner,
+			// against splits where the largest systems own a cluster and the
+			// rest one CTA each
 			p.tuned_nbig = nsys;
 			if (!cluster_size && !threads && nsys >= 8) {
 				struct Cand { int c, t, nbig; };
-				std::vector<Cand> cands = {{p.tuned_cluster, p.tuned_threads, nsys}};
-				for (int c : {8, 4})
-					for (int q : {8, 4})
-						cands.push_back({c, 1024, std::max(1, nsys / q)});
-				cands.push_back({8, 512, std::max(1, nsys / 4)});
+				std::vector<Cand> cands;
+				for (int ti = 0; ti < 3; ++ti)
+					if (best_c[ti])
+						cands.push_back({best_c[ti], tsizes[ti], nsys});
+				cands.push_back({2, 512, std::max(1, nsys / 16)});
+				cands.push_back({4, 1024, std::max(1, nsys / 32)});
 				BatchArgs f = a;
 				f.zero_guess = 1;
 				float best2 = 1e30f;
 				for (const Cand &cd : cands) {
 					f.nbig = cd.nbig;
-					cudaEventRecord(e0, ctx->stream);
-					int st = launch_batch(ctx, f, nsys, cd.c, cd.t);
-					cudaEventRecord(e1, ctx->stream);
-					if (st != FS_OK) {
-						cudaGetLastError();
-						continue;
-					}
-					cudaEventSynchronize(e1);
 					float ms = 0;
-					cudaEventElapsedTime(&ms, e0, e1);
-					if (ms < best2) {
+					if (time_launch(f, cd.c, cd.t, ms) && ms < best2) {
 						best2 = ms;
 						p.tuned_cluster = cd.c;
 						p.tuned_threads = cd.t;
@@ -582,6 +839,19 @@ int batch_solve(fs_ctx h, const fs_krylov_settings *s, fs_csr Ah, int nsys, cons
 }
 
 }  // namespace
+
+void destroy_batch_plans(const Csr *A) {
+	for (auto it = g_plans.begin(); it != g_plans.end();) {
+		if (it->first.first == A) {
+			free_plan(it->second);
+			it = g_plans.erase(it);
+		}
+		else {
+			++it;
+		}
+	}
+}
+
 }  // namespace fsg
 
 using namespace fsg;
@@ -629,5 +899,19 @@ extern "C" FS_API int fs_batch_schedule(fs_ctx h, fs_csr Ah, int nsys, const int
 	std::vector<int64_t> off(sys_offsets, sys_offsets + nsys + 1);
 	const int nbig = g_plans.find(std::make_pair((const Csr *)A, off))->second.tuned_nbig;
 	*cluster_systems = nbig < 0 ? nsys : nbig;
+	return FS_OK;
+}
+
+extern "C" FS_API int fs_batch_format(fs_ctx h, fs_csr Ah, int nsys, const int64_t *sys_offsets,
+                                      int *format) {
+	Ctx *ctx = reinterpret_cast<Ctx *>(h);
+	Csr *A = reinterpret_cast<Csr *>(Ah);
+	if (!ok_ctx(ctx) || !ok_csr(A) || !sys_offsets || !format || nsys < 1)
+		return FS_ERR_BAD_HANDLE;
+	std::vector<int64_t> off(sys_offsets, sys_offsets + nsys + 1);
+	auto it = g_plans.find(std::make_pair((const Csr *)A, off));
+	if (it == g_plans.end())
+		return set_err(ctx, FS_ERR_INVALID_ARG, "no batched solve has run on this partition");
+	*format = it->second.grid == 1 ? FS_BATCH_GRID : FS_BATCH_CSR;
 	return FS_OK;
 }

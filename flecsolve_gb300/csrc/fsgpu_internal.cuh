@@ -72,6 +72,8 @@ constexpr int kMaxSym = 4;      // positive column offsets of the symmetric stor
 
 struct FvmOp;
 void destroy_fvm(FvmOp *op);
+struct Csr;
+void destroy_batch_plans(const Csr *A);
 
 struct Csr {
 	int magic = kMagicCsr;
@@ -82,6 +84,7 @@ struct Csr {
 	double *val = nullptr;     // nnz (padded)
 	float *val32 = nullptr;    // float copy, built on first use
 	bool val32_valid = false;
+	unsigned values_gen = 0;   // advanced whenever the values change
 	int *blk = nullptr;        // row blocks, nblk + 1
 	int4 *blkinfo = nullptr;   // per block {r0, r1, rowptr[r0], rowptr[r1]}
 	int nblk = 0;

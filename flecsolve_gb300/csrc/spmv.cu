@@ -270,6 +270,7 @@ int ensure_dinv(Csr *A) {
 }
 
 void invalidate_values(Csr *A) {
+	A->values_gen++;
 	A->val32_valid = false;
 	A->dinv_valid = false;
 	A->t_vals_valid = false;
@@ -887,6 +888,7 @@ FS_API int fs_csr_destroy(fs_csr h) {
 	if (!ok_csr(A))
 		return FS_ERR_BAD_HANDLE;
 	cudaStreamSynchronize(A->ctx->stream);
+	destroy_batch_plans(A);
 	for (void *p : {(void *)A->rowptr, (void *)A->col, (void *)A->val, (void *)A->val32,
 	                (void *)A->blk, (void *)A->blkinfo, (void *)A->dinv, (void *)A->dinv32,
 	                (void *)A->pid, (void *)A->ptab, (void *)A->pwb, (void *)A->plen, (void *)A->pslot, (void *)A->pinv,

@@ -463,6 +463,15 @@ FS_API int fs_batch_tuning(fs_ctx ctx, fs_csr A, int nsys, const int64_t *sys_of
                            int *cluster_size, int *threads);
 FS_API int fs_batch_schedule(fs_ctx ctx, fs_csr A, int nsys, const int64_t *sys_offsets,
                              int *cluster_size, int *threads, int *cluster_systems);
+/* The storage the batched kernel's row sums read for this partition, checked
+ * on the first solve after the values change: FS_BATCH_GRID when every
+ * system is a 5-point operator on a square s x s grid (rows hold exactly
+ * their in-grid neighbours, columns sorted) whose lower entries equal their
+ * partners bit for bit -- the diagonal and two upper diagonals are read,
+ * no column ids, with the CSR row loop's bits -- else FS_BATCH_CSR. */
+#define FS_BATCH_CSR 0
+#define FS_BATCH_GRID 1
+FS_API int fs_batch_format(fs_ctx ctx, fs_csr A, int nsys, const int64_t *sys_offsets, int *format);
 /* the same solve with an explicit schedule: the cluster_systems largest
  * systems own a cluster of cluster_size CTAs, every other system one CTA
  * (cluster_size of them per cluster); sizes must be given */

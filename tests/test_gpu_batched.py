@@ -46,6 +46,66 @@ def test_batch_cg_each_system(ctx, batch, cluster, threads, cluster_systems):
         assert (c2, t2) == (c, t) and 1 <= nb <= len(infos)
 
 
+def _extend(A, off, b, M, bm):
+    """The batch (A, off, b) with one more system M (rhs bm) at the end."""
+    rp = np.concatenate([A.rowptr, A.rowptr[-1] + M.rowptr[1:]])
+    col = np.concatenate([A.col, M.col + A.nrows])
+    val = np.concatenate([A.val, M.val])
+    n = A.nrows + M.nrows
+    return (P.CSR(n, n, rp, col, val, "block-diagonal"), np.append(off, n),
+            np.concatenate([b, bm]))
+
+
+def test_batch_grid_storage_matches_csr(ctx, batch):
+    """A batch of square 2-D grids runs on the grid-stencil storage; the
+    same systems with one non-grid system appended (a 27-row 3-D Laplacian)
+    run on the column ids.  With one CTA per system the arithmetic of each
+    system is independent of the rest of the batch, so the two paths must
+    agree bit for bit, iteration counts included."""
+    A, off, b, sides = batch
+    M, _ = P.workload("laplace3d-3")
+    A2, off2, b2 = _extend(A, off, b, M, P.uniform(77, M.nrows))
+    out = []
+    for Am, om, bm in ((A, off, b), (A2, off2, b2)):
+        dA = fs.CSR(ctx, Am)
+        vb, vx = fs.Vector(ctx, bm), fs.Vector(ctx, Am.nrows)
+        infos = fs.batch_cg(dA, om, vb, vx, maxiter=4000, rtol=1e-8, cluster=1, threads=256,
+                            cluster_systems=0)
+        out.append((fs.batch_format(dA, om), infos, vx.numpy()))
+    assert out[0][0] == "grid" and out[1][0] == "csr"
+    n = A.nrows
+    assert np.array_equal(out[0][2], out[1][2][:n])
+    for k in range(len(off) - 1):
+        assert out[0][1][k].iters == out[1][1][k].iters, k
+        assert out[0][1][k].res_norm_final == out[1][1][k].res_norm_final, k
+    assert out[1][1][-1].status == "converged_rtol"
+
+
+def test_batch_grid_storage_follows_values(ctx, batch):
+    """The storage is re-checked when the values change: one lower entry
+    moved by one ulp (no longer equal to its partner) sends the batch to the
+    column ids, the original values bring the grid storage back, and both
+    solves converge."""
+    A, off, b, sides = batch
+    dA = fs.CSR(ctx, A)
+    vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
+    kw = dict(maxiter=4000, rtol=1e-8, cluster=1, threads=256, cluster_systems=0)
+    fs.batch_cg(dA, off, vb, vx, **kw)
+    assert fs.batch_format(dA, off) == "grid"
+    val = A.val.copy()
+    r = int(off[3]) + sides[3] + 1  # an interior row of system 3
+    k = next(q for q in range(A.rowptr[r], A.rowptr[r + 1]) if A.col[q] == r - 1)
+    val[k] = np.nextafter(val[k], np.inf)
+    dA.update_values(val)
+    infos = fs.batch_cg(dA, off, vb, vx, **kw)
+    assert fs.batch_format(dA, off) == "csr"
+    assert all(i.status == "converged_rtol" for i in infos)
+    dA.update_values(A.val)
+    infos = fs.batch_cg(dA, off, vb, vx, **kw)
+    assert fs.batch_format(dA, off) == "grid"
+    assert all(i.status == "converged_rtol" for i in infos)
+
+
 def test_batch_rejects_coupled_systems(ctx):
     A, _ = P.workload("poisson2d-10")
     dA = fs.CSR(ctx, A)
