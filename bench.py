@@ -541,15 +541,18 @@ def run_suite(args):
         ctx.sync()
         out["convdiff3d-192-mixed-gmres-60"] = {"iters": info.iters, "status": info.status}
     if asked("batched-profile"):
-        # profiling: 64 systems of side 96..160 in one launch, cluster 2 x 512
-        # threads (no autotuning launches)
-        A, off, b, _ = P.batch_diffusion2d(nsys=64, side_lo=96, side_hi=160)
+        # profiling: 128 systems of side 96..200 in one launch (about 0.3 GB
+        # of vectors and coefficients, more than L2), cluster 2 x 256 threads
+        # (no autotuning launches)
+        A, off, b, _ = P.batch_diffusion2d(nsys=128, side_lo=96, side_hi=200)
         dA = fs.CSR(ctx, A)
         vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
-        infos = fs.batch_cg(dA, off, vb, vx, maxiter=20000, rtol=1e-8, cluster=2, threads=512)
+        infos = fs.batch_cg(dA, off, vb, vx, maxiter=20000, rtol=1e-8, cluster=2, threads=256)
         ctx.sync()
-        out["batch64-diffusion2d-96-160"] = {"rows": A.nrows, "nnz": A.nnz,
-                                             "iters_sum": int(sum(i.iters for i in infos))}
+        out["batch128-diffusion2d-96-200"] = {
+            "rows": A.nrows, "nnz": A.nnz, "storage": fs.batch_format(dA, off),
+            "iters_sum": int(sum(i.iters for i in infos)),
+            "row_iterations": sum(int(off[k + 1] - off[k]) * infos[k].iters for k in range(len(infos)))}
     if want("blockcg-mixed"):
         # the mixed block solve alone (profiling): 16 right-hand sides of the
         # 96^3 Laplacian, one warm-up and one timed solve
