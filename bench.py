@@ -166,18 +166,27 @@ def gmres_solve_bytes(nrows, nnz, coding, nblk, iters, restarts, m=30, ortho="cg
     orthogonalisation -- staged CGS2: three passes reading v and the kp1
     vectors, the last writing V_k+1 = (3 (kp1 + 1) + 1) N s_b; MGS: kp1 + 1
     passes reading v, kp1 of them writing it, 2 kp1 basis reads, then the
-    normalisation (read v, write V_k+1) = (4 kp1 + 3) N s_b.  Per cycle end
-    the FP64 correction (kp1 = m basis vectors, D^-1, x read and written),
-    the FP64 residual SpMV (b read, r written) and basis_0 (read r, write
-    V_0)."""
+    normalisation (read v, write V_k+1) = (4 kp1 + 3) N s_b; delayed CGS2:
+    two passes reading v and the kp1 vectors, the second writing q_k (k > 0)
+    and u_k+1 = (2 (kp1 + 1) + 2) N s_b, and per full cycle one pass of dots
+    reading u_m and the m + 1 vectors.  Per cycle end the FP64 correction
+    (kp1 = m basis vectors, D^-1, x read and written), the FP64 residual SpMV
+    (b read, r written) and basis_0 (read r, write V_0)."""
     sb, n = basis_bytes, nrows
     total = 0
     spmv = spmv_bytes(n, nnz, sb, coding, nblk) + n * sb
     for it in range(iters):
         kp1 = it % m + 1
-        ortho_b = (3 * (kp1 + 1) + 1) if ortho == "cgs2" else (4 * kp1 + 3)
+        if ortho == "cgs2":
+            ortho_b = 3 * (kp1 + 1) + 1
+        elif ortho == "dcgs2":
+            ortho_b = 2 * (kp1 + 1) + (2 if kp1 > 1 else 1)
+        else:
+            ortho_b = 4 * kp1 + 3
         total += spmv + ortho_b * n * sb
     cycle = (m * sb + 8 + 16) * n + spmv_bytes(n, nnz, 8, coding, nblk) + 16 * n + (8 + sb) * n
+    if ortho == "dcgs2":
+        total += restarts * (m + 2) * n * sb
     return total + (restarts + 1) * cycle
 
 
@@ -436,8 +445,8 @@ def run_suite(args):
                          "status": info.status, "true_relres": _relres(S, b, vx.numpy())}
             if name.startswith("gmres") and "max_krylov_dim" in kw:
                 # bandwidth bound of the whole solve (algorithmic bytes / HBM peak)
-                mixed = name.endswith("mixed")
-                ortho = kw.get("ortho", "cgs2" if mixed else "mgs")
+                mixed = "mixed" in name
+                ortho = kw.get("ortho", "dcgs2" if mixed else "mgs")
                 nbytes = gmres_solve_bytes(A.nrows, A.nnz, dA.index_coding(), dA.nblk(), info.iters,
                                            info.restarts, kw["max_krylov_dim"], ortho,
                                            4 if mixed else 8)
@@ -459,7 +468,9 @@ def run_suite(args):
             ("bicgstab", fs.bicgstab, {}), ("bicgstab_mixed", fs.mixed_bicgstab, {}),
             ("gmres30_mgs", fs.gmres, dict(g30, ortho="mgs")),
             ("gmres30_cgs2", fs.gmres, dict(g30, ortho="cgs2")),
-            ("gmres30_mixed", fs.mixed_gmres, g30)])
+            ("gmres30_dcgs2", fs.gmres, dict(g30, ortho="dcgs2")),
+            ("gmres30_mixed", fs.mixed_gmres, g30),
+            ("gmres30_mixed_cgs2", fs.mixed_gmres, dict(g30, ortho="cgs2"))])
         ref = json.loads((ROOT / "tests" / "golden" / "full_size.json").read_text()).get("convdiff3d-192", {})
         out["convdiff3d-192"]["reference_iters"] = {k: v["iters"] for k, v in ref.items()}
     if want("batched"):

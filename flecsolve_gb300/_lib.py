@@ -29,7 +29,7 @@ BC_NONE, BC_DIRICHLET, BC_NEUMANN = 0, 1, 2
 CG, BICGSTAB, GMRES, CG_MIXED, BICGSTAB_MIXED, GMRES_MIXED, FCG, CG_PIPELINED = 0, 1, 2, 3, 4, 5, 6, 7
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_DIAG, PRECOND_CSR, PRECOND_SOLVER = 0, 1, 2, 3, 4
 LEFT, RIGHT = 0, 1
-ORTHO_CGS2, ORTHO_MGS, ORTHO_AUTO = 0, 1, 2
+ORTHO_CGS2, ORTHO_MGS, ORTHO_AUTO, ORTHO_DCGS2 = 0, 1, 2, 3
 REFINE_RESTART, REFINE_RELIABLE = 0, 1
 SPMV_FMA, SPMV_EXACT = 0, 1
 

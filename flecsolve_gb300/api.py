@@ -569,7 +569,8 @@ def _settings(method, maxiter, rtol, atol, use_zero_guess, **kw):
         if k == "pre_side":
             v = _lib.LEFT if v in ("left", _lib.LEFT) else _lib.RIGHT
         elif k == "ortho":
-            v = {"mgs": _lib.ORTHO_MGS, "cgs2": _lib.ORTHO_CGS2, "auto": _lib.ORTHO_AUTO}.get(v, v)
+            v = {"mgs": _lib.ORTHO_MGS, "cgs2": _lib.ORTHO_CGS2, "auto": _lib.ORTHO_AUTO,
+                 "dcgs2": _lib.ORTHO_DCGS2}.get(v, v)
         elif k == "refine":
             v = _lib.REFINE_RELIABLE if v in ("reliable", _lib.REFINE_RELIABLE) else _lib.REFINE_RESTART
         setattr(s, k, v)

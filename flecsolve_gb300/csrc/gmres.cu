@@ -181,6 +181,84 @@ __device__ void finish_step(GmState *g, KState *st, double *hist) {
 	}
 }
 
+// finish_step by the whole CTA: the column H(0..k+1, k) and the k earlier
+// rotations are staged in shared memory (`col`, 3 (k + 2) doubles) by all
+// threads, thread 0 runs the same rotations and tests on them, and the
+// column is written back by all threads -- the serial chain of global
+// loads and stores of the one-thread form costs a few microseconds per
+// rotation at large k.  Every thread of the CTA calls it.
+__device__ void finish_step_cta(GmState *g, KState *st, double *hist, double *col) {
+	const int k = g->k, ld = g->ld, tid = threadIdx.x;
+	double *cs = col + (k + 2), *sn = cs + (k + 2);
+	for (int i = tid; i <= k + 1; i += blockDim.x)
+		col[i] = g->H[i + ld * k];
+	for (int i = tid; i < k; i += blockDim.x) {
+		cs[i] = g->cs[i];
+		sn[i] = g->sn[i];
+	}
+	__syncthreads();
+	if (tid == 0) {
+		// the rotations of apply_givens / compute_givens, on the staged column
+		for (int i = 0; i < k; i++) {
+			const double x = col[i], y = col[i + 1], c = cs[i], s = sn[i];
+			col[i] = c * x + s * y;
+			col[i + 1] = -s * x + c * y;
+		}
+		const double vnorm = g->vnorm;
+		if (vnorm != 0.0) {
+			const double f = col[k], gg = col[k + 1];
+			double c, s;
+			if (gg == 0.0) {
+				c = 1.0;
+				s = 0.0;
+			}
+			else if (f == 0.0) {
+				c = 0.0;
+				s = (gg < 0.0) ? -1.0 : 1.0;
+			}
+			else {
+				double r = sqrt(f * f + gg * gg);
+				r = 1.0 / r;
+				c = fabs(f) * r;
+				s = copysign(gg * r, f);
+			}
+			g->cs[k] = c;
+			g->sn[k] = s;
+			col[k] = c * f + s * gg;
+			col[k + 1] = 0.0;
+			const double x = g->dw[k];
+			g->dw[k] = c * x;
+			g->dw[k + 1] = -s * x;
+		}
+		const double res = fabs(g->dw[k + 1]);
+		g->k = k + 1;
+		const int it = st->iter + 1;
+		st->iter = it;
+		st->res = res;
+		if (st->nhist < st->hist_cap)
+			hist[st->nhist] = res;
+		st->nhist += 1;
+		if (!isfinite(res))
+			st->flags |= KF_NONFINITE;
+		if (res < st->tol) {
+			st->done = 1;
+			st->status = FS_CONVERGED_RTOL;
+			st->info_iters = it;
+		}
+		else if (it >= st->maxiter || (st->flags & KF_NONFINITE)) {
+			st->done = 1;
+			st->status = FS_DIVERGED_ITERS;
+		}
+		else if (g->k == g->m) {
+			st->flags |= KF_RESTART;
+		}
+	}
+	__syncthreads();
+	for (int i = tid; i <= k + 1; i += blockDim.x)
+		g->H[i + ld * k] = col[i];
+	__syncthreads();
+}
+
 // gmres.hh:333-348, nr = k - 1
 __device__ void back_solve(GmState *g) {
 	const int nr = g->k - 1;
@@ -619,7 +697,8 @@ int gm_step(Solver *s, int k) {
 	else
 		FS_TRY((launch_spmv<T, false, false>(ctx, s->A, B.vals, Vk, nullptr,
 		                                     EpiScaleStore<T>{B.v, right ? nullptr : B.dinv, s->st})));
-	const bool mgs = s->set.ortho == FS_ORTHO_MGS || (s->set.ortho == FS_ORTHO_AUTO && sizeof(T) == 8);
+	const bool mgs = !s->gm_delayed && (s->set.ortho == FS_ORTHO_MGS ||
+	                                    (s->set.ortho == FS_ORTHO_AUTO && sizeof(T) == 8));
 	if (mgs) {
 		for (int j = 0; j <= kp1; ++j) {
 			k_gm_mgs<T><<<G, kT, 0, ctx->stream>>>(n, B.V, ld, j, kp1, B.v, g, s->st, s->part,
@@ -627,10 +706,20 @@ int gm_step(Solver *s, int k) {
 			FS_TRY(check_launch(ctx, "gmres mgs"));
 		}
 	}
+	else if (s->gm_delayed) {
+		// delayed CGS2: column k holds u_k; pass 4 finishes column k - 1 and
+		// pass 5 writes q_k over u_k and u_{k+1} into column k + 1
+		OrthoArgs<T> oa{B.v, B.V + (size_t)kp1 * ld, B.V + (size_t)k * ld, n, kp1,
+		                staged_stages(kp1), staged_stride(kp1), g, s->st, s->part, s->counter,
+		                s->hist, ctx->dev_err};
+		const BasisMaps &map = *reinterpret_cast<const BasisMaps *>(s->gm_map);
+		FS_TRY((staged_pass<T, 4>(ctx, oa, map)));
+		return staged_pass<T, 5>(ctx, oa, map);
+	}
 	else if (kp1 <= kStagedMax && s->gm_map_base == (const void *)B.V) {
 		// staged CGS2: three passes, the last one writes V_{k+1}
-		OrthoArgs<T> oa{B.v, B.V + (size_t)kp1 * ld, n, kp1, staged_stages(kp1), staged_stride(kp1),
-		                g, s->st, s->part, s->counter, s->hist, ctx->dev_err};
+		OrthoArgs<T> oa{B.v, B.V + (size_t)kp1 * ld, nullptr, n, kp1, staged_stages(kp1),
+		                staged_stride(kp1), g, s->st, s->part, s->counter, s->hist, ctx->dev_err};
 		const BasisMaps &map = *reinterpret_cast<const BasisMaps *>(s->gm_map);
 		FS_TRY((staged_pass<T, 1>(ctx, oa, map)));
 		FS_TRY((staged_pass<T, 2>(ctx, oa, map)));
@@ -679,6 +768,17 @@ int gm_body(Solver *s, void *a) {
 	const int64_t n = s->n;
 	for (int j = ga->first; j <= ga->last; ++j)
 		FS_TRY(gm_step<T>(s, j));
+	if (ga->with_restart && s->gm_delayed) {
+		// delayed CGS2: the cycle's last column is finished from u_m
+		// (column m = last + 1) by one more pass of dots
+		const int kp1 = ga->last + 2;
+		const int64_t ld = gm_ld(s);
+		T *V = (T *)s->basis;
+		OrthoArgs<T> oa{V + (size_t)(kp1 - 1) * ld, nullptr, nullptr, n, kp1, staged_stages(kp1),
+		                staged_stride(kp1), gm_state(s), s->st, s->part, s->counter, s->hist,
+		                ctx->dev_err};
+		FS_TRY((staged_pass<T, 6>(ctx, oa, *reinterpret_cast<const BasisMaps *>(s->gm_map))));
+	}
 	if (ga->with_restart) {
 		const bool right = s->set.pre_side != FS_LEFT;
 		if (ga->mixed) {
@@ -751,6 +851,14 @@ int gmres_run(Solver *s, Vec *b, Vec *x, fs_solve_info *info, bool mixed) {
 			}
 		}
 	}
+	// the delayed CGS2 needs the staged passes for every column of a cycle,
+	// including the last pass over m + 1 columns; with a diagnostic on the
+	// FP64 path (one graph a step, the restart tail in the last step's graph)
+	// CGS2 runs, so that a stop by the diagnostic leaves x at that step
+	const bool want_delayed =
+		s->set.ortho == FS_ORTHO_DCGS2 || (s->set.ortho == FS_ORTHO_AUTO && sizeof(T) == 4);
+	s->gm_delayed = want_delayed && s->gm_map_base == s->basis && cols <= kStagedMax &&
+	                (mixed || !s->diag);
 	FS_CUDA_TRY(ctx, cudaMemsetAsync(s->hdev, 0, sizeof(GmState), ctx->stream));
 	FS_TRY(solver_hist(s, std::max(1, maxiter)));
 	{
@@ -773,7 +881,7 @@ int gmres_run(Solver *s, Vec *b, Vec *x, fs_solve_info *info, bool mixed) {
 	FS_TRY(check_launch(ctx, "gmres start"));
 	FS_TRY(read_state(s));
 	const int steps = std::min(m, maxiter);
-	const int tag = (mixed ? 1 : 0) + 2 * (int)sizeof(T);
+	const int tag = (mixed ? 1 : 0) + 2 * (int)sizeof(T) + (s->gm_delayed ? 20 : 0);
 	int user_stop = 0;
 	int64_t seen = 0;
 	while (!s->hst->done && !user_stop) {
@@ -785,15 +893,19 @@ int gmres_run(Solver *s, Vec *b, Vec *x, fs_solve_info *info, bool mixed) {
 				FS_TRY(graph_run(s, GraphKey{b->d, x->d, 300000 + 2 * j + (j == steps - 1) + 1000 * tag},
 				                 gm_body<T>, &a));
 				FS_TRY(read_state(s));
-				if (s->hst->nhist > seen) {
-					double hv = 0;
-					FS_CUDA_TRY(ctx, cudaMemcpy(&hv, s->hist + (s->hst->nhist - 1), sizeof(double),
+				// one call per new estimate
+				const int64_t upto = std::min<int64_t>(s->hst->nhist, s->hist_cap);
+				if (upto > seen) {
+					double hv[2] = {0, 0};
+					const int64_t cnt = std::min<int64_t>(upto - seen, 2);
+					FS_CUDA_TRY(ctx, cudaMemcpy(hv, s->hist + (upto - cnt), cnt * sizeof(double),
 					                            cudaMemcpyDeviceToHost));
-					seen = s->hst->nhist;
-					if (s->diag(s->diag_user, reinterpret_cast<fs_vec>(x), hv)) {
-						user_stop = (int)seen;
+					for (int64_t e = 0; e < cnt && !user_stop; ++e)
+						if (s->diag(s->diag_user, reinterpret_cast<fs_vec>(x), hv[e]))
+							user_stop = (int)(upto - cnt + e + 1);
+					seen = upto;
+					if (user_stop)
 						break;
-					}
 				}
 			}
 		}

@@ -11,6 +11,27 @@
 //           ||v''|| == 0: the normalisation of gmres.hh:156-162 folded into
 //           the last update; skipped once the step stopped or restarts.
 //
+// Delayed CGS2 (Swirydowicz, Langou, Ananthan, Yang, Thomas, "Low
+// synchronization Gram-Schmidt and generalized minimal residual algorithms",
+// NLAA 28, 2021; the DCGS2 Arnoldi of Bielich, Langou, Thomas, Swirydowicz,
+// Yamazaki, Boman, Parallel Computing 112, 2022): the reorthogonalisation of
+// a vector is deferred to the next step, where it shares the pass of that
+// step's projection, so a step costs two passes over the basis, not three.
+// Column k holds u_k, the once-orthogonalised, unnormalised candidate for
+// q_k; the SpMV gives w = M u_k.  With Q = q_0..q_{k-1}:
+//   pass 4: t = Q^T w, gamma = u_k^T w, s = Q^T u_k, alpha = u_k^T u_k; the
+//           last CTA forms r = sqrt(alpha - s^T s), finishes Hessenberg
+//           column k - 1 (its tentative entries + s, and r below them:
+//           M q_{k-1} = Q (h_{k-1} + s) + r q_k), then tau = q_k^T w =
+//           (gamma - s^T t) / r and the tentative column k,
+//           h_k = Q_k^T M q_k = ([t; tau] - H s) / r, from the Arnoldi
+//           relation M Q = Q_k H;
+//   pass 5: q_k = (u_k - Q s) / r over column k, and the next candidate
+//           u_{k+1} = (w - Q t - tau q_k) / r into column k + 1;
+//   pass 6: at the end of a cycle, s = Q^T u_m and alpha finish column m - 1.
+// Step 0 starts from the normalised q_0 (r = 1, no s).  The convergence test
+// of column k - 1 runs in step k's pass 4, one SpMV later than in CGS2.
+//
 // Data movement.  Each pass streams tiles of v and of every basis vector into
 // a ring of shared-memory stages, issued by one producer lane as soon as the
 // consumers have released the stage on its `empty` mbarrier and completing on
@@ -50,6 +71,8 @@ constexpr int kOSlot = kOT * 8;          // bytes of one vector's tile
 constexpr int kOMaps = 4;                // box heights 8, 4, 2, 1
 constexpr size_t kOSmemBudget = 200 * 1024;
 static_assert(kStagedMax + 1 <= kPartPerBlock, "pass 2 writes kp1 + 1 partials per CTA");
+static_assert(2 * kStagedMax <= 8 * kPartPerBlock, "pass 4 writes 2 kp1 partials per CTA");
+static_assert(kStagedMax + 1 <= kGmDelayedCols, "delayed CGS2 Hessenberg columns");
 
 // the tensor maps of one basis: box heights 8, 4, 2 and 1 columns
 struct BasisMaps {
@@ -58,8 +81,9 @@ struct BasisMaps {
 
 template<class T>
 struct OrthoArgs {
-	const T *v;       // the new vector (A z or D^-1 A V_k)
-	T *out;           // pass 3: V_{k+1}
+	const T *v;       // the new vector (A z or D^-1 A V_k); pass 6: u_m
+	T *out;           // pass 3: V_{k+1}; pass 5: u_{k+1}
+	T *outq;          // pass 5: q_k (column k)
 	int64_t n;
 	int kp1;
 	int stages;
@@ -192,9 +216,9 @@ k_gm_staged(OrthoArgs<T> a, const __grid_constant__ BasisMaps maps) {
 	unsigned char *smem_raw = reinterpret_cast<unsigned char *>(
 		(reinterpret_cast<uintptr_t>(smem_dyn) + 127) & ~(uintptr_t)127);
 	__shared__ unsigned long long full[kOMaxStages], empty[kOMaxStages];
-	__shared__ T hs[kStagedMax + 1];
+	__shared__ T hs[kStagedMax + 1], ht[kStagedMax + 1];
 	__shared__ double sh[32 * kOWarps];
-	__shared__ double folded[32];
+	__shared__ double folded[64];
 	__shared__ int abort_flag;
 	if (stopped(a.st))
 		return;
@@ -221,12 +245,25 @@ k_gm_staged(OrthoArgs<T> a, const __grid_constant__ BasisMaps maps) {
 			hs[j] = (T)(a.g->h1[j] + a.g->h2[j]);
 		vn = a.g->vnorm;
 	}
+	double tau = 0.0;
+	if constexpr (PASS == 5) {
+		for (int j = tid; j < kp1 - 1; j += blockDim.x) {
+			hs[j] = (T)a.g->h1[j];
+			ht[j] = (T)a.g->h2[j];
+		}
+		vn = a.g->dg_r;
+		tau = a.g->dg_tau;
+	}
 	__syncthreads();
 	volatile int *abort_v = &abort_flag;
-	E acc[NA];
+	constexpr int NA2 = PASS == 4 ? NA : 1;
+	E acc[NA], acc2[NA2];
 #pragma unroll
 	for (int j = 0; j < NA; ++j)
 		acc[j] = EL::zero();
+#pragma unroll
+	for (int j = 0; j < NA2; ++j)
+		acc2[j] = EL::zero();
 	E accn = EL::zero();
 	if (warp == kOCons) {
 		// producer: one lane issues every copy of a tile
@@ -286,11 +323,40 @@ k_gm_staged(OrthoArgs<T> a, const __grid_constant__ BasisMaps maps) {
 			const int64_t e = ((int64_t)blockIdx.x + (int64_t)i * gridDim.x) * kOT + tid;
 			if (e < nelem) {
 				const E vi = sv[tid];
-				if constexpr (PASS == 1) {
+				if constexpr (PASS == 1 || PASS == 6) {
 #pragma unroll
 					for (int j = 0; j < NA; ++j)
 						if (j < kp1)
 							acc[j] = EL::fma(vi, sv[(j + 1) * kOT + tid], acc[j]);
+				}
+				else if constexpr (PASS == 4) {
+					// column k = kp1 - 1 is u_k: acc = [Q u_k]^T w, acc2 = [Q u_k]^T u_k
+					const E ui = sv[kp1 * kOT + tid];
+#pragma unroll
+					for (int j = 0; j < NA; ++j)
+						if (j < kp1) {
+							const E vj = sv[(j + 1) * kOT + tid];
+							acc[j] = EL::fma(vi, vj, acc[j]);
+							acc2[j] = EL::fma(ui, vj, acc2[j]);
+						}
+				}
+				else if constexpr (PASS == 5) {
+					const int k = kp1 - 1;
+					const E ui = sv[kp1 * kOT + tid];
+					E q = ui, u1 = vi;
+#pragma unroll
+					for (int j = 0; j < NA; ++j)
+						if (j < k) {
+							const E vj = sv[(j + 1) * kOT + tid];
+							q = EL::fma(EL::splat(-hs[j]), vj, q);
+							u1 = EL::fma(EL::splat(-ht[j]), vj, u1);
+						}
+					if (k > 0) {
+						q = EL::mul(q, inv);
+						EL::store(a.outq, e, a.n, q);
+					}
+					u1 = EL::fma(EL::splat((T)-tau), q, u1);
+					EL::store(a.out, e, a.n, EL::mul(u1, inv));
 				}
 				else {
 					E w = vi;
@@ -317,6 +383,81 @@ k_gm_staged(OrthoArgs<T> a, const __grid_constant__ BasisMaps maps) {
 				break;
 		}
 	}
+	if constexpr (PASS == 4 || PASS == 6) {
+		// pass 4: t and gamma (kp1 values), then s and alpha (kp1 values)
+		// in a second block of partials; pass 6: s and alpha
+		double vals[NA];
+#pragma unroll
+		for (int j = 0; j < NA; ++j)
+			vals[j] = j < kp1 ? EL::sum(acc[j]) : 0.0;
+		staged_block_sum<NA>(vals, kp1, a.part, sh);
+		double *part2 = a.part + (size_t)gridDim.x * kp1;
+		if constexpr (PASS == 4) {
+#pragma unroll
+			for (int j = 0; j < NA; ++j)
+				vals[j] = j < kp1 ? EL::sum(acc2[j]) : 0.0;
+			__syncthreads();  // sh of the first sum is read
+			staged_block_sum<NA>(vals, kp1, part2, sh);
+		}
+		if (last_block(a.counter)) {
+			staged_fold(a.part, kp1, folded, sh);
+			if constexpr (PASS == 4)
+				staged_fold(part2, kp1, folded + 32, sh);
+			// the scalar work, spread over the CTA where it is independent:
+			// every thread forms r and tau from shared memory; thread j
+			// finishes H(j, k - 1), thread i forms the tentative H(i, k)
+			GmState *g = a.g;
+			const int k = kp1 - 1, ldh = g->ld;
+			const double *s = PASS == 4 ? folded + 32 : folded;
+			const double *t = folded;
+			double ss = 0.0, st_ = 0.0;
+			for (int j = 0; j < k; ++j) {
+				ss += s[j] * s[j];
+				if constexpr (PASS == 4)
+					st_ += s[j] * t[j];
+			}
+			const double r = k > 0 ? sqrt(fmax(s[k] - ss, 0.0)) : 1.0;
+			const double rinv = r != 0.0 ? 1.0 / r : 1.0;
+			if (k > 0) {
+				// column k - 1 is final: its tentative entries + s, r below
+				const int c = k - 1;
+				if (tid < k) {
+					const double hv = g->Hr[tid + kGmDelayedCols * c] + s[tid];
+					g->Hr[tid + kGmDelayedCols * c] = hv;
+					g->H[tid + ldh * c] = hv;
+				}
+				if (tid == 0) {
+					g->Hr[k + kGmDelayedCols * c] = r;
+					g->H[k + ldh * c] = r;
+					g->vnorm = r;
+				}
+				__syncthreads();
+				finish_step_cta(g, a.st, a.hist, sh);
+			}
+			if constexpr (PASS == 4) {
+				const double tau_k = (t[k] - st_) * rinv;
+				// tentative column k: ([t; tau] - H s) / r over rows 0..k
+				if (tid <= k) {
+					const int i = tid;
+					double hs_i = 0.0;
+#pragma unroll 8
+					for (int j = i > 0 ? i - 1 : 0; j < k; ++j)
+						hs_i += g->Hr[i + kGmDelayedCols * j] * s[j];
+					g->Hr[i + kGmDelayedCols * k] = ((i < k ? t[i] : tau_k) - hs_i) * rinv;
+				}
+				if (tid < k) {
+					g->h1[tid] = s[tid];
+					g->h2[tid] = t[tid];
+				}
+				if (tid == 0) {
+					g->dg_tau = tau_k;
+					g->dg_r = r;
+				}
+			}
+			if (tid == 0)
+				*a.counter = 0;
+		}
+	}
 	if constexpr (PASS == 1 || PASS == 2) {
 		// pass 2 puts ||v'||^2 right after the kp1 dots
 		constexpr int NS = PASS == 2 ? NA + 1 : NA;
@@ -330,27 +471,30 @@ k_gm_staged(OrthoArgs<T> a, const __grid_constant__ BasisMaps maps) {
 		staged_block_sum<NS>(vals, nv, a.part, sh);
 		if (last_block(a.counter)) {
 			staged_fold(a.part, nv, folded, sh);
-			if (tid == 0) {
-				GmState *g = a.g;
-				if constexpr (PASS == 1) {
-					for (int j = 0; j < kp1; ++j)
-						g->h1[j] = folded[j];
+			GmState *g = a.g;
+			if constexpr (PASS == 1) {
+				if (tid < kp1)
+					g->h1[tid] = folded[tid];
+			}
+			else {
+				const int k = g->k, ldh = g->ld;
+				if (tid < kp1) {
+					g->h2[tid] = folded[tid];
+					g->H[tid + ldh * k] = g->h1[tid] + folded[tid];
 				}
-				else {
-					const int k = g->k, ldh = g->ld;
+				if (tid == 0) {
 					double s2 = 0.0;
-					for (int j = 0; j < kp1; ++j) {
-						g->h2[j] = folded[j];
-						g->H[j + ldh * k] = g->h1[j] + folded[j];
+					for (int j = 0; j < kp1; ++j)
 						s2 += folded[j] * folded[j];
-					}
 					const double vn2 = sqrt(fmax(folded[kp1] - s2, 0.0));
 					g->H[kp1 + ldh * k] = vn2;
 					g->vnorm = vn2;
-					finish_step(g, a.st, a.hist);
 				}
-				*a.counter = 0;
+				__syncthreads();
+				finish_step_cta(g, a.st, a.hist, sh);
 			}
+			if (tid == 0)
+				*a.counter = 0;
 		}
 	}
 }

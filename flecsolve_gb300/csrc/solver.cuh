@@ -49,11 +49,17 @@ struct KState {
 // GMRES least-squares state (gmres.cu): Hessenberg (column-major, ld = m+1),
 // rotations, right-hand side, back-solve result, the projections of the step
 constexpr int kGmMaxDim = 100;  // gmres.hh:31 krylov_dim_bound
+constexpr int kGmDelayedCols = 32;  // basis columns the delayed CGS2 takes (m <= 30)
 constexpr int kPartPerBlock = 32;  // partial sums per CTA a solver kernel may write
 struct GmState {
 	double H[(kGmMaxDim + 1) * (kGmMaxDim + 1)];
 	double cs[kGmMaxDim + 1], sn[kGmMaxDim + 1], dw[kGmMaxDim + 1], dy[kGmMaxDim + 1];
 	double h1[kGmMaxDim + 1], h2[kGmMaxDim + 1];
+	// delayed CGS2: the Hessenberg columns before the rotations (column k
+	// tentative until step k + 1 adds its reorthogonalisation coefficients)
+	// and the current step's tau and r
+	double Hr[kGmDelayedCols * kGmDelayedCols];
+	double dg_tau, dg_r;
 	double vnorm;  // H(k+1,k) before the rotation
 	int k;         // current Krylov dimension
 	int ld;        // Hessenberg leading dimension (min(m, maxiter) + 1)
@@ -102,6 +108,7 @@ struct Solver {
 	alignas(64) unsigned char gm_map[4 * 128];
 	const void *gm_map_base = nullptr;
 	int gm_map_key[3] = {0, 0, 0};    // element size, columns, n (low 31 bits)
+	bool gm_delayed = false;          // this solve orthogonalises with the delayed CGS2
 	double *hdev = nullptr;           // GMRES: dot results scratch
 	KState *st = nullptr;             // device
 	KState *hst = nullptr;            // pinned mirror

@@ -357,9 +357,16 @@ typedef struct {
 
 enum fs_gmres_side { FS_LEFT = 0, FS_RIGHT = 1 };
 /* GMRES orthogonalisation.  AUTO picks MGS for the FP64 basis (half the FP64
- * multiply-adds of CGS2, and the reference's order) and CGS2 for the FP32
- * basis of FS_GMRES_MIXED (3 reductions per step instead of k + 2). */
-enum fs_gmres_ortho { FS_ORTHO_CGS2 = 0, FS_ORTHO_MGS = 1, FS_ORTHO_AUTO = 2 };
+ * multiply-adds of CGS2, and the reference's order) and DCGS2 (below; CGS2
+ * where DCGS2 cannot run) for the FP32 basis of FS_GMRES_MIXED: 2 passes and
+ * 1 reduction per step instead of the k + 2 of MGS.
+ * DCGS2: CGS2 with each vector's reorthogonalisation delayed to the next
+ * step, where it shares that step's pass of dot products (two passes over
+ * the basis a step instead of three); the convergence test of a step runs
+ * one SpMV later.  It needs the staged passes (m <= 30 and a basis the tensor
+ * unit can address) and, for FS_GMRES, no diagnostic callback; otherwise
+ * CGS2 runs. */
+enum fs_gmres_ortho { FS_ORTHO_CGS2 = 0, FS_ORTHO_MGS = 1, FS_ORTHO_AUTO = 2, FS_ORTHO_DCGS2 = 3 };
 
 enum fs_refine_kind {
 	FS_REFINE_RESTART = 0,  /* outer FP64 residual, inner FP32 PCG restarted */

@@ -209,9 +209,11 @@ def test_convdiff3d_192_gmres30_against_reference(ctx, c3, ortho):
     assert e <= 2.0 * e_ref + 1e-12
 
 
-def test_convdiff3d_192_mixed_gmres30(ctx, c3):
+@pytest.mark.parametrize("ortho", ["auto", "cgs2"])
+def test_convdiff3d_192_mixed_gmres30(ctx, c3, ortho):
+    # auto: the delayed CGS2
     info, x = _solve(ctx, fs.mixed_gmres, c3["dA"], c3["vb"], c3["vx"], max_krylov_dim=30,
-                     restart=True)
+                     restart=True, ortho=ortho)
     assert info.status == "converged_rtol"
     assert info.iters <= 1.2 * FULL["convdiff3d-192"]["gmres"]["iters"] + 30
     assert _relres(c3["S"], c3["b"], x) <= 1e-8

@@ -295,7 +295,7 @@ def _run_gmres(ctx, A, b, x0=None, prec="jacobi", diag=None, **kw):
     return _run(ctx, fs.gmres, A, b, x0, prec, diag, **kw)
 
 
-@pytest.mark.parametrize("ortho", ["cgs2", "mgs"])
+@pytest.mark.parametrize("ortho", ["cgs2", "mgs", "dcgs2"])
 @pytest.mark.parametrize("name", GMRES_CASES)
 def test_gmres_against_reference_fixture(ctx, name, ortho):
     c = META["cases"][name]
@@ -342,16 +342,17 @@ def test_gmres_restart_consistency(ctx):
     assert info.res_norm_final == info_restart.res_norm_final
 
 
-def test_gmres_diagnostic_every_iteration(ctx):
+@pytest.mark.parametrize("ortho", ["auto", "dcgs2"])
+def test_gmres_diagnostic_every_iteration(ctx, ortho):
     A, b = P.workload("convdiff3d-12")
     calls = []
     info, x, _ = _run_gmres(ctx, A, b, diag=lambda xv, r: calls.append(r) or False,
-                            maxiter=500, rtol=1e-8, max_krylov_dim=10, restart=True)
+                            maxiter=500, rtol=1e-8, max_krylov_dim=10, restart=True, ortho=ortho)
     assert info.status == "converged_rtol" and len(calls) == info.iters
     r = O.solve("gmres", A, b, maxiter=500, rtol=1e-8, krylov_dim=10)
     assert abs(info.iters - r.iters) <= ITER_TOL
     info2, _, _ = _run_gmres(ctx, A, b, diag=lambda xv, r: len(calls) > 10**9 or r < 1e3,
-                             maxiter=500, rtol=1e-8, max_krylov_dim=10, restart=True)
+                             maxiter=500, rtol=1e-8, max_krylov_dim=10, restart=True, ortho=ortho)
     assert info2.status == "converged_user" and info2.iters >= 1
 
 
@@ -364,13 +365,15 @@ def test_gmres_validate_rejects_reference_asserts(ctx):
         _run_gmres(ctx, A, b, maxiter=1000, max_krylov_dim=101, restart=True)
 
 
+@pytest.mark.parametrize("ortho", ["auto", "dcgs2"])
 @pytest.mark.parametrize("wl", ["convdiff3d-24", "diffusion3d-20", "convdiff3d-13", "convdiff3d-7"])
-def test_gmres_cgs2_vs_oracle(ctx, wl):
+def test_gmres_cgs2_vs_oracle(ctx, wl, ortho):
     # odd sizes: a last tile of the staged passes that ends inside an element
     # pair (FP32) and a problem smaller than one tile
     A, b = P.workload(wl)
     r = O.solve("gmres", A, b, maxiter=5000, rtol=1e-8, krylov_dim=30)
-    info, x, _ = _run_gmres(ctx, A, b, maxiter=5000, rtol=1e-8, max_krylov_dim=30, restart=True)
+    info, x, _ = _run_gmres(ctx, A, b, maxiter=5000, rtol=1e-8, max_krylov_dim=30, restart=True,
+                            ortho=ortho)
     assert info.status == r.status == "converged_rtol"
     _order_bar("gmres", A, b, info.iters, maxiter=5000, rtol=1e-8, krylov_dim=30)
     _bicgstab_accuracy_bar(A, b, x, r.x)
@@ -390,7 +393,7 @@ def test_mixed_bicgstab(ctx, wl):
     assert info.iters <= 1.3 * r.iters + 5
 
 
-@pytest.mark.parametrize("ortho", ["auto", "mgs"])
+@pytest.mark.parametrize("ortho", ["auto", "mgs", "cgs2", "dcgs2"])
 @pytest.mark.parametrize("wl", ["convdiff3d-24", "diffusion3d-20", "convdiff3d-13", "convdiff3d-7"])
 def test_mixed_gmres(ctx, wl, ortho):
     """FP32 Arnoldi cycles re-anchored on the FP64 residual at every restart:
