@@ -540,17 +540,19 @@ def run_suite(args):
                          "s_per_iteration": sec / max(info.iters, 1),
                          "true_relres": _relres(S, b, vx.numpy())}
         out["cg-variants-diffusion3d-256"] = res
-    if asked("gmres-profile"):
+    for part, ortho in (("gmres-profile", "auto"), ("gmres-profile-cgs2", "cgs2")):
+        if not asked(part):
+            continue
         # profiling: two restart cycles (60 steps) of the mixed GMRES(30) on
-        # the 192^3 convection-diffusion system
+        # the 192^3 convection-diffusion system (auto: the delayed CGS2)
         A, b = P.workload("convdiff3d-192")
         dA = fs.CSR(ctx, A)
         vb, vx = fs.Vector(ctx, b), fs.Vector(ctx, A.nrows)
         slv = fs.mixed_gmres.solver(fs.mixed_gmres.settings(maxiter=60, rtol=1e-8, max_krylov_dim=30,
-                                                            restart=True))(dA, fs.op.jacobi)
+                                                            restart=True, ortho=ortho))(dA, fs.op.jacobi)
         info = slv(vb, vx)
         ctx.sync()
-        out["convdiff3d-192-mixed-gmres-60"] = {"iters": info.iters, "status": info.status}
+        out[f"convdiff3d-192-mixed-gmres-60-{ortho}"] = {"iters": info.iters, "status": info.status}
     if asked("batched-profile"):
         # profiling: 128 systems of side 96..200 in one launch (about 0.3 GB
         # of vectors and coefficients, more than L2), cluster 2 x 256 threads
