@@ -256,14 +256,10 @@ k_gm_staged(OrthoArgs<T> a, const __grid_constant__ BasisMaps maps) {
 	}
 	__syncthreads();
 	volatile int *abort_v = &abort_flag;
-	constexpr int NA2 = PASS == 4 ? NA : 1;
-	E acc[NA], acc2[NA2];
+	E acc[NA];
 #pragma unroll
 	for (int j = 0; j < NA; ++j)
 		acc[j] = EL::zero();
-#pragma unroll
-	for (int j = 0; j < NA2; ++j)
-		acc2[j] = EL::zero();
 	E accn = EL::zero();
 	if (warp == kOCons) {
 		// producer: one lane issues every copy of a tile
@@ -320,25 +316,34 @@ k_gm_staged(OrthoArgs<T> a, const __grid_constant__ BasisMaps maps) {
 				break;
 			}
 			const E *sv = reinterpret_cast<const E *>(smem_raw + (size_t)s * a.stride);
-			const int64_t e = ((int64_t)blockIdx.x + (int64_t)i * gridDim.x) * kOT + tid;
-			if (e < nelem) {
+			const int64_t tile0 = ((int64_t)blockIdx.x + (int64_t)i * gridDim.x) * kOT;
+			const int64_t e = tile0 + tid;
+			if constexpr (PASS == 4) {
+				// the consumers in two halves: warps 0-3 sum w . V_j, warps
+				// 4-7 u_k . V_j (u_k is column k = kp1 - 1), each thread over
+				// elements lt and lt + kOT / 2 of the tile -- one set of
+				// accumulators a thread, as in pass 1
+				const int lt = tid & (kOT / 2 - 1), grp = tid / (kOT / 2);
+				const int xslot = grp == 0 ? 0 : kp1;
+#pragma unroll
+				for (int h = 0; h < 2; ++h) {
+					const int el = lt + h * (kOT / 2);
+					if (tile0 + el < nelem) {
+						const E xv = sv[xslot * kOT + el];
+#pragma unroll
+						for (int j = 0; j < NA; ++j)
+							if (j < kp1)
+								acc[j] = EL::fma(xv, sv[(j + 1) * kOT + el], acc[j]);
+					}
+				}
+			}
+			else if (e < nelem) {
 				const E vi = sv[tid];
 				if constexpr (PASS == 1 || PASS == 6) {
 #pragma unroll
 					for (int j = 0; j < NA; ++j)
 						if (j < kp1)
 							acc[j] = EL::fma(vi, sv[(j + 1) * kOT + tid], acc[j]);
-				}
-				else if constexpr (PASS == 4) {
-					// column k = kp1 - 1 is u_k: acc = [Q u_k]^T w, acc2 = [Q u_k]^T u_k
-					const E ui = sv[kp1 * kOT + tid];
-#pragma unroll
-					for (int j = 0; j < NA; ++j)
-						if (j < kp1) {
-							const E vj = sv[(j + 1) * kOT + tid];
-							acc[j] = EL::fma(vi, vj, acc[j]);
-							acc2[j] = EL::fma(ui, vj, acc2[j]);
-						}
 				}
 				else if constexpr (PASS == 5) {
 					const int k = kp1 - 1;
@@ -384,18 +389,20 @@ k_gm_staged(OrthoArgs<T> a, const __grid_constant__ BasisMaps maps) {
 		}
 	}
 	if constexpr (PASS == 4 || PASS == 6) {
-		// pass 4: t and gamma (kp1 values), then s and alpha (kp1 values)
-		// in a second block of partials; pass 6: s and alpha
+		// pass 4: t and gamma (kp1 values, the first half of the consumers),
+		// then s and alpha (kp1 values, the second half) in a second block of
+		// partials; pass 6: s and alpha
+		const int grp = tid / (kOT / 2);
 		double vals[NA];
 #pragma unroll
 		for (int j = 0; j < NA; ++j)
-			vals[j] = j < kp1 ? EL::sum(acc[j]) : 0.0;
+			vals[j] = j < kp1 && (PASS == 6 || grp == 0) ? EL::sum(acc[j]) : 0.0;
 		staged_block_sum<NA>(vals, kp1, a.part, sh);
 		double *part2 = a.part + (size_t)gridDim.x * kp1;
 		if constexpr (PASS == 4) {
 #pragma unroll
 			for (int j = 0; j < NA; ++j)
-				vals[j] = j < kp1 ? EL::sum(acc2[j]) : 0.0;
+				vals[j] = j < kp1 && grp == 1 ? EL::sum(acc[j]) : 0.0;
 			__syncthreads();  // sh of the first sum is read
 			staged_block_sum<NA>(vals, kp1, part2, sh);
 		}
