@@ -338,7 +338,10 @@ class CSR:
         row offsets read), 2 = row patterns with symmetric storage (the
         diagonal and upper diagonals of a matrix that is symmetric bit for
         bit), 3 = the symmetric storage of a grid stencil addressed by grid
-        coordinates (no pattern ids, 16-byte loads).  `enable` switches it:
+        coordinates (no pattern ids, 16-byte loads), 4 = the general grid
+        storage that format 3 uses for a grid stencil whose values are not
+        symmetric (the lower diagonals at their own rows; not requestable by
+        itself).  `enable` switches it:
         True = the best format the matrix supports, False = column ids, or a
         mode number / name; a format the matrix (or its current values) does
         not support falls back to the next one down."""

@@ -950,7 +950,8 @@ int block_cg_run(Ctx *ctx, const fs_krylov_settings *s, Csr *A, bool jac, Vec *B
 	// coordinates; anything else: the CSR rows
 	BcgOp<V> op{A->rowptr, A->col, val, nullptr, 0, 0, 0, 0, 0};
 	FS_TRY(ensure_sym(A, mixed));
-	if (A->grid_nx > 0 && active_coding(A, mixed) >= kCodingSym) {
+	const int coding = active_coding(A, mixed);
+	if (A->grid_nx > 0 && (coding == kCodingSym || coding == kCodingGrid)) {
 		op.S = sym_vals<V>(A);
 		op.ld = A->sym_ld;
 		op.nx = A->grid_nx;

@@ -68,6 +68,7 @@ constexpr int kCodingColIds = 0;
 constexpr int kCodingPatterns = 1;
 constexpr int kCodingSym = 2;   // row patterns + symmetric storage (diagonal, upper diagonals)
 constexpr int kCodingGrid = 3;  // symmetric storage of a grid stencil: rows addressed by (i, j, k)
+constexpr int kCodingGridGen = 4;  // a grid stencil with asymmetric values: diagonal, upper and lower diagonals
 constexpr int kMaxSym = 4;      // positive column offsets of the symmetric storage
 
 struct FvmOp;
@@ -117,6 +118,12 @@ struct Csr {
 	float *sym32 = nullptr;
 	unsigned *sym_flag = nullptr;   // device: set by the build when a pair differs
 	bool sym64_valid = false, sym32_valid = false;
+	// general grid storage (a grid stencil whose values are not symmetric):
+	// the diagonal, the nsym upper diagonals a(r, r + d) and the nsym lower
+	// diagonals a(r, r - d), each at row r, (2 nsym + 1) x sym_ld
+	double *gen64 = nullptr;
+	float *gen32 = nullptr;
+	bool gen64_valid = false, gen32_valid = false;
 	int sym_state = -1;             // -1 not checked since the values changed, 0 no, 1 yes
 	// FMA-mode column-id SpMV kernel per value type (0 FP64, 1 FP32): 0 row
 	// blocks, L = 4..32 lanes per row of the vector kernel, 1 the vector
@@ -164,6 +171,9 @@ inline int active_coding(const Csr *A, bool f32 = false) {
 	if (A->coding >= kCodingSym && (f32 ? A->sym32_valid : A->sym64_valid))
 		return A->coding == kCodingGrid && A->grid_nx % 4 == 0 && A->grid_nx > 0 ? kCodingGrid
 		                                                                         : kCodingSym;
+	if (A->coding == kCodingGrid && A->grid_nx % 4 == 0 && A->grid_nx > 0 &&
+	    (f32 ? A->gen32_valid : A->gen64_valid))
+		return kCodingGridGen;
 	return kCodingPatterns;
 }
 
@@ -177,8 +187,9 @@ int ensure_val32(Csr *A);
 int spmv_lanes(Ctx *ctx, const Csr *A, bool f32);
 int ensure_dinv(Csr *A);
 // build the symmetric storage of A's current values for FP64 or FP32 SpMVs
-// when the format is requested and the values are symmetric (setup path: may
-// allocate and synchronise; never called during stream capture)
+// when the format is requested and the values are symmetric, or the general
+// grid storage when the grid format is requested and they are not (setup
+// path: may allocate and synchronise; never called during stream capture)
 int ensure_sym(Csr *A, bool f32);
 
 // ------------------------------------------------------------ errors --

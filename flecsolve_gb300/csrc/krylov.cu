@@ -931,7 +931,7 @@ int graph_run(Solver *s, const GraphKey &key_in, int (*body)(Solver *, void *), 
 	// are part of the key, so a format that changes with the values (the
 	// symmetric storage) or by request gets its own capture
 	GraphKey key = key_in;
-	key.fmt = active_coding(s->A, false) * 4 + active_coding(s->A, true) +
+	key.fmt = active_coding(s->A, false) * 8 + active_coding(s->A, true) +
 	          16 * (s->A->vec_lanes[0] + 1) + 1024 * (s->A->vec_lanes[1] + 1);
 	const auto gkey = std::make_pair((const Csr *)s->A, key);
 	auto it = s->graphs.find(gkey);

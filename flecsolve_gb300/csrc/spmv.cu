@@ -276,6 +276,8 @@ void invalidate_values(Csr *A) {
 	A->t_vals_valid = false;
 	A->sym64_valid = false;
 	A->sym32_valid = false;
+	A->gen64_valid = false;
+	A->gen32_valid = false;
 	A->sym_state = -1;
 }
 
@@ -309,9 +311,56 @@ __global__ void k_sym_build(int n, const int *__restrict__ rp, const double *__r
 	}
 }
 
-int ensure_sym(Csr *A, bool f32) {
-	if (!A->pslot || A->coding < kCodingSym || A->sym_state == 0)
+// The general grid storage of a grid stencil with asymmetric values: every
+// entry of row r at row r of its array (diagonal, upper diagonal d at
+// (1 + d) ld, lower diagonal d at (1 + nsym + d) ld, d = 0 .. nsym - 1).
+template<class V>
+__global__ void k_gen_build(int n, const int *__restrict__ rp, const double *__restrict__ val,
+                            const unsigned char *__restrict__ pid,
+                            const unsigned char *__restrict__ plen,
+                            const signed char *__restrict__ pslot, int nsym, int64_t ld,
+                            V *__restrict__ S) {
+	for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+		const int p = pid[r], len = plen[p], k0 = rp[r];
+		for (int j = 0; j < len; ++j) {
+			const int code = pslot[p * kPatW + j];
+			const int64_t slot = code >= 0 ? code : nsym - code;  // 0, 1..nsym, nsym+1..2 nsym
+			S[slot * ld + r] = (V)val[k0 + j];
+		}
+	}
+}
+
+static int ensure_gen(Csr *A, bool f32) {
+	if (A->coding != kCodingGrid || A->grid_nx <= 0 || A->grid_nx % 4 || A->sym_state != 0)
 		return FS_OK;
+	bool &valid = f32 ? A->gen32_valid : A->gen64_valid;
+	if (valid)
+		return FS_OK;
+	Ctx *ctx = A->ctx;
+	const size_t elems = (size_t)(2 * A->nsym + 1) * (size_t)A->sym_ld;
+	void **buf = f32 ? (void **)&A->gen32 : (void **)&A->gen64;
+	if (!*buf) {
+		const size_t bytes = elems * (f32 ? sizeof(float) : sizeof(double));
+		FS_CUDA_TRY(ctx, cudaMalloc(buf, bytes));
+		FS_CUDA_TRY(ctx, cudaMemsetAsync(*buf, 0, bytes, ctx->stream));
+	}
+	const int n = (int)A->nrows;
+	if (f32)
+		k_gen_build<float><<<grid_for(ctx, n, 256, 4), 256, 0, ctx->stream>>>(
+			n, A->rowptr, A->val, A->pid, A->plen, A->pslot, A->nsym, A->sym_ld, A->gen32);
+	else
+		k_gen_build<double><<<grid_for(ctx, n, 256, 4), 256, 0, ctx->stream>>>(
+			n, A->rowptr, A->val, A->pid, A->plen, A->pslot, A->nsym, A->sym_ld, A->gen64);
+	FS_TRY(check_launch(ctx, "general grid storage"));
+	valid = true;
+	return FS_OK;
+}
+
+int ensure_sym(Csr *A, bool f32) {
+	if (!A->pslot || A->coding < kCodingSym)
+		return FS_OK;
+	if (A->sym_state == 0)
+		return ensure_gen(A, f32);
 	bool &valid = f32 ? A->sym32_valid : A->sym64_valid;
 	if (valid)
 		return FS_OK;
@@ -346,6 +395,8 @@ int ensure_sym(Csr *A, bool f32) {
 		A->sym_state = bad ? 0 : 1;
 	}
 	valid = A->sym_state == 1;
+	if (A->sym_state == 0)
+		return ensure_gen(A, f32);
 	return FS_OK;
 }
 
@@ -894,7 +945,8 @@ FS_API int fs_csr_destroy(fs_csr h) {
 	                (void *)A->pid, (void *)A->ptab, (void *)A->pwb, (void *)A->plen, (void *)A->pslot, (void *)A->pinv,
 	                (void *)A->sofs, (void *)A->stab, (void *)A->sym64, (void *)A->sym32, (void *)A->sym_flag,
 	                (void *)A->t_colptr, (void *)A->t_row, (void *)A->t_perm, (void *)A->t_val,
-	                (void *)A->t_blk, (void *)A->t_blkinfo, (void *)A->bin_rows, (void *)A->bin_task})
+	                (void *)A->t_blk, (void *)A->t_blkinfo, (void *)A->bin_rows, (void *)A->bin_task,
+	                (void *)A->gen64, (void *)A->gen32})
 		if (p)
 			cudaFree(p);
 	destroy_fvm(A->fvm);

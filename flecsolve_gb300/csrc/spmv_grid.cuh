@@ -18,6 +18,11 @@
 // kernels, so results are identical bit for bit; boundary rows skip the
 // neighbours outside the grid exactly as their CSR rows lack them.
 //
+// GEN: a grid stencil whose values are not symmetric (convection-diffusion)
+// reads the general grid storage, where the lower diagonals l_d[r] =
+// a(r, r - d) sit at row r after the upper ones: the lower partners become
+// 16-byte loads at r like the upper diagonals, three more loads for W rows.
+//
 // Work: 256-thread CTAs, one W-row segment per thread and step (256 W rows a
 // step); chunks of consecutive steps strided over a persistent grid, as in
 // spmv_sym_kernel (neighbouring lines out of L1, neighbouring planes out of
@@ -39,7 +44,7 @@ struct CsrGrid {
 constexpr int kGridThreads = 256;
 constexpr int kGridChunk = 4;
 
-template<class V, bool EXACT, class G, class Epi>
+template<class V, bool EXACT, bool GEN, class G, class Epi>
 __global__ void __launch_bounds__(kGridThreads)
 spmv_grid_kernel(CsrGrid<V> A, G g_in, Epi epi) {
 	constexpr int NV = Epi::NV;
@@ -62,6 +67,10 @@ spmv_grid_kernel(CsrGrid<V> A, G g_in, Epi epi) {
 	const V *__restrict__ U1 = A.S + A.ld;
 	const V *__restrict__ U2 = A.S + 2 * A.ld;
 	const V *__restrict__ U3 = A.S + 3 * A.ld;
+	// GEN: the lower diagonals after the K upper ones
+	const V *__restrict__ L1 = A.S + (int64_t)(A.K + 1) * A.ld;
+	const V *__restrict__ L2 = A.S + (int64_t)(A.K + 2) * A.ld;
+	const V *__restrict__ L3 = A.S + (int64_t)(A.K + 3) * A.ld;
 	for (int k = 0;; ++k) {
 		const int chunk = (int)blockIdx.x + (k / A.chunk) * (int)gridDim.x;
 		const int step = chunk * A.chunk + k % A.chunk;
@@ -78,14 +87,17 @@ spmv_grid_kernel(CsrGrid<V> A, G g_in, Epi epi) {
 		const bool lo_x = i0 > 0, hi_x = i0 + W < A.nx;
 		const bool lo_y = has_y && jj > 0, hi_y = has_y && jj < A.ny - 1;
 		const bool lo_z = has_z && kk > 0, hi_z = has_z && kk < A.nz - 1;
-		V d[W], u1[W], u2[W], u3[W], u2m[W], u3m[W];
+		V d[W], u1[W], u2[W], u3[W], u2m[W], u3m[W], l1[W];
 		V x[W], xmy[W], xpy[W], xmz[W], xpz[W];
 		V u1m = V(0), xm1 = V(0), xp1 = V(0);
 		ld_vec16(D + r0, d);
 		ld_vec16(U1 + r0, u1);
 		g.at_vec(r0, x);
+		if constexpr (GEN)
+			ld_vec16(L1 + r0, l1);
 		if (lo_x) {
-			u1m = __ldg(U1 + r0 - 1);
+			if constexpr (!GEN)
+				u1m = __ldg(U1 + r0 - 1);
 			xm1 = g.at(r0 - 1);
 		}
 		if (hi_x)
@@ -93,7 +105,10 @@ spmv_grid_kernel(CsrGrid<V> A, G g_in, Epi epi) {
 		if (has_y) {
 			ld_vec16(U2 + r0, u2);
 			if (lo_y) {
-				ld_vec16(U2 + r0 - A.nx, u2m);
+				if constexpr (GEN)
+					ld_vec16(L2 + r0, u2m);
+				else
+					ld_vec16(U2 + r0 - A.nx, u2m);
 				g.at_vec(r0 - A.nx, xmy);
 			}
 			if (hi_y)
@@ -102,7 +117,10 @@ spmv_grid_kernel(CsrGrid<V> A, G g_in, Epi epi) {
 		if (has_z) {
 			ld_vec16(U3 + r0, u3);
 			if (lo_z) {
-				ld_vec16(U3 + (r0 - nxy), u3m);
+				if constexpr (GEN)
+					ld_vec16(L3 + r0, u3m);
+				else
+					ld_vec16(U3 + (r0 - nxy), u3m);
 				g.at_vec((int)(r0 - nxy), xmz);
 			}
 			if (hi_z)
@@ -122,10 +140,18 @@ spmv_grid_kernel(CsrGrid<V> A, G g_in, Epi epi) {
 				term(u3m[q], xmz[q]);
 			if (lo_y)
 				term(u2m[q], xmy[q]);
-			if (q > 0)
-				term(u1[q - 1], x[q - 1]);
-			else if (lo_x)
-				term(u1m, xm1);
+			if constexpr (GEN) {
+				if (q > 0)
+					term(l1[q], x[q - 1]);
+				else if (lo_x)
+					term(l1[0], xm1);
+			}
+			else {
+				if (q > 0)
+					term(u1[q - 1], x[q - 1]);
+				else if (lo_x)
+					term(u1m, xm1);
+			}
 			term(d[q], x[q]);
 			if (q < W - 1)
 				term(u1[q], x[q + 1]);
@@ -159,11 +185,18 @@ inline bool grid_aligned(const Csr *A, const V *x, const V *dscale) {
 	       A->nrows < (int64_t)1 << 30;
 }
 
-template<class V, bool EXACT, class G, class Epi>
+template<class V>
+inline const V *gen_vals(const Csr *A);
+template<>
+inline const double *gen_vals<double>(const Csr *A) { return A->gen64; }
+template<>
+inline const float *gen_vals<float>(const Csr *A) { return A->gen32; }
+
+template<class V, bool EXACT, bool GEN, class G, class Epi>
 static inline int launch_spmv_grid(Ctx *ctx, const Csr *A, const G &g, const Epi &epi) {
 	static int per_sm = 0;  // resident CTAs per SM of this instantiation
 	constexpr int W = 16 / (int)sizeof(V);
-	auto kern = spmv_grid_kernel<V, EXACT, G, Epi>;
+	auto kern = spmv_grid_kernel<V, EXACT, GEN, G, Epi>;
 	if (per_sm == 0) {
 		int nb = 0;
 		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kGridThreads, 0) != cudaSuccess ||
@@ -177,10 +210,11 @@ static inline int launch_spmv_grid(Ctx *ctx, const Csr *A, const G &g, const Epi
 	const int chunk = nstep >= kGridChunk * resident ? kGridChunk : 1;
 	const int nchunk = (nstep + chunk - 1) / chunk;
 	const int grid = std::max(1, std::min(nchunk, resident));
-	CsrGrid<V> d{sym_vals<V>(A), A->sym_ld, (int)A->nrows, A->grid_nx, A->grid_ny, A->grid_nz,
-	             A->nsym, chunk};
+	CsrGrid<V> d{GEN ? gen_vals<V>(A) : sym_vals<V>(A), A->sym_ld, (int)A->nrows, A->grid_nx,
+	             A->grid_ny, A->grid_nz, A->nsym, chunk};
 	return check_launch_rc(ctx, launch_pdl(ctx->stream, kern, grid, kGridThreads, 0, d, g, epi),
-	                       "spmv (grid stencil, symmetric storage)");
+	                       GEN ? "spmv (grid stencil, general storage)"
+	                           : "spmv (grid stencil, symmetric storage)");
 }
 
 }  // namespace fsg

@@ -444,8 +444,9 @@ static inline int launch_spmv_as(Ctx *ctx, const CsrDev<V> &d, const V *x, const
 namespace fsg {
 
 // The index format in use: the symmetric storage when it is built for the
-// current values (and `vals` are A's own values), else the warp-specialised
-// row-pattern kernel when the matrix carries patterns, else column ids.
+// current values (and `vals` are A's own values), the general grid storage of
+// a grid stencil with asymmetric values, else the warp-specialised row-pattern
+// kernel when the matrix carries patterns, else column ids.
 template<class V, bool EXACT, bool SCALE, class Epi>
 static inline int launch_spmv(Ctx *ctx, const Csr *A, const V *vals, const V *x,
                               const V *dscale, const Epi &epi) {
@@ -460,11 +461,17 @@ static inline int launch_spmv(Ctx *ctx, const Csr *A, const V *vals, const V *x,
 	const bool own_vals = vals == (F32 ? (const V *)A->val32 : (const V *)A->val);
 	if (coding == kCodingGrid && own_vals && grid_aligned<V>(A, x, dscale)) {
 		if constexpr (SCALE)
-			return launch_spmv_grid<V, EXACT>(ctx, A, GatherScale<V>{x, dscale}, epi);
+			return launch_spmv_grid<V, EXACT, false>(ctx, A, GatherScale<V>{x, dscale}, epi);
 		else
-			return launch_spmv_grid<V, EXACT>(ctx, A, GatherX<V>{x}, epi);
+			return launch_spmv_grid<V, EXACT, false>(ctx, A, GatherX<V>{x}, epi);
 	}
-	if (coding >= kCodingSym && own_vals) {
+	if (coding == kCodingGridGen && own_vals && grid_aligned<V>(A, x, dscale)) {
+		if constexpr (SCALE)
+			return launch_spmv_grid<V, EXACT, true>(ctx, A, GatherScale<V>{x, dscale}, epi);
+		else
+			return launch_spmv_grid<V, EXACT, true>(ctx, A, GatherX<V>{x}, epi);
+	}
+	if ((coding == kCodingSym || coding == kCodingGrid) && own_vals) {
 		if constexpr (SCALE)
 			return launch_spmv_sym<V, EXACT>(ctx, A, GatherScale<V>{x, dscale}, epi);
 		else

@@ -172,7 +172,12 @@ FS_API int fs_csr_values_device_ptr(fs_csr A, double **dval);
  *    neighbours inside the grid, found at creation) with nx a multiple of 4:
  *    rows are addressed by their grid coordinates, no pattern id is read, and
  *    16-byte loads serve 4 (FP32) or 2 (FP64) rows.  Other matrices use
- *    format 2.  Formats 1-3 give the bits of format 0.
+ *    format 2.
+ *  4 general grid stencil (active only, through a request of format 3): a
+ *    grid stencil as in format 3 whose values are not symmetric, read from
+ *    the diagonal, the upper diagonals and the lower diagonals a(r, r - d)
+ *    stored at row r.
+ *  Formats 1-4 give the bits of format 0.
  * enable: 0 .. 3 requests a format (a matrix falls back to the best format it
  * supports), -1 leaves it unchanged; *active (may be NULL) = the format the
  * FP64 SpMV uses now. */

@@ -43,12 +43,14 @@ def _pattern_rect(n2, rows, cols):
 
 
 PATTERN_CASES = ["poisson2d-128", "poisson2d-127", "diffusion3d-24", "diffusion3d-23",
-                 "convdiff3d-20", "rect-wide", "rect-tall", "line-1000", "box-12x5x7"]
+                 "convdiff3d-20", "convdiff3d-21", "rect-wide", "rect-tall", "line-1000",
+                 "box-12x5x7", "asym-line-1000", "asym-box-16x9x1", "asym-box-12x5x7"]
 
 
-def _grid_stencil(nx, ny, nz, seed):
+def _grid_stencil(nx, ny, nz, seed, asym=False):
     """A symmetric diffusion-like stencil on an nx x ny x nz grid (1-D when
-    ny = nz = 1, 2-D when nz = 1) with seeded off-diagonals."""
+    ny = nz = 1, 2-D when nz = 1) with seeded off-diagonals; `asym`: the lower
+    entries drawn separately (the same structure, values not symmetric)."""
     import scipy.sparse as sp
     rng = np.random.default_rng(seed)
     n = nx * ny * nz
@@ -61,9 +63,10 @@ def _grid_stencil(nx, ny, nz, seed):
     for d in range(K):
         keep = c[d] < dims[d] - 1
         v = rng.uniform(-1.0, -0.1, int(keep.sum()))
+        vl = rng.uniform(-1.0, -0.1, int(keep.sum())) if asym else v
         rows += [r[keep], r[keep] + offs[d]]
         cols += [r[keep] + offs[d], r[keep]]
-        vals += [v, v]
+        vals += [v, vl]
     M = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
                       shape=(n, n))
     M.sort_indices()
@@ -75,6 +78,12 @@ def _pattern_matrix(name):
         return _grid_stencil(1000, 1, 1, 5)
     if name == "box-12x5x7":
         return _grid_stencil(12, 5, 7, 6)
+    if name == "asym-line-1000":
+        return _grid_stencil(1000, 1, 1, 7, asym=True)
+    if name == "asym-box-16x9x1":
+        return _grid_stencil(16, 9, 1, 8, asym=True)
+    if name == "asym-box-12x5x7":
+        return _grid_stencil(12, 5, 7, 9, asym=True)
     if name == "rect-wide":
         return _pattern_rect(61, 3001, 61 * 61)   # ncols > nrows, odd sizes
     if name == "rect-tall":
@@ -90,24 +99,34 @@ def test_row_pattern_spmv_matches_column_ids(ctx, wl):
     entries read from their partners) and the row-pattern SpMV (coding 1,
     warp-specialised, row offsets from pattern lengths) give the same bits as
     the one reading column ids (coding 0), in every mode and type, on odd
-    sizes, 1-, 2- and 3-D grids and rectangular matrices.  A matrix that is
-    not symmetric bit for bit falls back to coding 1, a symmetric one that is
-    not a grid stencil with nx a multiple of 4 to coding 2."""
+    sizes, 1-, 2- and 3-D grids and rectangular matrices.  A grid stencil with
+    nx a multiple of 4 whose values are not symmetric reads the general grid
+    storage (active coding 4: the lower diagonals stored at their own rows);
+    another matrix that is not symmetric bit for bit falls back to coding 1, a
+    symmetric one that is not a grid stencil with nx a multiple of 4 to
+    coding 2."""
     A = _pattern_matrix(wl)
     x = P.uniform(43, A.ncols)
     dA = fs.CSR(ctx, A)
     S = A.to_scipy()
     symmetric = A.nrows == A.ncols and (S != S.T).nnz == 0
     nx, ny, nz = dA.grid_dims()
-    if wl.startswith(("poisson2d", "diffusion3d", "line", "box")):
-        side = int(wl.split("-")[1].split("x")[0])
+    if wl.startswith(("poisson2d", "diffusion3d", "convdiff3d", "line", "box", "asym")):
+        side = int(wl.split("-")[-1].split("x")[0])
         assert nx == side and nx * ny * nz == A.nrows
-    grid = symmetric and nx > 0 and nx % 4 == 0
-    best = 3 if grid else (2 if symmetric else 1)
-    assert dA.index_coding() == best
+    grid_ok = nx > 0 and nx % 4 == 0
+
+    def expect(req):
+        if req == 0:
+            return 0
+        if req >= 3 and grid_ok:
+            return 3 if symmetric else 4
+        return 2 if req >= 2 and symmetric else 1
+
+    assert dA.index_coding() == expect(3)
     out = {}
     for coding in (3, 2, 1, 0):
-        assert dA.index_coding(coding) == min(coding, best)
+        assert dA.index_coding(coding) == expect(coding)
         for dt in ("f64", "f32"):
             vx, vy = fs.Vector(ctx, x.astype(np.float32) if dt == "f32" else x, dt), fs.Vector(ctx, A.nrows, dt)
             for exact in (True, False):
@@ -126,8 +145,8 @@ def test_row_pattern_spmv_matches_column_ids(ctx, wl):
 def test_symmetric_storage_follows_value_changes(ctx):
     """The symmetric storage is derived from the current values: a value
     change that breaks the symmetry switches the operator (and a bound
-    solver's captured iterations) to the row-pattern kernel; restoring it
-    switches back.  Results follow the values every time."""
+    solver's captured iterations) to the general grid storage (coding 4);
+    restoring it switches back.  Results follow the values every time."""
     A, b = P.workload("diffusion3d-24")
     x = P.uniform(46, A.ncols)
     dA = fs.CSR(ctx, A)
@@ -140,7 +159,7 @@ def test_symmetric_storage_follows_value_changes(ctx):
         if step == 1:
             M.val[A.rowptr[100] + 1] *= 1.5     # one lower entry no longer matches its partner
         dA.update_values(M.val)
-        assert dA.index_coding() == (1 if step == 1 else 3)
+        assert dA.index_coding() == (4 if step == 1 else 3)
         dA.apply(vx, vy, exact=True)
         assert np.array_equal(vy.numpy(), O.spmv(M, x))
         vsol = fs.Vector(ctx, A.nrows)
