@@ -13,6 +13,7 @@
 // graph return at their first instruction.
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "solver.cuh"
 
@@ -547,9 +548,29 @@ __global__ void k_bi_p(int64_t n, V *__restrict__ p, const V *__restrict__ v,
 	else {
 		const double bd = (st->rho / st->rho_old) * (st->alpha / st->omega);
 		const V beta = (V)bd, om = (V)st->omega;
-		FOR_EACH(i, n) {
-			V t = fma(-om, v[i], p[i]);
-			p[i] = fma(beta, t, res[i]);
+		auto one = [&](V &pi, V vi, V ri) { pi = fma(beta, fma(-om, vi, pi), ri); };
+		if constexpr (std::is_same_v<V, float>) {
+			// four elements a thread and pass (16-byte accesses; the solver's
+			// FP32 vectors are 16-byte aligned), the last n mod 4 one by one
+			const int64_t n4 = n >> 2;
+			float4 *p4 = reinterpret_cast<float4 *>(p);
+			const float4 *v4 = reinterpret_cast<const float4 *>(v);
+			const float4 *r4 = reinterpret_cast<const float4 *>(res);
+			FOR_EACH(i, n4) {
+				float4 pv = p4[i];
+				const float4 vv = v4[i], rv = r4[i];
+				one(pv.x, vv.x, rv.x);
+				one(pv.y, vv.y, rv.y);
+				one(pv.z, vv.z, rv.z);
+				one(pv.w, vv.w, rv.w);
+				p4[i] = pv;
+			}
+			for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+			     i += (int64_t)gridDim.x * blockDim.x)
+				one(p[i], v[i], res[i]);
+		}
+		else {
+			FOR_EACH(i, n) one(p[i], v[i], res[i]);
 		}
 	}
 }
@@ -591,10 +612,31 @@ k_bi_s(int64_t n, V *__restrict__ s, const V *__restrict__ v, const V *__restric
 	const V a = (V)st->alpha;
 	Acc<V, 1> acc;
 	acc.init();
-	FOR_EACH(i, n) {
-		V si = fma(-a, v[i], res[i]);
-		s[i] = si;
+	auto one = [&](V &si, V vi, V ri) {
+		si = fma(-a, vi, ri);
 		acc.add_prod(0, si, si);
+	};
+	if constexpr (std::is_same_v<V, float>) {
+		// four elements a thread and pass, as k_bi_p
+		const int64_t n4 = n >> 2;
+		float4 *s4 = reinterpret_cast<float4 *>(s);
+		const float4 *v4 = reinterpret_cast<const float4 *>(v);
+		const float4 *r4 = reinterpret_cast<const float4 *>(res);
+		FOR_EACH(i, n4) {
+			float4 sv;
+			const float4 vv = v4[i], rv = r4[i];
+			one(sv.x, vv.x, rv.x);
+			one(sv.y, vv.y, rv.y);
+			one(sv.z, vv.z, rv.z);
+			one(sv.w, vv.w, rv.w);
+			s4[i] = sv;
+		}
+		for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+		     i += (int64_t)gridDim.x * blockDim.x)
+			one(s[i], v[i], res[i]);
+	}
+	else {
+		FOR_EACH(i, n) one(s[i], v[i], res[i]);
 	}
 	acc.to_part(part, sh);
 	if (last_block(counter)) {
@@ -674,16 +716,40 @@ k_bi_x(int64_t n, V *__restrict__ x, const V *__restrict__ p, const V *__restric
 	const V om = (V)st->omega;
 	Acc<V, 2> acc;
 	acc.init();
-	FOR_EACH(i, n) {
-		V ph = PK ? dinv[i] * p[i] : p[i];
-		V sh_ = PK ? dinv[i] * s[i] : s[i];
-		V xi = fma(a, ph, x[i]);
-		xi = fma(om, sh_, xi);
-		x[i] = xi;
-		V ri = fma(-om, t[i], s[i]);
-		res[i] = ri;
+	auto one = [&](V &xi, V &ri, V pi, V si, V ti, V rti, V di) {
+		const V ph = PK ? di * pi : pi;
+		const V sh_ = PK ? di * si : si;
+		xi = fma(om, sh_, fma(a, ph, xi));
+		ri = fma(-om, ti, si);
 		acc.add_prod(0, ri, ri);
-		acc.add_prod(1, rt[i], ri);
+		acc.add_prod(1, rti, ri);
+	};
+	if constexpr (std::is_same_v<V, float>) {
+		// four elements a thread and pass, as k_bi_p
+		const int64_t n4 = n >> 2;
+		float4 *x4 = reinterpret_cast<float4 *>(x), *r4 = reinterpret_cast<float4 *>(res);
+		const float4 *p4 = reinterpret_cast<const float4 *>(p);
+		const float4 *s4 = reinterpret_cast<const float4 *>(s);
+		const float4 *t4 = reinterpret_cast<const float4 *>(t);
+		const float4 *q4 = reinterpret_cast<const float4 *>(rt);
+		const float4 *d4 = reinterpret_cast<const float4 *>(dinv);
+		FOR_EACH(i, n4) {
+			float4 xv = x4[i], rv;
+			const float4 pv = p4[i], sv = s4[i], tv = t4[i], qv = q4[i];
+			const float4 dv = PK ? d4[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+			one(xv.x, rv.x, pv.x, sv.x, tv.x, qv.x, dv.x);
+			one(xv.y, rv.y, pv.y, sv.y, tv.y, qv.y, dv.y);
+			one(xv.z, rv.z, pv.z, sv.z, tv.z, qv.z, dv.z);
+			one(xv.w, rv.w, pv.w, sv.w, tv.w, qv.w, dv.w);
+			x4[i] = xv;
+			r4[i] = rv;
+		}
+		for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+		     i += (int64_t)gridDim.x * blockDim.x)
+			one(x[i], res[i], p[i], s[i], t[i], rt[i], PK ? dinv[i] : 0.f);
+	}
+	else {
+		FOR_EACH(i, n) one(x[i], res[i], p[i], s[i], t[i], rt[i], PK ? dinv[i] : V(0));
 	}
 	acc.to_part(part, sh);
 	if (last_block(counter)) {
