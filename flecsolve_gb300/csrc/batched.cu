@@ -21,10 +21,18 @@
 // until the residual is below `head` ||b|| (the first decades, where the
 // solution's large components form; FP32 recurrences from the first
 // iteration lose orthogonality on the larger 2-D systems and take up to 13 %
-// more iterations), then FP32 values and vectors, dots accumulated in FP64;
+// more iterations), then FP32 values and vectors, the dots' FP32 products
+// summed in compensated FP32 pairs per thread and in FP64 across the team;
 // the residual is replaced by the FP64 one, b - A x with the FP64 values,
 // whenever it has dropped by `delta` and at every stop, and the stopping test
 // is on that FP64 residual.
+//
+// Storage: a batch whose systems are all symmetric 5-point stencils on square
+// grids reads their diagonals and upper diagonals (no column ids; the CSR
+// row loop's bits), other batches the CSR.  The row loops take one row at a
+// time in the 1024-thread build and 4 or 8 FP32 rows (2 or 4 FP64) in the
+// 512- and 256-thread builds, every load of a batch of rows issued before
+// any store.
 //
 #include <cooperative_groups.h>
 
